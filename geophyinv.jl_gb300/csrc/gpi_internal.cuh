@@ -1,0 +1,160 @@
+// gpi_internal.cuh -- device layout and plan state of the GB300 FDTD engine.
+//
+// Storage layout (one array per field, per buffer, per wavefield):
+//   every field of a shot lives in an NZP x [NYP x] NXP block, z fastest,
+//   with a front pad of ZOFF rows / YOFF planes / XOFF columns, so that the
+//   reference's 1-based index (r, [y,] c) of ANY field sits at
+//       off = ((c - 1 + XOFF) * NYP + (y - 1 + YOFF)) * NZP + (r - 1 + ZOFF)
+//   (NYP = 1, YOFF = 1 in 2-D).  Fields of different staggered shapes thus
+//   share one index map and the pads absorb the stencil halos, so kernels
+//   need no bounds checks on reads.  NZP is a multiple of 32 floats, so a
+//   column starts on a 128-byte boundary.  Shots are stacked behind each
+//   other (shot stride = NZP * NYP * NXP).
+//
+//   State is double-buffered (ping-pong): a time step reads buffer `cur`
+//   and writes buffer `cur ^ 1`, which lets one kernel advance velocities
+//   and stresses together while neighbouring blocks recompute halo
+//   velocities from untouched inputs.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gpi_fdtd.h"
+
+namespace gpi {
+
+constexpr int NFIELD = 10;
+constexpr int ZOFF = 4, XOFF = 4, YOFF = 4;
+constexpr int MAXDER = 18;
+constexpr int NKIND = 4;  // injection kinds: vx, vy, vz, stress
+
+// Canonical derivative order (docs and oracle use the same):
+//   A2: dpdx dpdz dvxdx dvzdz
+//   E2: dtauxxdx dtauxzdx dtauzzdz dtauxzdz dvxdx dvzdz dvxdz dvzdx
+//   A3: dpdx dpdy dpdz dvxdx dvydy dvzdz
+//   E3: dtauxxdx dtauxydx dtauxzdx dtauyydy dtauxydy dtauyzdy dtauzzdz
+//       dtauyzdz dtauxzdz dvxdx dvydy dvzdz dvxdy dvxdz dvydx dvydz dvzdx dvzdy
+struct DerivSpec {
+  int axis;        // 0 z, 1 y, 2 x
+  int kz, ky, kx;  // shape kinds: 0 n, 1 n+h, 2 n-h, 3 n-2h
+};
+int deriv_specs(int physics, int ndim, const DerivSpec **out);
+void field_kinds(int field, int *kz, int *ky, int *kx);
+
+// One receiver (one CSC column) of one (shot, field).
+struct RecTask {
+  int32_t shot, field, e0, e1;  // entries [e0, e1)
+  int64_t out;                  // offset of record (it=0) in the record pool
+  int32_t stride;               // floats between consecutive time samples
+  int32_t pad;
+};
+// One injection cell (one row of one spray matrix) of one (shot, ipw, kind).
+struct InjCell {
+  int32_t row, col, ydx;  // reference 1-based indices in the target field (ydx = y in 3-D)
+  int32_t kind;           // 0 vx, 1 vy, 2 vz, 3 stress (p or the normal stresses)
+  int32_t e0, e1;         // (source, weight) pairs [e0, e1)
+  int32_t wav;            // index of the wavelet table entry (ns, pointer)
+  int32_t pad;
+  int64_t off;            // storage offset within the shot
+  int64_t roff0, roff1;   // rho storage offsets of the density average (velocity kinds)
+};
+
+struct Plan {
+  gpi_plan_desc d;
+  int h = 3;
+  int NZP = 0, NYP = 1, NXP = 0;
+  int64_t fstride = 0;  // floats per field per shot
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int present[NFIELD] = {0};
+  int nder = 0;
+  const DerivSpec *ds = nullptr;
+  // tiling of the step kernel
+  int TZ = 128, TY = 1, L = 128, nzb = 1, nyb = 1, nxb = 1;
+
+  // device memory
+  void *pool = nullptr;
+  size_t pool_bytes = 0;
+  float *state[2][2][NFIELD] = {};  // [buffer][ipw][field] -> shot 0
+  float *psi[2][2][MAXDER] = {};    // [buffer][ipw][q]
+  int64_t psi_stride[MAXDER] = {};  // floats per shot
+  float *coef[8] = {};              // update coefficients, storage layout
+  int ncoef = 0;
+  float *mod[3] = {};  // medium parameters, storage layout
+  int nmod = 0;
+  float *pml = nullptr;  // [nder][3][2*npml]
+  float *grad[2] = {};   // per-shot gradients [shot][storage] (adjoint)
+  float *bstore = nullptr;  // boundary store (forward_save -> adjoint)
+  int64_t bstep = 0;         // floats per step per shot
+  int64_t bsnap = 0;         // floats of the final snapshots per shot
+  int cur[2] = {0, 0};       // buffer holding the current state, per wavefield
+  int have_save = 0;
+
+  // receivers
+  std::vector<std::vector<int>> rec_n;               // [shot][field] -> nr (0 none)
+  std::vector<std::vector<std::vector<int64_t>>> rec_cp;   // host copies
+  std::vector<std::vector<std::vector<int64_t>>> rec_off;  // storage offsets
+  std::vector<std::vector<std::vector<float>>> rec_w;
+  float *rec_pool = nullptr;
+  size_t rec_pool_floats = 0;
+  std::vector<std::vector<int64_t>> rec_base;  // [shot][field] offset in pool
+  RecTask *d_rtask = nullptr;
+  int n_rtask = 0;
+  int64_t *d_roff = nullptr;
+  float *d_rw = nullptr;
+  bool rec_dirty = true;
+
+  // sources: per (ipw, shot, field) CSC + wavelets (host), compiled to cells
+  struct Src {
+    int ns = 0;
+    std::vector<int64_t> cp, rv;
+    std::vector<float> nz, wav;
+  };
+  std::vector<std::vector<std::vector<Src>>> src;  // [ipw][shot][field]
+  bool src_dirty = true;
+  InjCell *d_cells = nullptr;
+  int n_cells = 0;
+  int32_t *d_pair_j = nullptr;
+  float *d_pair_w = nullptr;
+  float **d_wav = nullptr;  // per wavelet table entry: device pointer (nt x ns)
+  int32_t *d_wav_ns = nullptr;
+  std::vector<float *> wav_bufs;
+  float *d_amount = nullptr;               // per cell, current step
+  std::vector<int32_t> group_ptr;          // [(ipw*nshots + shot)*NKIND + kind] -> cell range
+  int32_t *d_group_ptr = nullptr;
+
+  int64_t launches = 0;
+};
+
+// error helpers
+int fail(Plan *p, int code, const std::string &msg);
+#define GPI_CUDA(p, call)                                                              \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) return gpi::fail((p), GPI_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+inline int64_t soff(const Plan &p, int r, int y, int c) {
+  return ((int64_t)(c - 1 + XOFF) * p.NYP + (p.d.ndim == 3 ? (y - 1 + YOFF) : 0)) * p.NZP + (r - 1 + ZOFF);
+}
+int nkind(int kind, int n, int h);
+
+// kernels (per physics)
+int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly);
+int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly);
+int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
+int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
+int aux_step(Plan *p, int it, int mode);
+int compute_coefficients(Plan *p);
+int boundary_io(Plan *p, int it, int dir);
+int snap_io(Plan *p, int tau, int dir);
+
+}  // namespace gpi
+
+struct gpi_plan {
+  gpi::Plan p;
+};

@@ -1,0 +1,808 @@
+// gpi_plan.cu -- plan lifecycle and the C ABI of libgpi_fdtd.so.
+//
+// The plan is the device-side twin of the reference's PFdtd: P_common's
+// coefficient arrays (src/fdtd/types.jl:133-166) plus, for every
+// supersource, the per-worker wavefields, CPML memory and records
+// (src/fdtd/types.jl:8-22, :81-88).  Shots are batched inside each launch
+// instead of being looped over by Distributed workers.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "gpi_internal.cuh"
+
+namespace gpi {
+
+static thread_local std::string g_create_err;
+
+int fail(Plan *p, int code, const std::string &msg) {
+  if (p)
+    p->err = msg;
+  else
+    g_create_err = msg;
+  return code;
+}
+
+// ---------------------------------------------------------------------------
+// derivative-field tables (get_mgrid shapes, src/fields.jl:92-671)
+// ---------------------------------------------------------------------------
+enum { KF = 0, KV = 1, KH = 2, KI = 3 };
+static const DerivSpec DA2[] = {{2, KI, KF, KH}, {0, KH, KF, KI}, {2, KF, KF, KF}, {0, KF, KF, KF}};
+static const DerivSpec DE2[] = {{2, KI, KF, KH}, {2, KH, KF, KI}, {0, KH, KF, KI}, {0, KI, KF, KH},
+                                {2, KF, KF, KF}, {0, KF, KF, KF}, {0, KH, KF, KH}, {2, KH, KF, KH}};
+static const DerivSpec DA3[] = {{2, KI, KI, KH}, {1, KI, KH, KI}, {0, KH, KI, KI},
+                                {2, KF, KF, KF}, {1, KF, KF, KF}, {0, KF, KF, KF}};
+static const DerivSpec DE3[] = {{2, KI, KI, KH}, {2, KI, KH, KI}, {2, KH, KI, KI}, {1, KI, KH, KI},
+                                {1, KI, KI, KH}, {1, KH, KI, KI}, {0, KH, KI, KI}, {0, KI, KH, KI},
+                                {0, KI, KI, KH}, {2, KF, KF, KF}, {1, KF, KF, KF}, {0, KF, KF, KF},
+                                {1, KI, KH, KH}, {0, KH, KI, KH}, {2, KI, KH, KH}, {0, KH, KH, KI},
+                                {2, KH, KI, KH}, {1, KH, KH, KI}};
+
+int deriv_specs(int physics, int ndim, const DerivSpec **out) {
+  if (physics == GPI_ACOUSTIC) {
+    *out = ndim == 2 ? DA2 : DA3;
+    return ndim == 2 ? 4 : 6;
+  }
+  *out = ndim == 2 ? DE2 : DE3;
+  return ndim == 2 ? 8 : 18;
+}
+
+static const int FK[NFIELD][3] = {{KF, KF, KF}, {KF, KF, KV}, {KF, KV, KF}, {KV, KF, KF}, {KF, KF, KF},
+                                  {KF, KF, KF}, {KF, KF, KF}, {KI, KH, KH}, {KH, KI, KH}, {KH, KH, KI}};
+void field_kinds(int f, int *kz, int *ky, int *kx) {
+  *kz = FK[f][0];
+  *ky = FK[f][1];
+  *kx = FK[f][2];
+}
+int nkind(int kind, int n, int h) {
+  switch (kind) {
+    case KV: return n + h;
+    case KH: return n - h;
+    case KI: return n - 2 * h;
+    default: return n;
+  }
+}
+static void field_shape(const Plan &p, int f, int n[3]) {
+  n[0] = nkind(FK[f][0], p.d.nz, p.h);
+  n[1] = p.d.ndim == 3 ? nkind(FK[f][1], p.d.ny, p.h) : 1;
+  n[2] = nkind(FK[f][2], p.d.nx, p.h);
+}
+static int64_t field_len(const Plan &p, int f) {
+  int n[3];
+  field_shape(p, f, n);
+  return (int64_t)n[0] * n[1] * n[2];
+}
+
+static int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// tiling of the step kernels: z-blocks of TZ rows, (3-D: TY planes),
+// x-chunks of L columns; the chunk count is chosen so that the grid is a
+// near multiple of the 152 SMs.
+static void choose_tiling(Plan &p) {
+  const int sms = 152;
+  if (p.d.ndim == 2) {
+    p.TZ = 128;
+    p.TY = 1;
+    p.nzb = (p.d.nz + p.TZ - 1) / p.TZ;
+    p.nyb = 1;
+    int resident = sms * 8;  // blocks resident at once (128 threads, <= 64 regs)
+    int per_chunk = p.nzb * p.d.nshots;
+    int best = 1;
+    double best_eff = 0;
+    for (int nxb = 1; nxb <= std::max(1, p.d.nx / 48); nxb++) {
+      int64_t blocks = (int64_t)nxb * per_chunk;
+      double waves = (double)blocks / resident;
+      double eff = waves / std::ceil(waves);
+      int L = (p.d.nx + nxb - 1) / nxb;
+      double halo = 3.0 / L;  // redundant velocity columns
+      eff *= (1.0 - halo);
+      if (blocks < resident / 2) eff *= (double)blocks / (resident / 2);
+      if (eff > best_eff + 1e-9) {
+        best_eff = eff;
+        best = nxb;
+      }
+    }
+    p.nxb = best;
+    p.L = (p.d.nx + best - 1) / best;
+    p.nxb = (p.d.nx + p.L - 1) / p.L;
+  } else {
+    p.TZ = 32;
+    p.TY = 8;
+    p.nzb = (p.d.nz + p.TZ - 1) / p.TZ;
+    p.nyb = (p.d.ny + p.TY - 1) / p.TY;
+    int per_chunk = p.nzb * p.nyb * p.d.nshots;
+    int resident = sms * 6;
+    int best = 1;
+    double best_eff = 0;
+    for (int nxb = 1; nxb <= std::max(1, p.d.nx / 16); nxb++) {
+      int64_t blocks = (int64_t)nxb * per_chunk;
+      double waves = (double)blocks / resident;
+      double eff = waves / std::ceil(waves);
+      int L = (p.d.nx + nxb - 1) / nxb;
+      eff *= (1.0 - 3.0 / L);
+      if (blocks < resident / 2) eff *= (double)blocks / (resident / 2);
+      if (eff > best_eff + 1e-9) {
+        best_eff = eff;
+        best = nxb;
+      }
+    }
+    p.nxb = best;
+    p.L = (p.d.nx + best - 1) / best;
+    p.nxb = (p.d.nx + p.L - 1) / p.L;
+  }
+}
+
+static int64_t psi_len(const Plan &p, int axis) {
+  const int64_t w = 2 * (int64_t)p.d.npml;
+  if (p.d.ndim == 2) return axis == 2 ? w * p.NZP : (int64_t)p.NXP * w;
+  if (axis == 2) return w * p.NYP * p.NZP;
+  if (axis == 1) return (int64_t)p.NXP * w * p.NZP;
+  return (int64_t)p.NXP * p.NYP * w;
+}
+
+static int nsaved(const Plan &p, int *ids) {
+  if (p.d.physics == GPI_ACOUSTIC) {
+    ids[0] = GPI_P;
+    return 1;
+  }
+  ids[0] = GPI_TAUXX;
+  ids[1] = GPI_TAUXZ;
+  ids[2] = GPI_TAUZZ;
+  return 3;
+}
+
+int create(const gpi_plan_desc *desc, gpi_plan **out) {
+  if (!desc || !out) return fail(nullptr, GPI_E_INVALID, "null argument");
+  *out = nullptr;
+  const gpi_plan_desc &d = *desc;
+  if (d.physics != GPI_ACOUSTIC && d.physics != GPI_ELASTIC) return fail(nullptr, GPI_E_INVALID, "physics");
+  if (d.ndim != 2 && d.ndim != 3) return fail(nullptr, GPI_E_INVALID, "ndim must be 2 or 3");
+  if (d.order != 4) return fail(nullptr, GPI_E_UNSUPPORTED, "the engine implements order 4 only");
+  if (d.nt < 1 || d.nshots < 1 || (d.npw != 1 && d.npw != 2)) return fail(nullptr, GPI_E_INVALID, "nt/nshots/npw");
+  if (d.npml < 1 || d.nbound < 1) return fail(nullptr, GPI_E_INVALID, "npml/nbound");
+  if (!(d.dt > 0) || !(d.dz > 0) || !(d.dx > 0) || (d.ndim == 3 && !(d.dy > 0)))
+    return fail(nullptr, GPI_E_INVALID, "dt and grid steps must be positive");
+  const int h = d.order - 1;
+  const int ny = d.ndim == 3 ? d.ny : 1;
+  // CPML strips of the min and max faces must not overlap on any derivative
+  // field (the shortest derivative axis is n - 2h).
+  const int nmin = std::min(d.nz, d.ndim == 3 ? std::min(d.ny, d.nx) : d.nx) - 2 * h;
+  if (nmin < 2 * d.npml + 1) return fail(nullptr, GPI_E_INVALID, "grid too small for two PML strips");
+  gpi_plan *pl = new gpi_plan();
+  Plan &p = pl->p;
+  p.d = d;
+  p.d.ny = ny;
+  p.d.rigid_faces |= d.pml_faces;  // fdtd.jl:215: rigid U pml
+  p.h = h;
+  cudaGetDevice(&p.device);
+  p.nder = deriv_specs(d.physics, d.ndim, &p.ds);
+  p.present[GPI_VX] = p.present[GPI_VZ] = 1;
+  if (d.ndim == 3) p.present[GPI_VY] = 1;
+  if (d.physics == GPI_ACOUSTIC)
+    p.present[GPI_P] = 1;
+  else {
+    p.present[GPI_TAUXX] = p.present[GPI_TAUZZ] = p.present[GPI_TAUXZ] = 1;
+    if (d.ndim == 3) p.present[GPI_TAUYY] = p.present[GPI_TAUXY] = p.present[GPI_TAUYZ] = 1;
+  }
+  choose_tiling(p);
+  p.NZP = (int)round_up((int64_t)p.nzb * p.TZ + 2 * ZOFF + 4, 32);
+  p.NXP = d.nx + h + 2 * XOFF + 4;
+  p.NYP = d.ndim == 3 ? (int)(p.nyb * p.TY + 2 * YOFF + 4) : 1;
+  p.fstride = (int64_t)p.NZP * p.NYP * p.NXP;
+
+  // ---- pool layout ----
+  std::vector<std::pair<float **, int64_t>> allocs;
+  int nf = 0;
+  for (int f = 0; f < NFIELD; f++) nf += p.present[f];
+  for (int b = 0; b < 2; b++)
+    for (int ipw = 0; ipw < d.npw; ipw++)
+      for (int f = 0; f < NFIELD; f++)
+        if (p.present[f]) allocs.push_back({&p.state[b][ipw][f], p.fstride * d.nshots});
+  for (int q = 0; q < p.nder; q++) {
+    const int ax = p.ds[q].axis;
+    const int fmin = ax == 0 ? GPI_ZMIN : ax == 1 ? GPI_YMIN : GPI_XMIN;
+    const int fmax = ax == 0 ? GPI_ZMAX : ax == 1 ? GPI_YMAX : GPI_XMAX;
+    if (!(d.pml_faces & (fmin | fmax))) continue;
+    p.psi_stride[q] = psi_len(p, ax);
+    for (int b = 0; b < 2; b++)
+      for (int ipw = 0; ipw < d.npw; ipw++) allocs.push_back({&p.psi[b][ipw][q], p.psi_stride[q] * d.nshots});
+  }
+  p.nmod = d.physics == GPI_ACOUSTIC ? 2 : 3;
+  p.ncoef = d.physics == GPI_ACOUSTIC ? d.ndim + 1 : (d.ndim == 2 ? 5 : 8);
+  for (int i = 0; i < p.nmod; i++) allocs.push_back({&p.mod[i], p.fstride});
+  for (int i = 0; i < p.ncoef; i++) allocs.push_back({&p.coef[i], p.fstride});
+  allocs.push_back({&p.pml, (int64_t)p.nder * 3 * 2 * d.npml});
+  if (d.npw == 2) {
+    for (int i = 0; i < p.nmod && i < 2; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
+    int ids[3];
+    int ns = nsaved(p, ids);
+    p.bstep = 0;
+    p.bsnap = 0;
+    for (int q = 0; q < ns; q++) {
+      int n[3];
+      field_shape(p, ids[q], n);
+      for (int ax = 0; ax < 3; ax++) {
+        if (ax == 1 && d.ndim == 2) continue;
+        int64_t s = 2 * (int64_t)d.nbound;
+        for (int o = 0; o < 3; o++)
+          if (o != ax) s *= n[o];
+        p.bstep += s;
+      }
+      p.bsnap += p.fstride;
+    }
+    p.bsnap += p.fstride * (d.ndim == 3 ? 3 : 2);
+    allocs.push_back({&p.bstore, (p.bstep * d.nt + p.bsnap) * d.nshots});
+  }
+  size_t total = 0;
+  for (auto &a : allocs) total += (size_t)round_up(a.second, 64) * sizeof(float);
+  cudaError_t e = cudaMalloc(&p.pool, total);
+  if (e != cudaSuccess) {
+    delete pl;
+    cudaGetLastError();
+    return fail(nullptr, GPI_E_NOMEM, "cudaMalloc of " + std::to_string(total) + " bytes failed");
+  }
+  p.pool_bytes = total;
+  char *c = (char *)p.pool;
+  for (auto &a : allocs) {
+    *a.first = (float *)c;
+    c += (size_t)round_up(a.second, 64) * sizeof(float);
+  }
+  e = cudaMemset(p.pool, 0, total);
+  if (e != cudaSuccess) {
+    cudaFree(p.pool);
+    delete pl;
+    return fail(nullptr, GPI_E_CUDA, cudaGetErrorString(e));
+  }
+  // identity PML (kI = 1) until gpi_set_pml is called
+  {
+    std::vector<float> pm((size_t)p.nder * 3 * 2 * d.npml, 0.f);
+    for (int q = 0; q < p.nder; q++)
+      for (int i = 0; i < 2 * d.npml; i++) {
+        pm[((size_t)q * 3 + 1) * 2 * d.npml + i] = 1.f;
+        pm[((size_t)q * 3 + 2) * 2 * d.npml + i] = 1.f;
+      }
+    cudaMemcpy(p.pml, pm.data(), pm.size() * sizeof(float), cudaMemcpyHostToDevice);
+  }
+  p.rec_n.assign(d.nshots, std::vector<int>(NFIELD, 0));
+  p.rec_cp.assign(d.nshots, std::vector<std::vector<int64_t>>(NFIELD));
+  p.rec_off.assign(d.nshots, std::vector<std::vector<int64_t>>(NFIELD));
+  p.rec_w.assign(d.nshots, std::vector<std::vector<float>>(NFIELD));
+  p.rec_base.assign(d.nshots, std::vector<int64_t>(NFIELD, -1));
+  p.src.assign(2, std::vector<std::vector<Plan::Src>>(d.nshots, std::vector<Plan::Src>(NFIELD)));
+  *out = pl;
+  return GPI_OK;
+}
+
+static void free_dev(void *&x) {
+  if (x) cudaFree(x);
+  x = nullptr;
+}
+
+static void free_sources(Plan &p) {
+  free_dev((void *&)p.d_cells);
+  free_dev((void *&)p.d_pair_j);
+  free_dev((void *&)p.d_pair_w);
+  free_dev((void *&)p.d_wav);
+  free_dev((void *&)p.d_wav_ns);
+  free_dev((void *&)p.d_amount);
+  free_dev((void *&)p.d_group_ptr);
+  for (auto b : p.wav_bufs) cudaFree(b);
+  p.wav_bufs.clear();
+  p.n_cells = 0;
+}
+static void free_receivers(Plan &p) {
+  free_dev((void *&)p.rec_pool);
+  free_dev((void *&)p.d_rtask);
+  free_dev((void *&)p.d_roff);
+  free_dev((void *&)p.d_rw);
+  p.n_rtask = 0;
+}
+
+void destroy(gpi_plan *pl) {
+  if (!pl) return;
+  Plan &p = pl->p;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaSetDevice(p.device);
+  if (p.stream) cudaStreamSynchronize(p.stream);
+  free_sources(p);
+  free_receivers(p);
+  free_dev(p.pool);
+  cudaSetDevice(dev);
+  delete pl;
+}
+
+// ---------------------------------------------------------------------------
+// medium and PML
+// ---------------------------------------------------------------------------
+static int to_storage(Plan &p, float *dst, const float *src, int n1, int n2, int n3, int on_device) {
+  // column-major (n1, n2, n3) -> padded storage
+  cudaMemcpy3DParms m = {};
+  m.srcPtr = make_cudaPitchedPtr((void *)src, (size_t)n1 * sizeof(float), n1, n2);
+  m.dstPtr = make_cudaPitchedPtr((void *)dst, (size_t)p.NZP * sizeof(float), p.NZP, p.NYP);
+  m.srcPos = make_cudaPos(0, 0, 0);
+  m.dstPos = make_cudaPos((size_t)ZOFF * sizeof(float), p.d.ndim == 3 ? YOFF : 0, XOFF);
+  m.extent = make_cudaExtent((size_t)n1 * sizeof(float), n2, n3);
+  m.kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  GPI_CUDA(&p, cudaMemcpy3DAsync(&m, p.stream));
+  return GPI_OK;
+}
+static int from_storage(Plan &p, float *dst, const float *src, int n1, int n2, int n3, int on_device) {
+  cudaMemcpy3DParms m = {};
+  m.srcPtr = make_cudaPitchedPtr((void *)src, (size_t)p.NZP * sizeof(float), p.NZP, p.NYP);
+  m.dstPtr = make_cudaPitchedPtr((void *)dst, (size_t)n1 * sizeof(float), n1, n2);
+  m.srcPos = make_cudaPos((size_t)ZOFF * sizeof(float), p.d.ndim == 3 ? YOFF : 0, XOFF);
+  m.dstPos = make_cudaPos(0, 0, 0);
+  m.extent = make_cudaExtent((size_t)n1 * sizeof(float), n2, n3);
+  m.kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  GPI_CUDA(&p, cudaMemcpy3DAsync(&m, p.stream));
+  return GPI_OK;
+}
+
+int set_medium(Plan &p, const float *const *mod, int on_device) {
+  if (!mod) return fail(&p, GPI_E_INVALID, "mod is null");
+  for (int i = 0; i < p.nmod; i++) {
+    if (!mod[i]) return fail(&p, GPI_E_INVALID, "mod array missing");
+    int rc = to_storage(p, p.mod[i], mod[i], p.d.nz, p.d.ny, p.d.nx, on_device);
+    if (rc) return rc;
+  }
+  int rc = compute_coefficients(&p);
+  if (rc) return rc;
+  if (!on_device) GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  p.src_dirty = true;  // injection scaling reads rho / dtK at run time, nothing to redo
+  return GPI_OK;
+}
+
+int set_pml(Plan &p, int q, const float *a, const float *b, const float *kI) {
+  if (q < 0 || q >= p.nder || !a || !b || !kI) return fail(&p, GPI_E_INVALID, "pml field index or null array");
+  const size_t n = 2 * (size_t)p.d.npml;
+  float *dst = p.pml + (size_t)q * 3 * n;
+  GPI_CUDA(&p, cudaMemcpyAsync(dst, a, n * sizeof(float), cudaMemcpyHostToDevice, p.stream));
+  GPI_CUDA(&p, cudaMemcpyAsync(dst + n, b, n * sizeof(float), cudaMemcpyHostToDevice, p.stream));
+  GPI_CUDA(&p, cudaMemcpyAsync(dst + 2 * n, kI, n * sizeof(float), cudaMemcpyHostToDevice, p.stream));
+  GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  return GPI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sources and receivers
+// ---------------------------------------------------------------------------
+static bool is_vel(int f) { return f == GPI_VX || f == GPI_VY || f == GPI_VZ; }
+static bool is_stress_src(int f) { return f == GPI_P || f == GPI_TAUXX || f == GPI_TAUYY || f == GPI_TAUZZ; }
+static int kind_of(int f) { return f == GPI_VX ? 0 : f == GPI_VY ? 1 : f == GPI_VZ ? 2 : 3; }
+
+static int check_csc(Plan &p, int field, int n, const int64_t *cp, const int64_t *rv) {
+  if (field < 0 || field >= NFIELD || !p.present[field]) return fail(&p, GPI_E_INVALID, "field not part of this physics");
+  if (n < 0 || (n > 0 && (!cp || !rv))) return fail(&p, GPI_E_INVALID, "csc arrays");
+  const int64_t len = field_len(p, field);
+  if (n > 0 && cp[0] != 0) return fail(&p, GPI_E_INVALID, "colptr[0] must be 0");
+  for (int j = 0; j < n; j++) {
+    if (cp[j + 1] < cp[j]) return fail(&p, GPI_E_INVALID, "colptr not monotone");
+    for (int64_t k = cp[j]; k < cp[j + 1]; k++)
+      if (rv[k] < 0 || rv[k] >= len) return fail(&p, GPI_E_INVALID, "row index outside the field");
+  }
+  return GPI_OK;
+}
+
+int set_sources(Plan &p, int ipw, int shot, int field, int ns, const int64_t *cp, const int64_t *rv, const float *nz,
+                const float *wav) {
+  if (ipw < 1 || ipw > p.d.npw) return fail(&p, GPI_E_INVALID, "ipw");
+  if (shot < 0 || shot >= p.d.nshots) return fail(&p, GPI_E_INVALID, "shot index");
+  if (field < 0 || field >= NFIELD || !p.present[field]) return fail(&p, GPI_E_INVALID, "source field not in this physics");
+  if (ns < 0 || (ns > 0 && !wav)) return fail(&p, GPI_E_INVALID, "wavelets");
+  Plan::Src &s = p.src[ipw - 1][shot][field];
+  s = Plan::Src();
+  if (ipw == 1) {
+    if (!is_vel(field) && !is_stress_src(field)) return fail(&p, GPI_E_INVALID, "sources act on p, tauii or velocities");
+    int rc = check_csc(p, field, ns, cp, rv);
+    if (rc) return rc;
+    if (ns > 0 && !nz) return fail(&p, GPI_E_INVALID, "nzval");
+    s.cp.assign(cp, cp + ns + 1);
+    s.rv.assign(rv, rv + (ns ? cp[ns] : 0));
+    s.nz.assign(nz, nz + (ns ? cp[ns] : 0));
+  } else {
+    // adjoint wavefield: injected through rinterpolatew of `field`
+    // (add_velocity_source!, src/fdtd/source.jl:141-156, velocities only)
+    if (!is_vel(field)) return fail(&p, GPI_E_UNSUPPORTED, "adjoint sources act on velocity fields only");
+    if (p.rec_n[shot][field] != ns) return fail(&p, GPI_E_STATE, "adjoint sources need the receivers of that field first");
+  }
+  s.ns = ns;
+  s.wav.assign(wav, wav + (size_t)ns * p.d.nt);
+  p.src_dirty = true;
+  return GPI_OK;
+}
+
+int clear_sources(Plan &p, int ipw, int shot) {
+  if (ipw < 1 || ipw > p.d.npw) return fail(&p, GPI_E_INVALID, "ipw");
+  for (int s = 0; s < p.d.nshots; s++)
+    if (shot < 0 || shot == s)
+      for (int f = 0; f < NFIELD; f++) p.src[ipw - 1][s][f] = Plan::Src();
+  p.src_dirty = true;
+  return GPI_OK;
+}
+
+// 0-based linear index of a field -> reference (r, y, c), 1-based
+static void unravel(const Plan &p, int field, int64_t lin, int *r, int *y, int *c) {
+  int n[3];
+  field_shape(p, field, n);
+  *r = (int)(lin % n[0]) + 1;
+  *y = (int)((lin / n[0]) % n[1]) + 1;
+  *c = (int)(lin / ((int64_t)n[0] * n[1])) + 1;
+}
+
+int set_receivers(Plan &p, int shot, int field, int nr, const int64_t *cp, const int64_t *rv, const float *nz) {
+  if (shot < 0 || shot >= p.d.nshots) return fail(&p, GPI_E_INVALID, "shot index");
+  int rc = check_csc(p, field, nr, cp, rv);
+  if (rc) return rc;
+  if (nr > 0 && !nz) return fail(&p, GPI_E_INVALID, "nzval");
+  p.rec_n[shot][field] = nr;
+  p.rec_cp[shot][field].assign(cp, cp + nr + 1);
+  std::vector<int64_t> off;
+  const int64_t nnz = nr ? cp[nr] : 0;
+  off.resize(nnz);
+  for (int64_t k = 0; k < nnz; k++) {
+    int r, y, c;
+    unravel(p, field, rv[k], &r, &y, &c);
+    off[k] = soff(p, r, y, c);
+  }
+  p.rec_off[shot][field] = off;
+  p.rec_w[shot][field].assign(nz, nz + nnz);
+  p.rec_dirty = true;
+  p.src_dirty = true;  // adjoint injection follows the receivers
+  return GPI_OK;
+}
+
+static int compile_receivers(Plan &p) {
+  free_receivers(p);
+  std::vector<RecTask> tasks;
+  std::vector<int64_t> offs;
+  std::vector<float> ws;
+  size_t pool = 0;
+  for (int s = 0; s < p.d.nshots; s++)
+    for (int f = 0; f < NFIELD; f++) {
+      const int nr = p.rec_n[s][f];
+      p.rec_base[s][f] = -1;
+      if (nr <= 0) continue;
+      p.rec_base[s][f] = (int64_t)pool;
+      const auto &cp = p.rec_cp[s][f];
+      for (int j = 0; j < nr; j++) {
+        RecTask t;
+        t.shot = s;
+        t.field = f;
+        t.e0 = (int32_t)(offs.size() + cp[j]);
+        t.e1 = (int32_t)(offs.size() + cp[j + 1]);
+        t.out = (int64_t)pool + j;
+        t.stride = nr;
+        t.pad = 0;
+        tasks.push_back(t);
+      }
+      offs.insert(offs.end(), p.rec_off[s][f].begin(), p.rec_off[s][f].end());
+      ws.insert(ws.end(), p.rec_w[s][f].begin(), p.rec_w[s][f].end());
+      pool += (size_t)nr * p.d.nt;
+    }
+  p.rec_pool_floats = pool;
+  p.n_rtask = (int)tasks.size();
+  if (pool) GPI_CUDA(&p, cudaMalloc(&p.rec_pool, pool * sizeof(float)));
+  if (!tasks.empty()) {
+    GPI_CUDA(&p, cudaMalloc(&p.d_rtask, tasks.size() * sizeof(RecTask)));
+    GPI_CUDA(&p, cudaMemcpy(p.d_rtask, tasks.data(), tasks.size() * sizeof(RecTask), cudaMemcpyHostToDevice));
+  }
+  if (!offs.empty()) {
+    GPI_CUDA(&p, cudaMalloc(&p.d_roff, offs.size() * sizeof(int64_t)));
+    GPI_CUDA(&p, cudaMalloc(&p.d_rw, ws.size() * sizeof(float)));
+    GPI_CUDA(&p, cudaMemcpy(p.d_roff, offs.data(), offs.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, cudaMemcpy(p.d_rw, ws.data(), ws.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  p.rec_dirty = false;
+  return GPI_OK;
+}
+
+// Turn the spray matrices into injection cells grouped by (ipw, shot, kind)
+// and sorted by (column, y, row): the step kernels sweep columns in order
+// and pick the cells of the current column.  Velocity cells outside the
+// @inn domain are dropped, as muladd_with_density_* ignores them
+// (src/fdtd/source.jl:166-177).
+static int compile_sources(Plan &p) {
+  free_sources(p);
+  const int h = p.h;
+  struct Tmp {
+    InjCell c;
+    std::vector<std::pair<int, float>> pairs;
+  };
+  std::vector<std::vector<Tmp>> groups((size_t)2 * p.d.nshots * NKIND);
+  std::vector<float *> wavptr;
+  std::vector<int32_t> wavns;
+  for (int ipw = 0; ipw < p.d.npw; ipw++)
+    for (int s = 0; s < p.d.nshots; s++)
+      for (int f = 0; f < NFIELD; f++) {
+        const Plan::Src &src = p.src[ipw][s][f];
+        if (src.ns <= 0) continue;
+        const int kind = kind_of(f);
+        // spray matrix
+        const std::vector<int64_t> *cp, *rows = nullptr;
+        const std::vector<float> *w;
+        std::vector<int64_t> lin;
+        if (ipw == 0) {
+          cp = &src.cp;
+          rows = &src.rv;
+          w = &src.nz;
+        } else {
+          if (p.rec_n[s][f] != src.ns) return fail(&p, GPI_E_STATE, "adjoint sources and receivers disagree");
+          cp = &p.rec_cp[s][f];
+          w = &p.rec_w[s][f];
+          // receivers are stored as storage offsets; recover (r, y, c)
+          lin.clear();
+        }
+        float *dw = nullptr;
+        GPI_CUDA(&p, cudaMalloc(&dw, src.wav.size() * sizeof(float)));
+        GPI_CUDA(&p, cudaMemcpy(dw, src.wav.data(), src.wav.size() * sizeof(float), cudaMemcpyHostToDevice));
+        p.wav_bufs.push_back(dw);
+        const int widx = (int)wavptr.size();
+        wavptr.push_back(dw);
+        wavns.push_back(src.ns);
+        std::map<int64_t, size_t> where;  // row -> index in this projection's cells
+        std::vector<Tmp> cells;
+        for (int j = 0; j < src.ns; j++)
+          for (int64_t k = (*cp)[j]; k < (*cp)[j + 1]; k++) {
+            int r, y, c;
+            int64_t key;
+            if (ipw == 0) {
+              unravel(p, f, (*rows)[k], &r, &y, &c);
+              key = (*rows)[k];
+            } else {
+              // invert the storage offset of the receiver entry
+              int64_t o = p.rec_off[s][f][k];
+              r = (int)(o % p.NZP) - ZOFF + 1;
+              int64_t rest = o / p.NZP;
+              y = p.d.ndim == 3 ? (int)(rest % p.NYP) - YOFF + 1 : 1;
+              c = (int)(rest / p.NYP) - XOFF + 1;
+              key = o;
+            }
+            auto it = where.find(key);
+            if (it == where.end()) {
+              Tmp t;
+              t.c.row = r;
+              t.c.ydx = y;
+              t.c.col = c;
+              t.c.wav = widx;
+              t.c.kind = kind;
+              t.c.pad = 0;
+              t.c.off = soff(p, r, y, c);
+              t.c.roff0 = t.c.roff1 = 0;
+              where[key] = cells.size();
+              cells.push_back(t);
+              it = where.find(key);
+            }
+            cells[it->second].pairs.push_back({j, (*w)[k]});
+          }
+        int n[3];
+        field_shape(p, f, n);
+        for (auto &t : cells) {
+          if (kind < 3) {
+            const int r = t.c.row, y = t.c.ydx, c = t.c.col;
+            bool in = r - h >= 1 && r - h <= n[0] - 2 * h && c - h >= 1 && c - h <= n[2] - 2 * h;
+            if (p.d.ndim == 3) in = in && y - h >= 1 && y - h <= n[1] - 2 * h;
+            if (!in) continue;
+            // @av_{x,y,z}i(rho) at the @inn cell (iz, iy, ix) = cell - h
+            int z = r - h, yy = p.d.ndim == 3 ? y - h : 1, x = c - h;
+            int zz = z + (kind != 2 ? h : 0), y2 = p.d.ndim == 3 ? yy + (kind != 1 ? h : 0) : 1, xx = x + (kind != 0 ? h : 0);
+            t.c.roff0 = soff(p, zz, y2, xx);
+            t.c.roff1 = soff(p, zz + (kind == 2), y2 + (kind == 1), xx + (kind == 0));
+          }
+          groups[((size_t)ipw * p.d.nshots + s) * NKIND + kind].push_back(t);
+        }
+      }
+  std::vector<InjCell> cells;
+  std::vector<int32_t> pj;
+  std::vector<float> pw;
+  p.group_ptr.assign(groups.size() + 1, 0);
+  for (size_t g = 0; g < groups.size(); g++) {
+    auto &G = groups[g];
+    std::stable_sort(G.begin(), G.end(), [](const Tmp &a, const Tmp &b) {
+      if (a.c.col != b.c.col) return a.c.col < b.c.col;
+      if (a.c.ydx != b.c.ydx) return a.c.ydx < b.c.ydx;
+      return a.c.row < b.c.row;
+    });
+    p.group_ptr[g] = (int32_t)cells.size();
+    for (auto &t : G) {
+      t.c.e0 = (int32_t)pj.size();
+      for (auto &pr : t.pairs) {
+        pj.push_back(pr.first);
+        pw.push_back(pr.second);
+      }
+      t.c.e1 = (int32_t)pj.size();
+      cells.push_back(t.c);
+    }
+  }
+  p.group_ptr[groups.size()] = (int32_t)cells.size();
+  p.n_cells = (int)cells.size();
+  GPI_CUDA(&p, cudaMalloc(&p.d_group_ptr, p.group_ptr.size() * sizeof(int32_t)));
+  GPI_CUDA(&p, cudaMemcpy(p.d_group_ptr, p.group_ptr.data(), p.group_ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  if (p.n_cells) {
+    GPI_CUDA(&p, cudaMalloc(&p.d_cells, cells.size() * sizeof(InjCell)));
+    GPI_CUDA(&p, cudaMemcpy(p.d_cells, cells.data(), cells.size() * sizeof(InjCell), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, cudaMalloc(&p.d_pair_j, pj.size() * sizeof(int32_t)));
+    GPI_CUDA(&p, cudaMalloc(&p.d_pair_w, pw.size() * sizeof(float)));
+    GPI_CUDA(&p, cudaMemcpy(p.d_pair_j, pj.data(), pj.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, cudaMemcpy(p.d_pair_w, pw.data(), pw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, cudaMalloc(&p.d_amount, cells.size() * sizeof(float)));
+  }
+  if (!wavptr.empty()) {
+    GPI_CUDA(&p, cudaMalloc(&p.d_wav, wavptr.size() * sizeof(float *)));
+    GPI_CUDA(&p, cudaMalloc(&p.d_wav_ns, wavns.size() * sizeof(int32_t)));
+    GPI_CUDA(&p, cudaMemcpy(p.d_wav, wavptr.data(), wavptr.size() * sizeof(float *), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, cudaMemcpy(p.d_wav_ns, wavns.data(), wavns.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  }
+  p.src_dirty = false;
+  return GPI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// run
+// ---------------------------------------------------------------------------
+static int step(Plan &p, int ipw_mask, int it, int mode, int vonly) {
+  if (p.d.physics == GPI_ACOUSTIC)
+    return p.d.ndim == 2 ? step_acoustic2d(&p, ipw_mask, it, mode, vonly) : step_acoustic3d(&p, ipw_mask, it, mode, vonly);
+  return p.d.ndim == 2 ? step_elastic2d(&p, ipw_mask, it, mode, vonly) : step_elastic3d(&p, ipw_mask, it, mode, vonly);
+}
+
+static int zero_state(Plan &p) {
+  for (int b = 0; b < 2; b++)
+    for (int ipw = 0; ipw < p.d.npw; ipw++) {
+      for (int f = 0; f < NFIELD; f++)
+        if (p.state[b][ipw][f])
+          GPI_CUDA(&p, cudaMemsetAsync(p.state[b][ipw][f], 0, p.fstride * p.d.nshots * sizeof(float), p.stream));
+      for (int q = 0; q < p.nder; q++)
+        if (p.psi[b][ipw][q])
+          GPI_CUDA(&p, cudaMemsetAsync(p.psi[b][ipw][q], 0, p.psi_stride[q] * p.d.nshots * sizeof(float), p.stream));
+    }
+  p.cur[0] = p.cur[1] = 0;
+  return GPI_OK;
+}
+
+int run(Plan &p, int mode) {
+  if (mode != GPI_FORWARD && mode != GPI_FORWARD_SAVE && mode != GPI_ADJOINT) return fail(&p, GPI_E_INVALID, "mode");
+  if (mode != GPI_FORWARD && p.d.npw != 2) return fail(&p, GPI_E_INVALID, "forward_save/adjoint need npw = 2");
+  if (mode == GPI_ADJOINT && !p.have_save) return fail(&p, GPI_E_STATE, "adjoint run needs a forward_save run first");
+  if (mode == GPI_ADJOINT && !(p.d.physics == GPI_ACOUSTIC && p.d.ndim == 2))
+    return fail(&p, GPI_E_UNSUPPORTED, "the reference computes gradients for 2-D acoustic media only");
+  if (mode == GPI_FORWARD_SAVE && p.d.ndim == 3 && p.d.physics == GPI_ELASTIC)
+    return fail(&p, GPI_E_UNSUPPORTED, "the reference defines no boundary store for 3-D elastic media");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != p.device) GPI_CUDA(&p, cudaSetDevice(p.device));
+  int rc = GPI_OK;
+  if (p.rec_dirty) rc = compile_receivers(p);
+  if (!rc && p.src_dirty) rc = compile_sources(p);
+  if (!rc) rc = zero_state(p);
+  p.launches = 0;
+  if (!rc && p.rec_pool) rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
+  if (!rc && mode == GPI_ADJOINT) {
+    for (int i = 0; i < 2; i++)
+      if (p.grad[i]) rc = cudaMemsetAsync(p.grad[i], 0, p.fstride * p.d.nshots * sizeof(float), p.stream) ? GPI_E_CUDA : rc;
+    if (!rc) rc = snap_io(&p, 1, 1);
+    if (!rc) rc = snap_io(&p, 0, 1);
+  }
+  const int mask = mode == GPI_ADJOINT ? 3 : 1;
+  for (int it = 1; !rc && it <= p.d.nt; it++) {
+    rc = aux_step(&p, it, mode);
+    if (!rc && mode == GPI_ADJOINT) rc = boundary_io(&p, p.d.nt - it + 1, 1);
+    if (!rc) rc = step(p, mask, it, mode, 0);
+    if (!rc && mode == GPI_FORWARD_SAVE) rc = boundary_io(&p, it, 0);
+  }
+  if (!rc) rc = aux_step(&p, p.d.nt + 1, mode);  // velocity records of the last step
+  if (!rc && mode == GPI_FORWARD_SAVE) rc = snap_io(&p, 1, 0);
+  if (!rc) rc = step(p, 1, p.d.nt + 1, mode, 1);  // the extra velocity half step (propagate.jl:254-255)
+  if (!rc && mode == GPI_FORWARD_SAVE) rc = snap_io(&p, 0, 0);
+  if (!rc) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));
+  }
+  if (!rc && mode == GPI_FORWARD_SAVE) p.have_save = 1;
+  if (dev != p.device) cudaSetDevice(dev);
+  return rc;
+}
+
+int get_records(Plan &p, int shot, int field, float *out, int on_device) {
+  if (shot < 0 || shot >= p.d.nshots || field < 0 || field >= NFIELD) return fail(&p, GPI_E_INVALID, "shot/field");
+  const int nr = p.rec_n[shot][field];
+  if (nr <= 0 || p.rec_base[shot][field] < 0) return fail(&p, GPI_E_STATE, "no receivers for this field (or no run yet)");
+  const int nt = p.d.nt;
+  const float *src = p.rec_pool + p.rec_base[shot][field];
+  // pool layout [it][ir] -> Recs layout (it fastest): a pitched 2-D transpose
+  // done as nr strided copies keeps this call allocation-free
+  for (int ir = 0; ir < nr; ir++) {
+    GPI_CUDA(&p, cudaMemcpy2DAsync(out + (size_t)ir * nt, sizeof(float), src + ir, (size_t)nr * sizeof(float),
+                                   sizeof(float), nt, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                   p.stream));
+  }
+  if (!on_device) GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  return GPI_OK;
+}
+
+int get_field(Plan &p, int ipw, int shot, int field, float *out, int on_device) {
+  if (ipw < 1 || ipw > p.d.npw || shot < 0 || shot >= p.d.nshots || field < 0 || field >= NFIELD || !p.present[field])
+    return fail(&p, GPI_E_INVALID, "ipw/shot/field");
+  int n[3];
+  field_shape(p, field, n);
+  const float *src = p.state[p.cur[ipw - 1]][ipw - 1][field] + p.fstride * shot;
+  int rc = from_storage(p, out, src, n[0], n[1], n[2], on_device);
+  if (rc) return rc;
+  if (!on_device) GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  return GPI_OK;
+}
+
+int reduce_gradient(Plan *p, int param, float *dst);  // k_common.cu
+
+int get_gradient(Plan &p, int param, float *out, int on_device) {
+  if (p.d.npw != 2 || param < 0 || param > 1 || !p.grad[param]) return fail(&p, GPI_E_INVALID, "no gradient for this parameter");
+  // sum over shots into shot 0's slot of a scratch area: reuse bstore's
+  // snapshot region is not allowed (it is state), so reduce in place into a
+  // temporary owned by the plan
+  float *tmp = nullptr;
+  GPI_CUDA(&p, cudaMallocAsync(&tmp, p.fstride * sizeof(float), p.stream));
+  int rc = reduce_gradient(&p, param, tmp);
+  if (!rc) rc = from_storage(p, out, tmp, p.d.nz, p.d.ny, p.d.nx, on_device);
+  cudaFreeAsync(tmp, p.stream);
+  if (rc) return rc;
+  GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  return GPI_OK;
+}
+
+}  // namespace gpi
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace gpi;
+
+extern "C" {
+
+int gpi_plan_create(const gpi_plan_desc *desc, gpi_plan **out) { return gpi::create(desc, out); }
+void gpi_plan_destroy(gpi_plan *plan) { gpi::destroy(plan); }
+const char *gpi_last_error(const gpi_plan *plan) { return plan ? plan->p.err.c_str() : g_create_err.c_str(); }
+int gpi_set_stream(gpi_plan *plan, void *stream) {
+  if (!plan) return GPI_E_INVALID;
+  plan->p.stream = (cudaStream_t)stream;
+  return GPI_OK;
+}
+int gpi_plan_bytes(const gpi_plan *plan, size_t *bytes) {
+  if (!plan || !bytes) return GPI_E_INVALID;
+  *bytes = plan->p.pool_bytes;
+  return GPI_OK;
+}
+int gpi_set_medium(gpi_plan *plan, const float *const *mod, int on_device) {
+  return plan ? gpi::set_medium(plan->p, mod, on_device) : GPI_E_INVALID;
+}
+int gpi_set_pml(gpi_plan *plan, int q, const float *a, const float *b, const float *kI) {
+  return plan ? gpi::set_pml(plan->p, q, a, b, kI) : GPI_E_INVALID;
+}
+int gpi_set_sources(gpi_plan *plan, int ipw, int shot, int field, int ns, const int64_t *colptr, const int64_t *rowval,
+                    const float *nzval, const float *wavelets) {
+  return plan ? gpi::set_sources(plan->p, ipw, shot, field, ns, colptr, rowval, nzval, wavelets) : GPI_E_INVALID;
+}
+int gpi_clear_sources(gpi_plan *plan, int ipw, int shot) { return plan ? gpi::clear_sources(plan->p, ipw, shot) : GPI_E_INVALID; }
+int gpi_set_receivers(gpi_plan *plan, int shot, int field, int nr, const int64_t *colptr, const int64_t *rowval,
+                      const float *nzval) {
+  return plan ? gpi::set_receivers(plan->p, shot, field, nr, colptr, rowval, nzval) : GPI_E_INVALID;
+}
+int gpi_run(gpi_plan *plan, int mode) { return plan ? gpi::run(plan->p, mode) : GPI_E_INVALID; }
+int gpi_get_records(gpi_plan *plan, int shot, int field, float *out, int on_device) {
+  return plan ? gpi::get_records(plan->p, shot, field, out, on_device) : GPI_E_INVALID;
+}
+int gpi_get_gradient(gpi_plan *plan, int param, float *out, int on_device) {
+  return plan ? gpi::get_gradient(plan->p, param, out, on_device) : GPI_E_INVALID;
+}
+int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int on_device) {
+  return plan ? gpi::get_field(plan->p, ipw, shot, field, out, on_device) : GPI_E_INVALID;
+}
+int gpi_last_launches(const gpi_plan *plan, int64_t *launches) {
+  if (!plan || !launches) return GPI_E_INVALID;
+  *launches = plan->p.launches;
+  return GPI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,367 @@
+// k_common.cu -- small kernels shared by every physics:
+//   * update coefficients from the medium (update_dmod!, src/fdtd/medium.jl:143-221)
+//   * per-step auxiliary work: receiver gathers (record!, src/fdtd/receiver.jl:3-15)
+//     and source amounts (mul!(pv, ssprayw, w) + muladd_*, src/fdtd/source.jl:61-177)
+//   * boundary store for time reversal (src/fdtd/boundary.jl:1-306)
+//   * shot-sum of gradients (sum_grads!, src/fdtd/gradient.jl:2-14)
+//   * record transposition to the Recs layout (src/fdtd/receiver.jl:17-46)
+// All arithmetic keeps the reference's operation order; the library is built
+// without FMA contraction so that every product and sum rounds as written.
+#include "gpi_internal.cuh"
+
+namespace gpi {
+
+struct Geo {
+  int nz, ny, nx, NZP, NYP, ndim, h;
+  __device__ __forceinline__ int64_t off(int r, int y, int c) const {
+    return ((int64_t)(c - 1 + XOFF) * NYP + (ndim == 3 ? (y - 1 + YOFF) : 0)) * NZP + (r - 1 + ZOFF);
+  }
+};
+static Geo geo(const Plan &p) { return Geo{p.d.nz, p.d.ny, p.d.nx, p.NZP, p.NYP, p.d.ndim, p.h}; }
+
+// ---------------------------------------------------------------------------
+// coefficients: each is stored at the cell it multiplies
+// ---------------------------------------------------------------------------
+struct CoefArgs {
+  Geo g;
+  float dt;
+  int physics;
+  const float *mod[3];
+  float *coef[8];
+};
+
+__device__ __forceinline__ float invav2(float a, float b, float dt) { return dt / ((a + b) * 0.5f); }
+
+__global__ void k_coef(CoefArgs a) {
+  const Geo &g = a.g;
+  const int h = g.h;
+  const int64_t n1 = g.nz + h, n2 = g.ndim == 3 ? g.ny + h : 1, n3 = g.nx + h;
+  const int64_t total = n1 * n2 * n3;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(i % n1) + 1;
+    const int y = (int)((i / n1) % n2) + 1;
+    const int c = (int)(i / (n1 * n2)) + 1;
+    const int64_t o = g.off(r, y, c);
+    const bool three = g.ndim == 3;
+    const float *rho = a.mod[a.physics == GPI_ACOUSTIC ? 1 : 2];
+    const bool yin = !three || (y >= h + 1 && y <= g.ny - h);
+    // dtinvav{x}irho at the vx cell (r, y, c): rho[r, y, c-h], rho[r, y, c-h+1]
+    if (r >= h + 1 && r <= g.nz - h && yin && c >= h + 1 && c <= g.nx)
+      a.coef[0][o] = invav2(rho[g.off(r, y, c - h)], rho[g.off(r, y, c - h + 1)], a.dt);
+    // dtinvav{z}irho at the vz cell (r, y, c): rho[r-h, y, c], rho[r-h+1, y, c]
+    const int iz = three ? 2 : 1;
+    if (r >= h + 1 && r <= g.nz && yin && c >= h + 1 && c <= g.nx - h)
+      a.coef[iz][o] = invav2(rho[g.off(r - h, y, c)], rho[g.off(r - h + 1, y, c)], a.dt);
+    // dtinvav{y}irho at the vy cell (r, y, c): rho[r, y-h, c], rho[r, y-h+1, c]
+    if (three && r >= h + 1 && r <= g.nz - h && y >= h + 1 && y <= g.ny && c >= h + 1 && c <= g.nx - h)
+      a.coef[1][o] = invav2(rho[g.off(r, y - h, c)], rho[g.off(r, y - h + 1, c)], a.dt);
+    const bool full = r <= g.nz && y <= (three ? g.ny : 1) && c <= g.nx;
+    if (a.physics == GPI_ACOUSTIC) {
+      if (full) {
+        const float t = 1.0f / a.mod[0][o];  // broadcast!(inv, dtK, invK)
+        a.coef[three ? 3 : 2][o] = t * a.dt; // rmul!(dtK, dt)
+      }
+      continue;
+    }
+    const float *im = a.mod[1];
+    if (full) {
+      const float il = a.mod[0][o];
+      const float lam = 1.0f / il;
+      a.coef[three ? 7 : 4][o] = lam * a.dt;
+      // inv(invλ) + 2.0 * inv(invμ) runs in Float64 (Float64 literal)
+      const double m64 = (double)lam + 2.0 * (double)(1.0f / im[o]);
+      a.coef[three ? 6 : 3][o] = (float)m64 * a.dt;
+    }
+    if (!three) {
+      // dtavmu at the tauxz cell: dt / @av(invmu)
+      if (r <= g.nz - h && c <= g.nx - h)
+        a.coef[2][o] = a.dt / ((im[g.off(r, 1, c)] + im[g.off(r + 1, 1, c)] + im[g.off(r, 1, c + 1)] +
+                                im[g.off(r + 1, 1, c + 1)]) * 0.25f);
+    } else {
+      // dtavxzimu at the tauxz cell (nz-h, ny-2h, nx-h): @av_xzi
+      if (r <= g.nz - h && y <= g.ny - 2 * h && c <= g.nx - h)
+        a.coef[3][o] = a.dt / ((im[g.off(r, y + h, c)] + im[g.off(r + 1, y + h, c)] + im[g.off(r, y + h, c + 1)] +
+                                im[g.off(r + 1, y + h, c + 1)]) * 0.25f);
+      // dtavxyimu at the tauxy cell (nz-2h, ny-h, nx-h): @av_xyi
+      if (r <= g.nz - 2 * h && y <= g.ny - h && c <= g.nx - h)
+        a.coef[4][o] = a.dt / ((im[g.off(r + h, y, c)] + im[g.off(r + h, y + 1, c)] + im[g.off(r + h, y, c + 1)] +
+                                im[g.off(r + h, y + 1, c + 1)]) * 0.25f);
+      // dtavyzimu at the tauyz cell (nz-h, ny-h, nx-2h): @av_yzi
+      if (r <= g.nz - h && y <= g.ny - h && c <= g.nx - 2 * h)
+        a.coef[5][o] = a.dt / ((im[g.off(r, y, c + h)] + im[g.off(r + 1, y, c + h)] + im[g.off(r, y + 1, c + h)] +
+                                im[g.off(r + 1, y + 1, c + h)]) * 0.25f);
+    }
+  }
+}
+
+int compute_coefficients(Plan *p) {
+  CoefArgs a;
+  a.g = geo(*p);
+  a.dt = (float)p->d.dt;
+  a.physics = p->d.physics;
+  for (int i = 0; i < 3; i++) a.mod[i] = p->mod[i];
+  for (int i = 0; i < 8; i++) a.coef[i] = p->coef[i];
+  for (int i = 0; i < p->ncoef; i++) GPI_CUDA(p, cudaMemsetAsync(p->coef[i], 0, p->fstride * sizeof(float), p->stream));
+  k_coef<<<152 * 8, 256, 0, p->stream>>>(a);
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// per-step auxiliary kernel
+// ---------------------------------------------------------------------------
+struct AuxArgs {
+  const RecTask *tasks;
+  int ntask;
+  const int64_t *roff;
+  const float *rw;
+  float *rec;
+  int it, nt;
+  const float *field[NFIELD];  // wavefield 1, current buffer, shot 0
+  int64_t fs;
+  const InjCell *cells;
+  int ncells;
+  const int32_t *pj;
+  const float *pw;
+  float *const *wav;
+  float *amount;
+  const float *rho;
+  const float *kcoef;  // dtK or dtM
+  float dt;
+};
+
+__global__ void k_aux(AuxArgs a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.ntask) {
+    // record!: p is sampled before step it, velocities after step it-1
+    const RecTask t = a.tasks[i];
+    const bool isv = t.field == GPI_VX || t.field == GPI_VY || t.field == GPI_VZ;
+    const int tidx = isv ? a.it - 2 : a.it - 1;
+    if (tidx < 0 || tidx >= a.nt) return;
+    if (!isv && a.it > a.nt) return;
+    const float *f = a.field[t.field] + t.shot * a.fs;
+    float s = 0.f;
+    for (int e = t.e0; e < t.e1; e++) s = s + a.rw[e] * f[a.roff[e]];
+    a.rec[t.out + (int64_t)tidx * t.stride] = s;
+    return;
+  }
+  i -= a.ntask;
+  if (i >= a.ncells || a.it > a.nt) return;
+  const InjCell c = a.cells[i];
+  const float *w = a.wav[c.wav] + (a.it - 1);
+  float pv = 0.f;
+  for (int e = c.e0; e < c.e1; e++) pv = pv + a.pw[e] * w[(int64_t)a.pj[e] * a.nt];
+  float amt;
+  if (c.kind < 3)
+    amt = pv / ((a.rho[c.roff0] + a.rho[c.roff1]) * 0.5f) * a.dt;  // muladd_with_density_v*!
+  else
+    amt = pv * a.kcoef[c.off];  // muladd_tauii!
+  a.amount[i] = amt;
+}
+
+int aux_step(Plan *p, int it, int mode) {
+  (void)mode;
+  const int n = p->n_rtask + (it <= p->d.nt ? p->n_cells : 0);
+  if (n == 0) return GPI_OK;
+  AuxArgs a;
+  a.tasks = p->d_rtask;
+  a.ntask = p->n_rtask;
+  a.roff = p->d_roff;
+  a.rw = p->d_rw;
+  a.rec = p->rec_pool;
+  a.it = it;
+  a.nt = p->d.nt;
+  for (int f = 0; f < NFIELD; f++) a.field[f] = p->state[p->cur[0]][0][f];
+  a.fs = p->fstride;
+  a.cells = p->d_cells;
+  a.ncells = p->n_cells;
+  a.pj = p->d_pair_j;
+  a.pw = p->d_pair_w;
+  a.wav = p->d_wav;
+  a.amount = p->d_amount;
+  a.rho = p->mod[p->d.physics == GPI_ACOUSTIC ? 1 : 2];
+  a.kcoef = p->d.physics == GPI_ACOUSTIC ? p->coef[p->ncoef - 1] : p->coef[p->ncoef - 2];
+  a.dt = (float)p->d.dt;
+  k_aux<<<(n + 127) / 128, 128, 0, p->stream>>>(a);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// boundary store (time reversal).  Per step and shot: for each saved stress
+// field, the x strips (nz_f x 2nb), [the y strips,] the z strips (2nb x nx_f)
+// of boundary_save! (boundary.jl:217-264); then the final snapshots.
+// ---------------------------------------------------------------------------
+struct StripArgs {
+  Geo g;
+  float *field;  // shot 0
+  int64_t fs;
+  float *store;  // shot 0, this step, this (field, axis) block
+  int64_t sstride;  // floats per shot in the store
+  int n1, n2, n3;   // field shape
+  int axis, nb, np;
+  int dir;          // 0 save (negated), 1 force
+  int nshots;
+};
+
+__global__ void k_strip(StripArgs a) {
+  const int b1 = a.axis == 0 ? 2 * a.nb : a.n1;
+  const int b2 = a.axis == 1 ? 2 * a.nb : a.n2;
+  const int b3 = a.axis == 2 ? 2 * a.nb : a.n3;
+  const int64_t per = (int64_t)b1 * b2 * b3;
+  const int64_t total = per * a.nshots;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int shot = (int)(i / per);
+    const int64_t k = i % per;
+    int i1 = (int)(k % b1), i2 = (int)((k / b1) % b2), i3 = (int)(k / ((int64_t)b1 * b2));
+    int idx[3] = {i1, i2, i3};
+    // strip entry j in [0, 2nb): j < nb -> np + j + 1 ; else n - np - nb + (j - nb) + 1
+    const int j = idx[a.axis];
+    const int nf = a.axis == 0 ? a.n1 : a.axis == 1 ? a.n2 : a.n3;
+    const int fidx = j < a.nb ? a.np + j + 1 : nf - a.np - a.nb + (j - a.nb) + 1;
+    int fi[3] = {i1 + 1, i2 + 1, i3 + 1};
+    fi[a.axis] = fidx;
+    float *f = a.field + shot * a.fs + a.g.off(fi[0], fi[1], fi[2]);
+    float *s = a.store + shot * a.sstride + k;
+    if (a.dir == 0)
+      *s = -*f;
+    else
+      *f = *s;
+  }
+}
+
+static int saved_fields(const Plan &p, int *ids) {
+  if (p.d.physics == GPI_ACOUSTIC) {
+    ids[0] = GPI_P;
+    return 1;
+  }
+  ids[0] = GPI_TAUXX;
+  ids[1] = GPI_TAUXZ;
+  ids[2] = GPI_TAUZZ;
+  return 3;
+}
+
+int boundary_io(Plan *p, int it, int dir) {
+  int ids[3];
+  const int nsv = saved_fields(*p, ids);
+  const int64_t sstride = p->bstep * p->d.nt + p->bsnap;
+  float *st = p->bstore + (int64_t)(it - 1) * p->bstep;
+  for (int q = 0; q < nsv; q++) {
+    int kz, ky, kx;
+    field_kinds(ids[q], &kz, &ky, &kx);
+    const int n1 = nkind(kz, p->d.nz, p->h), n2 = p->d.ndim == 3 ? nkind(ky, p->d.ny, p->h) : 1,
+              n3 = nkind(kx, p->d.nx, p->h);
+    for (int axis = 2; axis >= 0; axis--) {
+      if (axis == 1 && p->d.ndim == 2) continue;
+      StripArgs a;
+      a.g = geo(*p);
+      a.field = p->state[p->cur[0]][0][ids[q]];
+      a.fs = p->fstride;
+      a.store = st;
+      a.sstride = sstride;
+      a.n1 = n1;
+      a.n2 = n2;
+      a.n3 = n3;
+      a.axis = axis;
+      a.nb = p->d.nbound;
+      const int fmin = axis == 0 ? GPI_ZMIN : axis == 1 ? GPI_YMIN : GPI_XMIN;
+      a.np = (p->d.pml_faces & fmin) ? p->d.npml : 0;
+      a.dir = dir;
+      a.nshots = p->d.nshots;
+      int64_t per = 2 * (int64_t)p->d.nbound * (axis == 0 ? 1 : n1) * (axis == 1 ? 1 : n2) * (axis == 2 ? 1 : n3);
+      int blocks = (int)std::min<int64_t>((per * p->d.nshots + 255) / 256, 152 * 16);
+      k_strip<<<blocks, 256, 0, p->stream>>>(a);
+      p->launches++;
+      GPI_CUDA(p, cudaGetLastError());
+      st += per;
+    }
+  }
+  return GPI_OK;
+}
+
+// final snapshots: -tau (or -p) at nt and v after the extra half step, kept
+// in storage layout after the strips of the last step
+__global__ void k_snap(float *dst, const float *src, int64_t n, int64_t dstride, int64_t sstride, int nshots, int neg) {
+  const int64_t total = n * nshots;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int s = (int)(i / n);
+    const int64_t k = i % n;
+    const float v = src[s * sstride + k];
+    dst[s * dstride + k] = neg ? -v : v;
+  }
+}
+
+int snap_io(Plan *p, int tau, int dir) {
+  int ids[3];
+  const int nsv = saved_fields(*p, ids);
+  const int64_t sstride = p->bstep * p->d.nt + p->bsnap;
+  float *base = p->bstore + p->bstep * p->d.nt;
+  const int vids[3] = {GPI_VX, GPI_VY, GPI_VZ};
+  int slot = 0;
+  auto one = [&](int f, int neg) -> int {
+    float *snap = base + slot * p->fstride;
+    float *fld = p->state[p->cur[0]][0][f];
+    const int blocks = 152 * 8;
+    if (dir == 0)
+      k_snap<<<blocks, 256, 0, p->stream>>>(snap, fld, p->fstride, sstride, p->fstride, p->d.nshots, neg);
+    else
+      k_snap<<<blocks, 256, 0, p->stream>>>(fld, snap, p->fstride, p->fstride, sstride, p->d.nshots, 0);
+    p->launches++;
+    GPI_CUDA(p, cudaGetLastError());
+    return GPI_OK;
+  };
+  for (int q = 0; q < nsv; q++, slot++)
+    if (tau) {
+      int rc = one(ids[q], 1);
+      if (rc) return rc;
+    }
+  for (int q = 0; q < 3; q++) {
+    if (q == 1 && p->d.ndim == 2) continue;
+    if (!tau) {
+      int rc = one(vids[q], 0);
+      if (rc) return rc;
+    }
+    slot++;
+  }
+  return GPI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// gradient: sum over shots (the reference adds per-shot arrays on the host)
+// ---------------------------------------------------------------------------
+__global__ void k_shot_sum(float *dst, const float *src, int64_t n, int nshots) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < nshots; k++) s = s + src[k * n + i];
+    dst[i] = s;
+  }
+}
+int reduce_gradient(Plan *p, int param, float *dst) {
+  k_shot_sum<<<152 * 8, 256, 0, p->stream>>>(dst, p->grad[param], p->fstride, p->d.nshots);
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+// records: pool [it][ir] -> Recs layout [ir][it]
+__global__ void k_transpose(float *out, const float *in, int nt, int nr) {
+  __shared__ float tile[32][33];
+  const int it0 = blockIdx.x * 32, ir0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int it = it0 + k, ir = ir0 + threadIdx.x;
+    if (it < nt && ir < nr) tile[k][threadIdx.x] = in[(int64_t)it * nr + ir];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int ir = ir0 + k, it = it0 + threadIdx.x;
+    if (it < nt && ir < nr) out[(int64_t)ir * nt + it] = tile[threadIdx.x][k];
+  }
+}
+int transpose_records(Plan *p, float *out, const float *in, int nt, int nr) {
+  dim3 grid((nt + 31) / 32, (nr + 31) / 32);
+  k_transpose<<<grid, dim3(32, 8), 0, p->stream>>>(out, in, nt, nr);
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+}  // namespace gpi

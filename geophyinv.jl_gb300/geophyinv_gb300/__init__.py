@@ -1,0 +1,14 @@
+"""GB300 engine for GeoPhyInv's FDTD hot path.
+
+The CUDA engine (libgpi_fdtd.so, C ABI in include/gpi_fdtd.h) runs the
+staggered-grid acoustic/elastic time loop, CPML, sources, receivers and the
+adjoint-state gradient; this package is the Python host mirror of the
+reference's Julia API (SeisForwExpt, update!, gradient!, lossvalue).
+"""
+from .fdtd import (AGeomss, AcousticMedium, ElasticMedium, FdtdAcoustic, FdtdElastic, Fields, L2DistLoss,  # noqa
+                   Recs, SeisForwExpt, Srcs, get_modelvector, gradient, lossvalue, update)
+from .setup import Grid, findfreq_peak, ricker  # noqa
+
+__all__ = ["AGeomss", "AcousticMedium", "ElasticMedium", "FdtdAcoustic", "FdtdElastic", "Fields", "Grid",
+           "L2DistLoss", "Recs", "SeisForwExpt", "Srcs", "findfreq_peak", "get_modelvector", "gradient",
+           "lossvalue", "ricker", "update"]

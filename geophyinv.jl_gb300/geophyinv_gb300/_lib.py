@@ -1,0 +1,81 @@
+"""ctypes binding of libgpi_fdtd.so (declared in include/gpi_fdtd.h).
+
+This is the same binding a Julia host makes with `ccall`; the Python host
+uses it to drive the engine.  Loading fails loudly when the library has not
+been built: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+from . import _build
+
+GPI_OK = 0
+STATUS = {0: "GPI_OK", -1: "GPI_E_INVALID", -2: "GPI_E_NOMEM", -3: "GPI_E_CUDA", -4: "GPI_E_UNSUPPORTED",
+          -5: "GPI_E_STATE"}
+ACOUSTIC, ELASTIC = 0, 1
+FORWARD, FORWARD_SAVE, ADJOINT = 0, 1, 2
+FACE = {"zmin": 1, "zmax": 2, "ymin": 4, "ymax": 8, "xmin": 16, "xmax": 32}
+FIELD = {"p": 0, "vx": 1, "vy": 2, "vz": 3, "tauxx": 4, "tauyy": 5, "tauzz": 6, "tauxy": 7, "tauxz": 8, "tauyz": 9}
+
+EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_stream", "gpi_plan_bytes",
+           "gpi_set_medium", "gpi_set_pml", "gpi_set_sources", "gpi_clear_sources", "gpi_set_receivers",
+           "gpi_run", "gpi_get_records", "gpi_get_gradient", "gpi_get_field", "gpi_last_launches"]
+
+
+class PlanDesc(ctypes.Structure):
+    _fields_ = [("physics", ctypes.c_int32), ("ndim", ctypes.c_int32), ("order", ctypes.c_int32),
+                ("nz", ctypes.c_int32), ("ny", ctypes.c_int32), ("nx", ctypes.c_int32),
+                ("npml", ctypes.c_int32), ("nbound", ctypes.c_int32), ("pml_faces", ctypes.c_int32),
+                ("rigid_faces", ctypes.c_int32), ("free_faces", ctypes.c_int32), ("nt", ctypes.c_int32),
+                ("nshots", ctypes.c_int32), ("npw", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4),
+                ("dt", ctypes.c_double), ("dz", ctypes.c_double), ("dy", ctypes.c_double), ("dx", ctypes.c_double)]
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+_LIB = None
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load():
+    """Load the engine; raises if it is missing (build it with _build.build())."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        raise EngineError("libgpi_fdtd.so is not built (%s); run __graft_entry__.build() or "
+                          "geophyinv_gb300._build.build()" % path)
+    L = ctypes.CDLL(path)
+    vp, i32, i64p, fp = ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p
+    L.gpi_plan_create.argtypes = [ctypes.POINTER(PlanDesc), ctypes.POINTER(ctypes.c_void_p)]
+    L.gpi_plan_destroy.argtypes = [vp]
+    L.gpi_plan_destroy.restype = None
+    L.gpi_last_error.argtypes = [vp]
+    L.gpi_last_error.restype = ctypes.c_char_p
+    L.gpi_set_stream.argtypes = [vp, vp]
+    L.gpi_plan_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
+    L.gpi_set_medium.argtypes = [vp, vp, i32]
+    L.gpi_set_pml.argtypes = [vp, i32, fp, fp, fp]
+    L.gpi_set_sources.argtypes = [vp, i32, i32, i32, i32, i64p, i64p, fp, fp]
+    L.gpi_clear_sources.argtypes = [vp, i32, i32]
+    L.gpi_set_receivers.argtypes = [vp, i32, i32, i32, i64p, i64p, fp]
+    L.gpi_run.argtypes = [vp, i32]
+    L.gpi_get_records.argtypes = [vp, i32, i32, fp, i32]
+    L.gpi_get_gradient.argtypes = [vp, i32, fp, i32]
+    L.gpi_get_field.argtypes = [vp, i32, i32, i32, fp, i32]
+    L.gpi_last_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    _LIB = L
+    return L
+
+
+def check(rc, plan=None):
+    if rc != GPI_OK:
+        L = load()
+        msg = L.gpi_last_error(plan).decode() if True else ""
+        raise EngineError("%s: %s" % (STATUS.get(rc, rc), msg))

@@ -1,0 +1,491 @@
+"""Host mirror of GeoPhyInv's FDTD experiment API on top of the C ABI.
+
+    pa = SeisForwExpt(FdtdAcoustic(), medium=..., ageom=..., srcwav=...,
+                      tgrid=..., rfields=["p"], pml_faces=[...])
+    update(pa)                    # update!(pa)            (src/fdtd/propagate.jl:74-135)
+    pa["data"]                    # records, one Recs per supersource
+    update(pa, medium)            # update!(pa, medium)    (src/fdtd/medium.jl:128-140)
+    update(pa, srcwav, [1])       # update!(pa, srcwav, src_types) (src/fdtd/source.jl:192-246)
+    gradient(g, m, loss, dobs, pa, ["invK", "rho"])   (src/fdtd/func_grad.jl:11-49)
+    lossvalue(m, loss, dobs, pa, mparams)             (src/fdtd/func_grad.jl:1-9)
+
+The constructor follows PFdtd (src/fdtd/fdtd.jl:61-297): checks, padding,
+derived parameters, plan allocation, wavelets and peak frequency, CPML
+profiles, projection matrices.  All supersources of an experiment run in one
+plan (the reference distributes them over Distributed workers).
+"""
+import ctypes
+import copy
+import warnings
+
+import numpy as np
+
+from . import _lib
+from . import setup as S
+from .setup import Grid
+
+ALL_FACES = ["zmin", "zmax", "ymin", "ymax", "xmax", "xmin"]
+
+
+class FdtdAcoustic:
+    """FdtdAcoustic{FullWave}(mode, npw) (src/physics_types.jl:25-49)."""
+    physics = "acoustic"
+
+    def __init__(self, mode="forward", npw=None):
+        self.mode = mode
+        self.npw = npw if npw is not None else (1 if mode == "forward" else 2)
+
+
+class FdtdElastic(FdtdAcoustic):
+    physics = "elastic"
+
+
+class AcousticMedium:
+    """AcousticMedium (src/media/media.jl:40-51): grid per axis, vp, rho (Float32)."""
+    params = ("vp", "rho")
+
+    def __init__(self, grid, vp, rho):
+        self.grid = list(grid)
+        self.vp = np.asarray(vp, np.float32)
+        self.rho = np.asarray(rho, np.float32)
+        assert self.vp.shape == tuple(len(g) for g in self.grid) == self.rho.shape
+
+    @property
+    def ndim(self):
+        return len(self.grid)
+
+    def copy(self):
+        return copy.deepcopy(self)
+
+
+class ElasticMedium(AcousticMedium):
+    params = ("vp", "vs", "rho")
+
+    def __init__(self, grid, vp, vs, rho):
+        super().__init__(grid, vp, rho)
+        self.vs = np.asarray(vs, np.float32)
+        assert self.vs.shape == self.vp.shape
+
+
+class AGeomss:
+    """Positions of one supersource (src/ageom/ageom.jl:4-16): s and r map
+    axis names to coordinate arrays."""
+
+    def __init__(self, s, r):
+        self.s = {k: np.atleast_1d(np.asarray(v, np.float64)) for k, v in s.items()}
+        self.r = {k: np.atleast_1d(np.asarray(v, np.float64)) for k, v in r.items()}
+        self.ns = len(next(iter(self.s.values())))
+        self.nr = len(next(iter(self.r.values())))
+
+    def points(self, which, ndim):
+        d = self.s if which == "s" else self.r
+        return np.stack([d[a] for a in S.axis_names(ndim)], 1)
+
+
+class Srcs:
+    """Srcs / Recs (src/database/database.jl:18-43): d[field] is nt x n."""
+
+    def __init__(self, n, grid, fields, d=None):
+        self.n = n
+        self.grid = grid
+        self.fields = list(fields)
+        self.d = d if d is not None else {f: np.zeros((len(grid), n), np.float32) for f in self.fields}
+
+    def copy(self):
+        return copy.deepcopy(self)
+
+
+Recs = Srcs
+
+
+def Fields(attrib, ndim):
+    """Non-derivative fields of a physics (src/fields.jl:9-25)."""
+    v = ["vx", "vz"] if ndim == 2 else ["vx", "vy", "vz"]
+    if attrib.physics == "acoustic":
+        return ["p"] + v
+    t = ["tauxx", "tauzz", "tauxz"] if ndim == 2 else ["tauxx", "tauyy", "tauzz", "tauxy", "tauxz", "tauyz"]
+    return t + v
+
+
+class L2DistLoss:
+    """LossFunctions 0.11.2 L2DistLoss: value (output - target)^2 and
+    deriv 2 (output - target), called as loss(dobs, dcal)."""
+
+    def value(self, output, target):
+        return float(np.sum((np.asarray(output, np.float64) - np.asarray(target, np.float64)) ** 2))
+
+    def deriv(self, output, target):
+        return (np.float32(2) * (np.asarray(output, np.float32) - np.asarray(target, np.float32))).astype(np.float32)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class SeisForwExpt:
+    """PFdtd (src/fdtd/fdtd.jl:61-297) driving one libgpi_fdtd plan."""
+
+    def __init__(self, attrib, *, medium, ageom, srcwav, tgrid, rfields=("vz",), pml_faces=ALL_FACES,
+                 rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False):
+        L = _lib.load()
+        self.L = L
+        self.attrib = attrib
+        self.order = order
+        self.h = order - 1
+        self.npml = 40 + self.h
+        self.nbound = 3
+        N = medium.ndim
+        self.ndim = N
+        self.tgrid = tgrid
+        self.nt = len(tgrid)
+        self.dt = tgrid.step
+        self.rfields = list(rfields)
+        fields = Fields(attrib, N)
+        for f in self.rfields:
+            assert f in fields, "receiver field %s not in %s" % (f, fields)
+        if isinstance(ageom, AGeomss):
+            ageom = [ageom]
+        ageom = list(ageom)
+        srcwav = list(srcwav) if isinstance(srcwav, (list, tuple)) else [srcwav]
+        assert len(ageom) == len(srcwav), "ageom and srcwav mismatch"
+        for s in srcwav:
+            for f in s.fields:
+                assert f in fields, "source field %s not in %s" % (f, fields)
+        self.ageom = ageom
+        self.nss = len(ageom)
+        # adjoint geometry/wavelets of the second wavefield (fdtd.jl:90-99)
+        self.srcwav = [[s.copy() for s in srcwav]]
+        if attrib.npw == 2:
+            self.srcwav.append([Srcs(a.nr, tgrid, self.rfields) for a in ageom])
+        self._check_inside(medium)
+        self.pml_mask = S.face_mask(pml_faces)
+        rigid = pml_faces if rigid_faces is None else rigid_faces
+        self.rigid_mask = S.face_mask(rigid) | self.pml_mask
+        self.free_mask = S.face_mask(stressfree_faces)
+        self.ref_compat_proj = ref_compat_proj
+        self.medium = medium.copy()
+        self._set_exmedium(self.medium)
+        n = [len(g) for g in self.exgrid]
+        d = _lib.PlanDesc()
+        d.physics = _lib.ACOUSTIC if attrib.physics == "acoustic" else _lib.ELASTIC
+        d.ndim = N
+        d.order = order
+        d.nz, d.ny, d.nx = (n[0], n[1], n[2]) if N == 3 else (n[0], 1, n[1])
+        st = [g.step for g in medium.grid]
+        d.dz, d.dy, d.dx = (st[0], st[1], st[2]) if N == 3 else (st[0], 1.0, st[1])
+        d.npml = self.npml
+        d.nbound = self.nbound
+        d.pml_faces = self.pml_mask
+        d.rigid_faces = self.rigid_mask
+        d.free_faces = self.free_mask
+        d.nt = self.nt
+        d.nshots = self.nss
+        d.npw = attrib.npw
+        d.dt = self.dt
+        self.desc = d
+        plan = ctypes.c_void_p()
+        rc = L.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan))
+        if rc != 0:
+            raise _lib.EngineError("gpi_plan_create: %s: %s" % (_lib.STATUS.get(rc, rc), L.gpi_last_error(None).decode()))
+        self.plan = plan
+        if stream is not None:
+            self._check(L.gpi_set_stream(plan, ctypes.c_void_p(stream)))
+        self._upload_medium()
+        self._set_receivers()
+        self._src_types = [1] * attrib.npw
+        update(self, self.srcwav[0] if attrib.npw == 1 else [self.srcwav[0], self.srcwav[1]],
+               [1] if attrib.npw == 1 else [1, 0], _pml=False)
+        self._update_pml()
+        self.check_stability(verbose)
+        self.data = [[Recs(a.nr, tgrid, self.rfields) for a in ageom] for _ in range(attrib.npw)]
+        self.gradients = None
+
+    # ------------------------------------------------------------------
+    def _check(self, rc):
+        if rc != 0:
+            raise _lib.EngineError("%s: %s" % (_lib.STATUS.get(rc, rc), self.L.gpi_last_error(self.plan).decode()))
+
+    def __del__(self):
+        p = getattr(self, "plan", None)
+        if p:
+            self.L.gpi_plan_destroy(p)
+            self.plan = None
+
+    def close(self):
+        self.__del__()
+
+    def _check_inside(self, medium):
+        g = medium.grid
+        names = S.axis_names(medium.ndim)
+        for a in self.ageom:
+            for which in ("s", "r"):
+                P = a.points(which, medium.ndim)
+                for i in range(medium.ndim):
+                    if np.any((P[:, i] - g[i].first) * (g[i].last - P[:, i]) < 0.0):
+                        raise ValueError("sources or receivers not inside medium (%s)" % names[i])
+
+    def _set_exmedium(self, medium):
+        """padarray + MediumParameters (fdtd.jl:137-153, media.jl:260-304)."""
+        self.exgrid = S.padgrid(medium.grid, self.npml, self.pml_mask)
+        vp = S.padarray(medium.vp, self.npml, self.pml_mask)
+        rho = S.padarray(medium.rho, self.npml, self.pml_mask)
+        self.exvp = vp
+        if self.attrib.physics == "acoustic":
+            self.mparams = ["invK", "rho"]
+            self.mod = {"invK": S.invK(vp, rho), "rho": rho}
+        else:
+            vs = S.padarray(medium.vs, self.npml, self.pml_mask)
+            self.exvs = vs
+            self.mparams = ["invlambda", "invmu", "rho"]
+            self.mod = {"invlambda": S.invlambda(vp, vs, rho), "invmu": S.invmu(vs, rho), "rho": rho}
+        self.ref_mod = {k: S.ref_bounds(v)[0] for k, v in self.mod.items()}
+
+    def _upload_medium(self):
+        arrs = [np.asfortranarray(self.mod[k], np.float32) for k in self.mparams]
+        self._mod_keep = arrs
+        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        self._check(self.L.gpi_set_medium(self.plan, ptrs, 0))
+
+    def _proj(self, field, points):
+        return S.projection(field, self.exgrid, points, self.order, self.ref_compat_proj)
+
+    def _set_receivers(self):
+        self._rproj = []
+        for iss, a in enumerate(self.ageom):
+            pts = a.points("r", self.ndim)
+            per = {}
+            for f in self.rfields:
+                cp, rv, nz = self._proj(f, pts)
+                per[f] = (cp, rv, nz)
+                self._check(self.L.gpi_set_receivers(self.plan, iss, _lib.FIELD[f], a.nr, _ptr(cp), _ptr(rv), _ptr(nz)))
+            self._rproj.append(per)
+
+    def _update_pml(self):
+        """update_pml! (src/fdtd/cpml.jl:144-155), once, with the peak frequency
+        of the wavelets."""
+        _, vb = S.ref_bounds(self.exvp)
+        velavg = np.float32((vb[0] + vb[1]) / np.float32(2.0))
+        self.pml = S.cpml_all(self.attrib.physics, self.ndim, self.order, self.medium.grid, self.pml_mask,
+                              np.float32(self.dt), velavg, np.float32(self.freqpeak))
+        for q, (a, b, k) in enumerate(self.pml):
+            self._check(self.L.gpi_set_pml(self.plan, q, _ptr(a), _ptr(b), _ptr(k)))
+
+    def check_stability(self, verbose=False):
+        """check_stability (src/fdtd/stability.jl:8-60): warnings only."""
+        _, vb = S.ref_bounds(self.medium.vp)
+        vmax = float(vb[1])
+        if self.attrib.physics == "elastic":
+            _, vsb = S.ref_bounds(self.medium.vs)
+            vmax = float(np.sqrt(vb[1] ** 2 + vsb[1] ** 2))
+        dmin = min(g.step for g in self.medium.grid)
+        dtmax = (1.0 / np.sqrt(self.ndim)) * dmin / vmax
+        if self.dt > dtmax:
+            warnings.warn("decrease time sampling (%.2e) below %.2e" % (self.dt, dtmax))
+
+    def __getitem__(self, key):
+        if key == "data":
+            return self.data[0]
+        if key == "srcwav":
+            return self.srcwav
+        raise KeyError(key)
+
+    # ------------------------------------------------------------------
+    def run(self, mode):
+        self._check(self.L.gpi_run(self.plan, mode))
+
+    def records(self, iss, field):
+        out = np.zeros((self.nt, self.ageom[iss].nr), np.float32, order="F")
+        self._check(self.L.gpi_get_records(self.plan, iss, _lib.FIELD[field], _ptr(out), 0))
+        return out
+
+    def field(self, name, ipw=1, iss=0):
+        n = [len(g) for g in self.exgrid]
+        kinds = S.FIELD_KINDS[name]
+        shape = []
+        for ax, g in enumerate(n):
+            k = kinds[ax if self.ndim == 3 else (0 if ax == 0 else 2)]
+            shape.append(g + self.h if k == S.KV else g - self.h if k == S.KH else g - 2 * self.h if k == S.KI else g)
+        out = np.zeros(shape, np.float32, order="F")
+        self._check(self.L.gpi_get_field(self.plan, ipw, iss, _lib.FIELD[name], _ptr(out), 0))
+        return out
+
+    def gradient_raw(self, param):
+        n = [len(g) for g in self.exgrid]
+        out = np.zeros(n, np.float32, order="F")
+        self._check(self.L.gpi_get_gradient(self.plan, param, _ptr(out), 0))
+        return out
+
+    def launches(self):
+        v = ctypes.c_int64()
+        self._check(self.L.gpi_last_launches(self.plan, ctypes.byref(v)))
+        return v.value
+
+
+# ----------------------------------------------------------------------
+# update! dispatch
+# ----------------------------------------------------------------------
+def update(pa, *args, _pml=True, **kw):
+    """update!(pa) / update!(pa, medium) / update!(pa, srcwav, src_types) /
+    update!(pa, m, mparams)."""
+    if not args:
+        return _update_run(pa)
+    a0 = args[0]
+    if isinstance(a0, AcousticMedium):
+        return _update_medium(pa, a0)
+    if isinstance(a0, np.ndarray) and a0.ndim == 1:
+        return _update_modelvector(pa, a0, args[1])
+    return _update_srcwav(pa, a0, args[1] if len(args) > 1 else None)
+
+
+def _update_run(pa):
+    """update!(pa) (src/fdtd/propagate.jl:74-135)."""
+    mode = {"forward": _lib.FORWARD, "forward_save": _lib.FORWARD_SAVE, "adjoint": _lib.ADJOINT}[pa.attrib.mode]
+    if pa.attrib.npw == 1:
+        mode = _lib.FORWARD
+    pa.run(mode)
+    if mode != _lib.ADJOINT:
+        for iss in range(pa.nss):
+            for f in pa.rfields:
+                pa.data[0][iss].d[f] = pa.records(iss, f)
+    return pa
+
+
+def _update_medium(pa, medium):
+    """update!(pa, medium) (src/fdtd/medium.jl:128-140): no new allocation,
+    PML not recomputed."""
+    pa.medium = medium.copy()
+    pa._set_exmedium(pa.medium)
+    pa._upload_medium()
+    return pa
+
+
+def _update_srcwav(pa, srcwav, src_types=None):
+    """update!(pa, srcwav, src_types) (src/fdtd/source.jl:192-246)."""
+    if isinstance(srcwav, Srcs):
+        srcwav = [[srcwav]]
+    elif srcwav and isinstance(srcwav[0], Srcs):
+        srcwav = [srcwav]
+    if src_types is None:
+        src_types = [1] * len(srcwav)
+    assert len(srcwav) == len(pa.srcwav) or len(srcwav) == 1
+    for ipw, sw in enumerate(srcwav):
+        pa.srcwav[ipw] = [s.copy() for s in sw]
+    peaks = []
+    for ipw in range(pa.attrib.npw):
+        st = src_types[ipw] if ipw < len(src_types) else 0
+        pa._check(pa.L.gpi_clear_sources(pa.plan, ipw + 1, -1))
+        for iss in range(pa.nss):
+            sw = pa.srcwav[ipw][iss]
+            fpeaks = []
+            for f in sw.fields:
+                w = np.asarray(sw.d[f], np.float32)
+                if st == 0:
+                    w = np.zeros_like(w)
+                elif st == -1:
+                    if f not in ("vx", "vy", "vz"):
+                        raise ValueError("time-reversed sources act on velocities only (source.jl:8-19)")
+                    w = S.reverse_source(w)
+                if np.all(w == 0):
+                    continue
+                fpeaks.append(S.findfreq_peak(w, pa.dt))
+                wf = np.asfortranarray(w, np.float32)
+                if ipw == 0:
+                    cp, rv, nz = pa._proj(f, pa.ageom[iss].points("s", pa.ndim))
+                    pa._check(pa.L.gpi_set_sources(pa.plan, 1, iss, _lib.FIELD[f], sw.n, _ptr(cp), _ptr(rv),
+                                                   _ptr(nz), _ptr(wf)))
+                else:
+                    pa._check(pa.L.gpi_set_sources(pa.plan, 2, iss, _lib.FIELD[f], sw.n, None, None, None,
+                                                   _ptr(wf)))
+            if fpeaks and ipw == 0:
+                peaks.append(np.mean(fpeaks))
+    if peaks:
+        pa.freqpeak = np.float32(np.mean(peaks))
+    elif not hasattr(pa, "freqpeak"):
+        pa.freqpeak = np.float32(0.0)
+    pa._src_types = list(src_types)
+    return pa
+
+
+# ----------------------------------------------------------------------
+# model vector (log-parameterised inner grid) and the FWI gradient
+# ----------------------------------------------------------------------
+def _inner(pa):
+    sl = []
+    names = S.axis_names(pa.ndim)
+    for g, d in zip(pa.exgrid, names):
+        lo = pa.npml if pa.pml_mask & S.FACE_BITS[d + "min"] else 0
+        hi = pa.npml if pa.pml_mask & S.FACE_BITS[d + "max"] else 0
+        sl.append(slice(lo, len(g) - hi))
+    return tuple(sl)
+
+
+def get_modelvector(pa, mparams):
+    """m = log(mod / ref) on the inner grid (src/fdtd/medium.jl:3-7, :55-76)."""
+    inn = _inner(pa)
+    return np.concatenate([np.log(pa.mod[k][inn] * (np.float32(1) / pa.ref_mod[k])).astype(np.float32).ravel(order="F")
+                           for k in mparams])
+
+
+def _update_modelvector(pa, m, mparams):
+    """update!(pa, m, mparams) (src/fdtd/medium.jl:31-52)."""
+    inn = _inner(pa)
+    chunks = np.split(np.asarray(m, np.float32), len(mparams))
+    for k, x in zip(mparams, chunks):
+        view = pa.mod[k][inn]
+        pa.mod[k][inn] = (np.exp(x.reshape(view.shape, order="F")) * pa.ref_mod[k]).astype(np.float32)
+    pa._upload_medium()
+    return pa
+
+
+def lossvalue(m, loss, dobs, pa, mparams=("invK", "rho")):
+    """lossvalue (src/fdtd/func_grad.jl:1-9)."""
+    update(pa, m, list(mparams))
+    mode_save = pa.attrib.mode
+    pa.attrib.mode = "forward_save"
+    update(pa, pa.srcwav, [1, 0])
+    update(pa)
+    pa.attrib.mode = mode_save
+    return _loss(loss, dobs, pa.data[0])
+
+
+def _loss(loss, dobs, dcal):
+    return sum(loss.value(o.d[f], c.d[f]) for o, c in zip(dobs, dcal) for f in o.fields)
+
+
+def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
+    """gradient!(g, m, loss, dobs, pa, mparams) (src/fdtd/func_grad.jl:11-49):
+    forward_save, adjoint sources deriv(loss, dobs, dcal) reversed in time,
+    adjoint run with src_types [-1, 1], chain rule g * exp(m) * ref."""
+    mparams = list(mparams)
+    update(pa, m, mparams)
+    mode_save = pa.attrib.mode
+    pa.attrib.mode = "forward_save"
+    update(pa, pa.srcwav, [1, 0])
+    update(pa)
+    adj = []
+    for o, c in zip(dobs, pa.data[0]):
+        s = Srcs(o.n, pa.tgrid, pa.rfields)
+        for f in pa.rfields:
+            s.d[f] = loss.deriv(o.d[f], c.d[f])[::-1].copy()  # reverse!(srcwav[2])
+        adj.append(s)
+    pa.srcwav[1] = adj
+    update(pa, pa.srcwav, [-1, 1])
+    pa.attrib.mode = "adjoint"
+    update(pa)
+    inn = _inner(pa)
+    chunks = np.split(np.asarray(m, np.float32), len(mparams))
+    out = []
+    pidx = {"invK": 0, "rho": 1}
+    raw = {}
+    for k, x in zip(mparams, chunks):
+        gr = pa.gradient_raw(pidx[k])
+        raw[k] = gr
+        gm = gr[inn]
+        gm = gm * np.exp(x.reshape(gm.shape, order="F")) * pa.ref_mod[k]
+        out.append(gm.astype(np.float32).ravel(order="F"))
+    gv = np.concatenate(out)
+    if g is not None:
+        g[:] = gv
+    pa.gradients = raw
+    pa.attrib.mode = mode_save
+    return _loss(loss, dobs, pa.data[0])

@@ -1,0 +1,249 @@
+"""Host-side setup of an FDTD experiment (the Julia host's job in the
+reference): padding of the medium, derived parameters, CPML profiles,
+sparse projection matrices, wavelets.  Vectorised numpy; the numbers follow
+the reference's floating-point types (Float32 media and weights, Float64
+PML profile from Float32 inputs).
+"""
+import math
+
+import numpy as np
+
+FACE_BITS = {"zmin": 1, "zmax": 2, "ymin": 4, "ymax": 8, "xmin": 16, "xmax": 32}
+KF, KV, KH, KI = 0, 1, 2, 3
+FIELD_KINDS = {
+    "p": (KF, KF, KF), "vx": (KF, KF, KV), "vy": (KF, KV, KF), "vz": (KV, KF, KF),
+    "tauxx": (KF, KF, KF), "tauyy": (KF, KF, KF), "tauzz": (KF, KF, KF),
+    "tauxy": (KI, KH, KH), "tauxz": (KH, KI, KH), "tauyz": (KH, KH, KI),
+}
+# derivative fields in the engine's canonical order: (name, axis, kinds)
+DERIV = {
+    ("acoustic", 2): [("dpdx", 2, (KI, KF, KH)), ("dpdz", 0, (KH, KF, KI)),
+                      ("dvxdx", 2, (KF, KF, KF)), ("dvzdz", 0, (KF, KF, KF))],
+    ("elastic", 2): [("dtauxxdx", 2, (KI, KF, KH)), ("dtauxzdx", 2, (KH, KF, KI)),
+                     ("dtauzzdz", 0, (KH, KF, KI)), ("dtauxzdz", 0, (KI, KF, KH)),
+                     ("dvxdx", 2, (KF, KF, KF)), ("dvzdz", 0, (KF, KF, KF)),
+                     ("dvxdz", 0, (KH, KF, KH)), ("dvzdx", 2, (KH, KF, KH))],
+    ("acoustic", 3): [("dpdx", 2, (KI, KI, KH)), ("dpdy", 1, (KI, KH, KI)), ("dpdz", 0, (KH, KI, KI)),
+                      ("dvxdx", 2, (KF, KF, KF)), ("dvydy", 1, (KF, KF, KF)), ("dvzdz", 0, (KF, KF, KF))],
+    ("elastic", 3): [("dtauxxdx", 2, (KI, KI, KH)), ("dtauxydx", 2, (KI, KH, KI)),
+                     ("dtauxzdx", 2, (KH, KI, KI)), ("dtauyydy", 1, (KI, KH, KI)),
+                     ("dtauxydy", 1, (KI, KI, KH)), ("dtauyzdy", 1, (KH, KI, KI)),
+                     ("dtauzzdz", 0, (KH, KI, KI)), ("dtauyzdz", 0, (KI, KH, KI)),
+                     ("dtauxzdz", 0, (KI, KI, KH)), ("dvxdx", 2, (KF, KF, KF)),
+                     ("dvydy", 1, (KF, KF, KF)), ("dvzdz", 0, (KF, KF, KF)),
+                     ("dvxdy", 1, (KI, KH, KH)), ("dvxdz", 0, (KH, KI, KH)),
+                     ("dvydx", 2, (KI, KH, KH)), ("dvydz", 0, (KH, KH, KI)),
+                     ("dvzdx", 2, (KH, KI, KH)), ("dvzdy", 1, (KH, KH, KI))],
+}
+
+
+class Grid:
+    """A uniform axis (Julia's StepRangeLen{Float64}): start, step, length."""
+
+    def __init__(self, start, step, n):
+        self.start, self.step, self.n = float(start), float(step), int(n)
+
+    @classmethod
+    def range(cls, start, stop, length):
+        return cls(start, (stop - start) / (length - 1), length)
+
+    def __len__(self):
+        return self.n
+
+    def values(self):
+        return self.start + self.step * np.arange(self.n)
+
+    @property
+    def first(self):
+        return self.start
+
+    @property
+    def last(self):
+        return self.start + self.step * (self.n - 1)
+
+    def __repr__(self):
+        return "Grid(%g, step=%g, n=%d)" % (self.start, self.step, self.n)
+
+
+def axis_names(ndim):
+    return "zyx" if ndim == 3 else "zx"
+
+
+def face_mask(faces):
+    m = 0
+    for f in faces:
+        m |= FACE_BITS.get(str(f).lstrip(":"), 0)
+    return m
+
+
+def padgrid(grid, npml, mask):
+    """padmgrid (src/media/media.jl:298-316)."""
+    out = []
+    for g, d in zip(grid, axis_names(len(grid))):
+        lo = npml if mask & FACE_BITS[d + "min"] else 0
+        hi = npml if mask & FACE_BITS[d + "max"] else 0
+        out.append(Grid(g.start - lo * g.step, g.step, g.n + lo + hi))
+    return out
+
+
+def padarray(m, npml, mask):
+    """Replicate-pad on PML faces only (padarray!, src/media/media.jl:280-296)."""
+    pads = []
+    for d in axis_names(m.ndim):
+        pads.append((npml if mask & FACE_BITS[d + "min"] else 0, npml if mask & FACE_BITS[d + "max"] else 0))
+    return np.pad(np.asarray(m, np.float32), pads, mode="edge")
+
+
+def ref_bounds(m, frac=0.1):
+    """Medium parameter reference value and bounds (src/media/media.jl:24-33)."""
+    m = np.asarray(m, np.float32)
+    ref = np.float32(m.mean(dtype=np.float32))
+    f = np.float32(frac)
+    lo = max(np.float32(0.0), np.float32(m.min() - f * ref))
+    return ref, (np.float32(lo), np.float32(m.max() + f * ref))
+
+
+def invK(vp, rho):
+    vp = np.asarray(vp, np.float32)
+    return (np.float32(1.0) / ((vp * vp) * np.asarray(rho, np.float32))).astype(np.float32)
+
+
+def invlambda(vp, vs, rho):
+    vp, vs = np.asarray(vp, np.float32), np.asarray(vs, np.float32)
+    return (np.float32(1.0) / (((vp * vp) - np.float32(2.0) * (vs * vs)) * np.asarray(rho, np.float32))).astype(np.float32)
+
+
+def invmu(vs, rho):
+    vs = np.asarray(vs, np.float32)
+    return (np.float32(1.0) / ((vs * vs) * np.asarray(rho, np.float32))).astype(np.float32)
+
+
+def field_axis(g, kind, h):
+    """Positions of a staggered field along one axis (get_mgrid)."""
+    if kind == KV:
+        return g.start - 0.5 * g.step * h + g.step * np.arange(g.n + h)
+    if kind == KH:
+        return g.start + 0.5 * g.step * h + g.step * np.arange(g.n - h)
+    if kind == KI:
+        return g.start + g.step * h + g.step * np.arange(g.n - 2 * h)
+    return g.values()
+
+
+def cpml_profile(x, g, flags, dt32, velavg32, fpeak32, npml):
+    """a, b, kI on the first/last npml points of axis x (update_pml!,
+    src/fdtd/cpml.jl:8-103); Float64 arithmetic, Float32 result."""
+    xl = g.first - 2 * g.step
+    xr = g.last + 2 * g.step
+    thick = (npml - 1) * g.step
+    amax = math.pi * float(fpeak32)
+    d0 = -(2.0 + 1) * float(velavg32) * math.log(0.001) / (2.0 * thick)
+    d = np.zeros(len(x))
+    alpha = np.zeros(len(x))
+    for on, ab in ((flags[0], xl - x), (flags[1], x - xr)):
+        if not on:
+            continue
+        sel = ab >= 0.0
+        an = ab[sel] / thick
+        d[sel] = d0 * an ** 2.0
+        alpha[sel] = amax * (1.0 - an) + 0.01 * amax
+    alpha[alpha < 0.0] = 0.0
+    k = np.ones(len(x))
+    b = np.exp(-(d / k + alpha) * float(dt32))
+    a = np.zeros(len(x))
+    nzd = np.abs(d) > 1e-6
+    a[nzd] = d[nzd] * (b[nzd] - 1.0) / (k[nzd] * (d[nzd] + k[nzd] * alpha[nzd]))
+    sel = np.r_[0:npml, len(x) - npml:len(x)]
+    return a[sel].astype(np.float32), b[sel].astype(np.float32), (1.0 / k[sel]).astype(np.float32)
+
+
+def cpml_all(physics, ndim, order, grid, mask, dt32, velavg32, fpeak32):
+    """update_pml! for every derivative field (src/fdtd/cpml.jl:125-155)."""
+    h = order - 1
+    npml = 40 + h
+    ex = padgrid(grid, npml, mask)
+    names = axis_names(ndim)
+    out = []
+    for _, axis, kinds in DERIV[(physics, ndim)]:
+        ia = axis if ndim == 3 else (0 if axis == 0 else 1)
+        x = field_axis(ex[ia], kinds[axis], h)
+        d = names[ia]
+        flags = (bool(mask & FACE_BITS[d + "min"]), bool(mask & FACE_BITS[d + "max"]))
+        out.append(cpml_profile(x, grid[ia], flags, dt32, velavg32, fpeak32, npml))
+    return out
+
+
+def _bracket(x, v):
+    """get_neighbour_indices (src/proj_mat.jl:69-79), vectorised, 0-based."""
+    n = len(x)
+    idx = np.searchsorted(x, v, side="left") + 1
+    i1 = np.where(idx == 1, 0, np.where(idx >= n, n - 2, idx - 2))
+    f = np.where(v < x.min(), 0.0, np.where(v > x.max(), 1.0, (v - x[i1]) / (x[i1 + 1] - x[i1])))
+    return i1, f
+
+
+def projection(field, exgrid, points, order, ref_compat=True):
+    """Sparse CSC (colptr, rowval, nzval) from the field grid to `points`
+    (get_proj_matrix + bilinear_interp, src/proj_mat.jl:85-247).  points:
+    array (npts, ndim) of (z, [y,] x).  In 3-D the reference pairs the z grid
+    with the x coordinate and vice versa (bilinear_interp(x, y, z, zi, yi,
+    xi) called with (mz, my, mx, pz, py, px)); ref_compat keeps that."""
+    ndim = len(exgrid)
+    h = order - 1
+    kinds = FIELD_KINDS[field]
+    kinds = (kinds[0], kinds[2]) if ndim == 2 else kinds
+    axes = [field_axis(g, k, h) for g, k in zip(exgrid, kinds)]
+    P = np.asarray(points, dtype=np.float64).reshape(-1, ndim)
+    npts = len(P)
+    if ndim == 3 and ref_compat:
+        P = P[:, [2, 1, 0]]
+    idx, fr = zip(*[_bracket(ax, P[:, i]) for i, ax in enumerate(axes)])
+    dims = [len(ax) for ax in axes]
+    rows, vals = [], []
+    corners = [(0, 0), (0, 1), (1, 0), (1, 1)] if ndim == 2 else \
+        [(a, b, c) for a in (0, 1) for b in (0, 1) for c in (0, 1)]
+    for cor in corners:
+        lin = np.zeros(npts, np.int64)
+        w = np.ones(npts)
+        stride = 1
+        for ax in range(ndim):
+            lin += (idx[ax] + cor[ax]) * stride
+            stride *= dims[ax]
+        # weight product in the reference's order ((1-dz)(1-dy))(1-dx)
+        for ax in range(ndim):
+            w = w * (fr[ax] if cor[ax] else (1.0 - fr[ax]))
+        rows.append(lin)
+        vals.append(w.astype(np.float32))
+    rows = np.stack(rows, 1)
+    vals = np.stack(vals, 1)
+    order_ = np.argsort(rows, axis=1, kind="stable")
+    rows = np.take_along_axis(rows, order_, 1)
+    vals = np.take_along_axis(vals, order_, 1)
+    colptr = np.arange(npts + 1, dtype=np.int64) * rows.shape[1]
+    return colptr, rows.reshape(-1).astype(np.int64), vals.reshape(-1).astype(np.float32)
+
+
+def ricker(fqdom, tgrid, tpeak=None, maxamp=1.0):
+    """Ricker wavelet (src/srcwav/wavelets.jl:14-72)."""
+    if tpeak is None:
+        tpeak = tgrid.first + 1.5 / fqdom
+    pf = (math.pi * math.pi) * fqdom ** 2.0
+    t = tgrid.values()
+    ts = (t - tpeak) * (t - tpeak)
+    return (1.0 - 2.0 * pf * ts) * np.exp(-1.0 * pf * ts) * maxamp
+
+
+def findfreq_peak(w, dt):
+    """Peak frequency of |rfft|^2 over all columns (findfreq, src/Utils/freq.jl:28-57)."""
+    w = np.asarray(w, np.float32)
+    w = w[:, None] if w.ndim == 1 else w
+    ax = np.abs(np.fft.rfft(w, axis=0)) ** 2
+    i = int(np.argmax(ax.T.reshape(-1)))
+    return np.fft.rfftfreq(w.shape[0], dt)[i % ax.shape[0]]
+
+
+def reverse_source(w):
+    """Source of the time-reversed wavefield (get_source(..., Val{-1}),
+    src/fdtd/source.jl:8-19): -w shifted by one sample, reversed, row 1 zero."""
+    ww = np.roll(-np.asarray(w, np.float32), -1, axis=0)[::-1].copy()
+    ww[0] = 0
+    return ww

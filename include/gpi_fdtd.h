@@ -1,0 +1,130 @@
+/*
+ * gpi_fdtd.h -- C ABI of the GB300 FDTD engine (libgpi_fdtd.so).
+ *
+ * The engine replaces the per-worker time loop of GeoPhyInv.jl
+ * (mod_x_proc!, src/fdtd/propagate.jl:138-261) and the device-side parts of
+ * its setup.  A Julia host keeps SeisForwExpt / update! and reaches the
+ * engine through `ccall` on these entry points; every entry point below
+ * names the reference function it stands in for.
+ *
+ * Conventions
+ *   - all arrays are column-major (z fastest), like Julia arrays;
+ *   - the grid is the EXTENDED grid (physical grid plus PML padding),
+ *     exactly pac.exmedium.grid of the reference;
+ *   - sparse projections are CSC with 0-based column pointers and 0-based
+ *     linear row indices into the field's own array (get_mgrid shapes);
+ *   - every call returns 0 on success or a negative GPI_E* code; the
+ *     message of the last failure of a plan is gpi_last_error(plan);
+ *   - a plan is bound to the CUDA device that was current at creation and
+ *     to one stream; calls on one plan are not re-entrant.
+ */
+#ifndef GPI_FDTD_H
+#define GPI_FDTD_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPI_ABI_VERSION 1
+
+enum gpi_status {
+  GPI_OK = 0,
+  GPI_E_INVALID = -1,     /* bad argument or inconsistent sizes */
+  GPI_E_NOMEM = -2,       /* device allocation failed (HBM budget) */
+  GPI_E_CUDA = -3,        /* CUDA runtime error */
+  GPI_E_UNSUPPORTED = -4, /* combination the engine does not implement */
+  GPI_E_STATE = -5        /* call out of order (e.g. adjoint before forward_save) */
+};
+
+enum gpi_physics { GPI_ACOUSTIC = 0, GPI_ELASTIC = 1 };
+enum gpi_mode { GPI_FORWARD = 0, GPI_FORWARD_SAVE = 1, GPI_ADJOINT = 2 };
+/* faces, named as the reference's symbols :zmin, :zmax, :ymin, ... */
+enum gpi_face { GPI_ZMIN = 1, GPI_ZMAX = 2, GPI_YMIN = 4, GPI_YMAX = 8, GPI_XMIN = 16, GPI_XMAX = 32 };
+/* wavefields (the non-derivative Fields of src/fields.jl:27-42) */
+enum gpi_field {
+  GPI_P = 0, GPI_VX = 1, GPI_VY = 2, GPI_VZ = 3,
+  GPI_TAUXX = 4, GPI_TAUYY = 5, GPI_TAUZZ = 6,
+  GPI_TAUXY = 7, GPI_TAUXZ = 8, GPI_TAUYZ = 9
+};
+/* medium parameters (MediumParameters, src/fdtd/medium.jl:81-95):
+ * acoustic {invK, rho}, elastic {invlambda, invmu, rho} */
+enum gpi_param { GPI_INVK = 0, GPI_RHO = 1, GPI_INVLAMBDA = 0, GPI_INVMU = 1, GPI_RHO_E = 2 };
+
+typedef struct gpi_plan gpi_plan;
+
+typedef struct {
+  int32_t physics;     /* gpi_physics */
+  int32_t ndim;        /* 2 or 3 */
+  int32_t order;       /* stencil order (_fd_order); the engine implements 4 */
+  int32_t nz, ny, nx;  /* extended grid sizes (ny = 1 for 2-D) */
+  int32_t npml;        /* PML width, _fd_npml = 40 + order - 1 */
+  int32_t nbound;      /* boundary strip width, _fd_nbound = 3 */
+  int32_t pml_faces;   /* gpi_face bit mask */
+  int32_t rigid_faces; /* rigid faces; the engine adds pml_faces (fdtd.jl:215) */
+  int32_t free_faces;  /* stress-free faces (only GPI_ZMIN is honoured, as in the reference) */
+  int32_t nt;          /* time steps */
+  int32_t nshots;      /* supersources held by the plan */
+  int32_t npw;         /* propagating wavefields: 1 (forward) or 2 (forward_save + adjoint) */
+  int32_t reserved[4];
+  double dt, dz, dy, dx; /* time step and grid steps (dy ignored in 2-D) */
+} gpi_plan_desc;
+
+/* PFdtd constructor, device half (src/fdtd/fdtd.jl:61-297, :340-385):
+ * allocates wavefields, CPML memory, coefficient arrays, record buffers. */
+int gpi_plan_create(const gpi_plan_desc *desc, gpi_plan **out);
+/* Frees everything the plan owns (the reference relies on the GC). */
+void gpi_plan_destroy(gpi_plan *plan);
+/* Message of the last failing call on `plan` (or of the last failing
+ * gpi_plan_create when plan is NULL). */
+const char *gpi_last_error(const gpi_plan *plan);
+/* Run on this CUDA stream (cudaStream_t); NULL is the legacy default stream. */
+int gpi_set_stream(gpi_plan *plan, void *stream);
+/* Device bytes the plan holds. */
+int gpi_plan_bytes(const gpi_plan *plan, size_t *bytes);
+
+/* update!(pac, medium) -> update_dmod! (src/fdtd/medium.jl:131-221):
+ * mod[i] is the i-th MediumParameters array on the extended grid
+ * (nz*ny*nx floats); on_device != 0 means device pointers. */
+int gpi_set_medium(gpi_plan *plan, const float *const *mod, int on_device);
+
+/* update_pml! result (src/fdtd/cpml.jl:8-155): for derivative field q
+ * (canonical order of the physics, see docs) the arrays a, b, kI, each of
+ * length 2*npml. */
+int gpi_set_pml(gpi_plan *plan, int q, const float *a, const float *b, const float *kI);
+
+/* Source spray matrix and wavelets of one supersource (fill_wavelets!,
+ * src/fdtd/source.jl:24-58, and ssprayw, src/fdtd/ageom.jl:33-45).
+ * ipw = 1 for the first wavefield.  ipw = 2 sets the adjoint sources of
+ * the second wavefield, injected through the receiver interpolation
+ * matrix of `field` (src/fdtd/source.jl:141-156); colptr/rowval/nzval are
+ * then ignored and ns must equal the receiver count.  wavelets: nt x ns. */
+int gpi_set_sources(gpi_plan *plan, int ipw, int shot, int field, int ns, const int64_t *colptr,
+                    const int64_t *rowval, const float *nzval, const float *wavelets);
+/* Remove every source of wavefield ipw of one shot (-1: all shots). */
+int gpi_clear_sources(gpi_plan *plan, int ipw, int shot);
+/* Receiver interpolation matrix (rinterpolatew, src/fdtd/ageom.jl:46-54). */
+int gpi_set_receivers(gpi_plan *plan, int shot, int field, int nr, const int64_t *colptr,
+                      const int64_t *rowval, const float *nzval);
+
+/* mod_x_proc! over every shot of the plan in the given mode
+ * (src/fdtd/propagate.jl:74-261).  Asynchronous on the plan's stream. */
+int gpi_run(gpi_plan *plan, int mode);
+
+/* update_datamat!/update_data! (src/fdtd/receiver.jl:17-46): records of
+ * one shot and field as nt x nr (column-major, Recs.d layout). */
+int gpi_get_records(gpi_plan *plan, int shot, int field, float *out, int on_device);
+/* sum_grads! (src/fdtd/gradient.jl:2-14): the gradient w.r.t. medium
+ * parameter `param`, summed over the plan's shots, on the extended grid. */
+int gpi_get_gradient(gpi_plan *plan, int param, float *out, int on_device);
+/* Final state of a field of wavefield ipw for one shot (w1[:t]) in its
+ * reference shape. */
+int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int on_device);
+/* Number of engine kernel launches issued by the last gpi_run. */
+int gpi_last_launches(const gpi_plan *plan, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,303 @@
+"""ctypes driver of the CPU ORACLE (test infrastructure only).
+
+Runs the C restatement of the reference time loop (libgpo.so, built from
+oracle/fdtd_oracle_*.c by oracle/Makefile) on a plain-dict experiment
+description and returns records and gradients.  It mirrors the control flow
+of the reference drivers:
+
+  * forward          -> update!(pa)            (src/fdtd/propagate.jl:74-135)
+  * gradient         -> gradient!(g, m, ...)   (src/fdtd/func_grad.jl:11-49)
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+
+Experiment description (all positions in metres, arrays Float32):
+  physics      "acoustic" | "elastic"
+  ndim         2 | 3
+  order        stencil order (4)
+  grid         physical grid [(start, step, n)] per axis (z, [y,] x)
+  vp, rho, vs  physical media (vs for elastic)
+  pml_faces, rigid_faces, free_faces   bit masks (setup_ref.FACE_BITS)
+  dt, nt
+  shots        list of {"src": {field: (positions, wavelets nt x ns)},
+                        "rec": positions}
+  rfields      list of recorded fields
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from . import setup_ref as S
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build():
+    """Compile libgpo.so with the committed Makefile."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "_build", "libgpo.so")
+        if not os.path.exists(path):
+            build()
+        _LIB = ctypes.CDLL(path)
+        for sfx in ("f32", "f64"):
+            getattr(_LIB, "gpo_create_" + sfx).restype = ctypes.c_void_p
+            getattr(_LIB, "gpo_create_" + sfx).argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+            getattr(_LIB, "gpo_shot_" + sfx).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            getattr(_LIB, "gpo_get_field_" + sfx).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+            getattr(_LIB, "gpo_destroy_" + sfx).argtypes = [ctypes.c_void_p]
+        _LIB.gpo_get_dmod_f32.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_int)]
+    return _LIB
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [("physics", ctypes.c_int), ("ndim", ctypes.c_int), ("order", ctypes.c_int),
+                ("nz", ctypes.c_int), ("ny", ctypes.c_int), ("nx", ctypes.c_int),
+                ("npml", ctypes.c_int), ("nbound", ctypes.c_int), ("pml_faces", ctypes.c_int),
+                ("rigid_faces", ctypes.c_int), ("free_faces", ctypes.c_int), ("nt", ctypes.c_int),
+                ("nthreads", ctypes.c_int),
+                ("dt", ctypes.c_double), ("dz", ctypes.c_double), ("dy", ctypes.c_double), ("dx", ctypes.c_double)]
+
+
+class _Proj(ctypes.Structure):
+    _fields_ = [("field", ctypes.c_int), ("n", ctypes.c_int), ("colptr", ctypes.c_void_p),
+                ("rowval", ctypes.c_void_p), ("nzval", ctypes.c_void_p), ("data", ctypes.c_void_p)]
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Prepared:
+    """Everything the time loop needs, derived from an experiment description
+    exactly as the reference constructor does (PFdtd, src/fdtd/fdtd.jl:61-297)."""
+
+    def __init__(self, ex, dtype=np.float32, ref_compat=True):
+        self.ex = ex
+        self.dtype = dtype
+        self.physics = ex["physics"]
+        self.ndim = ex["ndim"]
+        self.order = ex.get("order", 4)
+        self.h = self.order - 1
+        self.npml = S.npml_of(self.order)
+        self.faces = ex["pml_faces"]
+        self.rigid = ex.get("rigid_faces", self.faces) | self.faces
+        self.free = ex.get("free_faces", 0)
+        self.nt = ex["nt"]
+        self.dt = ex["dt"]
+        self.grid = ex["grid"]
+        self.exgrid = S.padmgrid(self.grid, self.npml, self.faces)
+        vp = S.padarray(np.asarray(ex["vp"], np.float32), self.npml, self.faces)
+        rho = S.padarray(np.asarray(ex["rho"], np.float32), self.npml, self.faces)
+        if self.physics == "acoustic":
+            self.mod = S.derived_acoustic(vp, rho)
+        else:
+            vs = S.padarray(np.asarray(ex["vs"], np.float32), self.npml, self.faces)
+            self.mod = S.derived_elastic(vp, vs, rho)
+        _, vb = S.bounds(vp)
+        self.velavg = np.float32((vb[0] + vb[1]) / np.float32(2))
+        # wavelets of wavefield 1 set the peak frequency (fill_wavelets!, source.jl:24-58)
+        peaks = []
+        for shot in ex["shots"]:
+            fp = [S.findfreq_peak(w, self.dt) for (_, w) in shot["src"].values()]
+            peaks.append(np.mean(fp))
+        self.fpeak = np.float32(np.mean(peaks))
+        self.pml = S.pml_all(self.physics, self.ndim, self.order, self.grid, self.faces,
+                             np.float32(self.dt), self.velavg, self.fpeak)
+        self.ref_compat = ref_compat
+        self.shape = [g[2] for g in self.exgrid]
+
+    def desc(self, nthreads=0):
+        d = _Desc()
+        d.physics = 0 if self.physics == "acoustic" else 1
+        d.ndim = self.ndim
+        d.order = self.order
+        n = self.shape
+        d.nz, d.ny, d.nx = (n[0], n[1], n[2]) if self.ndim == 3 else (n[0], 1, n[1])
+        st = [g[1] for g in self.grid]
+        d.dz, d.dy, d.dx = (st[0], st[1], st[2]) if self.ndim == 3 else (st[0], 1.0, st[1])
+        d.npml = self.npml
+        d.nbound = 3
+        d.pml_faces = self.faces
+        d.rigid_faces = self.rigid
+        d.free_faces = self.free
+        d.nt = self.nt
+        d.nthreads = nthreads
+        d.dt = self.dt
+        return d
+
+    def proj(self, field, points):
+        return S.proj_matrix(field, self.exgrid, points, self.ndim, self.order, self.ref_compat)
+
+
+class Oracle:
+    """Owns one oracle context (wavefields, boundary stores)."""
+
+    def __init__(self, prep, nthreads=0):
+        self.p = prep
+        self.sfx = "f32" if prep.dtype == np.float32 else "f64"
+        L = lib()
+        self.L = L
+        self._keep = []
+        mods = [np.ascontiguousarray(m.astype(prep.dtype).reshape(-1, order="F")) for m in prep.mod]
+        pml = []
+        for a, b, k in prep.pml:
+            pml += [np.ascontiguousarray(a.astype(prep.dtype)), np.ascontiguousarray(b.astype(prep.dtype)),
+                    np.ascontiguousarray(k.astype(prep.dtype))]
+        self._keep += mods + pml
+        mp = (ctypes.c_void_p * len(mods))(*[m.ctypes.data for m in mods])
+        pp = (ctypes.c_void_p * len(pml))(*[x.ctypes.data for x in pml])
+        self.d = prep.desc(nthreads)
+        self.ctx = getattr(L, "gpo_create_" + self.sfx)(ctypes.byref(self.d), mp, pp, len(prep.ex["shots"]))
+
+    def close(self):
+        if self.ctx:
+            getattr(self.L, "gpo_destroy_" + self.sfx)(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        self.close()
+
+    def _projs(self, items, nt):
+        arrs = (_Proj * max(1, len(items)))()
+        for i, (field, (cp, rv, nz), data) in enumerate(items):
+            nzv = np.ascontiguousarray(nz.astype(self.p.dtype))
+            self._keep += [cp, rv, nzv, data]
+            arrs[i].field = S.FIELD_ID[field]
+            arrs[i].n = len(cp) - 1
+            arrs[i].colptr = cp.ctypes.data
+            arrs[i].rowval = rv.ctypes.data
+            arrs[i].nzval = nzv.ctypes.data
+            arrs[i].data = data.ctypes.data
+        return arrs
+
+    def shot(self, ishot, mode, src, rec, adj=(), grads=None):
+        """src: list of (field, csc, wavelets nt x n Fortran); rec: list of
+        (field, csc) -> returns {field: records nt x nr}."""
+        nt = self.p.nt
+        dt = self.p.dtype
+        srcs = [(f, csc, np.asfortranarray(np.asarray(w, dt))) for f, csc, w in src]
+        outs = {}
+        recs = []
+        for f, csc in rec:
+            out = np.zeros((nt, len(csc[0]) - 1), dtype=dt, order="F")
+            outs[f] = out
+            recs.append((f, csc, out))
+        adjs = [(f, csc, np.asfortranarray(np.asarray(w, dt))) for f, csc, w in adj]
+        sp = self._projs(srcs, nt)
+        rp = self._projs(recs, nt)
+        ap = self._projs(adjs, nt)
+        gK = gR = None
+        if grads is not None:
+            gK, gR = grads
+        rc = getattr(self.L, "gpo_shot_" + self.sfx)(
+            self.ctx, ishot, mode, len(srcs), sp, len(recs), rp, len(adjs), ap,
+            None if gK is None else gK.ctypes.data, None if gR is None else gR.ctypes.data)
+        self._keep = self._keep[: 0]
+        if rc != 0:
+            raise RuntimeError("oracle shot failed: %d" % rc)
+        return outs
+
+    def field(self, name, ipw=1):
+        from ctypes import byref, c_int
+        n1, n2, n3 = c_int(), c_int(), c_int()
+        L = self.L
+        L.gpo_field_shape.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                      ctypes.POINTER(c_int)]
+        L.gpo_field_shape(ctypes.byref(self.d), S.FIELD_ID[name], byref(n1), byref(n2), byref(n3))
+        out = np.zeros(n1.value * n2.value * n3.value, dtype=self.p.dtype)
+        rc = getattr(L, "gpo_get_field_" + self.sfx)(self.ctx, ipw, S.FIELD_ID[name], out.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("no field %s" % name)
+        shp = (n1.value, n3.value) if self.p.ndim == 2 else (n1.value, n2.value, n3.value)
+        return out.reshape(shp, order="F")
+
+    def dmod(self, idx):
+        from ctypes import byref, c_int
+        n1, n2, n3 = c_int(), c_int(), c_int()
+        if self.L.gpo_get_dmod_f32(self.ctx, idx, None, byref(n1), byref(n2), byref(n3)) != 0:
+            raise IndexError(idx)
+        out = np.zeros(n1.value * n2.value * n3.value, dtype=np.float32)
+        self.L.gpo_get_dmod_f32(self.ctx, idx, out.ctypes.data, byref(n1), byref(n2), byref(n3))
+        shp = (n1.value, n3.value) if self.p.ndim == 2 else (n1.value, n2.value, n3.value)
+        return out.reshape(shp, order="F")
+
+
+def _shot_inputs(prep, shot, src_types=1):
+    src = []
+    for f, (pos, w) in shot["src"].items():
+        w = np.asarray(w, np.float32)
+        if w.ndim == 1:
+            w = w[:, None]
+        if src_types == -1:
+            w = S.source_reverse(w)
+        src.append((f, prep.proj(f, pos), w))
+    rec = [(f, prep.proj(f, shot["rec"])) for f in prep.ex["rfields"]]
+    return src, rec
+
+
+def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=False):
+    """update!(pa) in :forward mode: records[field] of shape (nshots, nt, nr)."""
+    prep = Prepared(ex, dtype, ref_compat)
+    orc = Oracle(prep, nthreads)
+    out = {f: [] for f in ex["rfields"]}
+    for i, shot in enumerate(ex["shots"]):
+        src, rec = _shot_inputs(prep, shot)
+        r = orc.shot(i, 0, src, rec)
+        for f in ex["rfields"]:
+            out[f].append(r[f])
+    res = {f: np.stack(v) for f, v in out.items()}
+    if return_oracle:
+        return res, orc
+    orc.close()
+    return res
+
+
+def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True):
+    """gradient!(g, m, L2DistLoss(), dobs, pa) for 2-D acoustic
+    (src/fdtd/func_grad.jl:11-49).  Returns (loss, {"invK": g, "rho": g},
+    dcal) with g the chain-ruled gradient on the inner (non-PML) grid and the
+    raw per-cell accumulations on the extended grid."""
+    prep = Prepared(ex, dtype, ref_compat)
+    orc = Oracle(prep, nthreads)
+    shape = prep.shape
+    gK = np.zeros(shape, dtype=dtype, order="F")
+    gR = np.zeros(shape, dtype=dtype, order="F")
+    dcal = {f: [] for f in ex["rfields"]}
+    # forward_save with src_types [1, 0]
+    for i, shot in enumerate(ex["shots"]):
+        src, rec = _shot_inputs(prep, shot, 1)
+        r = orc.shot(i, 1, src, rec)
+        for f in ex["rfields"]:
+            dcal[f].append(r[f])
+    dcal = {f: np.stack(v) for f, v in dcal.items()}
+    loss = sum(S.l2_value(dobs[f], dcal[f]) for f in ex["rfields"])
+    # adjoint with src_types [-1, 1]
+    for i, shot in enumerate(ex["shots"]):
+        src, _ = _shot_inputs(prep, shot, -1)
+        adj = []
+        for f in ex["rfields"]:
+            a = S.l2_deriv(dobs[f][i], dcal[f][i])[::-1].copy()
+            adj.append((f, prep.proj(f, shot["rec"]), a))
+        orc.shot(i, 2, src, [], adj, (gK, gR))
+    orc.close()
+    raw = {"invK": gK.copy(), "rho": gR.copy()}
+    inner = []
+    names = "zyx" if prep.ndim == 3 else "zx"
+    for i, d in enumerate(names):
+        lo = prep.npml if prep.faces & S.FACE_BITS[d + "min"] else 0
+        hi = prep.npml if prep.faces & S.FACE_BITS[d + "max"] else 0
+        inner.append(slice(lo, shape[i] - hi))
+    inner = tuple(inner)
+    g = {"invK": (raw["invK"] * prep.mod[0])[inner], "rho": (raw["rho"] * prep.mod[1])[inner]}
+    return loss, g, dcal, raw
