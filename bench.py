@@ -1,0 +1,294 @@
+"""Benchmark of the GB300 FDTD engine.
+
+Workload (N = 1): the 2-D elastic P-SV batch -- 1000 x 3000 cells at 5 m,
+40-cell CPML (43 padded cells per face as in the reference), 16 shots,
+4000 steps, Ricker 12 Hz explosive sources, 601 vx/vz receivers per shot.
+One bench step is one full forward modelling of the batch (update!(pa)).
+
+  value  Gcell-updates/s with all inputs resident on the GPU (gpi_run only)
+  e2e    the same metric through the public API with host buffers: upload
+         of the medium and wavelets, the run, download of all records
+  roofline  algorithmic bytes (60 B per cell update) / kernel time against
+         the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (C restatement of the reference, OpenMP on
+         all host cores) on a bounded sample of the same workload
+
+--impl reference times the CPU restatement of the reference on the host
+cores (the reference is Julia and cannot run here).  Multi-GPU: one process
+per GPU, each rank models its own batch of shots (shots are independent,
+weak scaling, no data-path collective).
+"""
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "geophyinv.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Gcell-updates/s"
+BYTES_PER_CELL = 60  # elastic 2-D: 4 B x (2 x 5 state + 5 coefficient arrays)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--nt", type=int, default=4000)
+    ap.add_argument("--nshots", type=int, default=16)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(nt, nshots):
+    from geophyinv_gb300 import configs
+
+    return configs.elastic2d_batch(nt=nt, nshots=nshots)
+
+
+def config_json(wl, n_gpus):
+    return {"workload": "elastic2d_psv_1000x3000_5m_16shots_4000steps",
+            "grid": [len(g) for g in wl.grid], "extended_grid": [len(g) + 86 for g in wl.grid],
+            "shots_per_gpu": len(wl.shots), "nt": wl.nt, "dt": wl.tgrid.step, "order": 4,
+            "receivers_per_shot": len(wl.shots[0][1]), "rfields": wl.rfields,
+            "parallelism": "shot replicas x%d" % n_gpus,
+            "l2": "not flushed: per-step working set %.2f GB >> 129 MB L2" % (
+                2 * 5 * wl.cells() * len(wl.shots) * 4 / 1e9)}
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_cell():
+    """DRAM bytes per cell update of the step kernel from the committed ncu
+    summary (a line 'dram_bytes_per_cell_update: X'), or None."""
+    path = os.path.join(ROOT, "profiles", "elastic2d_step_kernel.md")
+    try:
+        m = re.search(r"dram_bytes_per_cell_update:\s*([0-9.]+)", open(path).read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def cpu_sample(nt_cap=None, target_s=12.0):
+    """The CPU oracle (all host threads) on one shot of the workload for a
+    bounded number of time steps; returns (Gcell-updates/s, threads, sample)."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+
+    def run(nt):
+        wl = workload(nt, 1)
+        ex = wl.as_dict()
+        prep = O.Prepared(ex, np.float32)
+        orc = O.Oracle(prep, nthreads=threads)
+        src, rec = O._shot_inputs(prep, ex["shots"][0])
+        t0 = time.perf_counter()
+        orc.shot(0, 0, src, rec)
+        t = time.perf_counter() - t0
+        cells = int(np.prod(prep.shape))
+        orc.close()
+        return cells, t
+
+    cells, t = run(4)
+    per_step = t / 4
+    nt = int(max(8, min(nt_cap or 400, target_s / max(per_step, 1e-6))))
+    cells, t = run(nt)
+    rate = cells * nt / t / 1e9
+    return rate, threads, "1 of 16 shots, %d of 4000 steps, %d extended cells, %.1f s" % (nt, cells, t)
+
+
+def engine_arm(args, rank, world, local):
+    import torch
+
+    from geophyinv_gb300 import _lib, update
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    wl = workload(args.nt, args.nshots)
+    pa = wl.expt(stream=stream.cuda_stream)
+    medium = wl.medium()
+    srcwav = wl.srcwav()
+    cells = pa.nss * int(np.prod([len(g) for g in pa.exgrid]))
+    units = cells * pa.nt  # cell updates per bench step on this rank
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # --- value: inputs resident, one gpi_run per step ---
+    for _ in range(args.warmup):
+        pa.run(_lib.FORWARD)
+    barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        pa.run(_lib.FORWARD)
+        launches += pa.launches()
+    ev1.record(stream)
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop()
+    ms = max_over_ranks(ms)
+    value = world * units / (ms * 1e-3) / 1e9
+
+    # --- e2e: public API, host buffers in and out, every step ---
+    update(pa, medium)
+    update(pa, srcwav, [1])
+    update(pa)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        update(pa, medium)        # H2D medium (padding, derived parameters)
+        update(pa, srcwav, [1])   # H2D wavelets and spray matrices
+        update(pa)                # run + D2H records
+    barrier()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+    e2e = world * units / (e2e_ms * 1e-3) / 1e9
+    h2d = sum(int(np.prod(v.shape)) * 4 for v in pa.mod.values()) + sum(
+        s.d[f].size * 4 for s in srcwav for f in s.fields)
+    d2h = sum(pa.data[0][i].d[f].size * 4 for i in range(pa.nss) for f in pa.rfields)
+
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_CELL * cells / (ms * 1e-3 / pa.nt) / 1e9  # per launch, all time charged to it
+    tpc = traffic_per_cell()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded gradient + smoothed perturbation model)",
+        "config": config_json(wl, world),
+        "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4),
+                     "traffic": None if tpc is None else round(tpc * cells),
+                     "kernel": "k_e2 (fused elastic step), algorithmic 60 B/cell, launch time = run time / nt",
+                     "peak_source": peak_kind + " hbm_gbs"},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    return line, dist
+
+
+def reference_arm(args):
+    """CPU restatement of the reference (the oracle) on all host cores."""
+    rates = []
+    sample = ""
+    threads = os.cpu_count() or 1
+    for i in range(args.warmup + args.steps):
+        rate, threads, sample = cpu_sample(nt_cap=60, target_s=6.0)
+        if i >= args.warmup:
+            rates.append(rate)
+    v = float(np.mean(rates))
+    return {"metric": METRIC, "value": round(v, 4), "unit": "Gcell/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "elastic2d_psv_1000x3000_5m_16shots_4000steps", "sample": sample},
+            "cpu_baseline": {"value": round(v, 4), "unit": "Gcell/s", "cores": threads, "kind": "port",
+                             "sample": sample + "; C restatement of the reference time loop (Julia is absent)"},
+            "e2e": {"value": round(v, 4), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference_arm(args)))
+        return
+    line, dist = engine_arm(args, rank, world, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            rate, threads, sample = cpu_sample()
+            line["cpu_baseline"] = {"value": round(rate, 4), "unit": "Gcell/s", "cores": threads, "kind": "port",
+                                    "sample": sample}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -136,6 +136,9 @@ __global__ void k_aux(AuxArgs a) {
     // record!: p is sampled before step it, velocities after step it-1
     const RecTask t = a.tasks[i];
     const bool isv = t.field == GPI_VX || t.field == GPI_VY || t.field == GPI_VZ;
+    // the reference records p (before the step) and velocities (after the
+    // velocity sources) only; other rfields keep their zero records
+    if (!isv && t.field != GPI_P) return;
     const int tidx = isv ? a.it - 2 : a.it - 1;
     if (tidx < 0 || tidx >= a.nt) return;
     if (!isv && a.it > a.nt) return;

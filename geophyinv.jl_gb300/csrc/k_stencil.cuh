@@ -1,0 +1,67 @@
+// k_stencil.cuh -- device helpers shared by the fused step kernels.
+#pragma once
+#include "gpi_internal.cuh"
+
+namespace gpi {
+
+// 4th-order staggered difference 27 a2 - 27 a1 + a0 - a3
+// (@d_?a / @d_?i at order 4, src/fdtd/diff2D.jl:62-97)
+__device__ __forceinline__ float st4(float a0, float a1, float a2, float a3) {
+  return a2 * 27.0f - a1 * 27.0f + a0 - a3;
+}
+
+// CPML strip slot of derivative index i (1-based) on an axis of length nd,
+// -1 outside the strips (memory{x,y,z}!, src/fdtd/cpml.jl:184-211)
+__device__ __forceinline__ int pml_slot(int i, int nd, int npml, bool lo, bool hi) {
+  if (lo && i <= npml) return i - 1;
+  if (hi && i > nd - npml) return npml + i - (nd - npml) - 1;
+  return -1;
+}
+
+// psi = b psi + a d ; d = d kI + psi   (src/fdtd/cpml.jl:175-182)
+// pm points at this derivative's [a | b | kI] blocks of 2*npml each.
+__device__ __forceinline__ float cpml(float D, const float *pm, int npml, int j, const float *psA, float *psB,
+                                      int64_t po, bool own) {
+  const float psi = pm[2 * npml + j] * psA[po] + pm[j] * D;
+  if (own) psB[po] = psi;
+  return D * pm[4 * npml + j] + psi;
+}
+
+// binary search of the first injection cell with column >= col in [lo, hi)
+__device__ __forceinline__ int first_col(const InjCell *cells, int lo, int hi, int col) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (cells[mid].col < col)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Per-kind cursor over injection cells sorted by column: every thread of a
+// block walks the same cells column by column.
+struct InjCursor {
+  int cur, end, ncol;
+  __device__ __forceinline__ void init(const InjCell *cells, int b, int e) {
+    cur = b;
+    end = e;
+    ncol = cur < end ? cells[cur].col : 0x7fffffff;
+  }
+  // returns the [b, e) range of cells in column `col` and advances past it
+  __device__ __forceinline__ void range(const InjCell *cells, int col, int &b, int &e) {
+    b = cur;
+    if (ncol == col) {
+      while (cur < end && cells[cur].col == col) cur++;
+      ncol = cur < end ? cells[cur].col : 0x7fffffff;
+    }
+    e = cur;
+  }
+};
+
+__device__ __forceinline__ void inject(const InjCell *cells, const float *amount, int b, int e, int row, float &v) {
+  for (int k = b; k < e; k++)
+    if (cells[k].row == row) v = v + amount[k];
+}
+
+}  // namespace gpi

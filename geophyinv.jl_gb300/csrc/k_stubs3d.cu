@@ -10,8 +10,5 @@ int step_acoustic3d(Plan *p, int, int, int, int) {
 int step_elastic3d(Plan *p, int, int, int, int) {
   return fail(p, GPI_E_UNSUPPORTED, "3-D elastic kernels are not part of this build");
 }
-int step_elastic2d(Plan *p, int, int, int, int) {
-  return fail(p, GPI_E_UNSUPPORTED, "2-D elastic kernels are not part of this build");
-}
 
 }  // namespace gpi

@@ -49,6 +49,34 @@ def test_acoustic2d_full_config_matches_oracle(engine):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("surface", ["pml", "free"])
+def test_elastic2d_batch_matches_oracle(engine, surface):
+    """Reduced 2-D elastic batch: 3 surface shots, explosive tauxx source,
+    vx/vz records; with a PML top or a stress-free top (free_surface!)."""
+    wl = configs.elastic2d_batch(nz=110, nx=190, nt=400, nshots=3, nrec=31)
+    if surface == "free":
+        wl.pml_faces = ["zmax", "xmin", "xmax"]
+        wl.stressfree_faces = ["zmin"]
+    ref, orc = O.forward(wl.as_dict(), return_oracle=True)
+    pa = wl.expt()
+    update(pa)
+    _compare_records(pa, ref, wl)
+    for f in ("tauxx", "tauzz", "tauxz", "vx", "vz"):
+        e = rel(pa.field(f, iss=2), orc.field(f))
+        assert e < TOL, (f, e)
+    orc.close()
+
+
+@pytest.mark.gpu
+def test_elastic2d_velocity_source(engine):
+    wl = configs.elastic2d_batch(nz=100, nx=140, nt=300, nshots=2, nrec=19, src_field="vz")
+    ref = O.forward(wl.as_dict())
+    pa = wl.expt()
+    update(pa)
+    _compare_records(pa, ref, wl)
+
+
+@pytest.mark.gpu
 def test_acoustic2d_multishot_velocity_sources(engine):
     """Several supersources batched in one launch, vz sources, no PML on top
     (rigid faces = pml faces only), records of every shot."""
