@@ -124,6 +124,34 @@ int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int 
 /* Number of engine kernel launches issued by the last gpi_run. */
 int gpi_last_launches(const gpi_plan *plan, int64_t *launches);
 
+/* Size of the device scratch array used by gpi_forward_acoustic2d_noalloc. */
+#define GPI_NOALLOC_SCRATCH_BYTES (64u << 20)
+
+/* A complete 2-D acoustic forward run (one shot, order 4) that allocates no
+ * device memory.  No counterpart in the reference: it is for hosts that
+ * cannot call cudaMalloc while they model -- a process whose HBM budget is
+ * reserved up front by its own pool allocator, or a latency-critical loop
+ * that must not hit cudaMalloc/cudaFree, which can synchronise the device.
+ * All intermediates live in one static device array of
+ * GPI_NOALLOC_SCRATCH_BYTES per GPU (held until the process exits); larger
+ * problems are rejected with GPI_E_INVALID.  Calls share that array: calls
+ * that overlap on the GPU race.  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture begins.
+ *   desc      physics GPI_ACOUSTIC, ndim 2, order 4, nshots 1, npw 1
+ *   invK, rho device, extended grid, column-major (nz*nx each)
+ *   pml       device, 4 x 3 x 2*npml floats: a, b, kI of dpdx, dpdz, dvxdx, dvzdz
+ *   src_*     one spray matrix (host CSC, as gpi_set_sources) on src_field
+ *             (GPI_P, GPI_VX or GPI_VZ); wavelets: device, nt x ns
+ *   rfields   nrf (<= 3) receiver fields among p, vx, vz, each with nr[k]
+ *             (<= 4096) receivers as host CSC; records[k]: device, nt x nr[k]
+ * Asynchronous on `stream` (cudaStream_t) after the table uploads. */
+int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const float *invK, const float *rho, const float *pml,
+                                   int src_field, int ns, const int64_t *src_colptr, const int64_t *src_rowval,
+                                   const float *src_nzval, const float *wavelets, int nrf, const int *rfields,
+                                   const int *nr, const int64_t *const *rec_colptr, const int64_t *const *rec_rowval,
+                                   const float *const *rec_nzval, float *const *records, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
