@@ -128,6 +128,12 @@ struct Plan {
   int32_t *d_group_ptr = nullptr;
 
   int64_t launches = 0;
+  int *d_err = nullptr;
+  // tiles of the 2-D step kernels: interior tiles first (straight-line
+  // kernel), then the tiles that meet a strip, a face or a source
+  int3 *d_tiles = nullptr;
+  int n_tiles_fast = 0, n_tiles_gen = 0;
+  std::vector<InjCell> h_cells;  // set by a kernel whose pipeline wait gave up
 };
 
 // error helpers
@@ -148,6 +154,10 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
+int step_adjoint_acoustic2d(Plan *p, int it);
+// host: classify the (z-block, x-chunk, shot) tiles of a 2-D plan; writes
+// interior tiles first; returns the tile count (or -1 beyond `cap`)
+int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast);
 int aux_step(Plan *p, int it, int mode);
 int compute_coefficients(Plan *p);
 int boundary_io(Plan *p, int it, int dir);

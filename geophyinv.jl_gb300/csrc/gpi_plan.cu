@@ -88,7 +88,9 @@ static void choose_tiling(Plan &p) {
     p.TY = 1;
     p.nzb = (p.d.nz + p.TZ - 1) / p.TZ;
     p.nyb = 1;
-    int resident = sms * 8;  // blocks resident at once (128 threads, <= 64 regs)
+    // blocks resident at once (160 threads; shared memory: acoustic 34 KB,
+    // elastic 50 KB per block)
+    int resident = sms * (p.d.physics == GPI_ACOUSTIC ? 6 : 4);
     int per_chunk = p.nzb * p.d.nshots;
     int best = 1;
     double best_eff = 0;
@@ -215,6 +217,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   for (int i = 0; i < p.nmod; i++) allocs.push_back({&p.mod[i], p.fstride});
   for (int i = 0; i < p.ncoef; i++) allocs.push_back({&p.coef[i], p.fstride});
   allocs.push_back({&p.pml, (int64_t)p.nder * 3 * 2 * d.npml});
+  allocs.push_back({(float **)&p.d_err, 64});
   if (d.npw == 2) {
     for (int i = 0; i < p.nmod && i < 2; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
     int ids[3];
@@ -289,6 +292,8 @@ static void free_sources(Plan &p) {
   free_dev((void *&)p.d_wav_ns);
   free_dev((void *&)p.d_amount);
   free_dev((void *&)p.d_group_ptr);
+  free_dev((void *&)p.d_tiles);
+  p.h_cells.clear();
   for (auto b : p.wav_bufs) cudaFree(b);
   p.wav_bufs.clear();
   p.n_cells = 0;
@@ -619,6 +624,7 @@ static int compile_sources(Plan &p) {
   }
   p.group_ptr[groups.size()] = (int32_t)cells.size();
   p.n_cells = (int)cells.size();
+  p.h_cells = cells;
   GPI_CUDA(&p, cudaMalloc(&p.d_group_ptr, p.group_ptr.size() * sizeof(int32_t)));
   GPI_CUDA(&p, cudaMemcpy(p.d_group_ptr, p.group_ptr.data(), p.group_ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   if (p.n_cells) {
@@ -637,6 +643,56 @@ static int compile_sources(Plan &p) {
     GPI_CUDA(&p, cudaMemcpy(p.d_wav_ns, wavns.data(), wavns.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   }
   p.src_dirty = false;
+  return GPI_OK;
+}
+
+
+// A tile is interior when every cell it computes lies inside all update
+// domains, outside every CPML strip and away from mirror rows/columns, and
+// no source cell of its shot falls in its columns (src/fdtd/cpml.jl:184-211,
+// src/fdtd/dirichlet.jl:1-79 give the affected rows and columns).
+int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast) {
+  const int n = p.nzb * p.nxb * p.d.nshots;
+  if (n > cap) return -1;
+  const int npml = p.d.npml, nz = p.d.nz, nx = p.d.nx;
+  int k = 0, g = n;
+  for (int shot = 0; shot < p.d.nshots; shot++)
+    for (int xb = 0; xb < p.nxb; xb++)
+      for (int zb = 0; zb < p.nzb; zb++) {
+        const int z0 = 1 + zb * p.TZ, x0 = 1 + xb * p.L, x1 = std::min(x0 + p.L, nx + 1);
+        bool fast = z0 >= npml + 4 && z0 + p.TZ + 2 <= nz - npml - 3 && x0 >= npml + 4 && x1 + 2 <= nx - npml - 3;
+        for (int ipw = 0; fast && ipw < p.d.npw; ipw++)
+          for (int kind = 0; fast && kind < NKIND; kind++) {
+            const int gi = (ipw * p.d.nshots + shot) * NKIND + kind;
+            for (int c = gptr[gi]; c < gptr[gi + 1]; c++)
+              if (cells[c].col >= x0 - 3 && cells[c].col <= x1 + 3) {
+                fast = false;
+                break;
+              }
+          }
+        if (fast)
+          out[k++] = make_int3(zb, xb, shot);
+        else
+          out[--g] = make_int3(zb, xb, shot);
+      }
+  *nfast = k;
+  return n;
+}
+
+static int build_tiles(Plan &p) {
+  const int n = p.nzb * p.nxb * p.d.nshots;
+  std::vector<int3> t(n);
+  int nf = 0;
+  const int32_t *gp = p.group_ptr.empty() ? nullptr : p.group_ptr.data();
+  std::vector<int32_t> zero(2 * p.d.nshots * NKIND + 1, 0);
+  if (classify_tiles(p, p.h_cells.data(), gp ? gp : zero.data(), t.data(), n, &nf) < 0)
+    return fail(&p, GPI_E_INVALID, "tile list");
+  if (p.d_tiles) cudaFree(p.d_tiles);
+  p.d_tiles = nullptr;
+  GPI_CUDA(&p, cudaMalloc(&p.d_tiles, n * sizeof(int3)));
+  GPI_CUDA(&p, cudaMemcpy(p.d_tiles, t.data(), n * sizeof(int3), cudaMemcpyHostToDevice));
+  p.n_tiles_fast = nf;
+  p.n_tiles_gen = n - nf;
   return GPI_OK;
 }
 
@@ -676,7 +732,11 @@ int run(Plan &p, int mode) {
   if (dev != p.device) GPI_CUDA(&p, cudaSetDevice(p.device));
   int rc = GPI_OK;
   if (p.rec_dirty) rc = compile_receivers(p);
-  if (!rc && p.src_dirty) rc = compile_sources(p);
+  if (!rc && p.src_dirty) {
+    rc = compile_sources(p);
+    if (!rc && p.d.ndim == 2) rc = build_tiles(p);
+  }
+  if (!rc && p.d.ndim == 2 && !p.d_tiles) rc = build_tiles(p);
   if (!rc) rc = zero_state(p);
   p.launches = 0;
   if (!rc && p.rec_pool) rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
@@ -706,21 +766,37 @@ int run(Plan &p, int mode) {
   return rc;
 }
 
+// a kernel reports a pipeline wait that gave up through d_err
+static int check_err(Plan &p) {
+  int h = 0;
+  GPI_CUDA(&p, cudaMemcpy(&h, p.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    cudaMemset(p.d_err, 0, sizeof(int));
+    return fail(&p, GPI_E_CUDA, "a kernel's copy pipeline timed out; results of the last run are invalid");
+  }
+  return GPI_OK;
+}
+
+int transpose_records(Plan *p, float *out, const float *in, int nt, int nr);  // k_common.cu
+
 int get_records(Plan &p, int shot, int field, float *out, int on_device) {
   if (shot < 0 || shot >= p.d.nshots || field < 0 || field >= NFIELD) return fail(&p, GPI_E_INVALID, "shot/field");
   const int nr = p.rec_n[shot][field];
   if (nr <= 0 || p.rec_base[shot][field] < 0) return fail(&p, GPI_E_STATE, "no receivers for this field (or no run yet)");
   const int nt = p.d.nt;
   const float *src = p.rec_pool + p.rec_base[shot][field];
-  // pool layout [it][ir] -> Recs layout (it fastest): a pitched 2-D transpose
-  // done as nr strided copies keeps this call allocation-free
-  for (int ir = 0; ir < nr; ir++) {
-    GPI_CUDA(&p, cudaMemcpy2DAsync(out + (size_t)ir * nt, sizeof(float), src + ir, (size_t)nr * sizeof(float),
-                                   sizeof(float), nt, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                   p.stream));
-  }
-  if (!on_device) GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
-  return GPI_OK;
+  // pool layout [it][ir] -> Recs layout (it fastest)
+  if (on_device) return transpose_records(&p, out, src, nt, nr);
+  float *tmp = nullptr;
+  GPI_CUDA(&p, cudaMallocAsync(&tmp, (size_t)nt * nr * sizeof(float), p.stream));
+  int rc = transpose_records(&p, tmp, src, nt, nr);
+  if (!rc) rc = cudaMemcpyAsync(out, tmp, (size_t)nt * nr * sizeof(float), cudaMemcpyDeviceToHost, p.stream)
+                    ? fail(&p, GPI_E_CUDA, "records copy")
+                    : GPI_OK;
+  cudaFreeAsync(tmp, p.stream);
+  if (rc) return rc;
+  GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  return check_err(p);
 }
 
 int get_field(Plan &p, int ipw, int shot, int field, float *out, int on_device) {
@@ -731,7 +807,10 @@ int get_field(Plan &p, int ipw, int shot, int field, float *out, int on_device) 
   const float *src = p.state[p.cur[ipw - 1]][ipw - 1][field] + p.fstride * shot;
   int rc = from_storage(p, out, src, n[0], n[1], n[2], on_device);
   if (rc) return rc;
-  if (!on_device) GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  if (!on_device) {
+    GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+    return check_err(p);
+  }
   return GPI_OK;
 }
 

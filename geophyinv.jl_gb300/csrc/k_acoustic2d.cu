@@ -13,17 +13,16 @@
 //   p[r, c]  += (D_x(vx[r, c..c+3]) + D_z(vz[r..r+3, c])) * dtK
 // with D(a0..a3) = 27 a2 - 27 a1 + a0 - a3 scaled by 1/(24 d).
 //
-// Work decomposition: a block owns TZ rows x L columns of p of one shot and
-// sweeps its columns left to right.  Pressure columns live in an 8-column
-// shared-memory ring (rows z0-3 .. z0+TZ+2), the four vx columns the
-// x-derivative needs live in registers, the TZ+3 vz values of the current
-// column in shared memory.  The 3 vx columns right of the tile and the 3 vz
-// rows below it are recomputed from the input buffer instead of exchanged,
-// so the state is ping-ponged between two buffers and a step is one pass
-// over HBM: read p, vx, vz, cx, cz, dtK, write p, vx, vz (36 B per cell).
-#include <climits>
-
-#include "gpi_internal.cuh"
+// Work decomposition (same scheme as the elastic kernel): a block owns TZ
+// rows x L columns of p of one shot and sweeps its columns; one producer
+// thread streams each input column (p over rows z0-4..z0+TZ+3; vx, vz, cx, cz
+// over z0..z0+TZ+3; dtK over z0..z0+TZ-1) into an 8-slot shared-memory ring
+// with bulk asynchronous copies completing on mbarriers, four columns ahead.
+// Interior tiles run a straight-line path; tiles that touch a CPML strip, a
+// rigid face or a source run the general path with the CPML memory loaded
+// ahead of use.  Halo velocities are recomputed from the input buffer
+// (ping-pong state): one HBM pass per step, 36 B per cell update.
+#include "k_stencil.cuh"
 
 namespace gpi {
 
@@ -31,13 +30,12 @@ struct A2Args {
   int nz, nx, NZP;
   int64_t fs;
   int npml, faces, rigid;
-  float dxI, dzI, dtI;
-  int L, nzb, nxb, nshots;
-  // wavefield 1 (and 2 in adjoint mode): read buffer A, write buffer B
-  const float *pA[2], *vxA[2], *vzA[2];
-  float *pB[2], *vxB[2], *vzB[2];
-  const float *psA[2][4];
-  float *psB[2][4];
+  float dxI, dzI;
+  int L, nzb, nxb;
+  const float *pA, *vxA, *vzA;
+  float *pB, *vxB, *vzB;
+  const float *psA[4];
+  float *psB[4];
   int64_t pss[4];
   const float *cx, *cz, *dtK;
   const float *pml;  // [4][3][2*npml]
@@ -45,230 +43,347 @@ struct A2Args {
   const int32_t *gptr;
   const float *amount;
   int vonly;
-  // adjoint extras
-  const float *bstore;  // this step's strips (shot 0), x strips then z strips
-  int64_t bsstride;
-  int npx, npz, nb;
-  float *gK, *gR;
-  float *bufx, *bufz;   // gradient scratch (vx/vz "velocity_buffer" of wavefield 1)
+  int *err;
+  const int3 *tiles;  // (z-block, x-chunk, shot) per block
 };
 
-__device__ __forceinline__ float st4(float a0, float a1, float a2, float a3) {
-  return a2 * 27.0f - a1 * 27.0f + a0 - a3;
-}
+constexpr int A2_TZ = 128;
+constexpr int A2_THREADS = A2_TZ + 32;
+constexpr int A2_R8 = A2_TZ + 8;                       // p rows z0-4 .. z0+TZ+3
+constexpr int A2_R4 = A2_TZ + 4;                       // velocity-input rows z0 .. z0+TZ+3
+constexpr int A2_SLOT = A2_R8 + 4 * A2_R4 + A2_TZ;     // floats per ring slot
+constexpr size_t A2_SMEM = 128 + sizeof(float) * (8 * A2_SLOT + 2 * 8 * A2_R4);
 
-// CPML strip slot of derivative index i (1-based) on an axis of length nd
-__device__ __forceinline__ int pml_slot(int i, int nd, int npml, bool lo, bool hi) {
-  if (lo && i <= npml) return i - 1;
-  if (hi && i > nd - npml) return npml + i - (nd - npml) - 1;
-  return -1;
-}
-
-// psi = b psi + a d ; d = d kI + psi   (memory{x,z}!, src/fdtd/cpml.jl:175-182)
-__device__ __forceinline__ float cpml(float D, const float *pm, int npml, int j, const float *psA, float *psB,
-                                      int64_t po, bool own) {
-  const float psi = pm[2 * npml + j] * psA[po] + pm[j] * D;
-  if (own) psB[po] = psi;
-  return D * pm[4 * npml + j] + psi;
-}
-
-template <int TZ>
-__global__ void __launch_bounds__(TZ) k_a2_forward(const A2Args a) {
-  __shared__ float sp[8][TZ + 6];
-  __shared__ float svz[2][TZ + 4];
-  __shared__ int s_cur[3], s_end[3];
+template <bool FAST>
+__global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
+  constexpr int TZ = A2_TZ, R8 = A2_R8, R4 = A2_R4, SLOT = A2_SLOT;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+  float *ring = reinterpret_cast<float *>(smem + 128);  // [8][SLOT]: p | vx vz cx cz | dtK
+  float *svx = ring + 8 * SLOT;                          // [8][R4] new velocities
+  float *svz = svx + 8 * R4;
+  __shared__ int s_rng[3][2];
+  __shared__ int s_err;
   const int t = threadIdx.x;
-  int bid = blockIdx.x;
-  const int zb = bid % a.nzb;
-  bid /= a.nzb;
-  const int xb = bid % a.nxb;
-  const int shot = bid / a.nxb;
+  const int3 tile = a.tiles[blockIdx.x];
+  const int zb = tile.x, xb = tile.y, shot = tile.z;
   const int z0 = 1 + zb * TZ, x0 = 1 + xb * a.L;
   const int x1 = min(x0 + a.L, a.nx + 1);
+  const int xbase = x0 - 3, xlast = x1 + 2;
   const bool lastx = xb == a.nxb - 1, lastz = zb == a.nzb - 1;
   const int nz = a.nz, nx = a.nx, npml = a.npml, NZP = a.NZP;
   const int64_t so = (int64_t)shot * a.fs;
-  const float *__restrict__ pA = a.pA[0] + so;
-  const float *__restrict__ vxA = a.vxA[0] + so;
-  const float *__restrict__ vzA = a.vzA[0] + so;
-  float *__restrict__ pB = a.pB[0] + so;
-  float *__restrict__ vxB = a.vxB[0] + so;
-  float *__restrict__ vzB = a.vzB[0] + so;
   const bool xlo = a.faces & GPI_XMIN, xhi = a.faces & GPI_XMAX, zlo = a.faces & GPI_ZMIN, zhi = a.faces & GPI_ZMAX;
   const bool rxlo = a.rigid & GPI_XMIN, rxhi = a.rigid & GPI_XMAX, rzlo = a.rigid & GPI_ZMIN, rzhi = a.rigid & GPI_ZMAX;
-  const float *psA[4];
-  float *psB[4];
-#pragma unroll
-  for (int q = 0; q < 4; q++) {
-    psA[q] = a.psA[0][q] ? a.psA[0][q] + shot * a.pss[q] : nullptr;
-    psB[q] = a.psB[0][q] ? a.psB[0][q] + shot * a.pss[q] : nullptr;
-  }
-  const float *pm0 = a.pml, *pm1 = a.pml + 6 * npml, *pm2 = a.pml + 12 * npml, *pm3 = a.pml + 18 * npml;
-  const int r = z0 + t;
+  const int P6 = 6 * npml;
   auto S = [&](int rr, int cc) -> int64_t { return (int64_t)(cc + XOFF - 1) * NZP + (rr + ZOFF - 1); };
+  auto XS = [&](int j, int rr) -> int64_t { return (int64_t)j * NZP + (rr + ZOFF - 1); };
+  auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * 2 * npml + j; };
+  auto psA = [&](int i) -> const float * { return a.psA[i] + shot * a.pss[i]; };
+  auto psB = [&](int i) -> float * { return a.psB[i] + shot * a.pss[i]; };
+  auto slot = [&](int cc) -> int { return (cc - xbase) & 7; };
 
-  // injection cursors (cells sorted by column) for vx, vz and p
+  if (t == 0) {
+    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 1);
+    mbar_fence_init();
+    s_err = 0;
+  }
   if (t < 3) {
     const int kind = t == 0 ? 0 : t == 1 ? 2 : 3;
     const int g = shot * NKIND + kind;
-    int lo = a.gptr[g], hi = a.gptr[g + 1];
-    const int end = hi;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (a.cells[mid].col < x0)
-        lo = mid + 1;
-      else
-        hi = mid;
-    }
-    s_cur[t] = lo;
-    s_end[t] = end;
+    s_rng[t][0] = first_col(a.cells, a.gptr[g], a.gptr[g + 1], x0);
+    s_rng[t][1] = a.gptr[g + 1];
   }
-
-  auto load_p = [&](int cc) {
-    float *dst = sp[cc & 7];
-    for (int k = t; k < TZ + 6; k += TZ) dst[k] = pA[S(z0 - 3 + k, cc)];
-  };
-  // vx before the source (update_v! incl. CPML of dpdx)
-  auto vx_upd = [&](int cc, bool own) -> float {
-    const int64_t o = S(r, cc);
-    float v = vxA[o];
-    if (r >= 4 && r <= nz - 3 && cc >= 4 && cc <= nx) {
-      float D = st4(sp[(cc - 3) & 7][t + 3], sp[(cc - 2) & 7][t + 3], sp[(cc - 1) & 7][t + 3], sp[cc & 7][t + 3]) * a.dxI;
-      const int j = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
-      if (j >= 0) D = cpml(D, pm0, npml, j, psA[0], psB[0], (int64_t)j * NZP + (r + ZOFF - 1), own);
-      v = v + a.cx[o] * D;
-    }
-    return v;
-  };
-  auto vz_upd = [&](int q, int cc, bool own) -> float {
-    const int64_t o = S(q, cc);
-    float v = vzA[o];
-    if (q >= 4 && q <= nz && cc >= 4 && cc <= nx - 3) {
-      const float *col = sp[cc & 7];
-      const int k = q - z0;
-      float D = st4(col[k], col[k + 1], col[k + 2], col[k + 3]) * a.dzI;
-      const int j = pml_slot(q - 3, nz - 3, npml, zlo, zhi);
-      if (j >= 0) D = cpml(D, pm1, npml, j, psA[1], psB[1], (int64_t)(cc + XOFF - 1) * 2 * npml + j, own);
-      v = v + a.cz[o] * D;
-    }
-    return v;
-  };
-  auto inj = [&](int b, int e, int row, float &v) {
-    if (a.vonly) return;  // the extra half step after the loop adds no sources
-    for (int k = b; k < e; k++)
-      if (a.cells[k].row == row) v = v + a.amount[k];
-  };
-
   __syncthreads();
-  int cur0 = s_cur[0], end0 = s_end[0], cur1 = s_cur[1], end1 = s_end[1], cur2 = s_cur[2], end2 = s_end[2];
-  int ncol0 = cur0 < end0 ? a.cells[cur0].col : INT_MAX;
-  int ncol1 = cur1 < end1 ? a.cells[cur1].col : INT_MAX;
-  int ncol2 = cur2 < end2 ? a.cells[cur2].col : INT_MAX;
-  auto range = [&](int &cur, int end, int &ncol, int col, int &b, int &e) {
-    b = cur;
-    if (ncol == col) {
-      while (cur < end && a.cells[cur].col == col) cur++;
-      ncol = cur < end ? a.cells[cur].col : INT_MAX;
+
+  const bool producer = t == TZ;
+  int next = xbase;
+  auto issue = [&](int upto) {
+    for (; next <= upto && next <= xlast; next++) {
+      const int s = slot(next);
+      float *sl = ring + s * SLOT;
+      mbar_expect_tx(&bar[s], SLOT * 4);
+      const int64_t oV = S(z0, next);
+      bulk_g2s(sl, a.pA + so + S(z0 - 4, next), R8 * 4, &bar[s]);
+      float *v = sl + R8;
+      bulk_g2s(v + 0 * R4, a.vxA + so + oV, R4 * 4, &bar[s]);
+      bulk_g2s(v + 1 * R4, a.vzA + so + oV, R4 * 4, &bar[s]);
+      bulk_g2s(v + 2 * R4, a.cx + oV, R4 * 4, &bar[s]);
+      bulk_g2s(v + 3 * R4, a.cz + oV, R4 * 4, &bar[s]);
+      bulk_g2s(v + 4 * R4, a.dtK + oV, TZ * 4, &bar[s]);
     }
-    e = cur;
+  };
+  if (producer) issue(xbase + 7);
+  auto wait_col = [&](int cc) {
+    const int j = cc - xbase;
+    if (!mbar_wait(&bar[j & 7], (j >> 3) & 1)) s_err = 1;
   };
 
-  const bool rown = r <= nz;  // vx and p rows
-  float vpre_nx = 0.f;        // vx[r, nx] before its source (xmax mirror)
-  float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f;
-  // one vx column: update, mirrors, source, store
-  auto vx_col = [&](int cc, float um3, float um2) -> float {
-    // um3 / um2: vx at cc-2 / cc-1 (only used by the xmax mirror)
-    const bool own = rown && cc >= x0 && (cc < x1 || lastx);
-    float v;
-    if (rxhi && cc >= nx + 2) {
-      v = cc == nx + 3 ? -vpre_nx : -um2;  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
-    } else {
-      v = vx_upd(cc, own);
-      if (cc == nx) vpre_nx = v;
-    }
-    int b, e;
-    range(cur0, end0, ncol0, cc, b, e);
-    inj(b, e, r, v);
-    if (own) vxB[S(r, cc)] = v;
-    return v;
+  InjCursor cvx, cvz, cst;
+  cvx.init(a.cells, s_rng[0][0], s_rng[0][1]);
+  cvz.init(a.cells, s_rng[1][0], s_rng[1][1]);
+  cst.init(a.cells, s_rng[2][0], s_rng[2][1]);
+
+  // velocity row q (t < TZ, and 3 halo rows for vz); pressure row r
+  const int kq = t < TZ ? t : (t - TZ < 3 ? t : -1);
+  const int q = z0 + kq;
+  const bool vact = kq >= 0;
+  const bool ownr = kq >= 0 && (kq < TZ || lastz);
+  const bool vxr = kq >= 0 && kq < TZ && q >= 4 && q <= nz - 3, vzr = q >= 4 && q <= nz;
+  const int jq1 = pml_slot(q - 3, nz - 3, npml, zlo, zhi);  // dpdz (z strip)
+  const int gsrc = (rzlo && q <= 2) ? 5 - q : (rzhi && q >= nz + 2) ? 2 * nz + 3 - q : 0;
+  const int r = z0 + t;
+  const bool srow = t < TZ && r <= nz;
+  const int jr3 = pml_slot(r, nz, npml, zlo, zhi);  // dvzdz (z strip)
+
+  for (int cc = xbase; cc < x0 && cc <= xlast; cc++) wait_col(cc);
+
+  auto cpml_p = [&](float D, int q4, int j, float psi_old, float *dst, bool own) -> float {
+    const float *cf = a.pml + q4 * P6;
+    const float psi = cf[2 * npml + j] * psi_old + cf[j] * D;
+    if (own) *dst = psi;
+    return D * cf[4 * npml + j] + psi;
   };
 
-  // ---- prologue: p columns x0-3 .. x0+2, vx columns x0 .. x0+2 ----
-  for (int cc = x0 - 3; cc <= x0 + 2; cc++) load_p(cc);
-  __syncthreads();
-  u0 = vx_col(x0, 0.f, 0.f);
-  u1 = vx_col(x0 + 1, 0.f, u0);
-  u2 = vx_col(x0 + 2, u0, u1);
-
-  for (int c = x0; c < x1; c++) {
-    load_p(c + 3);
-    __syncthreads();
-    // vx column c+3
-    u3 = vx_col(c + 3, u1, u2);
-    if (rxlo && c + 3 == 4) {
-      // dirichletxmin!: vx[1] = -vx[4], vx[2] = -vx[3] (vx[4] before its source)
-      const float pre = vx_upd(4, false);
-      u0 = -pre;
-      u1 = -u2;
-      if (rown && x0 == 1) {
-        vxB[S(r, 1)] = u0;
-        vxB[S(r, 2)] = u1;
-      }
-    }
-    // vz column c, rows z0 .. z0+TZ+2
-    {
-      int b, e;
-      range(cur1, end1, ncol1, c, b, e);
-      for (int k = t; k < TZ + 3; k += TZ) {
-        const int q = z0 + k;
-        const bool own = (k < TZ || lastz) && q <= nz + 3 && c < x1;
-        float v;
-        if (rzlo && q <= 2)
-          v = -vz_upd(5 - q, c, false);  // dirichletzmin!: vz[1] = -vz[4], vz[2] = -vz[3]
-        else if (rzhi && q >= nz + 2)
-          v = -vz_upd(2 * nz + 3 - q, c, false);  // dirichletzmax!
-        else
-          v = vz_upd(q, c, own);
-        inj(b, e, q, v);
-        svz[c & 1][k] = v;
-        if (own) vzB[S(q, c)] = v;
-      }
-    }
-    __syncthreads();
-    // p at (r, c)
-    {
-      int b, e;
-      range(cur2, end2, ncol2, c, b, e);
-      if (rown) {
-        const int64_t o = S(r, c);
-        const float pold = sp[c & 7][t + 3];
-        float pn;
-        if (a.vonly) {
-          pn = pold;
-        } else {
-          float Dx = st4(u0, u1, u2, u3) * a.dxI;
-          int j = pml_slot(c, nx, npml, xlo, xhi);
-          if (j >= 0) Dx = cpml(Dx, pm2, npml, j, psA[2], psB[2], (int64_t)j * NZP + (r + ZOFF - 1), true);
-          const float *vz = svz[c & 1];
-          float Dz = st4(vz[t], vz[t + 1], vz[t + 2], vz[t + 3]) * a.dzI;
-          j = pml_slot(r, nz, npml, zlo, zhi);
-          if (j >= 0) Dz = cpml(Dz, pm3, npml, j, psA[3], psB[3], (int64_t)(c + XOFF - 1) * 2 * npml + j, true);
-          pn = pold + (Dx + Dz) * a.dtK[o];
-          inj(b, e, r, pn);
+  // Dispatch per warp and per column: a warp runs the straight-line code
+  // unless one of its rows or the current column touches a CPML strip, a
+  // rigid face, a domain edge or a source cell.
+  if constexpr (FAST) {
+    // interior tile: inside every update domain, no CPML, no face, no source
+    auto vel_fast = [&](int cc) {
+      if (!vact) return;
+      const int k = kq, kk = kq + 4, s = slot(cc);
+      const float *pc = ring + s * SLOT, *v0 = pc + R8;
+      const float vz = v0[R4 + k] + v0[3 * R4 + k] * (st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI);
+      svz[s * R4 + k] = vz;
+      if (kq < TZ) {
+        const float *p3 = ring + slot(cc - 3) * SLOT, *p2 = ring + slot(cc - 2) * SLOT,
+                    *p1 = ring + slot(cc - 1) * SLOT;
+        const float vx = v0[k] + v0[2 * R4 + k] * (st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI);
+        svx[s * R4 + k] = vx;
+        if (cc < x1) {
+          const int64_t o = so + S(q, cc);
+          a.vxB[o] = vx;
+          a.vzB[o] = vz;
         }
-        pB[o] = pn;
+      }
+    };
+    for (int c = x0 - 3; c < x1; c++) {
+      const int cc = c + 3;
+      wait_col(cc);
+      vel_fast(cc);
+      __syncthreads();
+      if (producer) issue(c + 7);
+      if (c >= x0 && t < TZ) {
+        const int k = t;
+        const float *pc = ring + slot(c) * SLOT;
+        const float *w = svz + slot(c) * R4;
+        const float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
+                             svx[slot(c + 3) * R4 + k]) * a.dxI;
+        const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
+        a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
       }
     }
-    u0 = u1;
-    u1 = u2;
-    u2 = u3;
+  } else {
+  const bool rfv_t = vact && (q <= 4 || q >= nz - 4);
+  const bool rfs_t = t < TZ && r >= nz - 4;
+  const bool rpv_t = vact && jq1 >= 0;
+  const bool rps_t = t < TZ && jr3 >= 0;
+  const bool rf_v = __any_sync(0xffffffffu, rfv_t), rf_s = __any_sync(0xffffffffu, rfs_t);
+  const bool rp_v = __any_sync(0xffffffffu, rpv_t), rp_s = __any_sync(0xffffffffu, rps_t);
+  auto colfull_v = [&](int cc) { return a.vonly || cc <= 4 || cc >= nx - 4; };
+  auto colfull_s = [&](int c) { return a.vonly || c >= nx - 4; };
+  auto colpml_v = [&](int cc) { return pml_slot(cc - 3, nx - 3, npml, xlo, xhi) >= 0; };
+  auto colpml_s = [&](int c) { return pml_slot(c, nx, npml, xlo, xhi) >= 0; };
+  {
+    // CPML strip, otherwise interior (psi prefetched by vel_psi / str_psi)
+    auto vel_strip = [&](int cc, float p0, float p1) {
+      if (!vact) return;
+      const int k = kq, kk = kq + 4, s = slot(cc);
+      const float *pc = ring + s * SLOT, *v0 = pc + R8;
+      const bool own = cc < x1 && kq < TZ;
+      float Dz = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
+      if (jq1 >= 0) Dz = cpml_p(Dz, 1, jq1, p1, psB(1) + ZS(cc, jq1), own);
+      const float vz = v0[R4 + k] + v0[3 * R4 + k] * Dz;
+      svz[s * R4 + k] = vz;
+      if (kq < TZ) {
+        const float *p3 = ring + slot(cc - 3) * SLOT, *p2 = ring + slot(cc - 2) * SLOT,
+                    *p1s = ring + slot(cc - 1) * SLOT;
+        float Dx = st4(p3[kk], p2[kk], p1s[kk], pc[kk]) * a.dxI;
+        const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
+        if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, p0, psB(0) + XS(j0, q), own);
+        const float vx = v0[k] + v0[2 * R4 + k] * Dx;
+        svx[s * R4 + k] = vx;
+        if (own) {
+          const int64_t o = so + S(q, cc);
+          a.vxB[o] = vx;
+          a.vzB[o] = vz;
+        }
+      }
+    };
+    auto str_strip = [&](int c, float p2, float p3) {
+      if (t >= TZ) return;
+      const int k = t;
+      const float *pc = ring + slot(c) * SLOT;
+      float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
+                     svx[slot(c + 3) * R4 + k]) * a.dxI;
+      const int j2 = pml_slot(c, nx, npml, xlo, xhi);
+      if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, p2, psB(2) + XS(j2, r), true);
+      const float *w = svz + slot(c) * R4;
+      float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
+      if (jr3 >= 0) Dz = cpml_p(Dz, 3, jr3, p3, psB(3) + ZS(c, jr3), true);
+      a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+    };
+    float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)
+    auto vel_psi = [&](int cc, float &p0, float &p1) {
+      p0 = p1 = 0.f;
+      if (!vact) return;
+      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
+      if (vxr && cc >= 4 && cc <= nx && j0 >= 0) p0 = psA(0)[XS(j0, q)];
+      if (vzr && cc >= 4 && cc <= nx - 3 && jq1 >= 0) p1 = psA(1)[ZS(cc, jq1)];
+    };
+    // vz at row qq of column cc before its source (source of a mirror row)
+    auto vz_any = [&](int qq, int cc) -> float {
+      const int kv = qq - z0;
+      const float *pc = ring + slot(cc) * SLOT, *v0 = pc + R8;
+      float v = v0[R4 + kv];
+      if (qq >= 4 && qq <= nz && cc >= 4 && cc <= nx - 3) {
+        const int kk = kv + 4;
+        float D = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
+        const int j = pml_slot(qq - 3, nz - 3, npml, zlo, zhi);
+        if (j >= 0) D = cpml_p(D, 1, j, psA(1)[ZS(cc, j)], nullptr, false);
+        v = v + v0[3 * R4 + kv] * D;
+      }
+      return v;
+    };
+    auto vel_edge = [&](int cc, float p0, float p1, int ib0, int ie0, int ib1, int ie1) {
+      if (!vact) return;
+      const int k = kq, kk = kq + 4, s = slot(cc);
+      const float *pc = ring + s * SLOT, *v0 = pc + R8;
+      const bool ownc = cc >= x0 && (cc < x1 || lastx);
+      if (kq < TZ) {
+        const bool ownx = ownc && ownr && q <= nz;
+        float vx;
+        if (rxhi && cc >= nx + 2) {
+          vx = cc == nx + 3 ? -vpre : -svx[slot(cc - 1) * R4 + k];  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
+        } else {
+          vx = v0[k];
+          if (vxr && cc >= 4 && cc <= nx) {
+            const float *p3 = ring + slot(cc - 3) * SLOT, *p2 = ring + slot(cc - 2) * SLOT,
+                        *p1 = ring + slot(cc - 1) * SLOT;
+            float D = st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI;
+            const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
+            if (j0 >= 0) D = cpml_p(D, 0, j0, p0, psB(0) + XS(j0, q), ownx);
+            vx = vx + v0[2 * R4 + k] * D;
+          }
+          if (cc == nx) vpre = vx;
+        }
+        if (rxlo && cc == 4) {
+          // dirichletxmin!: vx[1] = -vx[4] (before its source), vx[2] = -vx[3]
+          const float g1 = -vx, g2 = -svx[slot(3) * R4 + k];
+          svx[slot(1) * R4 + k] = g1;
+          svx[slot(2) * R4 + k] = g2;
+          if (x0 == 1 && ownr && q <= nz) {
+            a.vxB[so + S(q, 1)] = g1;
+            a.vxB[so + S(q, 2)] = g2;
+          }
+        }
+        if (!a.vonly) inject(a.cells, a.amount, ib0, ie0, q, vx);
+        svx[s * R4 + k] = vx;
+        if (ownx) a.vxB[so + S(q, cc)] = vx;
+      }
+      float vz;
+      if (gsrc) {
+        vz = -vz_any(gsrc, cc);  // dirichletzmin!/zmax!
+      } else {
+        vz = v0[R4 + k];
+        if (vzr && cc >= 4 && cc <= nx - 3) {
+          float D = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
+          if (jq1 >= 0) D = cpml_p(D, 1, jq1, p1, psB(1) + ZS(cc, jq1), ownc && ownr && cc <= nx);
+          vz = vz + v0[3 * R4 + k] * D;
+        }
+      }
+      if (!a.vonly) inject(a.cells, a.amount, ib1, ie1, q, vz);
+      svz[s * R4 + k] = vz;
+      if (ownc && ownr && cc <= nx && q <= nz + 3) a.vzB[so + S(q, cc)] = vz;
+    };
+    auto str_psi = [&](int c, float &p2, float &p3) {
+      p2 = p3 = 0.f;
+      if (!srow) return;
+      const int j2 = pml_slot(c, nx, npml, xlo, xhi);
+      if (j2 >= 0) p2 = psA(2)[XS(j2, r)];
+      if (jr3 >= 0) p3 = psA(3)[ZS(c, jr3)];
+    };
+    auto str_edge = [&](int c, float p2, float p3, int bs, int es) {
+      if (!srow) return;
+      const int k = t;
+      const float *pc = ring + slot(c) * SLOT;
+      float pn = pc[k + 4];
+      if (!a.vonly) {
+        float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
+                       svx[slot(c + 3) * R4 + k]) * a.dxI;
+        const int j2 = pml_slot(c, nx, npml, xlo, xhi);
+        if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, p2, psB(2) + XS(j2, r), true);
+        const float *w = svz + slot(c) * R4;
+        float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
+        if (jr3 >= 0) Dz = cpml_p(Dz, 3, jr3, p3, psB(3) + ZS(c, jr3), true);
+        pn = pn + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+        inject(a.cells, a.amount, bs, es, r, pn);  // add_stress_source!
+      }
+      a.pB[so + S(r, c)] = pn;
+    };
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+    // one sweep: iterations c < x0 only compute the first velocity columns
+    for (int c = x0 - 3; c < x1; c++) {
+      const int cc = c + 3;
+      int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+      cvx.range(a.cells, cc, ib0, ie0);
+      cvz.range(a.cells, cc, ib1, ie1);
+      if (c >= x0) cst.range(a.cells, c, bs, es);
+      // general code for domain edges, mirrors and sources; otherwise the
+      // straight-line code, with CPML terms where a strip is met
+      const bool gv = rf_v || colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
+      const bool gs = rf_s || colfull_s(c) || bs < es;
+      if (gv || rp_v || colpml_v(cc)) vel_psi(cc, p0, p1);
+      if (c >= x0 && (gs || rp_s || colpml_s(c))) str_psi(c, p2, p3);
+      wait_col(cc);
+      if (gv)
+        vel_edge(cc, p0, p1, ib0, ie0, ib1, ie1);
+      else
+        vel_strip(cc, p0, p1);
+      __syncthreads();
+      if (producer) issue(c + 7);
+      if (c >= x0) {
+        if (gs)
+          str_edge(c, p2, p3, bs, es);
+        else
+          str_strip(c, p2, p3);
+      }
+    }
+  }
+  }
+  __syncthreads();
+  if (s_err && t == 0) {
+    for (int cc = max(xbase, xlast - 7); cc <= xlast; cc++) {
+      const int j = cc - xbase;
+      mbar_wait(&bar[j & 7], (j >> 3) & 1);
+    }
+    atomicExch(a.err, 1);
   }
 }
 
-int step_adjoint_acoustic2d(Plan *p, int it);
-
-static void fill_args(Plan *p, A2Args &a) {
+int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
+  if (mode == GPI_ADJOINT && !vonly) return step_adjoint_acoustic2d(p, it);
+  (void)ipw_mask;
+  static int attr_dev[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_dev[dev]) {
+    GPI_CUDA(p, cudaFuncSetAttribute(k_a2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A2_SMEM));
+    GPI_CUDA(p, cudaFuncSetAttribute(k_a2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A2_SMEM));
+    attr_dev[dev] = 1;
+  }
+  A2Args a;
   a.nz = p->d.nz;
   a.nx = p->d.nx;
   a.NZP = p->NZP;
@@ -276,29 +391,23 @@ static void fill_args(Plan *p, A2Args &a) {
   a.npml = p->d.npml;
   a.faces = p->d.pml_faces;
   a.rigid = p->d.rigid_faces;
-  const double den = 24.0;
-  a.dxI = (float)(1.0 / (p->d.dx * den));
-  a.dzI = (float)(1.0 / (p->d.dz * den));
-  a.dtI = (float)(1.0 / p->d.dt);
+  a.dxI = (float)(1.0 / (p->d.dx * 24.0));
+  a.dzI = (float)(1.0 / (p->d.dz * 24.0));
   a.L = p->L;
   a.nzb = p->nzb;
   a.nxb = p->nxb;
-  a.nshots = p->d.nshots;
-  for (int w = 0; w < 2; w++) {
-    const int A = p->cur[w], B = p->cur[w] ^ 1;
-    const int ww = w < p->d.npw ? w : 0;
-    a.pA[w] = p->state[A][ww][GPI_P];
-    a.vxA[w] = p->state[A][ww][GPI_VX];
-    a.vzA[w] = p->state[A][ww][GPI_VZ];
-    a.pB[w] = p->state[B][ww][GPI_P];
-    a.vxB[w] = p->state[B][ww][GPI_VX];
-    a.vzB[w] = p->state[B][ww][GPI_VZ];
-    for (int q = 0; q < 4; q++) {
-      a.psA[w][q] = p->psi[A][ww][q];
-      a.psB[w][q] = p->psi[B][ww][q];
-    }
+  const int A = p->cur[0], B = A ^ 1;
+  a.pA = p->state[A][0][GPI_P];
+  a.vxA = p->state[A][0][GPI_VX];
+  a.vzA = p->state[A][0][GPI_VZ];
+  a.pB = p->state[B][0][GPI_P];
+  a.vxB = p->state[B][0][GPI_VX];
+  a.vzB = p->state[B][0][GPI_VZ];
+  for (int q = 0; q < 4; q++) {
+    a.psA[q] = p->psi[A][0][q];
+    a.psB[q] = p->psi[B][0][q];
+    a.pss[q] = p->psi_stride[q];
   }
-  for (int q = 0; q < 4; q++) a.pss[q] = p->psi_stride[q];
   a.cx = p->coef[0];
   a.cz = p->coef[1];
   a.dtK = p->coef[2];
@@ -306,31 +415,22 @@ static void fill_args(Plan *p, A2Args &a) {
   a.cells = p->d_cells;
   a.gptr = p->d_group_ptr;
   a.amount = p->d_amount;
-  a.vonly = 0;
-  a.bstore = nullptr;
-  a.bsstride = 0;
-  a.npx = a.npz = a.nb = 0;
-  a.gK = a.gR = nullptr;
-  a.bufx = a.bufz = nullptr;
-}
-
-int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
-  if (mode == GPI_ADJOINT && !vonly) return step_adjoint_acoustic2d(p, it);
-  (void)ipw_mask;
-  A2Args a;
-  fill_args(p, a);
   a.vonly = vonly;
-  const int blocks = p->nzb * p->nxb * p->d.nshots;
-  k_a2_forward<128><<<blocks, 128, 0, p->stream>>>(a);
-  p->launches++;
+  a.err = p->d_err;
+  a.tiles = p->d_tiles;
+  const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
+  if (nf) {
+    k_a2<true><<<nf, A2_THREADS, A2_SMEM, p->stream>>>(a);
+    p->launches++;
+  }
+  a.tiles = p->d_tiles + nf;
+  if (ng) {
+    k_a2<false><<<ng, A2_THREADS, A2_SMEM, p->stream>>>(a);
+    p->launches++;
+  }
   GPI_CUDA(p, cudaGetLastError());
   p->cur[0] ^= 1;
   return GPI_OK;
-}
-
-int step_adjoint_acoustic2d(Plan *p, int it) {
-  (void)it;
-  return fail(p, GPI_E_UNSUPPORTED, "adjoint step not built yet");
 }
 
 }  // namespace gpi

@@ -12,13 +12,18 @@
 //   tzz[r, c] -= dtM D_z vz[r..r+3, c] + dtl D_x vx[r, c..c+3]
 //   txz[r, c] -= mu (D_z vx[r..r+3, c+3] + D_x vz[r+3, c..c+3]),  r <= nz-3, c <= nx-3
 //
-// A block owns TZ rows x L columns of the normal-stress grid of one shot and
-// sweeps its columns.  The three stress fields stream through an 8-column
-// shared-memory ring (rows z0-3 .. z0+TZ+2); the velocities of the 4 columns
-// the stress update needs sit in a 4-column ring (rows z0 .. z0+TZ+2).  Halo
-// velocities are recomputed from the input buffer (ping-pong state), so a
-// step is one pass over HBM: read 5 state + 5 coefficient arrays, write 5
-// state arrays (60 B per cell).
+// Work decomposition.  A block owns TZ rows x L columns of the normal-stress
+// grid of one shot and sweeps its columns.  For every column it needs ten
+// input columns (three stresses over rows z0-4..z0+TZ+3, the two old
+// velocities and their coefficients over z0..z0+TZ+3, dtM, dtl, mu over
+// z0..z0+TZ-1); one producer thread streams them into an 8-column ring in
+// shared memory with bulk asynchronous copies (cp.async.bulk, the TMA
+// engine) that complete on one mbarrier per ring slot, four columns ahead
+// of the compute.  TZ threads (plus 3 of an extra warp for the halo rows)
+// compute from shared memory only.  Halo velocities (3 columns right of and
+// 3 rows below the tile) are recomputed from the input buffer, so the state
+// is ping-ponged and a time step is one pass over HBM: 10 arrays read,
+// 5 written, 60 B per cell update.
 #include "k_stencil.cuh"
 
 namespace gpi {
@@ -40,225 +45,452 @@ struct E2Args {
   const int32_t *gptr;
   const float *amount;
   int vonly;
+  int *err;  // set when a pipeline wait gives up
+  const int3 *tiles;  // (z-block, x-chunk, shot) per block
 };
 
-template <int TZ>
-__global__ void __launch_bounds__(TZ) k_e2(const E2Args a) {
-  constexpr int TR = TZ + 6;  // stress ring rows: z0-3 .. z0+TZ+2
-  constexpr int VR = TZ + 3;  // velocity ring rows: z0 .. z0+TZ+2
-  __shared__ float sxx[8][TR], szz[8][TR], sxz[8][TR];
-  __shared__ float svx[4][VR], svz[4][VR];
+constexpr int E2_TZ = 128;
+constexpr int E2_THREADS = E2_TZ + 32;
+constexpr int E2_R8 = E2_TZ + 8;                                // stress rows z0-4 .. z0+TZ+3
+constexpr int E2_R4 = E2_TZ + 4;                                // velocity-input rows z0 .. z0+TZ+3
+constexpr int E2_SLOT = 3 * E2_R8 + 4 * E2_R4 + 3 * E2_TZ;      // floats per ring slot
+constexpr size_t E2_SMEM = 128 + sizeof(float) * (8 * E2_SLOT + 2 * 8 * E2_R4);
+
+template <bool FAST>
+__global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
+  constexpr int TZ = E2_TZ, R8 = E2_R8, R4 = E2_R4, SLOT = E2_SLOT;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // one mbarrier per ring slot
+  float *ring = reinterpret_cast<float *>(smem + 128);  // [8][SLOT]
+  float *svx = ring + 8 * SLOT;                          // [8][R4] new velocities
+  float *svz = svx + 8 * R4;
   __shared__ int s_rng[3][2];
+  __shared__ int s_err;
   const int t = threadIdx.x;
-  int bid = blockIdx.x;
-  const int zb = bid % a.nzb;
-  bid /= a.nzb;
-  const int xb = bid % a.nxb;
-  const int shot = bid / a.nxb;
+  const int3 tile = a.tiles[blockIdx.x];
+  const int zb = tile.x, xb = tile.y, shot = tile.z;
   const int z0 = 1 + zb * TZ, x0 = 1 + xb * a.L;
   const int x1 = min(x0 + a.L, a.nx + 1);
+  const int xbase = x0 - 3, xlast = x1 + 2;  // input columns of this block
   const bool lastx = xb == a.nxb - 1, lastz = zb == a.nzb - 1;
   const int nz = a.nz, nx = a.nx, npml = a.npml, NZP = a.NZP;
   const int64_t so = (int64_t)shot * a.fs;
-  const float *__restrict__ txxA = a.txxA + so;
-  const float *__restrict__ tzzA = a.tzzA + so;
-  const float *__restrict__ txzA = a.txzA + so;
-  const float *__restrict__ vxA = a.vxA + so;
-  const float *__restrict__ vzA = a.vzA + so;
-  float *__restrict__ txxB = a.txxB + so;
-  float *__restrict__ tzzB = a.tzzB + so;
-  float *__restrict__ txzB = a.txzB + so;
-  float *__restrict__ vxB = a.vxB + so;
-  float *__restrict__ vzB = a.vzB + so;
   const bool xlo = a.faces & GPI_XMIN, xhi = a.faces & GPI_XMAX, zlo = a.faces & GPI_ZMIN, zhi = a.faces & GPI_ZMAX;
   const bool rxlo = a.rigid & GPI_XMIN, rxhi = a.rigid & GPI_XMAX, rzlo = a.rigid & GPI_ZMIN, rzhi = a.rigid & GPI_ZMAX;
   const bool fsurf = a.free & GPI_ZMIN;
-  const float *psA[8];
-  float *psB[8];
-#pragma unroll
-  for (int q = 0; q < 8; q++) {
-    psA[q] = a.psA[q] ? a.psA[q] + shot * a.pss[q] : nullptr;
-    psB[q] = a.psB[q] ? a.psB[q] + shot * a.pss[q] : nullptr;
-  }
-  const int P6 = 6 * npml;  // floats per derivative in a.pml
+  const int P6 = 6 * npml;  // floats per derivative field in a.pml
   auto S = [&](int rr, int cc) -> int64_t { return (int64_t)(cc + XOFF - 1) * NZP + (rr + ZOFF - 1); };
-  auto XS = [&](int j, int rr) -> int64_t { return (int64_t)j * NZP + (rr + ZOFF - 1); };        // x strip
-  auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * 2 * npml + j; };   // z strip
+  auto XS = [&](int j, int rr) -> int64_t { return (int64_t)j * NZP + (rr + ZOFF - 1); };       // x strip
+  auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * 2 * npml + j; };  // z strip
+  auto psA = [&](int q) -> const float * { return a.psA[q] + shot * a.pss[q]; };
+  auto psB = [&](int q) -> float * { return a.psB[q] + shot * a.pss[q]; };
+  // ring views of input column cc
+  auto slot = [&](int cc) -> int { return (cc - xbase) & 7; };
+  auto T = [&](int f, int cc) -> const float * { return ring + slot(cc) * SLOT + f * R8; };           // txx tzz txz
+  auto V = [&](int f, int cc) -> const float * { return ring + slot(cc) * SLOT + 3 * R8 + f * R4; };  // vx vz cx cz
+  auto C = [&](int f, int cc) -> const float * {
+    return ring + slot(cc) * SLOT + 3 * R8 + 4 * R4 + f * TZ;  // dtM dtl mu
+  };
 
+  if (t == 0) {
+    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 1);
+    mbar_fence_init();
+    s_err = 0;
+  }
   if (t < 3) {
     const int kind = t == 0 ? 0 : t == 1 ? 2 : 3;
     const int g = shot * NKIND + kind;
     s_rng[t][0] = first_col(a.cells, a.gptr[g], a.gptr[g + 1], x0);
     s_rng[t][1] = a.gptr[g + 1];
   }
-
-  auto load_tau = [&](int cc) {
-    const int s = cc & 7;
-    for (int k = t; k < TR; k += TZ) {
-      const int64_t o = S(z0 - 3 + k, cc);
-      sxx[s][k] = txxA[o];
-      szz[s][k] = tzzA[o];
-      sxz[s][k] = txzA[o];
-    }
-  };
-  // vx at (q, cc) before its source (k = q - z0 indexes the rings)
-  auto vx_upd = [&](int q, int cc, bool own) -> float {
-    const int64_t o = S(q, cc);
-    float v = vxA[o];
-    if (q >= 4 && q <= nz - 3 && cc >= 4 && cc <= nx) {
-      const int k = q - z0 + 3;  // stress-ring row of q
-      float Dx = st4(sxx[(cc - 3) & 7][k], sxx[(cc - 2) & 7][k], sxx[(cc - 1) & 7][k], sxx[cc & 7][k]) * a.dxI;
-      int j = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
-      if (j >= 0) Dx = cpml(Dx, a.pml + 0 * P6, npml, j, psA[0], psB[0], XS(j, q), own);
-      const float *cz = sxz[(cc - 3) & 7];
-      float Dz = st4(cz[k - 3], cz[k - 2], cz[k - 1], cz[k]) * a.dzI;
-      j = pml_slot(q - 3, nz - 6, npml, zlo, zhi);
-      if (j >= 0) Dz = cpml(Dz, a.pml + 3 * P6, npml, j, psA[3], psB[3], ZS(cc, j), own);
-      v = v - a.cx[o] * (Dx + Dz);
-    }
-    return v;
-  };
-  auto vz_upd = [&](int q, int cc, bool own) -> float {
-    const int64_t o = S(q, cc);
-    float v = vzA[o];
-    if (q >= 4 && q <= nz && cc >= 4 && cc <= nx - 3) {
-      const int k = q - z0 + 3;
-      float Dx = st4(sxz[(cc - 3) & 7][k - 3], sxz[(cc - 2) & 7][k - 3], sxz[(cc - 1) & 7][k - 3], sxz[cc & 7][k - 3]) *
-                 a.dxI;
-      int j = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
-      if (j >= 0) Dx = cpml(Dx, a.pml + 1 * P6, npml, j, psA[1], psB[1], XS(j, q), own);
-      const float *zz = szz[cc & 7];
-      float Dz = st4(zz[k - 3], zz[k - 2], zz[k - 1], zz[k]) * a.dzI;
-      j = pml_slot(q - 3, nz - 3, npml, zlo, zhi);
-      if (j >= 0) Dz = cpml(Dz, a.pml + 2 * P6, npml, j, psA[2], psB[2], ZS(cc, j), own);
-      v = v - a.cz[o] * (Dx + Dz);
-    }
-    return v;
-  };
-
   __syncthreads();
+
+  // ---- producer: one thread issues the bulk copies of a column ----
+  const bool producer = t == TZ;
+  int next = xbase;
+  auto issue = [&](int upto) {
+    for (; next <= upto && next <= xlast; next++) {
+      const int s = slot(next);
+      float *sl = ring + s * SLOT;
+      mbar_expect_tx(&bar[s], SLOT * 4);
+      const int64_t oT = so + S(z0 - 4, next), oV = S(z0, next);
+      bulk_g2s(sl + 0 * R8, a.txxA + oT, R8 * 4, &bar[s]);
+      bulk_g2s(sl + 1 * R8, a.tzzA + oT, R8 * 4, &bar[s]);
+      bulk_g2s(sl + 2 * R8, a.txzA + oT, R8 * 4, &bar[s]);
+      float *v = sl + 3 * R8;
+      bulk_g2s(v + 0 * R4, a.vxA + so + oV, R4 * 4, &bar[s]);
+      bulk_g2s(v + 1 * R4, a.vzA + so + oV, R4 * 4, &bar[s]);
+      bulk_g2s(v + 2 * R4, a.cx + oV, R4 * 4, &bar[s]);
+      bulk_g2s(v + 3 * R4, a.cz + oV, R4 * 4, &bar[s]);
+      float *cf = v + 4 * R4;
+      bulk_g2s(cf + 0 * TZ, a.dtM + oV, TZ * 4, &bar[s]);
+      bulk_g2s(cf + 1 * TZ, a.dtl + oV, TZ * 4, &bar[s]);
+      bulk_g2s(cf + 2 * TZ, a.mu + oV, TZ * 4, &bar[s]);
+    }
+  };
+  if (producer) issue(xbase + 7);
+  auto wait_col = [&](int cc) {
+    const int j = cc - xbase;
+    if (!mbar_wait(&bar[j & 7], (j >> 3) & 1)) s_err = 1;
+  };
+
   InjCursor cvx, cvz, cst;
   cvx.init(a.cells, s_rng[0][0], s_rng[0][1]);
   cvz.init(a.cells, s_rng[1][0], s_rng[1][1]);
   cst.init(a.cells, s_rng[2][0], s_rng[2][1]);
 
-  // pre-source vx at column nx for the rows this thread computes (xmax mirror)
-  float vpre[2] = {0.f, 0.f};
-  // velocities of column cc for rows z0+k, k = t and t+TZ (< VR): update,
-  // mirrors, sources; stored in the rings and (owned) in buffer B
-  auto vel_col = [&](int cc) {
-    int b0, e0, b1, e1;
-    cvx.range(a.cells, cc, b0, e0);
-    cvz.range(a.cells, cc, b1, e1);
-    const int s = cc & 3;
-    const bool ownc = cc >= x0 && (cc < x1 || lastx);
-    int i = 0;
-    for (int k = t; k < VR; k += TZ, i++) {
-      const int q = z0 + k;
-      const bool ownr = k < TZ || lastz;
-      // vx
+  // this thread's velocity row: t < TZ -> z0+t, halo lanes -> z0+TZ+0..2
+  const int kq = t < TZ ? t : (t - TZ < 3 ? t : -1);
+  const int q = z0 + kq;
+  const bool vact = kq >= 0;
+  const bool ownr = kq >= 0 && (kq < TZ || lastz);
+
+  // ---- per-thread row constants: velocity row q, stress row r ----
+  const bool vxr = q >= 4 && q <= nz - 3, vzr = q >= 4 && q <= nz;
+  const int jq3 = pml_slot(q - 3, nz - 6, npml, zlo, zhi);  // dtauxzdz (z strip)
+  const int jq2 = pml_slot(q - 3, nz - 3, npml, zlo, zhi);  // dtauzzdz (z strip)
+  // vz mirror source of a ghost row (dirichletzmin!/zmax!), 0 otherwise
+  const int gsrc = (rzlo && q <= 2) ? 5 - q : (rzhi && q >= nz + 2) ? 2 * nz + 3 - q : 0;
+  const int r = z0 + t;
+  const bool srow = t < TZ && r <= nz;
+  const int jr5 = pml_slot(r, nz, npml, zlo, zhi);      // dvzdz (z strip)
+  const int jr6 = pml_slot(r, nz - 3, npml, zlo, zhi);  // dvxdz (z strip)
+  const bool xzrow = r <= nz - 3;
+  const bool fsrow = fsurf && r == 1;
+
+  // CPML with a prefetched psi: psi' = b psi + a D ; D' = D kI + psi'
+  auto cpml_p = [&](float D, int q8, int j, float psi_old, float *dst, bool own) -> float {
+    const float *cf = a.pml + q8 * P6;
+    const float psi = cf[2 * npml + j] * psi_old + cf[j] * D;
+    if (own) *dst = psi;
+    return D * cf[4 * npml + j] + psi;
+  };
+  // vz at row qq of column cc before its source (source of a mirror row)
+  auto vz_any = [&](int qq, int cc) -> float {
+    const int kv = qq - z0;
+    float v = V(1, cc)[kv];
+    if (qq >= 4 && qq <= nz && cc >= 4 && cc <= nx - 3) {
+      const int k = qq - z0 + 4;
+      float Dx = st4(T(2, cc - 3)[k - 3], T(2, cc - 2)[k - 3], T(2, cc - 1)[k - 3], T(2, cc)[k - 3]) * a.dxI;
+      int j = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
+      if (j >= 0) Dx = cpml_p(Dx, 1, j, psA(1)[XS(j, qq)], nullptr, false);
+      const float *zz = T(1, cc);
+      float Dz = st4(zz[k - 3], zz[k - 2], zz[k - 1], zz[k]) * a.dzI;
+      j = pml_slot(qq - 3, nz - 3, npml, zlo, zhi);
+      if (j >= 0) Dz = cpml_p(Dz, 2, j, psA(2)[ZS(cc, j)], nullptr, false);
+      v = v - V(3, cc)[kv] * (Dx + Dz);
+    }
+    return v;
+  };
+  // tzz at row 2 of column c before its source (free_surface_mirror!)
+  auto tzz_row2 = [&](int c) -> float {
+    const int kk = 1;
+    const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
+                *u3 = svx + slot(c + 3) * R4, *w = svz + slot(c) * R4;
+    float dvxdx = st4(u0[kk], u1[kk], u2[kk], u3[kk]) * a.dxI;
+    int j = pml_slot(c, nx, npml, xlo, xhi);
+    if (j >= 0) dvxdx = cpml_p(dvxdx, 4, j, psA(4)[XS(j, 2)], nullptr, false);
+    float dvzdz = st4(w[kk], w[kk + 1], w[kk + 2], w[kk + 3]) * a.dzI;
+    j = pml_slot(2, nz, npml, zlo, zhi);
+    if (j >= 0) dvzdz = cpml_p(dvzdz, 5, j, psA(5)[ZS(c, j)], nullptr, false);
+    return T(1, c)[kk + 4] - (C(0, c)[kk] * dvzdz) - (C(1, c)[kk] * (dvxdx));
+  };
+  float vpre = 0.f;  // vx[q, nx] before its source (xmax mirror)
+  // ---- prologue: stresses of columns x0-3 .. x0-1 ----
+  for (int cc = xbase; cc < x0 && cc <= xlast; cc++) wait_col(cc);
+
+  // Dispatch per warp and per column: a warp runs the straight-line code
+  // unless one of its rows or the current column touches a CPML strip, a
+  // rigid or free face, a domain edge or a source cell.
+  if constexpr (FAST) {
+    // interior tile: inside every update domain, no CPML, no face, no source
+    auto vel_fast = [&](int cc) {
+      if (!vact) return;
+      const int k = kq, kk = kq + 4, s = slot(cc);
+      const float *b3 = ring + slot(cc - 3) * SLOT, *b2 = ring + slot(cc - 2) * SLOT,
+                  *b1 = ring + slot(cc - 1) * SLOT, *b0 = ring + s * SLOT;
+      const float *v0 = b0 + 3 * R8, *z3 = b3 + 2 * R8, *zz = b0 + R8;
+      const float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
+      const float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
+      const float vx = v0[k] - v0[2 * R4 + k] * (Dx + Dz);
+      const float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
+      const float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
+      const float vz = v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2);
+      svx[s * R4 + k] = vx;
+      svz[s * R4 + k] = vz;
+      if (cc < x1 && kq < TZ) {
+        const int64_t o = so + S(q, cc);
+        a.vxB[o] = vx;
+        a.vzB[o] = vz;
+      }
+    };
+    auto str_fast = [&](int c) {
+      if (t >= TZ) return;
+      const int k = t;
+      const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
+                  *u3 = svx + slot(c + 3) * R4;
+      const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
+                  *w3 = svz + slot(c + 3) * R4;
+      const float *bc = ring + slot(c) * SLOT, *cf = bc + 3 * R8 + 4 * R4;
+      const float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
+      const float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
+      const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
+      const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
+      const float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
+      const float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
+      const float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
+      const float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
+      const int64_t o = so + S(z0 + t, c);
+      a.txxB[o] = txx;
+      a.tzzB[o] = tzz;
+      a.txzB[o] = txz;
+    };
+    for (int c = x0 - 3; c < x1; c++) {
+      const int cc = c + 3;
+      wait_col(cc);
+      vel_fast(cc);
+      __syncthreads();
+      if (producer) issue(c + 7);
+      if (c >= x0) str_fast(c);
+    }
+  } else {
+  // rows / columns that need the full general code: domain edges, mirror
+  // rows and columns, the free surface (sources are checked per column)
+  const bool rfv_t = vact && (q <= 4 || q >= nz - 4);
+  const bool rfs_t = t < TZ && (r <= 1 || r >= nz - 4);
+  // rows whose only special property is a CPML strip
+  const bool rpv_t = vact && (jq2 >= 0 || jq3 >= 0);
+  const bool rps_t = t < TZ && (jr5 >= 0 || jr6 >= 0);
+  const bool rf_v = __any_sync(0xffffffffu, rfv_t), rf_s = __any_sync(0xffffffffu, rfs_t);
+  const bool rp_v = __any_sync(0xffffffffu, rpv_t), rp_s = __any_sync(0xffffffffu, rps_t);
+  auto colfull_v = [&](int cc) { return a.vonly || cc <= 4 || cc >= nx - 4; };
+  auto colfull_s = [&](int c) { return a.vonly || c <= 1 || c >= nx - 4; };
+  auto colpml_v = [&](int cc) {
+    return pml_slot(cc - 3, nx - 3, npml, xlo, xhi) >= 0 || pml_slot(cc - 3, nx - 6, npml, xlo, xhi) >= 0;
+  };
+  auto colpml_s = [&](int c) {
+    return pml_slot(c, nx, npml, xlo, xhi) >= 0 || pml_slot(c, nx - 3, npml, xlo, xhi) >= 0;
+  };
+  {
+    // CPML strip, otherwise interior: the straight-line code plus the
+    // memory-variable updates (psi prefetched by vel_psi / str_psi)
+    auto vel_strip = [&](int cc, float p0, float p1, float p2, float p3) {
+      if (!vact) return;
+      const int k = kq, kk = kq + 4, s = slot(cc);
+      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
+      const bool own = cc < x1 && kq < TZ;
+      const float *b3 = ring + slot(cc - 3) * SLOT, *b2 = ring + slot(cc - 2) * SLOT,
+                  *b1 = ring + slot(cc - 1) * SLOT, *b0 = ring + s * SLOT;
+      const float *v0 = b0 + 3 * R8, *z3 = b3 + 2 * R8, *zz = b0 + R8;
+      float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
+      if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, p0, psB(0) + XS(j0, q), own);
+      float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
+      if (jq3 >= 0) Dz = cpml_p(Dz, 3, jq3, p3, psB(3) + ZS(cc, jq3), own);
+      const float vx = v0[k] - v0[2 * R4 + k] * (Dx + Dz);
+      float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
+      if (j1 >= 0) Dx2 = cpml_p(Dx2, 1, j1, p1, psB(1) + XS(j1, q), own);
+      float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
+      if (jq2 >= 0) Dz2 = cpml_p(Dz2, 2, jq2, p2, psB(2) + ZS(cc, jq2), own);
+      const float vz = v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2);
+      svx[s * R4 + k] = vx;
+      svz[s * R4 + k] = vz;
+      if (own) {
+        const int64_t o = so + S(q, cc);
+        a.vxB[o] = vx;
+        a.vzB[o] = vz;
+      }
+    };
+    auto str_strip = [&](int c, float p4, float p5, float p6, float p7) {
+      if (t >= TZ) return;
+      const int k = t;
+      const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
+      const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
+                  *u3 = svx + slot(c + 3) * R4;
+      const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
+                  *w3 = svz + slot(c + 3) * R4;
+      const float *bc = ring + slot(c) * SLOT, *cf = bc + 3 * R8 + 4 * R4;
+      float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
+      if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, p4, psB(4) + XS(j4, r), true);
+      float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
+      if (jr5 >= 0) dvzdz = cpml_p(dvzdz, 5, jr5, p5, psB(5) + ZS(c, jr5), true);
+      const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
+      const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
+      const float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
+      float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
+      if (jr6 >= 0) dvxdz = cpml_p(dvxdz, 6, jr6, p6, psB(6) + ZS(c, jr6), true);
+      float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
+      if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, p7, psB(7) + XS(j7, r), true);
+      const float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
+      const int64_t o = so + S(r, c);
+      a.txxB[o] = txx;
+      a.tzzB[o] = tzz;
+      a.txzB[o] = txz;
+    };
+    // psi of velocity column cc for this thread's row, loaded ahead of use
+    auto vel_psi = [&](int cc, float &p0, float &p1, float &p2, float &p3) {
+      p0 = p1 = p2 = p3 = 0.f;
+      if (!vact) return;
+      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
+      if (vxr && cc >= 4 && cc <= nx) {
+        if (j0 >= 0) p0 = psA(0)[XS(j0, q)];
+        if (jq3 >= 0) p3 = psA(3)[ZS(cc, jq3)];
+      }
+      if (vzr && cc >= 4 && cc <= nx - 3) {
+        if (j1 >= 0) p1 = psA(1)[XS(j1, q)];
+        if (jq2 >= 0) p2 = psA(2)[ZS(cc, jq2)];
+      }
+    };
+    // velocities of column cc: update_v! with CPML, mirrors, sources
+    auto vel_edge = [&](int cc, float p0, float p1, float p2, float p3, int ib0, int ie0, int ib1, int ie1) {
+      if (!vact) return;
+      const int k = kq, kk = kq + 4, s = slot(cc);
+      const bool vxc = cc >= 4 && cc <= nx, vzc = cc >= 4 && cc <= nx - 3;
+      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
+      const bool ownc = cc >= x0 && (cc < x1 || lastx);
+      const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && cc <= nx && q <= nz + 3;
+      const float *b3 = ring + slot(cc - 3) * SLOT, *b2 = ring + slot(cc - 2) * SLOT,
+                  *b1 = ring + slot(cc - 1) * SLOT, *bq = ring + s * SLOT;
+      const float *v0 = bq + 3 * R8, *z3 = b3 + 2 * R8;
       float vx;
       if (rxhi && cc >= nx + 2) {
-        vx = cc == nx + 3 ? -vpre[i] : -svx[(cc - 1) & 3][k];  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
+        vx = cc == nx + 3 ? -vpre : -svx[slot(cc - 1) * R4 + k];  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
       } else {
-        vx = vx_upd(q, cc, ownc && ownr && q <= nz);
-        if (cc == nx) vpre[i] = vx;
+        vx = v0[k];
+        if (vxr && vxc) {
+          float Dx = st4(b3[kk], b2[kk], b1[kk], bq[kk]) * a.dxI;
+          if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, p0, psB(0) + XS(j0, q), ownx);
+          float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
+          if (jq3 >= 0) Dz = cpml_p(Dz, 3, jq3, p3, psB(3) + ZS(cc, jq3), ownx);
+          vx = vx - v0[2 * R4 + k] * (Dx + Dz);
+        }
+        if (cc == nx) vpre = vx;
       }
-      if (!a.vonly) inject(a.cells, a.amount, b0, e0, q, vx);
-      svx[s][k] = vx;
-      if (ownc && ownr && q <= nz) vxB[S(q, cc)] = vx;
       if (rxlo && cc == 4) {
         // dirichletxmin!: vx[1] = -vx[4] (before its source), vx[2] = -vx[3]
-        const float pre = vx_upd(q, 4, false);
-        svx[1][k] = -pre;
-        svx[2][k] = -svx[3][k];
+        const float g1 = -vx, g2 = -svx[slot(3) * R4 + k];
+        svx[slot(1) * R4 + k] = g1;
+        svx[slot(2) * R4 + k] = g2;
         if (x0 == 1 && ownr && q <= nz) {
-          vxB[S(q, 1)] = svx[1][k];
-          vxB[S(q, 2)] = svx[2][k];
+          a.vxB[so + S(q, 1)] = g1;
+          a.vxB[so + S(q, 2)] = g2;
         }
       }
-      // vz
+      if (!a.vonly) inject(a.cells, a.amount, ib0, ie0, q, vx);
+      svx[s * R4 + k] = vx;
+      if (ownx) a.vxB[so + S(q, cc)] = vx;
       float vz;
-      if (rzlo && q <= 2)
-        vz = -vz_upd(5 - q, cc, false);  // dirichletzmin!
-      else if (rzhi && q >= nz + 2)
-        vz = -vz_upd(2 * nz + 3 - q, cc, false);  // dirichletzmax!
-      else
-        vz = vz_upd(q, cc, ownc && ownr && cc <= nx);
-      if (!a.vonly) inject(a.cells, a.amount, b1, e1, q, vz);
-      svz[s][k] = vz;
-      if (ownc && ownr && cc <= nx && q <= nz + 3) vzB[S(q, cc)] = vz;
-    }
-  };
-
-  // stresses at (r, c) from the velocity rings; returns tzz before sources
-  const int r = z0 + t;
-  auto txx_tzz = [&](int rr, int c, int k, float &txx, float &tzz, bool own) {
-    const int64_t o = S(rr, c);
-    const float *u0 = svx[c & 3], *u1 = svx[(c + 1) & 3], *u2 = svx[(c + 2) & 3], *u3 = svx[(c + 3) & 3];
-    const float *w = svz[c & 3];
-    float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
-    int j = pml_slot(c, nx, npml, xlo, xhi);
-    if (j >= 0) dvxdx = cpml(dvxdx, a.pml + 4 * P6, npml, j, psA[4], psB[4], XS(j, rr), own);
-    float dvzdz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
-    j = pml_slot(rr, nz, npml, zlo, zhi);
-    if (j >= 0) dvzdz = cpml(dvzdz, a.pml + 5 * P6, npml, j, psA[5], psB[5], ZS(c, j), own);
-    const float M = a.dtM[o], Lm = a.dtl[o];
-    const int kk = k + 3;
-    txx = sxx[c & 7][kk] - (M * dvxdx) - (Lm * (dvzdz));
-    tzz = szz[c & 7][kk] - (M * dvzdz) - (Lm * (dvxdx));
-  };
-
-  // ---- prologue ----
-  for (int cc = x0 - 3; cc <= x0 + 2; cc++) load_tau(cc);
-  __syncthreads();
-  for (int cc = x0; cc <= x0 + 2; cc++) vel_col(cc);
-
-  for (int c = x0; c < x1; c++) {
-    load_tau(c + 3);
-    __syncthreads();
-    vel_col(c + 3);
-    __syncthreads();
-    int bs, es;
-    cst.range(a.cells, c, bs, es);
-    if (r <= nz) {
-      const int64_t o = S(r, c);
-      const int k = t;
-      float txx, tzz, txz = 0.f;
-      const bool hasxz = r <= nz - 3 && c <= nx - 3;
-      if (a.vonly) {
-        txx = sxx[c & 7][k + 3];
-        tzz = szz[c & 7][k + 3];
-        txz = sxz[c & 7][k + 3];
+      if (gsrc) {
+        vz = -vz_any(gsrc, cc);
       } else {
-        txx_tzz(r, c, k, txx, tzz, true);
-        if (hasxz) {
-          // compute_stressij!: txz -= mu (dvxdz + dvzdx)
-          float dvxdz = st4(svx[(c + 3) & 3][k], svx[(c + 3) & 3][k + 1], svx[(c + 3) & 3][k + 2],
-                            svx[(c + 3) & 3][k + 3]) * a.dzI;
-          int j = pml_slot(r, nz - 3, npml, zlo, zhi);
-          if (j >= 0) dvxdz = cpml(dvxdz, a.pml + 6 * P6, npml, j, psA[6], psB[6], ZS(c, j), true);
-          float dvzdx = st4(svz[c & 3][k + 3], svz[(c + 1) & 3][k + 3], svz[(c + 2) & 3][k + 3],
-                            svz[(c + 3) & 3][k + 3]) * a.dxI;
-          j = pml_slot(c, nx - 3, npml, xlo, xhi);
-          if (j >= 0) dvzdx = cpml(dvzdx, a.pml + 7 * P6, npml, j, psA[7], psB[7], XS(j, r), true);
-          txz = sxz[c & 7][k + 3] - a.mu[o] * (dvxdz + dvzdx);
+        vz = v0[R4 + k];
+        if (vzr && vzc) {
+          float Dx = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], bq[2 * R8 + kk - 3]) * a.dxI;
+          if (j1 >= 0) Dx = cpml_p(Dx, 1, j1, p1, psB(1) + XS(j1, q), ownz);
+          const float *zz = bq + R8;
+          float Dz = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
+          if (jq2 >= 0) Dz = cpml_p(Dz, 2, jq2, p2, psB(2) + ZS(cc, jq2), ownz);
+          vz = vz - v0[3 * R4 + k] * (Dx + Dz);
         }
-        if (fsurf && r == 1) {
+      }
+      if (!a.vonly) inject(a.cells, a.amount, ib1, ie1, q, vz);
+      svz[s * R4 + k] = vz;
+      if (ownz) a.vzB[so + S(q, cc)] = vz;
+    };
+    auto str_psi = [&](int c, float &p4, float &p5, float &p6, float &p7) {
+      p4 = p5 = p6 = p7 = 0.f;
+      if (!srow) return;
+      const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
+      if (j4 >= 0) p4 = psA(4)[XS(j4, r)];
+      if (jr5 >= 0) p5 = psA(5)[ZS(c, jr5)];
+      if (xzrow && c <= nx - 3) {
+        if (jr6 >= 0) p6 = psA(6)[ZS(c, jr6)];
+        if (j7 >= 0) p7 = psA(7)[XS(j7, r)];
+      }
+    };
+    // stresses of column c: compute_stressii!/ij!, free surface, sources
+    auto str_edge = [&](int c, float p4, float p5, float p6, float p7, int bs, int es) {
+      if (!srow) return;
+      const int k = t;
+      const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
+      const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
+                  *u3 = svx + slot(c + 3) * R4;
+      const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
+                  *w3 = svz + slot(c + 3) * R4;
+      const float *bc = ring + slot(c) * SLOT, *cf = bc + 3 * R8 + 4 * R4;
+      const int64_t o = so + S(r, c);
+      const bool hasxz = xzrow && c <= nx - 3;
+      float txx, tzz, txz = 0.f;
+      if (a.vonly) {
+        txx = bc[k + 4];
+        tzz = bc[R8 + k + 4];
+        txz = bc[2 * R8 + k + 4];
+      } else {
+        float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
+        if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, p4, psB(4) + XS(j4, r), true);
+        float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
+        if (jr5 >= 0) dvzdz = cpml_p(dvzdz, 5, jr5, p5, psB(5) + ZS(c, jr5), true);
+        const float M = cf[k], Lm = cf[TZ + k];
+        txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
+        tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
+        if (hasxz) {
+          float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
+          if (jr6 >= 0) dvxdz = cpml_p(dvxdz, 6, jr6, p6, psB(6) + ZS(c, jr6), true);
+          float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
+          if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, p7, psB(7) + XS(j7, r), true);
+          txz = bc[2 * R8 + k + 4] - cf[2 * TZ + k] * (dvxdz + dvzdx);
+        }
+        if (fsrow) {
           // free_surface_mirror!(tauzz), free_surface!(tauxz): tzz[1] = -tzz[2]
-          float t2x, t2z;
-          txx_tzz(2, c, 1, t2x, t2z, false);
-          tzz = -t2z;
+          tzz = -tzz_row2(c);
           txz = 0.f;
         }
         // add_stress_source!: txx += pv dtM; tzz += pv dtM
         inject(a.cells, a.amount, bs, es, r, txx);
         inject(a.cells, a.amount, bs, es, r, tzz);
       }
-      txxB[o] = txx;
-      tzzB[o] = tzz;
-      if (hasxz) txzB[o] = txz;
+      a.txxB[o] = txx;
+      a.tzzB[o] = tzz;
+      if (hasxz) a.txzB[o] = txz;
+    };
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, p4 = 0.f, p5 = 0.f, p6 = 0.f, p7 = 0.f;
+    // one sweep: iterations c < x0 only compute the first velocity columns
+    for (int c = x0 - 3; c < x1; c++) {
+      const int cc = c + 3;
+      int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+      cvx.range(a.cells, cc, ib0, ie0);
+      cvz.range(a.cells, cc, ib1, ie1);
+      if (c >= x0) cst.range(a.cells, c, bs, es);
+      // general code for domain edges, mirrors and sources; otherwise the
+      // straight-line code, with CPML terms where a strip is met
+      const bool gv = rf_v || colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
+      const bool gs = rf_s || colfull_s(c) || bs < es;
+      if (gv || rp_v || colpml_v(cc)) vel_psi(cc, p0, p1, p2, p3);
+      if (c >= x0 && (gs || rp_s || colpml_s(c))) str_psi(c, p4, p5, p6, p7);
+      wait_col(cc);
+      if (gv)
+        vel_edge(cc, p0, p1, p2, p3, ib0, ie0, ib1, ie1);
+      else
+        vel_strip(cc, p0, p1, p2, p3);
+      __syncthreads();
+      if (producer) issue(c + 7);
+      if (c >= x0) {
+        if (gs)
+          str_edge(c, p4, p5, p6, p7, bs, es);
+        else
+          str_strip(c, p4, p5, p6, p7);
+      }
     }
+  }
+  }
+  __syncthreads();
+  if (s_err && t == 0) {
+    // a wait gave up: let the copies still in flight land before the block's
+    // shared memory is released, then report
+    for (int cc = max(xbase, xlast - 7); cc <= xlast; cc++) {
+      const int j = cc - xbase;
+      mbar_wait(&bar[j & 7], (j >> 3) & 1);
+    }
+    atomicExch(a.err, 1);
   }
 }
 
@@ -266,6 +498,14 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   (void)ipw_mask;
   (void)it;
   (void)mode;
+  static int attr_dev[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_dev[dev]) {
+    GPI_CUDA(p, cudaFuncSetAttribute(k_e2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E2_SMEM));
+    GPI_CUDA(p, cudaFuncSetAttribute(k_e2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E2_SMEM));
+    attr_dev[dev] = 1;
+  }
   E2Args a;
   a.nz = p->d.nz;
   a.nx = p->d.nx;
@@ -306,9 +546,20 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.gptr = p->d_group_ptr;
   a.amount = p->d_amount;
   a.vonly = vonly;
-  const int blocks = p->nzb * p->nxb * p->d.nshots;
-  k_e2<128><<<blocks, 128, 0, p->stream>>>(a);
-  p->launches++;
+  a.err = p->d_err;
+  a.tiles = p->d_tiles;
+  // interior tiles on the straight-line kernel, the rest on the general one;
+  // the velocity-only half step runs every tile on the general kernel
+  const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
+  if (nf) {
+    k_e2<true><<<nf, E2_THREADS, E2_SMEM, p->stream>>>(a);
+    p->launches++;
+  }
+  a.tiles = p->d_tiles + nf;
+  if (ng) {
+    k_e2<false><<<ng, E2_THREADS, E2_SMEM, p->stream>>>(a);
+    p->launches++;
+  }
   GPI_CUDA(p, cudaGetLastError());
   p->cur[0] ^= 1;
   return GPI_OK;

@@ -48,6 +48,8 @@ static int32_t h_pj[kMaxPairs];
 static float h_pw[kMaxPairs];
 static int32_t h_gptr[2 * NKIND + 1];
 static float *h_wavptr[1];
+static constexpr int kMaxTiles = 1 << 16;
+static int3 h_tiles[kMaxTiles];
 static Plan g_plan;  // descriptor filled per call; its pointers point into the scratch
 
 static int nfail(int code, const char *msg) { return fail(nullptr, code, msg); }
@@ -140,6 +142,7 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
   }
   for (int i = 0; i < 2; i++) P.mod[i] = carve(P.fstride);
   for (int i = 0; i < 3; i++) P.coef[i] = carve(P.fstride);
+  P.d_err = (int *)carve(64);
 
   // ---- receivers: tasks and storage offsets ----
   int ntask = 0, nent = 0;
@@ -251,6 +254,12 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     P.d_group_ptr = (int32_t *)carve(2 * NKIND + 1);
     P.d_wav = (float **)carve(2);
     h_wavptr[0] = (float *)wavelets;
+    int nf = 0;
+    const int ntile = classify_tiles(P, h_cells, h_gptr, h_tiles, kMaxTiles, &nf);
+    if (ntile < 0) return nfail(GPI_E_INVALID, "grid too large for the no-alloc tile table");
+    P.n_tiles_fast = nf;
+    P.n_tiles_gen = ntile - nf;
+    P.d_tiles = (int3 *)carve((int64_t)(sizeof(int3) * ntile + 3) / 4);
     if (!room) return nfail(GPI_E_INVALID, "problem exceeds the 64 MiB no-alloc scratch");
     cudaStream_t s = P.stream;
     cudaMemcpyAsync(P.d_cells, h_cells, sizeof(InjCell) * m, cudaMemcpyHostToDevice, s);
@@ -258,6 +267,7 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     cudaMemcpyAsync(P.d_pair_w, h_pw, sizeof(float) * np, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.d_group_ptr, h_gptr, sizeof(h_gptr), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.d_wav, h_wavptr, sizeof(h_wavptr), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.d_tiles, h_tiles, sizeof(int3) * ntile, cudaMemcpyHostToDevice, s);
   }
   if (!room) return nfail(GPI_E_INVALID, "problem exceeds the 64 MiB no-alloc scratch");
   cudaStream_t s = P.stream;
@@ -270,6 +280,7 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     for (int q = 0; q < 4; q++) cudaMemsetAsync(P.psi[b][0][q], 0, P.psi_stride[q] * sizeof(float), s);
   }
   if (pool) cudaMemsetAsync(P.rec_pool, 0, pool * sizeof(float), s);
+  cudaMemsetAsync(P.d_err, 0, sizeof(int), s);
   // medium -> storage layout (device to device), then update coefficients
   for (int i = 0; i < 2; i++) {
     cudaMemcpy3DParms mp = {};

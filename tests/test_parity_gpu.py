@@ -68,6 +68,21 @@ def test_elastic2d_batch_matches_oracle(engine, surface):
 
 
 @pytest.mark.gpu
+def test_elastic2d_interior_tiles(engine):
+    """A grid large enough for tiles away from every strip and face, which
+    take the kernel's straight-line interior path."""
+    wl = configs.elastic2d_batch(nz=300, nx=420, nt=300, nshots=2, nrec=41)
+    ref, orc = O.forward(wl.as_dict(), return_oracle=True)
+    pa = wl.expt()
+    update(pa)
+    _compare_records(pa, ref, wl)
+    for f in ("tauxx", "tauzz", "tauxz", "vx", "vz"):
+        e = rel(pa.field(f, iss=1), orc.field(f))
+        assert e < TOL, (f, e)
+    orc.close()
+
+
+@pytest.mark.gpu
 def test_elastic2d_velocity_source(engine):
     wl = configs.elastic2d_batch(nz=100, nx=140, nt=300, nshots=2, nrec=19, src_field="vz")
     ref = O.forward(wl.as_dict())
