@@ -133,6 +133,9 @@ struct Plan {
   // kernel), then the tiles that meet a strip, a face or a source
   int3 *d_tiles = nullptr;
   int n_tiles_fast = 0, n_tiles_gen = 0;
+  // 2-D z-strip CPML memory: column stride and the window of a column that
+  // the general step kernel stages per ring slot
+  int zsw = 0, pzw = 0;
   std::vector<InjCell> h_cells;  // set by a kernel whose pipeline wait gave up
 };
 
@@ -148,6 +151,34 @@ inline int64_t soff(const Plan &p, int r, int y, int c) {
   return ((int64_t)(c - 1 + XOFF) * p.NYP + (p.d.ndim == 3 ? (y - 1 + YOFF) : 0)) * p.NZP + (r - 1 + ZOFF);
 }
 int nkind(int kind, int n, int h);
+
+// 2-D CPML memory of a z strip is stored as one column of 2*npml slots (top
+// strip, then bottom strip) per x index; the column stride is padded to 16
+// bytes so that a column window moves with one bulk copy.
+__host__ __device__ inline int zstrip_stride(int npml) { return (2 * npml + 3) & ~3; }
+// z strips read by a block of TZ rows starting at z0 (velocity halo and
+// mirror rows included, with margin): bit 0 the top strip, bit 1 the bottom
+__host__ __device__ inline int zstrip_touch(int z0, int TZ, int nz, int npml, bool lo, bool hi) {
+  int m = 0;
+  if (lo && z0 - 8 <= npml) m |= 1;
+  if (hi && z0 + TZ + 8 > nz - 6 - npml) m |= 2;
+  return m;
+}
+// first strip slot of the staged window of pzw slots (pzw from zstrip_window)
+__host__ __device__ inline int zstrip_off(int touch, int zsw, int pzw) { return touch == 2 ? zsw - pzw : 0; }
+// slots per column a block stages: the top half (from slot 0), the bottom
+// half (ending at the padded stride) or the whole column when a block meets
+// both strips; the largest over the z blocks of the plan
+inline int zstrip_window(int nzb, int TZ, int nz, int npml, bool lo, bool hi) {
+  const int zsw = zstrip_stride(npml);
+  int w = 0;
+  for (int zb = 0; zb < nzb; zb++) {
+    const int m = zstrip_touch(1 + zb * TZ, TZ, nz, npml, lo, hi);
+    const int need = m == 3 ? zsw : m == 1 ? (npml + 3) / 4 * 4 : m == 2 ? zsw - (npml & ~3) : 0;
+    w = w > need ? w : need;
+  }
+  return w;
+}
 
 // kernels (per physics)
 int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly);

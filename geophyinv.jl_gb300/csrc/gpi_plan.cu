@@ -139,7 +139,7 @@ static void choose_tiling(Plan &p) {
 
 static int64_t psi_len(const Plan &p, int axis) {
   const int64_t w = 2 * (int64_t)p.d.npml;
-  if (p.d.ndim == 2) return axis == 2 ? w * p.NZP : (int64_t)p.NXP * w;
+  if (p.d.ndim == 2) return axis == 2 ? w * p.NZP : (int64_t)p.NXP * p.zsw;
   if (axis == 2) return w * p.NYP * p.NZP;
   if (axis == 1) return (int64_t)p.NXP * w * p.NZP;
   return (int64_t)p.NXP * p.NYP * w;
@@ -171,8 +171,16 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   const int ny = d.ndim == 3 ? d.ny : 1;
   // CPML strips of the min and max faces must not overlap on any derivative
   // field (the shortest derivative axis is n - 2h).
-  const int nmin = std::min(d.nz, d.ndim == 3 ? std::min(d.ny, d.nx) : d.nx) - 2 * h;
-  if (nmin < 2 * d.npml + 1) return fail(nullptr, GPI_E_INVALID, "grid too small for two PML strips");
+  {
+    const int n3[3] = {d.nz, ny, d.nx};
+    const int lo3[3] = {GPI_ZMIN, GPI_YMIN, GPI_XMIN}, hi3[3] = {GPI_ZMAX, GPI_YMAX, GPI_XMAX};
+    for (int ax = 0; ax < 3; ax++) {
+      if (ax == 1 && d.ndim == 2) continue;
+      const int strips = ((d.pml_faces & lo3[ax]) ? 1 : 0) + ((d.pml_faces & hi3[ax]) ? 1 : 0);
+      if (n3[ax] - 2 * h < strips * d.npml + 1)
+        return fail(nullptr, GPI_E_INVALID, "grid too small for its PML strips");
+    }
+  }
   gpi_plan *pl = new gpi_plan();
   Plan &p = pl->p;
   p.d = d;
@@ -194,6 +202,10 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   p.NXP = d.nx + h + 2 * XOFF + 4;
   p.NYP = d.ndim == 3 ? (int)(p.nyb * p.TY + 2 * YOFF + 4) : 1;
   p.fstride = (int64_t)p.NZP * p.NYP * p.NXP;
+  if (d.ndim == 2) {
+    p.zsw = zstrip_stride(d.npml);
+    p.pzw = zstrip_window(p.nzb, p.TZ, d.nz, d.npml, d.pml_faces & GPI_ZMIN, d.pml_faces & GPI_ZMAX);
+  }
 
   // ---- pool layout ----
   std::vector<std::pair<float **, int64_t>> allocs;
@@ -664,8 +676,11 @@ int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int
         for (int ipw = 0; fast && ipw < p.d.npw; ipw++)
           for (int kind = 0; fast && kind < NKIND; kind++) {
             const int gi = (ipw * p.d.nshots + shot) * NKIND + kind;
+            // a block computes velocities of rows z0..z0+TZ+2 and columns
+            // x0..x1+2, stresses of rows z0..z0+TZ-1 and columns x0..x1-1
             for (int c = gptr[gi]; c < gptr[gi + 1]; c++)
-              if (cells[c].col >= x0 - 3 && cells[c].col <= x1 + 3) {
+              if (cells[c].col >= x0 - 3 && cells[c].col <= x1 + 3 && cells[c].row >= z0 - 1 &&
+                  cells[c].row <= z0 + p.TZ + 3) {
                 fast = false;
                 break;
               }

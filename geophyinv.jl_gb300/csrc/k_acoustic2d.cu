@@ -45,6 +45,7 @@ struct A2Args {
   int vonly;
   int *err;
   const int3 *tiles;  // (z-block, x-chunk, shot) per block
+  int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
 constexpr int A2_TZ = 128;
@@ -54,13 +55,22 @@ constexpr int A2_R4 = A2_TZ + 4;                       // velocity-input rows z0
 constexpr int A2_SLOT = A2_R8 + 4 * A2_R4 + A2_TZ;     // floats per ring slot
 constexpr size_t A2_SMEM = 128 + sizeof(float) * (8 * A2_SLOT + 2 * 8 * A2_R4);
 
+// CPML floats per ring slot of the general kernel: two z-strip windows
+// (dpdz, dvzdz) and the x-strip columns of dpdx and dvxdx
+inline int a2_psi_floats(const Plan &p) {
+  const bool zf = p.d.pml_faces & (GPI_ZMIN | GPI_ZMAX), xf = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
+  return (zf ? 2 * p.pzw : 0) + (xf ? 2 * A2_TZ : 0);
+}
+inline size_t a2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (A2_SLOT + psf) + 2 * 8 * A2_R4); }
+
 template <bool FAST>
-__global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
+__global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a) {
   constexpr int TZ = A2_TZ, R8 = A2_R8, R4 = A2_R4, SLOT = A2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
   float *ring = reinterpret_cast<float *>(smem + 128);  // [8][SLOT]: p | vx vz cx cz | dtK
-  float *svx = ring + 8 * SLOT;                          // [8][R4] new velocities
+  const int SL = FAST ? SLOT : SLOT + a.psf;            // floats per ring slot
+  float *svx = ring + 8 * SL;                            // [8][R4] new velocities
   float *svz = svx + 8 * R4;
   __shared__ int s_rng[3][2];
   __shared__ int s_err;
@@ -78,10 +88,19 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
   const int P6 = 6 * npml;
   auto S = [&](int rr, int cc) -> int64_t { return (int64_t)(cc + XOFF - 1) * NZP + (rr + ZOFF - 1); };
   auto XS = [&](int j, int rr) -> int64_t { return (int64_t)j * NZP + (rr + ZOFF - 1); };
-  auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * 2 * npml + j; };
+  auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * a.zsw + j; };
   auto psA = [&](int i) -> const float * { return a.psA[i] + shot * a.pss[i]; };
   auto psB = [&](int i) -> float * { return a.psB[i] + shot * a.pss[i]; };
   auto slot = [&](int cc) -> int { return (cc - xbase) & 7; };
+  // General kernel: the CPML memory of each column travels in its ring slot
+  // (z-strip windows of dpdz and dvzdz, x-strip columns of dpdx and dvxdx).
+  const int zt = FAST ? 0 : zstrip_touch(z0, TZ, nz, npml, zlo, zhi);
+  const int zoff = FAST ? 0 : zstrip_off(zt, a.zsw, a.pzw);
+  const int PZW = FAST ? 0 : a.pzw;
+  // z strip indexed by strip slot (i: 0 dpdz, 1 dvzdz), x strip by row
+  // (i: 0 dpdx, 1 dvxdx)
+  auto PZ = [&](int i, int cc) -> const float * { return ring + slot(cc) * SL + SLOT + i * PZW - zoff; };
+  auto PX = [&](int i, int cc) -> const float * { return ring + slot(cc) * SL + SLOT + 2 * PZW + i * TZ - z0; };
 
   if (t == 0) {
     for (int s = 0; s < 8; s++) mbar_init(&bar[s], 1);
@@ -101,8 +120,16 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
   auto issue = [&](int upto) {
     for (; next <= upto && next <= xlast; next++) {
       const int s = slot(next);
-      float *sl = ring + s * SLOT;
-      mbar_expect_tx(&bar[s], SLOT * 4);
+      float *sl = ring + s * SL;
+      uint32_t bytes = SLOT * 4;
+      int j0 = -1, j2 = -1;
+      if constexpr (!FAST) {
+        if (zt) bytes += 2 * PZW * 4;
+        j0 = pml_slot(next - 3, nx - 3, npml, xlo, xhi);
+        j2 = pml_slot(next, nx, npml, xlo, xhi);
+        bytes += ((j0 >= 0) + (j2 >= 0)) * TZ * 4;
+      }
+      mbar_expect_tx(&bar[s], bytes);
       const int64_t oV = S(z0, next);
       bulk_g2s(sl, a.pA + so + S(z0 - 4, next), R8 * 4, &bar[s]);
       float *v = sl + R8;
@@ -111,6 +138,17 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
       bulk_g2s(v + 2 * R4, a.cx + oV, R4 * 4, &bar[s]);
       bulk_g2s(v + 3 * R4, a.cz + oV, R4 * 4, &bar[s]);
       bulk_g2s(v + 4 * R4, a.dtK + oV, TZ * 4, &bar[s]);
+      if constexpr (!FAST) {
+        float *pz = sl + SLOT;
+        if (zt) {
+          const int64_t oz = ZS(next, zoff);
+          bulk_g2s(pz, psA(1) + oz, PZW * 4, &bar[s]);
+          bulk_g2s(pz + PZW, psA(3) + oz, PZW * 4, &bar[s]);
+        }
+        float *px = pz + 2 * PZW;
+        if (j0 >= 0) bulk_g2s(px, psA(0) + XS(j0, z0), TZ * 4, &bar[s]);
+        if (j2 >= 0) bulk_g2s(px + TZ, psA(2) + XS(j2, z0), TZ * 4, &bar[s]);
+      }
     }
   };
   if (producer) issue(xbase + 7);
@@ -131,18 +169,32 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
   const bool ownr = kq >= 0 && (kq < TZ || lastz);
   const bool vxr = kq >= 0 && kq < TZ && q >= 4 && q <= nz - 3, vzr = q >= 4 && q <= nz;
   const int jq1 = pml_slot(q - 3, nz - 3, npml, zlo, zhi);  // dpdz (z strip)
-  const int gsrc = (rzlo && q <= 2) ? 5 - q : (rzhi && q >= nz + 2) ? 2 * nz + 3 - q : 0;
+  // rows below nz+3 are never stored nor read
+  const int gsrc = (rzlo && q <= 2) ? 5 - q : (rzhi && q >= nz + 2 && q <= nz + 3) ? 2 * nz + 3 - q : 0;
   const int r = z0 + t;
   const bool srow = t < TZ && r <= nz;
   const int jr3 = pml_slot(r, nz, npml, zlo, zhi);  // dvzdz (z strip)
 
   for (int cc = xbase; cc < x0 && cc <= xlast; cc++) wait_col(cc);
 
+  // CPML: psi' = b psi + a D ; D' = D kI + psi'  (profile [a | b | kI])
   auto cpml_p = [&](float D, int q4, int j, float psi_old, float *dst, bool own) -> float {
     const float *cf = a.pml + q4 * P6;
-    const float psi = cf[2 * npml + j] * psi_old + cf[j] * D;
+    const float psi = __ldg(cf + 2 * npml + j) * psi_old + __ldg(cf + j) * D;
     if (own) *dst = psi;
-    return D * cf[4 * npml + j] + psi;
+    return D * __ldg(cf + 4 * npml + j) + psi;
+  };
+  // the z-strip profile of this thread's rows, loaded once
+  auto zprof = [&](int q4, int j) -> float3 {
+    if (FAST || j < 0) return make_float3(0.f, 0.f, 0.f);
+    const float *cf = a.pml + q4 * P6;
+    return make_float3(__ldg(cf + j), __ldg(cf + 2 * npml + j), __ldg(cf + 4 * npml + j));
+  };
+  const float3 cq1 = zprof(1, jq1), cr3 = zprof(3, jr3);
+  auto cpml_z = [&](float D, float3 cf, float psi_old, float *dst, bool own) -> float {
+    const float psi = cf.y * psi_old + cf.x * D;
+    if (own) *dst = psi;
+    return D * cf.z + psi;
   };
 
   // Dispatch per warp and per column: a warp runs the straight-line code
@@ -185,81 +237,88 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
       }
     }
   } else {
-  const bool rfv_t = vact && (q <= 4 || q >= nz - 4);
-  const bool rfs_t = t < TZ && r >= nz - 4;
-  const bool rpv_t = vact && jq1 >= 0;
-  const bool rps_t = t < TZ && jr3 >= 0;
-  const bool rf_v = __any_sync(0xffffffffu, rfv_t), rf_s = __any_sync(0xffffffffu, rfs_t);
-  const bool rp_v = __any_sync(0xffffffffu, rpv_t), rp_s = __any_sync(0xffffffffu, rps_t);
+  // columns that need the full general code: x edges and mirrors, sources
   auto colfull_v = [&](int cc) { return a.vonly || cc <= 4 || cc >= nx - 4; };
   auto colfull_s = [&](int c) { return a.vonly || c >= nx - 4; };
-  auto colpml_v = [&](int cc) { return pml_slot(cc - 3, nx - 3, npml, xlo, xhi) >= 0; };
-  auto colpml_s = [&](int c) { return pml_slot(c, nx, npml, xlo, xhi) >= 0; };
+  // per-row constants of the band path (vxr already excludes the halo rows)
+  const int kqc = vact ? kq : 0;
+  const bool vzb = vact && vzr;
+  const int jq1v = vzb ? jq1 : -1, jr3v = srow ? jr3 : -1;
+  // ghost rows of vz (dirichletzmin!/zmax!) read their mirror source from
+  // the lane that computes it, when that lane is in the same warp
+  const int lane = t & 31;
+  const int gdl = gsrc ? gsrc - q : 0;
+  const bool gok = lane + gdl >= 0 && lane + gdl < 32;
+  const int glane = gok ? lane + gdl : lane;
+  const bool gany = __any_sync(0xffffffffu, gsrc != 0);
   {
-    // CPML strip, otherwise interior (psi prefetched by vel_psi / str_psi)
-    auto vel_strip = [&](int cc, float p0, float p1) {
-      if (!vact) return;
-      const int k = kq, kk = kq + 4, s = slot(cc);
-      const float *pc = ring + s * SLOT, *v0 = pc + R8;
-      const bool own = cc < x1 && kq < TZ;
-      float Dz = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
-      if (jq1 >= 0) Dz = cpml_p(Dz, 1, jq1, p1, psB(1) + ZS(cc, jq1), own);
-      const float vz = v0[R4 + k] + v0[3 * R4 + k] * Dz;
-      svz[s * R4 + k] = vz;
-      if (kq < TZ) {
-        const float *p3 = ring + slot(cc - 3) * SLOT, *p2 = ring + slot(cc - 2) * SLOT,
-                    *p1s = ring + slot(cc - 1) * SLOT;
-        float Dx = st4(p3[kk], p2[kk], p1s[kk], pc[kk]) * a.dxI;
-        const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
-        if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, p0, psB(0) + XS(j0, q), own);
-        const float vx = v0[k] + v0[2 * R4 + k] * Dx;
-        svx[s * R4 + k] = vx;
-        if (own) {
-          const int64_t o = so + S(q, cc);
-          a.vxB[o] = vx;
-          a.vzB[o] = vz;
-        }
-      }
-    };
-    auto str_strip = [&](int c, float p2, float p3) {
-      if (t >= TZ) return;
-      const int k = t;
-      const float *pc = ring + slot(c) * SLOT;
-      float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
-                     svx[slot(c + 3) * R4 + k]) * a.dxI;
-      const int j2 = pml_slot(c, nx, npml, xlo, xhi);
-      if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, p2, psB(2) + XS(j2, r), true);
-      const float *w = svz + slot(c) * R4;
-      float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
-      if (jr3 >= 0) Dz = cpml_p(Dz, 3, jr3, p3, psB(3) + ZS(c, jr3), true);
-      a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
-    };
-    float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)
-    auto vel_psi = [&](int cc, float &p0, float &p1) {
-      p0 = p1 = 0.f;
-      if (!vact) return;
-      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
-      if (vxr && cc >= 4 && cc <= nx && j0 >= 0) p0 = psA(0)[XS(j0, q)];
-      if (vzr && cc >= 4 && cc <= nx - 3 && jq1 >= 0) p1 = psA(1)[ZS(cc, jq1)];
-    };
     // vz at row qq of column cc before its source (source of a mirror row)
     auto vz_any = [&](int qq, int cc) -> float {
       const int kv = qq - z0;
-      const float *pc = ring + slot(cc) * SLOT, *v0 = pc + R8;
+      const float *pc = ring + slot(cc) * SL, *v0 = pc + R8;
       float v = v0[R4 + kv];
       if (qq >= 4 && qq <= nz && cc >= 4 && cc <= nx - 3) {
         const int kk = kv + 4;
         float D = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
         const int j = pml_slot(qq - 3, nz - 3, npml, zlo, zhi);
-        if (j >= 0) D = cpml_p(D, 1, j, psA(1)[ZS(cc, j)], nullptr, false);
+        if (j >= 0) D = cpml_p(D, 1, j, PZ(0, cc)[j], nullptr, false);
         v = v + v0[3 * R4 + kv] * D;
       }
       return v;
     };
-    auto vel_edge = [&](int cc, float p0, float p1, int ib0, int ie0, int ib1, int ie1) {
+    // Columns away from the x edges and from sources: every row in one
+    // pass; rows outside an update domain keep their value, CPML terms where
+    // a strip is met (psi staged in the ring slot of the column)
+    auto vel_band = [&](int cc) {
+      const int k = kqc, kk = kqc + 4, s = slot(cc);
+      const float *pc = ring + s * SL, *v0 = pc + R8;
+      const bool ownc = cc < x1;
+      float vz = v0[R4 + k];
+      if (vzb) {
+        float Dz = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
+        if (jq1v >= 0) Dz = cpml_z(Dz, cq1, PZ(0, cc)[jq1v], psB(1) + ZS(cc, jq1v), ownc && ownr);
+        vz = vz + v0[3 * R4 + k] * Dz;
+      }
+      if (gany) {
+        const float g = __shfl_sync(0xffffffffu, vz, glane);
+        if (gsrc) vz = gok ? -g : -vz_any(gsrc, cc);
+      }
+      if (vact) svz[s * R4 + k] = vz;
+      const int64_t o = so + S(q, cc);
+      if (ownc && ownr && q <= nz + 3) a.vzB[o] = vz;
+      if (vact && kq < TZ) {
+        float vx = v0[k];
+        if (vxr) {
+          const float *p3 = ring + slot(cc - 3) * SL, *p2 = ring + slot(cc - 2) * SL,
+                      *p1s = ring + slot(cc - 1) * SL;
+          float Dx = st4(p3[kk], p2[kk], p1s[kk], pc[kk]) * a.dxI;
+          const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
+          if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownc && ownr && q <= nz);
+          vx = vx + v0[2 * R4 + k] * Dx;
+        }
+        svx[s * R4 + k] = vx;
+        if (ownc && ownr && q <= nz) a.vxB[o] = vx;
+      }
+    };
+    auto str_band = [&](int c) {
+      if (t >= TZ) return;  // the halo warp as a whole
+      if (!srow) return;
+      const int k = t;
+      const float *pc = ring + slot(c) * SL;
+      float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
+                     svx[slot(c + 3) * R4 + k]) * a.dxI;
+      const int j2 = pml_slot(c, nx, npml, xlo, xhi);
+      if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, PX(1, c)[r], psB(2) + XS(j2, r), true);
+      const float *w = svz + slot(c) * R4;
+      float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
+      if (jr3v >= 0) Dz = cpml_z(Dz, cr3, PZ(1, c)[jr3v], psB(3) + ZS(c, jr3v), true);
+      a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+    };
+    float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)
+    auto vel_edge = [&](int cc, int ib0, int ie0, int ib1, int ie1) {
       if (!vact) return;
       const int k = kq, kk = kq + 4, s = slot(cc);
-      const float *pc = ring + s * SLOT, *v0 = pc + R8;
+      const float *pc = ring + s * SL, *v0 = pc + R8;
       const bool ownc = cc >= x0 && (cc < x1 || lastx);
       if (kq < TZ) {
         const bool ownx = ownc && ownr && q <= nz;
@@ -269,11 +328,11 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
         } else {
           vx = v0[k];
           if (vxr && cc >= 4 && cc <= nx) {
-            const float *p3 = ring + slot(cc - 3) * SLOT, *p2 = ring + slot(cc - 2) * SLOT,
-                        *p1 = ring + slot(cc - 1) * SLOT;
+            const float *p3 = ring + slot(cc - 3) * SL, *p2 = ring + slot(cc - 2) * SL,
+                        *p1 = ring + slot(cc - 1) * SL;
             float D = st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI;
             const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
-            if (j0 >= 0) D = cpml_p(D, 0, j0, p0, psB(0) + XS(j0, q), ownx);
+            if (j0 >= 0) D = cpml_p(D, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
             vx = vx + v0[2 * R4 + k] * D;
           }
           if (cc == nx) vpre = vx;
@@ -299,7 +358,7 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
         vz = v0[R4 + k];
         if (vzr && cc >= 4 && cc <= nx - 3) {
           float D = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
-          if (jq1 >= 0) D = cpml_p(D, 1, jq1, p1, psB(1) + ZS(cc, jq1), ownc && ownr && cc <= nx);
+          if (jq1 >= 0) D = cpml_z(D, cq1, PZ(0, cc)[jq1], psB(1) + ZS(cc, jq1), ownc && ownr && cc <= nx);
           vz = vz + v0[3 * R4 + k] * D;
         }
       }
@@ -307,32 +366,24 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
       svz[s * R4 + k] = vz;
       if (ownc && ownr && cc <= nx && q <= nz + 3) a.vzB[so + S(q, cc)] = vz;
     };
-    auto str_psi = [&](int c, float &p2, float &p3) {
-      p2 = p3 = 0.f;
-      if (!srow) return;
-      const int j2 = pml_slot(c, nx, npml, xlo, xhi);
-      if (j2 >= 0) p2 = psA(2)[XS(j2, r)];
-      if (jr3 >= 0) p3 = psA(3)[ZS(c, jr3)];
-    };
-    auto str_edge = [&](int c, float p2, float p3, int bs, int es) {
+    auto str_edge = [&](int c, int bs, int es) {
       if (!srow) return;
       const int k = t;
-      const float *pc = ring + slot(c) * SLOT;
+      const float *pc = ring + slot(c) * SL;
       float pn = pc[k + 4];
       if (!a.vonly) {
         float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
                        svx[slot(c + 3) * R4 + k]) * a.dxI;
         const int j2 = pml_slot(c, nx, npml, xlo, xhi);
-        if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, p2, psB(2) + XS(j2, r), true);
+        if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, PX(1, c)[r], psB(2) + XS(j2, r), true);
         const float *w = svz + slot(c) * R4;
         float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
-        if (jr3 >= 0) Dz = cpml_p(Dz, 3, jr3, p3, psB(3) + ZS(c, jr3), true);
+        if (jr3 >= 0) Dz = cpml_z(Dz, cr3, PZ(1, c)[jr3], psB(3) + ZS(c, jr3), true);
         pn = pn + (Dx + Dz) * pc[R8 + 4 * R4 + k];
         inject(a.cells, a.amount, bs, es, r, pn);  // add_stress_source!
       }
       a.pB[so + S(r, c)] = pn;
     };
-    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
     // one sweep: iterations c < x0 only compute the first velocity columns
     for (int c = x0 - 3; c < x1; c++) {
       const int cc = c + 3;
@@ -340,24 +391,22 @@ __global__ void __launch_bounds__(A2_THREADS, 6) k_a2(const A2Args a) {
       cvx.range(a.cells, cc, ib0, ie0);
       cvz.range(a.cells, cc, ib1, ie1);
       if (c >= x0) cst.range(a.cells, c, bs, es);
-      // general code for domain edges, mirrors and sources; otherwise the
-      // straight-line code, with CPML terms where a strip is met
-      const bool gv = rf_v || colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
-      const bool gs = rf_s || colfull_s(c) || bs < es;
-      if (gv || rp_v || colpml_v(cc)) vel_psi(cc, p0, p1);
-      if (c >= x0 && (gs || rp_s || colpml_s(c))) str_psi(c, p2, p3);
+      // general code for x edges, mirrors and sources (block-uniform);
+      // otherwise the band code over every row
+      const bool gv = colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
+      const bool gs = colfull_s(c) || bs < es;
       wait_col(cc);
       if (gv)
-        vel_edge(cc, p0, p1, ib0, ie0, ib1, ie1);
+        vel_edge(cc, ib0, ie0, ib1, ie1);
       else
-        vel_strip(cc, p0, p1);
+        vel_band(cc);
       __syncthreads();
       if (producer) issue(c + 7);
       if (c >= x0) {
         if (gs)
-          str_edge(c, p2, p3, bs, es);
+          str_edge(c, bs, es);
         else
-          str_strip(c, p2, p3);
+          str_band(c);
       }
     }
   }
@@ -376,11 +425,11 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   if (mode == GPI_ADJOINT && !vonly) return step_adjoint_acoustic2d(p, it);
   (void)ipw_mask;
   static int attr_dev[64] = {0};
+  static size_t attr_gen[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !attr_dev[dev]) {
     GPI_CUDA(p, cudaFuncSetAttribute(k_a2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A2_SMEM));
-    GPI_CUDA(p, cudaFuncSetAttribute(k_a2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A2_SMEM));
     attr_dev[dev] = 1;
   }
   A2Args a;
@@ -418,6 +467,14 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.vonly = vonly;
   a.err = p->d_err;
   a.tiles = p->d_tiles;
+  a.zsw = p->zsw;
+  a.pzw = p->pzw;
+  a.psf = a2_psi_floats(*p);
+  const size_t gsmem = a2_smem_general(a.psf);
+  if (dev < 64 && attr_gen[dev] < gsmem) {
+    GPI_CUDA(p, cudaFuncSetAttribute(k_a2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
+    attr_gen[dev] = gsmem;
+  }
   const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
   if (nf) {
     k_a2<true><<<nf, A2_THREADS, A2_SMEM, p->stream>>>(a);
@@ -425,7 +482,7 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   }
   a.tiles = p->d_tiles + nf;
   if (ng) {
-    k_a2<false><<<ng, A2_THREADS, A2_SMEM, p->stream>>>(a);
+    k_a2<false><<<ng, A2_THREADS, gsmem, p->stream>>>(a);
     p->launches++;
   }
   GPI_CUDA(p, cudaGetLastError());

@@ -47,6 +47,7 @@ struct E2Args {
   int vonly;
   int *err;  // set when a pipeline wait gives up
   const int3 *tiles;  // (z-block, x-chunk, shot) per block
+  int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
 constexpr int E2_TZ = 128;
@@ -56,13 +57,23 @@ constexpr int E2_R4 = E2_TZ + 4;                                // velocity-inpu
 constexpr int E2_SLOT = 3 * E2_R8 + 4 * E2_R4 + 3 * E2_TZ;      // floats per ring slot
 constexpr size_t E2_SMEM = 128 + sizeof(float) * (8 * E2_SLOT + 2 * 8 * E2_R4);
 
+// CPML floats per ring slot of the general kernel: four z-strip windows
+// (derivatives 2, 3, 5, 6) and the x-strip columns of derivatives 0, 1
+// (velocity rows) and 4, 7 (stress rows)
+inline int e2_psi_floats(const Plan &p) {
+  const bool zf = p.d.pml_faces & (GPI_ZMIN | GPI_ZMAX), xf = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
+  return (zf ? 4 * p.pzw : 0) + (xf ? 2 * E2_R4 + 2 * E2_TZ : 0);
+}
+inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (E2_SLOT + psf) + 2 * 8 * E2_R4); }
+
 template <bool FAST>
-__global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
+__global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a) {
   constexpr int TZ = E2_TZ, R8 = E2_R8, R4 = E2_R4, SLOT = E2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // one mbarrier per ring slot
   float *ring = reinterpret_cast<float *>(smem + 128);  // [8][SLOT]
-  float *svx = ring + 8 * SLOT;                          // [8][R4] new velocities
+  const int SL = FAST ? SLOT : SLOT + a.psf;            // floats per ring slot
+  float *svx = ring + 8 * SL;                            // [8][R4] new velocities
   float *svz = svx + 8 * R4;
   __shared__ int s_rng[3][2];
   __shared__ int s_err;
@@ -81,15 +92,28 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
   const int P6 = 6 * npml;  // floats per derivative field in a.pml
   auto S = [&](int rr, int cc) -> int64_t { return (int64_t)(cc + XOFF - 1) * NZP + (rr + ZOFF - 1); };
   auto XS = [&](int j, int rr) -> int64_t { return (int64_t)j * NZP + (rr + ZOFF - 1); };       // x strip
-  auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * 2 * npml + j; };  // z strip
+  auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * a.zsw + j; };  // z strip
   auto psA = [&](int q) -> const float * { return a.psA[q] + shot * a.pss[q]; };
   auto psB = [&](int q) -> float * { return a.psB[q] + shot * a.pss[q]; };
+  // General kernel: the CPML memory of each column travels in its ring slot
+  // (z-strip windows of derivatives 2, 3, 5, 6 and x-strip columns of
+  // derivatives 0, 1, 4, 7), so no thread waits on a global load.
+  const int zt = FAST ? 0 : zstrip_touch(z0, TZ, nz, npml, zlo, zhi);
+  const int zoff = FAST ? 0 : zstrip_off(zt, a.zsw, a.pzw);
+  const int PZW = FAST ? 0 : a.pzw;
   // ring views of input column cc
   auto slot = [&](int cc) -> int { return (cc - xbase) & 7; };
-  auto T = [&](int f, int cc) -> const float * { return ring + slot(cc) * SLOT + f * R8; };           // txx tzz txz
-  auto V = [&](int f, int cc) -> const float * { return ring + slot(cc) * SLOT + 3 * R8 + f * R4; };  // vx vz cx cz
+  auto T = [&](int f, int cc) -> const float * { return ring + slot(cc) * SL + f * R8; };           // txx tzz txz
+  auto V = [&](int f, int cc) -> const float * { return ring + slot(cc) * SL + 3 * R8 + f * R4; };  // vx vz cx cz
   auto C = [&](int f, int cc) -> const float * {
-    return ring + slot(cc) * SLOT + 3 * R8 + 4 * R4 + f * TZ;  // dtM dtl mu
+    return ring + slot(cc) * SL + 3 * R8 + 4 * R4 + f * TZ;  // dtM dtl mu
+  };
+  // staged CPML memory of column cc: z strip indexed by strip slot
+  // (i: 0 dtauzzdz, 1 dtauxzdz, 2 dvzdz, 3 dvxdz), x strip by row (i: 0
+  // dtauxxdx, 1 dtauxzdx over velocity rows, 2 dvxdx, 3 dvzdx over stress rows)
+  auto PZ = [&](int i, int cc) -> const float * { return ring + slot(cc) * SL + SLOT + i * PZW - zoff; };
+  auto PX = [&](int i, int cc) -> const float * {
+    return ring + slot(cc) * SL + SLOT + 4 * PZW + (i < 2 ? i * R4 : 2 * R4 + (i - 2) * TZ) - z0;
   };
 
   if (t == 0) {
@@ -111,8 +135,19 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
   auto issue = [&](int upto) {
     for (; next <= upto && next <= xlast; next++) {
       const int s = slot(next);
-      float *sl = ring + s * SLOT;
-      mbar_expect_tx(&bar[s], SLOT * 4);
+      float *sl = ring + s * SL;
+      uint32_t bytes = SLOT * 4;
+      int jx[4] = {-1, -1, -1, -1};
+      if constexpr (!FAST) {
+        if (zt) bytes += 4 * PZW * 4;
+        jx[0] = pml_slot(next - 3, nx - 3, npml, xlo, xhi);
+        jx[1] = pml_slot(next - 3, nx - 6, npml, xlo, xhi);
+        jx[2] = pml_slot(next, nx, npml, xlo, xhi);
+        jx[3] = pml_slot(next, nx - 3, npml, xlo, xhi);
+        for (int i = 0; i < 4; i++)
+          if (jx[i] >= 0) bytes += (i < 2 ? R4 : TZ) * 4;
+      }
+      mbar_expect_tx(&bar[s], bytes);
       const int64_t oT = so + S(z0 - 4, next), oV = S(z0, next);
       bulk_g2s(sl + 0 * R8, a.txxA + oT, R8 * 4, &bar[s]);
       bulk_g2s(sl + 1 * R8, a.tzzA + oT, R8 * 4, &bar[s]);
@@ -126,6 +161,21 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
       bulk_g2s(cf + 0 * TZ, a.dtM + oV, TZ * 4, &bar[s]);
       bulk_g2s(cf + 1 * TZ, a.dtl + oV, TZ * 4, &bar[s]);
       bulk_g2s(cf + 2 * TZ, a.mu + oV, TZ * 4, &bar[s]);
+      if constexpr (!FAST) {
+        float *pz = sl + SLOT;
+        if (zt) {
+          const int64_t oz = ZS(next, zoff);
+          bulk_g2s(pz + 0 * PZW, psA(2) + oz, PZW * 4, &bar[s]);
+          bulk_g2s(pz + 1 * PZW, psA(3) + oz, PZW * 4, &bar[s]);
+          bulk_g2s(pz + 2 * PZW, psA(5) + oz, PZW * 4, &bar[s]);
+          bulk_g2s(pz + 3 * PZW, psA(6) + oz, PZW * 4, &bar[s]);
+        }
+        float *px = pz + 4 * PZW;
+        if (jx[0] >= 0) bulk_g2s(px, psA(0) + XS(jx[0], z0), R4 * 4, &bar[s]);
+        if (jx[1] >= 0) bulk_g2s(px + R4, psA(1) + XS(jx[1], z0), R4 * 4, &bar[s]);
+        if (jx[2] >= 0) bulk_g2s(px + 2 * R4, psA(4) + XS(jx[2], z0), TZ * 4, &bar[s]);
+        if (jx[3] >= 0) bulk_g2s(px + 2 * R4 + TZ, psA(7) + XS(jx[3], z0), TZ * 4, &bar[s]);
+      }
     }
   };
   if (producer) issue(xbase + 7);
@@ -149,8 +199,9 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
   const bool vxr = q >= 4 && q <= nz - 3, vzr = q >= 4 && q <= nz;
   const int jq3 = pml_slot(q - 3, nz - 6, npml, zlo, zhi);  // dtauxzdz (z strip)
   const int jq2 = pml_slot(q - 3, nz - 3, npml, zlo, zhi);  // dtauzzdz (z strip)
-  // vz mirror source of a ghost row (dirichletzmin!/zmax!), 0 otherwise
-  const int gsrc = (rzlo && q <= 2) ? 5 - q : (rzhi && q >= nz + 2) ? 2 * nz + 3 - q : 0;
+  // vz mirror source of a ghost row (dirichletzmin!/zmax!), 0 otherwise;
+  // rows below nz+3 are never stored nor read
+  const int gsrc = (rzlo && q <= 2) ? 5 - q : (rzhi && q >= nz + 2 && q <= nz + 3) ? 2 * nz + 3 - q : 0;
   const int r = z0 + t;
   const bool srow = t < TZ && r <= nz;
   const int jr5 = pml_slot(r, nz, npml, zlo, zhi);      // dvzdz (z strip)
@@ -158,12 +209,24 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
   const bool xzrow = r <= nz - 3;
   const bool fsrow = fsurf && r == 1;
 
-  // CPML with a prefetched psi: psi' = b psi + a D ; D' = D kI + psi'
+  // CPML: psi' = b psi + a D ; D' = D kI + psi'  (profile [a | b | kI])
   auto cpml_p = [&](float D, int q8, int j, float psi_old, float *dst, bool own) -> float {
     const float *cf = a.pml + q8 * P6;
-    const float psi = cf[2 * npml + j] * psi_old + cf[j] * D;
+    const float psi = __ldg(cf + 2 * npml + j) * psi_old + __ldg(cf + j) * D;
     if (own) *dst = psi;
-    return D * cf[4 * npml + j] + psi;
+    return D * __ldg(cf + 4 * npml + j) + psi;
+  };
+  // the z-strip profile of this thread's rows, loaded once
+  auto zprof = [&](int q8, int j) -> float3 {
+    if (FAST || j < 0) return make_float3(0.f, 0.f, 0.f);
+    const float *cf = a.pml + q8 * P6;
+    return make_float3(__ldg(cf + j), __ldg(cf + 2 * npml + j), __ldg(cf + 4 * npml + j));
+  };
+  const float3 cq2 = zprof(2, jq2), cq3 = zprof(3, jq3), cr5 = zprof(5, jr5), cr6 = zprof(6, jr6);
+  auto cpml_z = [&](float D, float3 cf, float psi_old, float *dst, bool own) -> float {
+    const float psi = cf.y * psi_old + cf.x * D;
+    if (own) *dst = psi;
+    return D * cf.z + psi;
   };
   // vz at row qq of column cc before its source (source of a mirror row)
   auto vz_any = [&](int qq, int cc) -> float {
@@ -173,11 +236,11 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
       const int k = qq - z0 + 4;
       float Dx = st4(T(2, cc - 3)[k - 3], T(2, cc - 2)[k - 3], T(2, cc - 1)[k - 3], T(2, cc)[k - 3]) * a.dxI;
       int j = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
-      if (j >= 0) Dx = cpml_p(Dx, 1, j, psA(1)[XS(j, qq)], nullptr, false);
+      if (j >= 0) Dx = cpml_p(Dx, 1, j, PX(1, cc)[qq], nullptr, false);
       const float *zz = T(1, cc);
       float Dz = st4(zz[k - 3], zz[k - 2], zz[k - 1], zz[k]) * a.dzI;
       j = pml_slot(qq - 3, nz - 3, npml, zlo, zhi);
-      if (j >= 0) Dz = cpml_p(Dz, 2, j, psA(2)[ZS(cc, j)], nullptr, false);
+      if (j >= 0) Dz = cpml_p(Dz, 2, j, PZ(0, cc)[j], nullptr, false);
       v = v - V(3, cc)[kv] * (Dx + Dz);
     }
     return v;
@@ -189,10 +252,10 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
                 *u3 = svx + slot(c + 3) * R4, *w = svz + slot(c) * R4;
     float dvxdx = st4(u0[kk], u1[kk], u2[kk], u3[kk]) * a.dxI;
     int j = pml_slot(c, nx, npml, xlo, xhi);
-    if (j >= 0) dvxdx = cpml_p(dvxdx, 4, j, psA(4)[XS(j, 2)], nullptr, false);
+    if (j >= 0) dvxdx = cpml_p(dvxdx, 4, j, PX(2, c)[2], nullptr, false);
     float dvzdz = st4(w[kk], w[kk + 1], w[kk + 2], w[kk + 3]) * a.dzI;
     j = pml_slot(2, nz, npml, zlo, zhi);
-    if (j >= 0) dvzdz = cpml_p(dvzdz, 5, j, psA(5)[ZS(c, j)], nullptr, false);
+    if (j >= 0) dvzdz = cpml_p(dvzdz, 5, j, PZ(2, c)[j], nullptr, false);
     return T(1, c)[kk + 4] - (C(0, c)[kk] * dvzdz) - (C(1, c)[kk] * (dvxdx));
   };
   float vpre = 0.f;  // vx[q, nx] before its source (xmax mirror)
@@ -254,102 +317,111 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
       if (c >= x0) str_fast(c);
     }
   } else {
-  // rows / columns that need the full general code: domain edges, mirror
-  // rows and columns, the free surface (sources are checked per column)
-  const bool rfv_t = vact && (q <= 4 || q >= nz - 4);
-  const bool rfs_t = t < TZ && (r <= 1 || r >= nz - 4);
-  // rows whose only special property is a CPML strip
-  const bool rpv_t = vact && (jq2 >= 0 || jq3 >= 0);
-  const bool rps_t = t < TZ && (jr5 >= 0 || jr6 >= 0);
-  const bool rf_v = __any_sync(0xffffffffu, rfv_t), rf_s = __any_sync(0xffffffffu, rfs_t);
-  const bool rp_v = __any_sync(0xffffffffu, rpv_t), rp_s = __any_sync(0xffffffffu, rps_t);
+  // columns that need the full general code: x edges and mirrors, sources
   auto colfull_v = [&](int cc) { return a.vonly || cc <= 4 || cc >= nx - 4; };
   auto colfull_s = [&](int c) { return a.vonly || c <= 1 || c >= nx - 4; };
-  auto colpml_v = [&](int cc) {
-    return pml_slot(cc - 3, nx - 3, npml, xlo, xhi) >= 0 || pml_slot(cc - 3, nx - 6, npml, xlo, xhi) >= 0;
-  };
-  auto colpml_s = [&](int c) {
-    return pml_slot(c, nx, npml, xlo, xhi) >= 0 || pml_slot(c, nx - 3, npml, xlo, xhi) >= 0;
-  };
+  // per-row constants of the band path: the row inside each update domain,
+  // the CPML slots only where the row is updated
+  const int kqc = vact ? kq : 0;
+  const bool vxb = vact && vxr, vzb = vact && vzr;
+  const int jq3v = vxb ? jq3 : -1, jq2v = vzb ? jq2 : -1;
+  const int jr5v = srow ? jr5 : -1, jr6v = (srow && xzrow) ? jr6 : -1;
+  // ghost rows of vz (dirichletzmin!/zmax!) read their mirror source from
+  // the lane that computes it, when that lane is in the same warp
+  const int lane = t & 31;
+  const int gdl = gsrc ? gsrc - q : 0;
+  const bool gok = lane + gdl >= 0 && lane + gdl < 32;
+  const int glane = gok ? lane + gdl : lane;
+  const bool gany = __any_sync(0xffffffffu, gsrc != 0);
+  const bool fsblk = fsurf && z0 == 1;  // the free-surface row is lane 0 of warp 0
   {
-    // CPML strip, otherwise interior: the straight-line code plus the
-    // memory-variable updates (psi prefetched by vel_psi / str_psi)
-    auto vel_strip = [&](int cc, float p0, float p1, float p2, float p3) {
-      if (!vact) return;
-      const int k = kq, kk = kq + 4, s = slot(cc);
-      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
-      const bool own = cc < x1 && kq < TZ;
-      const float *b3 = ring + slot(cc - 3) * SLOT, *b2 = ring + slot(cc - 2) * SLOT,
-                  *b1 = ring + slot(cc - 1) * SLOT, *b0 = ring + s * SLOT;
+    // Columns away from the x edges and from sources: every row in one
+    // pass; rows outside an update domain keep their value, CPML terms where
+    // a strip is met (psi staged in the ring slot of the column)
+    auto vel_band = [&](int cc) {
+      const int k = kqc, kk = kqc + 4, s = slot(cc);
+      const int j0 = vxb ? pml_slot(cc - 3, nx - 3, npml, xlo, xhi) : -1;
+      const int j1 = vzb ? pml_slot(cc - 3, nx - 6, npml, xlo, xhi) : -1;
+      const bool ownc = cc < x1;
+      const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && q <= nz + 3;
+      const float *b3 = ring + slot(cc - 3) * SL, *b2 = ring + slot(cc - 2) * SL,
+                  *b1 = ring + slot(cc - 1) * SL, *b0 = ring + s * SL;
       const float *v0 = b0 + 3 * R8, *z3 = b3 + 2 * R8, *zz = b0 + R8;
-      float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
-      if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, p0, psB(0) + XS(j0, q), own);
-      float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
-      if (jq3 >= 0) Dz = cpml_p(Dz, 3, jq3, p3, psB(3) + ZS(cc, jq3), own);
-      const float vx = v0[k] - v0[2 * R4 + k] * (Dx + Dz);
-      float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
-      if (j1 >= 0) Dx2 = cpml_p(Dx2, 1, j1, p1, psB(1) + XS(j1, q), own);
-      float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
-      if (jq2 >= 0) Dz2 = cpml_p(Dz2, 2, jq2, p2, psB(2) + ZS(cc, jq2), own);
-      const float vz = v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2);
-      svx[s * R4 + k] = vx;
-      svz[s * R4 + k] = vz;
-      if (own) {
-        const int64_t o = so + S(q, cc);
-        a.vxB[o] = vx;
-        a.vzB[o] = vz;
+      float vx = v0[k];
+      if (vxb) {
+        float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
+        if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
+        float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
+        if (jq3v >= 0) Dz = cpml_z(Dz, cq3, PZ(1, cc)[jq3v], psB(3) + ZS(cc, jq3v), ownx);
+        vx = vx - v0[2 * R4 + k] * (Dx + Dz);
       }
+      float vz = v0[R4 + k];
+      if (vzb) {
+        float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
+        if (j1 >= 0) Dx2 = cpml_p(Dx2, 1, j1, PX(1, cc)[q], psB(1) + XS(j1, q), ownz);
+        float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
+        if (jq2v >= 0) Dz2 = cpml_z(Dz2, cq2, PZ(0, cc)[jq2v], psB(2) + ZS(cc, jq2v), ownz);
+        vz = vz - v0[3 * R4 + k] * (Dx2 + Dz2);
+      }
+      if (gany) {
+        const float g = __shfl_sync(0xffffffffu, vz, glane);
+        if (gsrc) vz = gok ? -g : -vz_any(gsrc, cc);
+      }
+      if (vact) {
+        svx[s * R4 + k] = vx;
+        svz[s * R4 + k] = vz;
+      }
+      const int64_t o = so + S(q, cc);
+      if (ownx) a.vxB[o] = vx;
+      if (ownz) a.vzB[o] = vz;
     };
-    auto str_strip = [&](int c, float p4, float p5, float p6, float p7) {
-      if (t >= TZ) return;
+    auto str_band = [&](int c) {
+      if (t >= TZ) return;  // the halo warp as a whole
       const int k = t;
-      const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
+      const int j4 = srow ? pml_slot(c, nx, npml, xlo, xhi) : -1;
+      const int j7 = (srow && xzrow) ? pml_slot(c, nx - 3, npml, xlo, xhi) : -1;
       const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
                   *u3 = svx + slot(c + 3) * R4;
       const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
                   *w3 = svz + slot(c + 3) * R4;
-      const float *bc = ring + slot(c) * SLOT, *cf = bc + 3 * R8 + 4 * R4;
+      const float *bc = ring + slot(c) * SL, *cf = bc + 3 * R8 + 4 * R4;
       float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
-      if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, p4, psB(4) + XS(j4, r), true);
+      if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, PX(2, c)[r], psB(4) + XS(j4, r), true);
       float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
-      if (jr5 >= 0) dvzdz = cpml_p(dvzdz, 5, jr5, p5, psB(5) + ZS(c, jr5), true);
+      if (jr5v >= 0) dvzdz = cpml_z(dvzdz, cr5, PZ(2, c)[jr5v], psB(5) + ZS(c, jr5v), true);
       const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
       const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
-      const float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
+      float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
       float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
-      if (jr6 >= 0) dvxdz = cpml_p(dvxdz, 6, jr6, p6, psB(6) + ZS(c, jr6), true);
+      if (jr6v >= 0) dvxdz = cpml_z(dvxdz, cr6, PZ(3, c)[jr6v], psB(6) + ZS(c, jr6v), true);
       float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
-      if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, p7, psB(7) + XS(j7, r), true);
-      const float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
-      const int64_t o = so + S(r, c);
-      a.txxB[o] = txx;
-      a.tzzB[o] = tzz;
-      a.txzB[o] = txz;
-    };
-    // psi of velocity column cc for this thread's row, loaded ahead of use
-    auto vel_psi = [&](int cc, float &p0, float &p1, float &p2, float &p3) {
-      p0 = p1 = p2 = p3 = 0.f;
-      if (!vact) return;
-      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
-      if (vxr && cc >= 4 && cc <= nx) {
-        if (j0 >= 0) p0 = psA(0)[XS(j0, q)];
-        if (jq3 >= 0) p3 = psA(3)[ZS(cc, jq3)];
+      if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, PX(3, c)[r], psB(7) + XS(j7, r), true);
+      float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
+      if (fsblk) {
+        // free_surface_mirror!(tauzz), free_surface!(tauxz): tzz[1] = -tzz[2]
+        const float t2 = __shfl_down_sync(0xffffffffu, tzz, 1);
+        if (fsrow) {
+          tzz = -t2;
+          txz = 0.f;
+        }
       }
-      if (vzr && cc >= 4 && cc <= nx - 3) {
-        if (j1 >= 0) p1 = psA(1)[XS(j1, q)];
-        if (jq2 >= 0) p2 = psA(2)[ZS(cc, jq2)];
+      if (srow) {
+        const int64_t o = so + S(r, c);
+        a.txxB[o] = txx;
+        a.tzzB[o] = tzz;
+        if (xzrow) a.txzB[o] = txz;
       }
     };
     // velocities of column cc: update_v! with CPML, mirrors, sources
-    auto vel_edge = [&](int cc, float p0, float p1, float p2, float p3, int ib0, int ie0, int ib1, int ie1) {
+    auto vel_edge = [&](int cc, int ib0, int ie0, int ib1, int ie1) {
       if (!vact) return;
       const int k = kq, kk = kq + 4, s = slot(cc);
       const bool vxc = cc >= 4 && cc <= nx, vzc = cc >= 4 && cc <= nx - 3;
       const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
       const bool ownc = cc >= x0 && (cc < x1 || lastx);
       const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && cc <= nx && q <= nz + 3;
-      const float *b3 = ring + slot(cc - 3) * SLOT, *b2 = ring + slot(cc - 2) * SLOT,
-                  *b1 = ring + slot(cc - 1) * SLOT, *bq = ring + s * SLOT;
+      const float *b3 = ring + slot(cc - 3) * SL, *b2 = ring + slot(cc - 2) * SL,
+                  *b1 = ring + slot(cc - 1) * SL, *bq = ring + s * SL;
       const float *v0 = bq + 3 * R8, *z3 = b3 + 2 * R8;
       float vx;
       if (rxhi && cc >= nx + 2) {
@@ -358,9 +430,9 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
         vx = v0[k];
         if (vxr && vxc) {
           float Dx = st4(b3[kk], b2[kk], b1[kk], bq[kk]) * a.dxI;
-          if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, p0, psB(0) + XS(j0, q), ownx);
+          if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
           float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
-          if (jq3 >= 0) Dz = cpml_p(Dz, 3, jq3, p3, psB(3) + ZS(cc, jq3), ownx);
+          if (jq3 >= 0) Dz = cpml_z(Dz, cq3, PZ(1, cc)[jq3], psB(3) + ZS(cc, jq3), ownx);
           vx = vx - v0[2 * R4 + k] * (Dx + Dz);
         }
         if (cc == nx) vpre = vx;
@@ -385,10 +457,10 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
         vz = v0[R4 + k];
         if (vzr && vzc) {
           float Dx = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], bq[2 * R8 + kk - 3]) * a.dxI;
-          if (j1 >= 0) Dx = cpml_p(Dx, 1, j1, p1, psB(1) + XS(j1, q), ownz);
+          if (j1 >= 0) Dx = cpml_p(Dx, 1, j1, PX(1, cc)[q], psB(1) + XS(j1, q), ownz);
           const float *zz = bq + R8;
           float Dz = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
-          if (jq2 >= 0) Dz = cpml_p(Dz, 2, jq2, p2, psB(2) + ZS(cc, jq2), ownz);
+          if (jq2 >= 0) Dz = cpml_z(Dz, cq2, PZ(0, cc)[jq2], psB(2) + ZS(cc, jq2), ownz);
           vz = vz - v0[3 * R4 + k] * (Dx + Dz);
         }
       }
@@ -396,19 +468,8 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
       svz[s * R4 + k] = vz;
       if (ownz) a.vzB[so + S(q, cc)] = vz;
     };
-    auto str_psi = [&](int c, float &p4, float &p5, float &p6, float &p7) {
-      p4 = p5 = p6 = p7 = 0.f;
-      if (!srow) return;
-      const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
-      if (j4 >= 0) p4 = psA(4)[XS(j4, r)];
-      if (jr5 >= 0) p5 = psA(5)[ZS(c, jr5)];
-      if (xzrow && c <= nx - 3) {
-        if (jr6 >= 0) p6 = psA(6)[ZS(c, jr6)];
-        if (j7 >= 0) p7 = psA(7)[XS(j7, r)];
-      }
-    };
     // stresses of column c: compute_stressii!/ij!, free surface, sources
-    auto str_edge = [&](int c, float p4, float p5, float p6, float p7, int bs, int es) {
+    auto str_edge = [&](int c, int bs, int es) {
       if (!srow) return;
       const int k = t;
       const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
@@ -416,7 +477,7 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
                   *u3 = svx + slot(c + 3) * R4;
       const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
                   *w3 = svz + slot(c + 3) * R4;
-      const float *bc = ring + slot(c) * SLOT, *cf = bc + 3 * R8 + 4 * R4;
+      const float *bc = ring + slot(c) * SL, *cf = bc + 3 * R8 + 4 * R4;
       const int64_t o = so + S(r, c);
       const bool hasxz = xzrow && c <= nx - 3;
       float txx, tzz, txz = 0.f;
@@ -426,17 +487,17 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
         txz = bc[2 * R8 + k + 4];
       } else {
         float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
-        if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, p4, psB(4) + XS(j4, r), true);
+        if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, PX(2, c)[r], psB(4) + XS(j4, r), true);
         float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
-        if (jr5 >= 0) dvzdz = cpml_p(dvzdz, 5, jr5, p5, psB(5) + ZS(c, jr5), true);
+        if (jr5 >= 0) dvzdz = cpml_z(dvzdz, cr5, PZ(2, c)[jr5], psB(5) + ZS(c, jr5), true);
         const float M = cf[k], Lm = cf[TZ + k];
         txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
         tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
         if (hasxz) {
           float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
-          if (jr6 >= 0) dvxdz = cpml_p(dvxdz, 6, jr6, p6, psB(6) + ZS(c, jr6), true);
+          if (jr6 >= 0) dvxdz = cpml_z(dvxdz, cr6, PZ(3, c)[jr6], psB(6) + ZS(c, jr6), true);
           float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
-          if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, p7, psB(7) + XS(j7, r), true);
+          if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, PX(3, c)[r], psB(7) + XS(j7, r), true);
           txz = bc[2 * R8 + k + 4] - cf[2 * TZ + k] * (dvxdz + dvzdx);
         }
         if (fsrow) {
@@ -452,7 +513,6 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
       a.tzzB[o] = tzz;
       if (hasxz) a.txzB[o] = txz;
     };
-    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, p4 = 0.f, p5 = 0.f, p6 = 0.f, p7 = 0.f;
     // one sweep: iterations c < x0 only compute the first velocity columns
     for (int c = x0 - 3; c < x1; c++) {
       const int cc = c + 3;
@@ -460,24 +520,22 @@ __global__ void __launch_bounds__(E2_THREADS, 4) k_e2(const E2Args a) {
       cvx.range(a.cells, cc, ib0, ie0);
       cvz.range(a.cells, cc, ib1, ie1);
       if (c >= x0) cst.range(a.cells, c, bs, es);
-      // general code for domain edges, mirrors and sources; otherwise the
-      // straight-line code, with CPML terms where a strip is met
-      const bool gv = rf_v || colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
-      const bool gs = rf_s || colfull_s(c) || bs < es;
-      if (gv || rp_v || colpml_v(cc)) vel_psi(cc, p0, p1, p2, p3);
-      if (c >= x0 && (gs || rp_s || colpml_s(c))) str_psi(c, p4, p5, p6, p7);
+      // general code for x edges, mirrors and sources (block-uniform);
+      // otherwise the band code over every row
+      const bool gv = colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
+      const bool gs = colfull_s(c) || bs < es;
       wait_col(cc);
       if (gv)
-        vel_edge(cc, p0, p1, p2, p3, ib0, ie0, ib1, ie1);
+        vel_edge(cc, ib0, ie0, ib1, ie1);
       else
-        vel_strip(cc, p0, p1, p2, p3);
+        vel_band(cc);
       __syncthreads();
       if (producer) issue(c + 7);
       if (c >= x0) {
         if (gs)
-          str_edge(c, p4, p5, p6, p7, bs, es);
+          str_edge(c, bs, es);
         else
-          str_strip(c, p4, p5, p6, p7);
+          str_band(c);
       }
     }
   }
@@ -499,11 +557,11 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   (void)it;
   (void)mode;
   static int attr_dev[64] = {0};
+  static size_t attr_gen[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 64 && !attr_dev[dev]) {
     GPI_CUDA(p, cudaFuncSetAttribute(k_e2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E2_SMEM));
-    GPI_CUDA(p, cudaFuncSetAttribute(k_e2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E2_SMEM));
     attr_dev[dev] = 1;
   }
   E2Args a;
@@ -548,6 +606,14 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.vonly = vonly;
   a.err = p->d_err;
   a.tiles = p->d_tiles;
+  a.zsw = p->zsw;
+  a.pzw = p->pzw;
+  a.psf = e2_psi_floats(*p);
+  const size_t gsmem = e2_smem_general(a.psf);
+  if (dev < 64 && attr_gen[dev] < gsmem) {
+    GPI_CUDA(p, cudaFuncSetAttribute(k_e2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
+    attr_gen[dev] = gsmem;
+  }
   // interior tiles on the straight-line kernel, the rest on the general one;
   // the velocity-only half step runs every tile on the general kernel
   const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
@@ -557,7 +623,7 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   }
   a.tiles = p->d_tiles + nf;
   if (ng) {
-    k_e2<false><<<ng, E2_THREADS, E2_SMEM, p->stream>>>(a);
+    k_e2<false><<<ng, E2_THREADS, gsmem, p->stream>>>(a);
     p->launches++;
   }
   GPI_CUDA(p, cudaGetLastError());

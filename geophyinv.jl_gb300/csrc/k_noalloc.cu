@@ -119,6 +119,8 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
   P.NXP = d.nx + 3 + 2 * XOFF + 4;
   P.NYP = 1;
   P.fstride = (int64_t)P.NZP * P.NXP;
+  P.zsw = zstrip_stride(d.npml);
+  P.pzw = zstrip_window(P.nzb, P.TZ, d.nz, d.npml, d.pml_faces & GPI_ZMIN, d.pml_faces & GPI_ZMAX);
   P.nder = deriv_specs(GPI_ACOUSTIC, 2, &P.ds);
   P.nmod = 2;
   P.ncoef = 3;
@@ -137,7 +139,7 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
   for (int b = 0; b < 2; b++)
     for (int f : {GPI_P, GPI_VX, GPI_VZ}) P.state[b][0][f] = carve(P.fstride);
   for (int q = 0; q < 4; q++) {
-    P.psi_stride[q] = P.ds[q].axis == 2 ? 2 * (int64_t)d.npml * P.NZP : (int64_t)P.NXP * 2 * d.npml;
+    P.psi_stride[q] = P.ds[q].axis == 2 ? 2 * (int64_t)d.npml * P.NZP : (int64_t)P.NXP * P.zsw;
     for (int b = 0; b < 2; b++) P.psi[b][0][q] = carve(P.psi_stride[q]);
   }
   for (int i = 0; i < 2; i++) P.mod[i] = carve(P.fstride);

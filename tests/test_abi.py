@@ -49,5 +49,6 @@ def test_create_rejects_bad_descriptor(lib):
     assert rc == -4  # order 2 is not implemented by the engine
     assert b"order" in lib.gpi_last_error(None)
     d.order = 4
+    d.pml_faces = 0x3F  # CPML on every face
     d.nz = 60  # too small for two PML strips
     assert lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan)) == -1

@@ -103,3 +103,32 @@ def test_acoustic2d_multishot_velocity_sources(engine):
     pa = wl.expt()
     update(pa)
     _compare_records(pa, ref, wl)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nz,nze", [(41, 84), (73, 116)])
+def test_bottom_ghost_rows_at_warp_edges(engine, nz, nze):
+    """Depths whose padded grids have 127 and 159 rows (PML on both z faces,
+    or a free surface on top): the bottom ghost rows of vz (dirichletzmax!)
+    land on the first lanes of a warp or on the halo lanes, away from the
+    lanes of their mirror source rows."""
+    wl = configs.acoustic2d_layers(nz=nz, nx=120, nt=300, nrec=17)
+    ref, orc = O.forward(wl.as_dict(), return_oracle=True)
+    pa = wl.expt()
+    update(pa)
+    _compare_records(pa, ref, wl)
+    for f in ("p", "vx", "vz"):
+        e = rel(pa.field(f), orc.field(f))
+        assert e < TOL, (f, e)
+    orc.close()
+    wl = configs.elastic2d_batch(nz=nze, nx=130, nt=300, nshots=2, nrec=15)
+    wl.pml_faces = ["zmax", "xmin", "xmax"]
+    wl.stressfree_faces = ["zmin"]
+    ref, orc = O.forward(wl.as_dict(), return_oracle=True)
+    pa = wl.expt()
+    update(pa)
+    _compare_records(pa, ref, wl)
+    for f in ("tauxx", "tauzz", "tauxz", "vx", "vz"):
+        e = rel(pa.field(f, iss=1), orc.field(f))
+        assert e < TOL, (f, e)
+    orc.close()
