@@ -128,7 +128,7 @@ struct Plan {
   int32_t *d_group_ptr = nullptr;
 
   int64_t launches = 0;
-  int *d_err = nullptr;
+  int *d_err = nullptr;  // set by a kernel whose pipeline wait gave up
   // tiles of the 2-D step kernels: interior tiles first (straight-line
   // kernel), then the tiles that meet a strip, a face or a source
   int3 *d_tiles = nullptr;
@@ -136,7 +136,11 @@ struct Plan {
   // 2-D z-strip CPML memory: column stride and the window of a column that
   // the general step kernel stages per ring slot
   int zsw = 0, pzw = 0;
-  std::vector<InjCell> h_cells;  // set by a kernel whose pipeline wait gave up
+  // a second stream for the general step kernel, so that its blocks and the
+  // interior kernel's share the SMs (fork and join events on the plan stream)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 };
 
 // error helpers
@@ -190,6 +194,10 @@ int step_adjoint_acoustic2d(Plan *p, int it);
 // interior tiles first; returns the tile count (or -1 beyond `cap`)
 int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast);
 int aux_step(Plan *p, int it, int mode);
+// stream of the general step kernel; forks from the plan stream when both
+// kernels launch (join_general joins it back)
+cudaStream_t fork_general(Plan *p, bool both);
+int join_general(Plan *p, bool both);
 int compute_coefficients(Plan *p);
 int boundary_io(Plan *p, int it, int dir);
 int snap_io(Plan *p, int tau, int dir);

@@ -287,7 +287,33 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   p.rec_w.assign(d.nshots, std::vector<std::vector<float>>(NFIELD));
   p.rec_base.assign(d.nshots, std::vector<int64_t>(NFIELD, -1));
   p.src.assign(2, std::vector<std::vector<Plan::Src>>(d.nshots, std::vector<Plan::Src>(NFIELD)));
+  {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&p.side, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p.ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      if (p.ev_fork) cudaEventDestroy(p.ev_fork);
+      if (p.side) cudaStreamDestroy(p.side);
+      p.side = nullptr;
+      p.ev_fork = p.ev_join = nullptr;  // both kernels then run on the plan stream
+    }
+  }
   *out = pl;
+  return GPI_OK;
+}
+
+cudaStream_t fork_general(Plan *p, bool both) {
+  if (!both || !p->side) return p->stream;
+  if (cudaEventRecord(p->ev_fork, p->stream) != cudaSuccess || cudaStreamWaitEvent(p->side, p->ev_fork, 0) != cudaSuccess)
+    return p->stream;
+  return p->side;
+}
+int join_general(Plan *p, bool both) {
+  if (!both || !p->side) return GPI_OK;
+  GPI_CUDA(p, cudaEventRecord(p->ev_join, p->side));
+  GPI_CUDA(p, cudaStreamWaitEvent(p->stream, p->ev_join, 0));
   return GPI_OK;
 }
 
@@ -325,6 +351,12 @@ void destroy(gpi_plan *pl) {
   cudaGetDevice(&dev);
   cudaSetDevice(p.device);
   if (p.stream) cudaStreamSynchronize(p.stream);
+  if (p.side) {
+    cudaStreamSynchronize(p.side);
+    cudaStreamDestroy(p.side);
+  }
+  if (p.ev_fork) cudaEventDestroy(p.ev_fork);
+  if (p.ev_join) cudaEventDestroy(p.ev_join);
   free_sources(p);
   free_receivers(p);
   free_dev(p.pool);

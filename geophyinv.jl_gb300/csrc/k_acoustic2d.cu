@@ -475,17 +475,23 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
     GPI_CUDA(p, cudaFuncSetAttribute(k_a2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
     attr_gen[dev] = gsmem;
   }
+  // the general kernel (longer blocks) goes first, on its own stream, so
+  // that interior blocks fill the SMs around it and its tail
   const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
+  const bool both = nf && ng;
+  cudaStream_t gstream = fork_general(p, both);
+  if (ng) {
+    A2Args g = a;
+    g.tiles = p->d_tiles + nf;
+    k_a2<false><<<ng, A2_THREADS, gsmem, gstream>>>(g);
+    p->launches++;
+  }
   if (nf) {
     k_a2<true><<<nf, A2_THREADS, A2_SMEM, p->stream>>>(a);
     p->launches++;
   }
-  a.tiles = p->d_tiles + nf;
-  if (ng) {
-    k_a2<false><<<ng, A2_THREADS, gsmem, p->stream>>>(a);
-    p->launches++;
-  }
   GPI_CUDA(p, cudaGetLastError());
+  if (int rc = join_general(p, both)) return rc;
   p->cur[0] ^= 1;
   return GPI_OK;
 }

@@ -616,17 +616,23 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   }
   // interior tiles on the straight-line kernel, the rest on the general one;
   // the velocity-only half step runs every tile on the general kernel
+  // the general kernel (longer blocks) goes first, on its own stream, so
+  // that interior blocks fill the SMs around it and its tail
   const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
+  const bool both = nf && ng;
+  cudaStream_t gstream = fork_general(p, both);
+  if (ng) {
+    E2Args g = a;
+    g.tiles = p->d_tiles + nf;
+    k_e2<false><<<ng, E2_THREADS, gsmem, gstream>>>(g);
+    p->launches++;
+  }
   if (nf) {
     k_e2<true><<<nf, E2_THREADS, E2_SMEM, p->stream>>>(a);
     p->launches++;
   }
-  a.tiles = p->d_tiles + nf;
-  if (ng) {
-    k_e2<false><<<ng, E2_THREADS, gsmem, p->stream>>>(a);
-    p->launches++;
-  }
   GPI_CUDA(p, cudaGetLastError());
+  if (int rc = join_general(p, both)) return rc;
   p->cur[0] ^= 1;
   return GPI_OK;
 }
