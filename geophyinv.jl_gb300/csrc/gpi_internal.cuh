@@ -30,6 +30,9 @@ constexpr int NFIELD = 10;
 constexpr int ZOFF = 4, XOFF = 4, YOFF = 4;
 constexpr int MAXDER = 18;
 constexpr int NKIND = 4;  // injection kinds: vx, vy, vz, stress
+// rows of a 2-D step-kernel block: 124 stress rows + 3 halo velocity rows
+// fill four warps; a multiple of 4 keeps every column copy 16-byte aligned
+constexpr int TZ2 = 124;
 
 // Canonical derivative order (docs and oracle use the same):
 //   A2: dpdx dpdz dvxdx dvzdz

@@ -84,12 +84,12 @@ static int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 static void choose_tiling(Plan &p) {
   const int sms = 152;
   if (p.d.ndim == 2) {
-    p.TZ = 128;
+    p.TZ = TZ2;
     p.TY = 1;
     p.nzb = (p.d.nz + p.TZ - 1) / p.TZ;
     p.nyb = 1;
-    // blocks resident at once (160 threads; shared memory: acoustic 34 KB,
-    // elastic 50 KB per block)
+    // blocks resident at once (128 threads; shared memory: acoustic 33 KB,
+    // elastic 49 KB per block)
     int resident = sms * (p.d.physics == GPI_ACOUSTIC ? 6 : 4);
     int per_chunk = p.nzb * p.d.nshots;
     int best = 1;

@@ -48,8 +48,8 @@ struct A2Args {
   int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
-constexpr int A2_TZ = 128;
-constexpr int A2_THREADS = A2_TZ + 32;
+constexpr int A2_TZ = TZ2;                             // pressure rows per block
+constexpr int A2_THREADS = 128;                        // TZ + 3 velocity rows, one per thread
 constexpr int A2_R8 = A2_TZ + 8;                       // p rows z0-4 .. z0+TZ+3
 constexpr int A2_R4 = A2_TZ + 4;                       // velocity-input rows z0 .. z0+TZ+3
 constexpr int A2_SLOT = A2_R8 + 4 * A2_R4 + A2_TZ;     // floats per ring slot
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
   auto PX = [&](int i, int cc) -> const float * { return ring + slot(cc) * SL + SLOT + 2 * PZW + i * TZ - z0; };
 
   if (t == 0) {
-    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 1);
+    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 4);  // one arrival per warp
     mbar_fence_init();
     s_err = 0;
   }
@@ -115,43 +115,48 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
   }
   __syncthreads();
 
-  const bool producer = t == TZ;
+  // producers: lane 0 of each warp issues its share of a column's bulk
+  // copies and arrives on the slot's mbarrier with the bytes of its share
+  // (warp 0 p, warp 1 vx vz, warp 2 cx and the dpdz CPML window, warp 3 cz
+  // dtK and the dvzdz window; the x-strip CPML columns on warps 0 and 3)
+  const int wq = t >> 5;
+  const bool issuer = (t & 31) == 0;
   int next = xbase;
   auto issue = [&](int upto) {
     for (; next <= upto && next <= xlast; next++) {
       const int s = slot(next);
       float *sl = ring + s * SL;
-      uint32_t bytes = SLOT * 4;
-      int j0 = -1, j2 = -1;
+      float *v = sl + R8, *pz = sl + SLOT, *px = pz + 2 * PZW;
+      const int64_t oV = S(z0, next);
+      int jx = -1;
       if constexpr (!FAST) {
-        if (zt) bytes += 2 * PZW * 4;
-        j0 = pml_slot(next - 3, nx - 3, npml, xlo, xhi);
-        j2 = pml_slot(next, nx, npml, xlo, xhi);
-        bytes += ((j0 >= 0) + (j2 >= 0)) * TZ * 4;
+        if (wq == 0) jx = pml_slot(next - 3, nx - 3, npml, xlo, xhi);
+        if (wq == 3) jx = pml_slot(next, nx, npml, xlo, xhi);
+      }
+      uint32_t bytes = wq == 0 ? R8 * 4 : wq == 1 ? 2 * R4 * 4 : wq == 2 ? R4 * 4 : (R4 + TZ) * 4;
+      if constexpr (!FAST) {
+        if (zt && wq >= 2) bytes += PZW * 4;
+        if (jx >= 0) bytes += TZ * 4;
       }
       mbar_expect_tx(&bar[s], bytes);
-      const int64_t oV = S(z0, next);
-      bulk_g2s(sl, a.pA + so + S(z0 - 4, next), R8 * 4, &bar[s]);
-      float *v = sl + R8;
-      bulk_g2s(v + 0 * R4, a.vxA + so + oV, R4 * 4, &bar[s]);
-      bulk_g2s(v + 1 * R4, a.vzA + so + oV, R4 * 4, &bar[s]);
-      bulk_g2s(v + 2 * R4, a.cx + oV, R4 * 4, &bar[s]);
-      bulk_g2s(v + 3 * R4, a.cz + oV, R4 * 4, &bar[s]);
-      bulk_g2s(v + 4 * R4, a.dtK + oV, TZ * 4, &bar[s]);
+      if (wq == 0) {
+        bulk_g2s(sl, a.pA + so + S(z0 - 4, next), R8 * 4, &bar[s]);
+      } else if (wq == 1) {
+        bulk_g2s(v + 0 * R4, a.vxA + so + oV, R4 * 4, &bar[s]);
+        bulk_g2s(v + 1 * R4, a.vzA + so + oV, R4 * 4, &bar[s]);
+      } else if (wq == 2) {
+        bulk_g2s(v + 2 * R4, a.cx + oV, R4 * 4, &bar[s]);
+      } else {
+        bulk_g2s(v + 3 * R4, a.cz + oV, R4 * 4, &bar[s]);
+        bulk_g2s(v + 4 * R4, a.dtK + oV, TZ * 4, &bar[s]);
+      }
       if constexpr (!FAST) {
-        float *pz = sl + SLOT;
-        if (zt) {
-          const int64_t oz = ZS(next, zoff);
-          bulk_g2s(pz, psA(1) + oz, PZW * 4, &bar[s]);
-          bulk_g2s(pz + PZW, psA(3) + oz, PZW * 4, &bar[s]);
-        }
-        float *px = pz + 2 * PZW;
-        if (j0 >= 0) bulk_g2s(px, psA(0) + XS(j0, z0), TZ * 4, &bar[s]);
-        if (j2 >= 0) bulk_g2s(px + TZ, psA(2) + XS(j2, z0), TZ * 4, &bar[s]);
+        if (zt && wq >= 2) bulk_g2s(pz + (wq - 2) * PZW, psA(wq == 2 ? 1 : 3) + ZS(next, zoff), PZW * 4, &bar[s]);
+        if (jx >= 0) bulk_g2s(px + (wq == 0 ? 0 : TZ), psA(wq == 0 ? 0 : 2) + XS(jx, z0), TZ * 4, &bar[s]);
       }
     }
   };
-  if (producer) issue(xbase + 7);
+  if (issuer) issue(xbase + 7);
   auto wait_col = [&](int cc) {
     const int j = cc - xbase;
     if (!mbar_wait(&bar[j & 7], (j >> 3) & 1)) s_err = 1;
@@ -163,7 +168,7 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
   cst.init(a.cells, s_rng[2][0], s_rng[2][1]);
 
   // velocity row q (t < TZ, and 3 halo rows for vz); pressure row r
-  const int kq = t < TZ ? t : (t - TZ < 3 ? t : -1);
+  const int kq = t < TZ + 3 ? t : -1;
   const int q = z0 + kq;
   const bool vact = kq >= 0;
   const bool ownr = kq >= 0 && (kq < TZ || lastz);
@@ -225,7 +230,7 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
       wait_col(cc);
       vel_fast(cc);
       __syncthreads();
-      if (producer) issue(c + 7);
+      if (issuer) issue(c + 7);
       if (c >= x0 && t < TZ) {
         const int k = t;
         const float *pc = ring + slot(c) * SLOT;
@@ -301,7 +306,7 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
       }
     };
     auto str_band = [&](int c) {
-      if (t >= TZ) return;  // the halo warp as a whole
+      if (t >= TZ) return;  // halo lanes
       if (!srow) return;
       const int k = t;
       const float *pc = ring + slot(c) * SL;
@@ -401,7 +406,7 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
       else
         vel_band(cc);
       __syncthreads();
-      if (producer) issue(c + 7);
+      if (issuer) issue(c + 7);
       if (c >= x0) {
         if (gs)
           str_edge(c, bs, es);

@@ -50,8 +50,8 @@ struct E2Args {
   int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
-constexpr int E2_TZ = 128;
-constexpr int E2_THREADS = E2_TZ + 32;
+constexpr int E2_TZ = TZ2;                                      // stress rows per block
+constexpr int E2_THREADS = 128;                                 // TZ + 3 velocity rows, one per thread
 constexpr int E2_R8 = E2_TZ + 8;                                // stress rows z0-4 .. z0+TZ+3
 constexpr int E2_R4 = E2_TZ + 4;                                // velocity-input rows z0 .. z0+TZ+3
 constexpr int E2_SLOT = 3 * E2_R8 + 4 * E2_R4 + 3 * E2_TZ;      // floats per ring slot
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
   };
 
   if (t == 0) {
-    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 1);
+    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 4);  // one arrival per warp
     mbar_fence_init();
     s_err = 0;
   }
@@ -129,56 +129,67 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
   }
   __syncthreads();
 
-  // ---- producer: one thread issues the bulk copies of a column ----
-  const bool producer = t == TZ;
+  // ---- producers: lane 0 of each warp issues its share of a column's bulk
+  // copies and arrives on the slot's mbarrier with the bytes of its share
+  // (warp 0 the stresses, warp 1 vx vz cx, warp 2 cz dtM, warp 3 dtl mu; in
+  // the general kernel also the CPML memory, spread the same way) ----
+  const int wq = t >> 5;
+  const bool issuer = (t & 31) == 0;
   int next = xbase;
   auto issue = [&](int upto) {
     for (; next <= upto && next <= xlast; next++) {
       const int s = slot(next);
       float *sl = ring + s * SL;
-      uint32_t bytes = SLOT * 4;
-      int jx[4] = {-1, -1, -1, -1};
+      const int64_t oT = so + S(z0 - 4, next), oV = S(z0, next);
+      float *v = sl + 3 * R8, *cf = v + 4 * R4;
+      float *pz = sl + SLOT, *px = pz + 4 * PZW;
+      int jx = -1;
       if constexpr (!FAST) {
-        if (zt) bytes += 4 * PZW * 4;
-        jx[0] = pml_slot(next - 3, nx - 3, npml, xlo, xhi);
-        jx[1] = pml_slot(next - 3, nx - 6, npml, xlo, xhi);
-        jx[2] = pml_slot(next, nx, npml, xlo, xhi);
-        jx[3] = pml_slot(next, nx - 3, npml, xlo, xhi);
-        for (int i = 0; i < 4; i++)
-          if (jx[i] >= 0) bytes += (i < 2 ? R4 : TZ) * 4;
+        jx = wq == 0 ? pml_slot(next - 3, nx - 3, npml, xlo, xhi)
+           : wq == 1 ? pml_slot(next - 3, nx - 6, npml, xlo, xhi)
+           : wq == 2 ? pml_slot(next, nx, npml, xlo, xhi)
+                     : pml_slot(next, nx - 3, npml, xlo, xhi);
+      }
+      const int jrows = wq < 2 ? R4 : TZ;  // x-strip CPML rows of this warp's derivative
+      uint32_t bytes = wq == 0 ? 3 * R8 * 4 : wq == 1 ? 3 * R4 * 4 : wq == 2 ? (R4 + TZ) * 4 : 2 * TZ * 4;
+      if constexpr (!FAST) {
+        if (zt && wq >= 2) bytes += 2 * PZW * 4;
+        if (jx >= 0) bytes += jrows * 4;
       }
       mbar_expect_tx(&bar[s], bytes);
-      const int64_t oT = so + S(z0 - 4, next), oV = S(z0, next);
-      bulk_g2s(sl + 0 * R8, a.txxA + oT, R8 * 4, &bar[s]);
-      bulk_g2s(sl + 1 * R8, a.tzzA + oT, R8 * 4, &bar[s]);
-      bulk_g2s(sl + 2 * R8, a.txzA + oT, R8 * 4, &bar[s]);
-      float *v = sl + 3 * R8;
-      bulk_g2s(v + 0 * R4, a.vxA + so + oV, R4 * 4, &bar[s]);
-      bulk_g2s(v + 1 * R4, a.vzA + so + oV, R4 * 4, &bar[s]);
-      bulk_g2s(v + 2 * R4, a.cx + oV, R4 * 4, &bar[s]);
-      bulk_g2s(v + 3 * R4, a.cz + oV, R4 * 4, &bar[s]);
-      float *cf = v + 4 * R4;
-      bulk_g2s(cf + 0 * TZ, a.dtM + oV, TZ * 4, &bar[s]);
-      bulk_g2s(cf + 1 * TZ, a.dtl + oV, TZ * 4, &bar[s]);
-      bulk_g2s(cf + 2 * TZ, a.mu + oV, TZ * 4, &bar[s]);
+      if (wq == 0) {
+        bulk_g2s(sl + 0 * R8, a.txxA + oT, R8 * 4, &bar[s]);
+        bulk_g2s(sl + 1 * R8, a.tzzA + oT, R8 * 4, &bar[s]);
+        bulk_g2s(sl + 2 * R8, a.txzA + oT, R8 * 4, &bar[s]);
+      } else if (wq == 1) {
+        bulk_g2s(v + 0 * R4, a.vxA + so + oV, R4 * 4, &bar[s]);
+        bulk_g2s(v + 1 * R4, a.vzA + so + oV, R4 * 4, &bar[s]);
+        bulk_g2s(v + 2 * R4, a.cx + oV, R4 * 4, &bar[s]);
+      } else if (wq == 2) {
+        bulk_g2s(v + 3 * R4, a.cz + oV, R4 * 4, &bar[s]);
+        bulk_g2s(cf + 0 * TZ, a.dtM + oV, TZ * 4, &bar[s]);
+      } else {
+        bulk_g2s(cf + 1 * TZ, a.dtl + oV, TZ * 4, &bar[s]);
+        bulk_g2s(cf + 2 * TZ, a.mu + oV, TZ * 4, &bar[s]);
+      }
       if constexpr (!FAST) {
-        float *pz = sl + SLOT;
-        if (zt) {
+        if (zt && wq >= 2) {
+          // z-strip windows: warp 2 derivatives 2 3, warp 3 derivatives 5 6
           const int64_t oz = ZS(next, zoff);
-          bulk_g2s(pz + 0 * PZW, psA(2) + oz, PZW * 4, &bar[s]);
-          bulk_g2s(pz + 1 * PZW, psA(3) + oz, PZW * 4, &bar[s]);
-          bulk_g2s(pz + 2 * PZW, psA(5) + oz, PZW * 4, &bar[s]);
-          bulk_g2s(pz + 3 * PZW, psA(6) + oz, PZW * 4, &bar[s]);
+          const int i0 = wq == 2 ? 0 : 2;
+          bulk_g2s(pz + i0 * PZW, psA(wq == 2 ? 2 : 5) + oz, PZW * 4, &bar[s]);
+          bulk_g2s(pz + (i0 + 1) * PZW, psA(wq == 2 ? 3 : 6) + oz, PZW * 4, &bar[s]);
         }
-        float *px = pz + 4 * PZW;
-        if (jx[0] >= 0) bulk_g2s(px, psA(0) + XS(jx[0], z0), R4 * 4, &bar[s]);
-        if (jx[1] >= 0) bulk_g2s(px + R4, psA(1) + XS(jx[1], z0), R4 * 4, &bar[s]);
-        if (jx[2] >= 0) bulk_g2s(px + 2 * R4, psA(4) + XS(jx[2], z0), TZ * 4, &bar[s]);
-        if (jx[3] >= 0) bulk_g2s(px + 2 * R4 + TZ, psA(7) + XS(jx[3], z0), TZ * 4, &bar[s]);
+        if (jx >= 0) {
+          // x-strip column of derivative 0, 1, 4 or 7
+          const int q8 = wq == 0 ? 0 : wq == 1 ? 1 : wq == 2 ? 4 : 7;
+          float *dst = px + (wq < 2 ? wq * R4 : 2 * R4 + (wq - 2) * TZ);
+          bulk_g2s(dst, psA(q8) + XS(jx, z0), jrows * 4, &bar[s]);
+        }
       }
     }
   };
-  if (producer) issue(xbase + 7);
+  if (issuer) issue(xbase + 7);
   auto wait_col = [&](int cc) {
     const int j = cc - xbase;
     if (!mbar_wait(&bar[j & 7], (j >> 3) & 1)) s_err = 1;
@@ -190,7 +201,7 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
   cst.init(a.cells, s_rng[2][0], s_rng[2][1]);
 
   // this thread's velocity row: t < TZ -> z0+t, halo lanes -> z0+TZ+0..2
-  const int kq = t < TZ ? t : (t - TZ < 3 ? t : -1);
+  const int kq = t < TZ + 3 ? t : -1;
   const int q = z0 + kq;
   const bool vact = kq >= 0;
   const bool ownr = kq >= 0 && (kq < TZ || lastz);
@@ -313,7 +324,7 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       wait_col(cc);
       vel_fast(cc);
       __syncthreads();
-      if (producer) issue(c + 7);
+      if (issuer) issue(c + 7);
       if (c >= x0) str_fast(c);
     }
   } else {
@@ -376,7 +387,7 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       if (ownz) a.vzB[o] = vz;
     };
     auto str_band = [&](int c) {
-      if (t >= TZ) return;  // the halo warp as a whole
+      if (t >= TZ) return;  // halo lanes
       const int k = t;
       const int j4 = srow ? pml_slot(c, nx, npml, xlo, xhi) : -1;
       const int j7 = (srow && xzrow) ? pml_slot(c, nx - 3, npml, xlo, xhi) : -1;
@@ -397,7 +408,7 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
       if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, PX(3, c)[r], psB(7) + XS(j7, r), true);
       float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
-      if (fsblk) {
+      if (fsblk && t < 32) {
         // free_surface_mirror!(tauzz), free_surface!(tauxz): tzz[1] = -tzz[2]
         const float t2 = __shfl_down_sync(0xffffffffu, tzz, 1);
         if (fsrow) {
@@ -530,7 +541,7 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       else
         vel_band(cc);
       __syncthreads();
-      if (producer) issue(c + 7);
+      if (issuer) issue(c + 7);
       if (c >= x0) {
         if (gs)
           str_edge(c, bs, es);

@@ -110,12 +110,12 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
   P.d.rigid_faces |= d.pml_faces;
   P.h = 3;
   P.stream = (cudaStream_t)stream;
-  P.TZ = 128;
-  P.nzb = (d.nz + 127) / 128;
+  P.TZ = TZ2;
+  P.nzb = (d.nz + TZ2 - 1) / TZ2;
   P.L = 128;
   P.nxb = (d.nx + P.L - 1) / P.L;
   P.nyb = 1;
-  P.NZP = (int)(((int64_t)P.nzb * 128 + 2 * ZOFF + 4 + 31) / 32 * 32);
+  P.NZP = (int)(((int64_t)P.nzb * TZ2 + 2 * ZOFF + 4 + 31) / 32 * 32);
   P.NXP = d.nx + 3 + 2 * XOFF + 4;
   P.NYP = 1;
   P.fstride = (int64_t)P.NZP * P.NXP;

@@ -106,11 +106,11 @@ def test_acoustic2d_multishot_velocity_sources(engine):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nz,nze", [(41, 84), (73, 116)])
+@pytest.mark.parametrize("nz,nze", [(69, 112), (133, 176)])
 def test_bottom_ghost_rows_at_warp_edges(engine, nz, nze):
-    """Depths whose padded grids have 127 and 159 rows (PML on both z faces,
-    or a free surface on top): the bottom ghost rows of vz (dirichletzmax!)
-    land on the first lanes of a warp or on the halo lanes, away from the
+    """Depths whose padded grids have 155 and 219 rows (PML on both z faces,
+    or a free surface on top): with blocks of 124 rows the bottom ghost rows
+    of vz (dirichletzmax!) fall on lanes 0 and 1 of a warp, away from the
     lanes of their mirror source rows."""
     wl = configs.acoustic2d_layers(nz=nz, nx=120, nt=300, nrec=17)
     ref, orc = O.forward(wl.as_dict(), return_oracle=True)
