@@ -700,9 +700,12 @@ int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int
   if (n > cap) return -1;
   const int npml = p.d.npml, nz = p.d.nz, nx = p.d.nx;
   int k = 0, g = n;
-  for (int shot = 0; shot < p.d.nshots; shot++)
-    for (int xb = 0; xb < p.nxb; xb++)
-      for (int zb = 0; zb < p.nzb; zb++) {
+  // shots innermost: the blocks of one (z-block, x-chunk) of every shot run
+  // together and read the shared coefficient columns once from HBM, then
+  // from L2
+  for (int xb = 0; xb < p.nxb; xb++)
+    for (int zb = 0; zb < p.nzb; zb++)
+      for (int shot = 0; shot < p.d.nshots; shot++) {
         const int z0 = 1 + zb * p.TZ, x0 = 1 + xb * p.L, x1 = std::min(x0 + p.L, nx + 1);
         bool fast = z0 >= npml + 4 && z0 + p.TZ + 2 <= nz - npml - 3 && x0 >= npml + 4 && x1 + 2 <= nx - npml - 3;
         for (int ipw = 0; fast && ipw < p.d.npw; ipw++)
