@@ -135,14 +135,15 @@ struct Plan {
   // tiles of the 2-D step kernels: interior tiles first (straight-line
   // kernel), then the tiles that meet a strip, a face or a source
   int3 *d_tiles = nullptr;
-  int n_tiles_fast = 0, n_tiles_gen = 0;
+  int n_tiles_fast = 0, n_tiles_band = 0, n_tiles_edge = 0;
   // 2-D z-strip CPML memory: column stride and the window of a column that
   // the general step kernel stages per ring slot
   int zsw = 0, pzw = 0;
-  // a second stream for the general step kernel, so that its blocks and the
-  // interior kernel's share the SMs (fork and join events on the plan stream)
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // side streams for the edge and band step kernels, so that their blocks
+  // and the interior kernel's share the SMs (fork and join events on the
+  // plan stream)
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 };
 
@@ -194,13 +195,15 @@ int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_adjoint_acoustic2d(Plan *p, int it);
 // host: classify the (z-block, x-chunk, shot) tiles of a 2-D plan; writes
-// interior tiles first; returns the tile count (or -1 beyond `cap`)
-int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast);
+// interior tiles, then band tiles, then edge tiles; returns the tile count
+// (or -1 beyond `cap`)
+int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast,
+                   int *nband);
 int aux_step(Plan *p, int it, int mode);
-// stream of the general step kernel; forks from the plan stream when both
-// kernels launch (join_general joins it back)
-cudaStream_t fork_general(Plan *p, bool both);
-int join_general(Plan *p, bool both);
+// nside side streams forked from the plan stream (the plan stream itself
+// when side streams are unavailable); join_side joins them back
+int fork_side(Plan *p, int nside, cudaStream_t *out);
+int join_side(Plan *p, int nside);
 int compute_coefficients(Plan *p);
 int boundary_io(Plan *p, int it, int dir);
 int snap_io(Plan *p, int tau, int dir);

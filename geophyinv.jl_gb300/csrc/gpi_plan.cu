@@ -290,30 +290,43 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    if (cudaStreamCreateWithPriority(&p.side, cudaStreamNonBlocking, hi) != cudaSuccess ||
-        cudaEventCreateWithFlags(&p.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&p.ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    bool ok = cudaEventCreateWithFlags(&p.ev_fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; k < 2; k++)
+      ok = ok && cudaStreamCreateWithPriority(&p.side[k], cudaStreamNonBlocking, hi) == cudaSuccess &&
+           cudaEventCreateWithFlags(&p.ev_join[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      // every step kernel then runs on the plan stream
       cudaGetLastError();
       if (p.ev_fork) cudaEventDestroy(p.ev_fork);
-      if (p.side) cudaStreamDestroy(p.side);
-      p.side = nullptr;
-      p.ev_fork = p.ev_join = nullptr;  // both kernels then run on the plan stream
+      for (int k = 0; k < 2; k++) {
+        if (p.side[k]) cudaStreamDestroy(p.side[k]);
+        if (p.ev_join[k]) cudaEventDestroy(p.ev_join[k]);
+        p.side[k] = nullptr;
+        p.ev_join[k] = nullptr;
+      }
+      p.ev_fork = nullptr;
     }
   }
   *out = pl;
   return GPI_OK;
 }
 
-cudaStream_t fork_general(Plan *p, bool both) {
-  if (!both || !p->side) return p->stream;
-  if (cudaEventRecord(p->ev_fork, p->stream) != cudaSuccess || cudaStreamWaitEvent(p->side, p->ev_fork, 0) != cudaSuccess)
-    return p->stream;
-  return p->side;
+int fork_side(Plan *p, int nside, cudaStream_t *out) {
+  for (int k = 0; k < nside; k++) out[k] = p->stream;
+  if (nside == 0 || !p->side[0]) return GPI_OK;
+  GPI_CUDA(p, cudaEventRecord(p->ev_fork, p->stream));
+  for (int k = 0; k < nside; k++) {
+    GPI_CUDA(p, cudaStreamWaitEvent(p->side[k], p->ev_fork, 0));
+    out[k] = p->side[k];
+  }
+  return GPI_OK;
 }
-int join_general(Plan *p, bool both) {
-  if (!both || !p->side) return GPI_OK;
-  GPI_CUDA(p, cudaEventRecord(p->ev_join, p->side));
-  GPI_CUDA(p, cudaStreamWaitEvent(p->stream, p->ev_join, 0));
+int join_side(Plan *p, int nside) {
+  if (nside == 0 || !p->side[0]) return GPI_OK;
+  for (int k = 0; k < nside; k++) {
+    GPI_CUDA(p, cudaEventRecord(p->ev_join[k], p->side[k]));
+    GPI_CUDA(p, cudaStreamWaitEvent(p->stream, p->ev_join[k], 0));
+  }
   return GPI_OK;
 }
 
@@ -351,12 +364,14 @@ void destroy(gpi_plan *pl) {
   cudaGetDevice(&dev);
   cudaSetDevice(p.device);
   if (p.stream) cudaStreamSynchronize(p.stream);
-  if (p.side) {
-    cudaStreamSynchronize(p.side);
-    cudaStreamDestroy(p.side);
+  for (int k = 0; k < 2; k++) {
+    if (p.side[k]) {
+      cudaStreamSynchronize(p.side[k]);
+      cudaStreamDestroy(p.side[k]);
+    }
+    if (p.ev_join[k]) cudaEventDestroy(p.ev_join[k]);
   }
   if (p.ev_fork) cudaEventDestroy(p.ev_fork);
-  if (p.ev_join) cudaEventDestroy(p.ev_join);
   free_sources(p);
   free_receivers(p);
   free_dev(p.pool);
@@ -691,58 +706,75 @@ static int compile_sources(Plan &p) {
 }
 
 
-// A tile is interior when every cell it computes lies inside all update
-// domains, outside every CPML strip and away from mirror rows/columns, and
-// no source cell of its shot falls in its columns (src/fdtd/cpml.jl:184-211,
-// src/fdtd/dirichlet.jl:1-79 give the affected rows and columns).
-int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast) {
+// Tile classes of the 2-D step kernels (src/fdtd/cpml.jl:184-211 and
+// src/fdtd/dirichlet.jl:1-79 give the affected rows and columns):
+//   0 interior: every cell it computes lies inside all update domains,
+//     outside every CPML strip and away from mirror rows/columns;
+//   1 band: columns away from the x edges and x strips, rows that may meet
+//     a z strip, a z mirror or the free surface;
+//   2 edge: everything else (x edges, x strips, source cells).
+// A block computes velocities of rows z0..z0+TZ+2 and columns x0..x1+2 and
+// stresses of rows z0..z0+TZ-1 and columns x0..x1-1 from input columns
+// x0-3..x1+2.
+static int tile_class(const Plan &p, const InjCell *cells, const int32_t *gptr, int zb, int xb, int shot) {
+  const int npml = p.d.npml, nz = p.d.nz, nx = p.d.nx;
+  const int z0 = 1 + zb * p.TZ, x0 = 1 + xb * p.L, x1 = std::min(x0 + p.L, nx + 1);
+  for (int ipw = 0; ipw < p.d.npw; ipw++)
+    for (int kind = 0; kind < NKIND; kind++) {
+      const int gi = (ipw * p.d.nshots + shot) * NKIND + kind;
+      for (int c = gptr[gi]; c < gptr[gi + 1]; c++)
+        if (cells[c].col >= x0 - 3 && cells[c].col <= x1 + 3 && cells[c].row >= z0 - 1 &&
+            cells[c].row <= z0 + p.TZ + 3)
+          return 2;
+    }
+  const bool xpml = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
+  // no x-edge column (mirrors, domain ends) and no x-strip column
+  const bool xin = x0 > 4 && x1 + 2 < nx - 4 && (!xpml || (x0 > npml + 3 && x1 <= nx - 5 - npml));
+  if (!xin) return 2;
+  const bool zin = z0 >= npml + 4 && z0 + p.TZ + 2 <= nz - npml - 3;
+  return zin && x0 >= npml + 4 && x1 + 2 <= nx - npml - 3 ? 0 : 1;
+}
+
+int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast,
+                   int *nband) {
   const int n = p.nzb * p.nxb * p.d.nshots;
   if (n > cap) return -1;
-  const int npml = p.d.npml, nz = p.d.nz, nx = p.d.nx;
-  int k = 0, g = n;
-  // shots innermost: the blocks of one (z-block, x-chunk) of every shot run
-  // together and read the shared coefficient columns once from HBM, then
-  // from L2
-  for (int xb = 0; xb < p.nxb; xb++)
-    for (int zb = 0; zb < p.nzb; zb++)
-      for (int shot = 0; shot < p.d.nshots; shot++) {
-        const int z0 = 1 + zb * p.TZ, x0 = 1 + xb * p.L, x1 = std::min(x0 + p.L, nx + 1);
-        bool fast = z0 >= npml + 4 && z0 + p.TZ + 2 <= nz - npml - 3 && x0 >= npml + 4 && x1 + 2 <= nx - npml - 3;
-        for (int ipw = 0; fast && ipw < p.d.npw; ipw++)
-          for (int kind = 0; fast && kind < NKIND; kind++) {
-            const int gi = (ipw * p.d.nshots + shot) * NKIND + kind;
-            // a block computes velocities of rows z0..z0+TZ+2 and columns
-            // x0..x1+2, stresses of rows z0..z0+TZ-1 and columns x0..x1-1
-            for (int c = gptr[gi]; c < gptr[gi + 1]; c++)
-              if (cells[c].col >= x0 - 3 && cells[c].col <= x1 + 3 && cells[c].row >= z0 - 1 &&
-                  cells[c].row <= z0 + p.TZ + 3) {
-                fast = false;
-                break;
-              }
-          }
-        if (fast)
-          out[k++] = make_int3(zb, xb, shot);
-        else
-          out[--g] = make_int3(zb, xb, shot);
-      }
-  *nfast = k;
+  int cnt[3] = {0, 0, 0};
+  for (int pass = 0; pass < 2; pass++) {
+    int at[3] = {0, cnt[0], cnt[0] + cnt[1]};
+    // shots innermost: the blocks of one (z-block, x-chunk) of every shot run
+    // together and read the shared coefficient columns once from HBM, then
+    // from L2
+    for (int xb = 0; xb < p.nxb; xb++)
+      for (int zb = 0; zb < p.nzb; zb++)
+        for (int shot = 0; shot < p.d.nshots; shot++) {
+          const int k = tile_class(p, cells, gptr, zb, xb, shot);
+          if (pass == 0)
+            cnt[k]++;
+          else
+            out[at[k]++] = make_int3(zb, xb, shot);
+        }
+  }
+  *nfast = cnt[0];
+  *nband = cnt[1];
   return n;
 }
 
 static int build_tiles(Plan &p) {
   const int n = p.nzb * p.nxb * p.d.nshots;
   std::vector<int3> t(n);
-  int nf = 0;
+  int nf = 0, nb = 0;
   const int32_t *gp = p.group_ptr.empty() ? nullptr : p.group_ptr.data();
   std::vector<int32_t> zero(2 * p.d.nshots * NKIND + 1, 0);
-  if (classify_tiles(p, p.h_cells.data(), gp ? gp : zero.data(), t.data(), n, &nf) < 0)
+  if (classify_tiles(p, p.h_cells.data(), gp ? gp : zero.data(), t.data(), n, &nf, &nb) < 0)
     return fail(&p, GPI_E_INVALID, "tile list");
   if (p.d_tiles) cudaFree(p.d_tiles);
   p.d_tiles = nullptr;
   GPI_CUDA(&p, cudaMalloc(&p.d_tiles, n * sizeof(int3)));
   GPI_CUDA(&p, cudaMemcpy(p.d_tiles, t.data(), n * sizeof(int3), cudaMemcpyHostToDevice));
   p.n_tiles_fast = nf;
-  p.n_tiles_gen = n - nf;
+  p.n_tiles_band = nb;
+  p.n_tiles_edge = n - nf - nb;
   return GPI_OK;
 }
 

@@ -63,8 +63,13 @@ inline int a2_psi_floats(const Plan &p) {
 }
 inline size_t a2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (A2_SLOT + psf) + 2 * 8 * A2_R4); }
 
-template <bool FAST>
-__global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a) {
+// MODE 0: interior tiles (no CPML, face or source: straight-line code);
+// MODE 1: tiles that meet only z-strip CPML rows or z faces (the band code
+// over every column); MODE 2: tiles with x-edge, x-strip or source columns
+// (the band code plus the general code per column).
+template <int MODE>
+__global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Args a) {
+  constexpr bool FAST = MODE == 0, XPSI = MODE == 2;
   constexpr int TZ = A2_TZ, R8 = A2_R8, R4 = A2_R4, SLOT = A2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
@@ -101,6 +106,9 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
   // (i: 0 dpdx, 1 dvxdx)
   auto PZ = [&](int i, int cc) -> const float * { return ring + slot(cc) * SL + SLOT + i * PZW - zoff; };
   auto PX = [&](int i, int cc) -> const float * { return ring + slot(cc) * SL + SLOT + 2 * PZW + i * TZ - z0; };
+  // the same by ring slot
+  auto PZs = [&](int i, int s) -> const float * { return ring + s * SL + SLOT + i * PZW - zoff; };
+  auto PXs = [&](int i, int s) -> const float * { return ring + s * SL + SLOT + 2 * PZW + i * TZ - z0; };
 
   if (t == 0) {
     for (int s = 0; s < 8; s++) mbar_init(&bar[s], 4);  // one arrival per warp
@@ -129,7 +137,7 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
       float *v = sl + R8, *pz = sl + SLOT, *px = pz + 2 * PZW;
       const int64_t oV = S(z0, next);
       int jx = -1;
-      if constexpr (!FAST) {
+      if constexpr (XPSI) {
         if (wq == 0) jx = pml_slot(next - 3, nx - 3, npml, xlo, xhi);
         if (wq == 3) jx = pml_slot(next, nx, npml, xlo, xhi);
       }
@@ -201,23 +209,37 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
     if (own) *dst = psi;
     return D * cf.z + psi;
   };
+  // the same as selects: the memory variable applies where `on`
+  auto cpml_zs = [&](float D, float3 cf, float psi_old, bool on, float *dst, bool own) -> float {
+    const float psi = cf.y * psi_old + cf.x * D;
+    if (on && own) *dst = psi;
+    return on ? D * cf.z + psi : D;
+  };
+  auto cpml_xs = [&](float D, int q4, int j, float psi_old, bool on, float *dst, bool own) -> float {
+    const float *cf = a.pml + q4 * P6;
+    const float psi = __ldg(cf + 2 * npml + j) * psi_old + __ldg(cf + j) * D;
+    if (on && own) *dst = psi;
+    return on ? D * __ldg(cf + 4 * npml + j) + psi : D;
+  };
 
   // Dispatch per warp and per column: a warp runs the straight-line code
   // unless one of its rows or the current column touches a CPML strip, a
   // rigid face, a domain edge or a source cell.
   if constexpr (FAST) {
-    // interior tile: inside every update domain, no CPML, no face, no source
-    auto vel_fast = [&](int cc) {
+    // interior tile: inside every update domain, no CPML, no face, no
+    // source.  The sweep below is unrolled by the ring length, so every ring
+    // and velocity-buffer slot is a compile-time offset.
+    // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
+    auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
       if (!vact) return;
-      const int k = kq, kk = kq + 4, s = slot(cc);
-      const float *pc = ring + s * SLOT, *v0 = pc + R8;
+      const int k = kq, kk = kq + 4;
+      const float *pc = ring + s0 * SLOT, *v0 = pc + R8;
       const float vz = v0[R4 + k] + v0[3 * R4 + k] * (st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI);
-      svz[s * R4 + k] = vz;
+      svz[s0 * R4 + k] = vz;
       if (kq < TZ) {
-        const float *p3 = ring + slot(cc - 3) * SLOT, *p2 = ring + slot(cc - 2) * SLOT,
-                    *p1 = ring + slot(cc - 1) * SLOT;
+        const float *p3 = ring + s3 * SLOT, *p2 = ring + s2 * SLOT, *p1 = ring + s1 * SLOT;
         const float vx = v0[k] + v0[2 * R4 + k] * (st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI);
-        svx[s * R4 + k] = vx;
+        svx[s0 * R4 + k] = vx;
         if (cc < x1) {
           const int64_t o = so + S(q, cc);
           a.vxB[o] = vx;
@@ -225,20 +247,29 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
         }
       }
     };
-    for (int c = x0 - 3; c < x1; c++) {
-      const int cc = c + 3;
-      wait_col(cc);
-      vel_fast(cc);
-      __syncthreads();
-      if (issuer) issue(c + 7);
-      if (c >= x0 && t < TZ) {
-        const int k = t;
-        const float *pc = ring + slot(c) * SLOT;
-        const float *w = svz + slot(c) * R4;
-        const float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
-                             svx[slot(c + 3) * R4 + k]) * a.dxI;
-        const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
-        a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+    // pressure of column c from velocity slots s0..s3 = columns c..c+3
+    auto str_fast = [&](int c, int s0, int s1, int s2, int s3) {
+      if (t >= TZ) return;
+      const int k = t;
+      const float *pc = ring + s0 * SLOT;
+      const float *w = svz + s0 * R4;
+      const float Dx = st4(svx[s0 * R4 + k], svx[s1 * R4 + k], svx[s2 * R4 + k], svx[s3 * R4 + k]) * a.dxI;
+      const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
+      a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+    };
+    // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+    const int ncol = x1 - xbase;
+    for (int i0 = 0; i0 < ncol; i0 += 8) {
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int it = i0 + u;
+        if (it >= ncol) break;
+        const int c = xbase + it;
+        if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+        vel_fast(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
+        __syncthreads();
+        if (issuer) issue(c + 7);
+        if (c >= x0) str_fast(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
       }
     }
   } else {
@@ -249,6 +280,8 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
   const int kqc = vact ? kq : 0;
   const bool vzb = vact && vzr;
   const int jq1v = vzb ? jq1 : -1, jr3v = srow ? jr3 : -1;
+  // in-window strip slots to read when a row is outside its strip
+  const int jq1c = jq1v >= 0 ? jq1v : zoff, jr3c = jr3v >= 0 ? jr3v : zoff;
   // ghost rows of vz (dirichletzmin!/zmax!) read their mirror source from
   // the lane that computes it, when that lane is in the same warp
   const int lane = t & 31;
@@ -274,144 +307,162 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
     // Columns away from the x edges and from sources: every row in one
     // pass; rows outside an update domain keep their value, CPML terms where
     // a strip is met (psi staged in the ring slot of the column)
-    auto vel_band = [&](int cc) {
-      const int k = kqc, kk = kqc + 4, s = slot(cc);
+    // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
+    auto vel_band = [&](int cc, int s3, int s2, int s1, int s0) {
+      const int k = kqc, kk = kqc + 4, s = s0;
       const float *pc = ring + s * SL, *v0 = pc + R8;
+      const float *p3 = ring + s3 * SL, *p2 = ring + s2 * SL, *p1s = ring + s1 * SL;
       const bool ownc = cc < x1;
-      float vz = v0[R4 + k];
-      if (vzb) {
-        float Dz = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
-        if (jq1v >= 0) Dz = cpml_z(Dz, cq1, PZ(0, cc)[jq1v], psB(1) + ZS(cc, jq1v), ownc && ownr);
-        vz = vz + v0[3 * R4 + k] * Dz;
+      const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && q <= nz + 3;
+      // branch-free: every row computes its derivatives; rows outside an
+      // update domain keep their value, rows outside a strip their plain
+      // derivative (selects)
+      float Dz = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
+      float Dx = st4(p3[kk], p2[kk], p1s[kk], pc[kk]) * a.dxI;
+      Dz = cpml_zs(Dz, cq1, PZs(0, s)[jq1c], jq1v >= 0, psB(1) + ZS(cc, jq1c), ownc && ownr);
+      if constexpr (XPSI) {
+        const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
+        if (j0 >= 0) Dx = cpml_xs(Dx, 0, j0, PXs(0, s)[q], vxr, psB(0) + XS(j0, q), ownx);
       }
+      float vz = vzb ? v0[R4 + k] + v0[3 * R4 + k] * Dz : v0[R4 + k];
+      const float vx = vxr ? v0[k] + v0[2 * R4 + k] * Dx : v0[k];
       if (gany) {
         const float g = __shfl_sync(0xffffffffu, vz, glane);
         if (gsrc) vz = gok ? -g : -vz_any(gsrc, cc);
       }
       if (vact) svz[s * R4 + k] = vz;
+      if (vact && kq < TZ) svx[s * R4 + k] = vx;
       const int64_t o = so + S(q, cc);
-      if (ownc && ownr && q <= nz + 3) a.vzB[o] = vz;
-      if (vact && kq < TZ) {
-        float vx = v0[k];
-        if (vxr) {
-          const float *p3 = ring + slot(cc - 3) * SL, *p2 = ring + slot(cc - 2) * SL,
-                      *p1s = ring + slot(cc - 1) * SL;
-          float Dx = st4(p3[kk], p2[kk], p1s[kk], pc[kk]) * a.dxI;
-          const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
-          if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownc && ownr && q <= nz);
-          vx = vx + v0[2 * R4 + k] * Dx;
-        }
-        svx[s * R4 + k] = vx;
-        if (ownc && ownr && q <= nz) a.vxB[o] = vx;
-      }
+      if (ownz) a.vzB[o] = vz;
+      if (ownx && kq < TZ) a.vxB[o] = vx;
     };
-    auto str_band = [&](int c) {
-      if (t >= TZ) return;  // halo lanes
-      if (!srow) return;
-      const int k = t;
-      const float *pc = ring + slot(c) * SL;
-      float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
-                     svx[slot(c + 3) * R4 + k]) * a.dxI;
-      const int j2 = pml_slot(c, nx, npml, xlo, xhi);
-      if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, PX(1, c)[r], psB(2) + XS(j2, r), true);
-      const float *w = svz + slot(c) * R4;
+    // pressure of column c from velocity slots s0..s3 = columns c..c+3;
+    // halo lanes recompute the last row and store nothing
+    auto str_band = [&](int c, int s0, int s1, int s2, int s3) {
+      const int k = t < TZ ? t : TZ - 1, rk = z0 + k;
+      const float *pc = ring + s0 * SL;
+      float Dx = st4(svx[s0 * R4 + k], svx[s1 * R4 + k], svx[s2 * R4 + k], svx[s3 * R4 + k]) * a.dxI;
+      const float *w = svz + s0 * R4;
       float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
-      if (jr3v >= 0) Dz = cpml_z(Dz, cr3, PZ(1, c)[jr3v], psB(3) + ZS(c, jr3v), true);
-      a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
-    };
-    float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)
-    auto vel_edge = [&](int cc, int ib0, int ie0, int ib1, int ie1) {
-      if (!vact) return;
-      const int k = kq, kk = kq + 4, s = slot(cc);
-      const float *pc = ring + s * SL, *v0 = pc + R8;
-      const bool ownc = cc >= x0 && (cc < x1 || lastx);
-      if (kq < TZ) {
-        const bool ownx = ownc && ownr && q <= nz;
-        float vx;
-        if (rxhi && cc >= nx + 2) {
-          vx = cc == nx + 3 ? -vpre : -svx[slot(cc - 1) * R4 + k];  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
-        } else {
-          vx = v0[k];
-          if (vxr && cc >= 4 && cc <= nx) {
-            const float *p3 = ring + slot(cc - 3) * SL, *p2 = ring + slot(cc - 2) * SL,
-                        *p1 = ring + slot(cc - 1) * SL;
-            float D = st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI;
-            const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
-            if (j0 >= 0) D = cpml_p(D, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
-            vx = vx + v0[2 * R4 + k] * D;
-          }
-          if (cc == nx) vpre = vx;
-        }
-        if (rxlo && cc == 4) {
-          // dirichletxmin!: vx[1] = -vx[4] (before its source), vx[2] = -vx[3]
-          const float g1 = -vx, g2 = -svx[slot(3) * R4 + k];
-          svx[slot(1) * R4 + k] = g1;
-          svx[slot(2) * R4 + k] = g2;
-          if (x0 == 1 && ownr && q <= nz) {
-            a.vxB[so + S(q, 1)] = g1;
-            a.vxB[so + S(q, 2)] = g2;
-          }
-        }
-        if (!a.vonly) inject(a.cells, a.amount, ib0, ie0, q, vx);
-        svx[s * R4 + k] = vx;
-        if (ownx) a.vxB[so + S(q, cc)] = vx;
-      }
-      float vz;
-      if (gsrc) {
-        vz = -vz_any(gsrc, cc);  // dirichletzmin!/zmax!
-      } else {
-        vz = v0[R4 + k];
-        if (vzr && cc >= 4 && cc <= nx - 3) {
-          float D = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
-          if (jq1 >= 0) D = cpml_z(D, cq1, PZ(0, cc)[jq1], psB(1) + ZS(cc, jq1), ownc && ownr && cc <= nx);
-          vz = vz + v0[3 * R4 + k] * D;
-        }
-      }
-      if (!a.vonly) inject(a.cells, a.amount, ib1, ie1, q, vz);
-      svz[s * R4 + k] = vz;
-      if (ownc && ownr && cc <= nx && q <= nz + 3) a.vzB[so + S(q, cc)] = vz;
-    };
-    auto str_edge = [&](int c, int bs, int es) {
-      if (!srow) return;
-      const int k = t;
-      const float *pc = ring + slot(c) * SL;
-      float pn = pc[k + 4];
-      if (!a.vonly) {
-        float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
-                       svx[slot(c + 3) * R4 + k]) * a.dxI;
+      if constexpr (XPSI) {
         const int j2 = pml_slot(c, nx, npml, xlo, xhi);
-        if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, PX(1, c)[r], psB(2) + XS(j2, r), true);
-        const float *w = svz + slot(c) * R4;
-        float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
-        if (jr3 >= 0) Dz = cpml_z(Dz, cr3, PZ(1, c)[jr3], psB(3) + ZS(c, jr3), true);
-        pn = pn + (Dx + Dz) * pc[R8 + 4 * R4 + k];
-        inject(a.cells, a.amount, bs, es, r, pn);  // add_stress_source!
+        if (j2 >= 0) Dx = cpml_xs(Dx, 2, j2, PXs(1, s0)[rk], srow, psB(2) + XS(j2, rk), true);
       }
-      a.pB[so + S(r, c)] = pn;
+      Dz = cpml_zs(Dz, cr3, PZs(1, s0)[jr3c], jr3v >= 0, psB(3) + ZS(c, jr3c), true);
+      const float pn = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+      if (srow) a.pB[so + S(r, c)] = pn;
     };
-    // one sweep: iterations c < x0 only compute the first velocity columns
-    for (int c = x0 - 3; c < x1; c++) {
-      const int cc = c + 3;
-      int ib0, ie0, ib1, ie1, bs = 0, es = 0;
-      cvx.range(a.cells, cc, ib0, ie0);
-      cvz.range(a.cells, cc, ib1, ie1);
-      if (c >= x0) cst.range(a.cells, c, bs, es);
-      // general code for x edges, mirrors and sources (block-uniform);
-      // otherwise the band code over every row
-      const bool gv = colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
-      const bool gs = colfull_s(c) || bs < es;
-      wait_col(cc);
-      if (gv)
-        vel_edge(cc, ib0, ie0, ib1, ie1);
-      else
-        vel_band(cc);
-      __syncthreads();
-      if (issuer) issue(c + 7);
-      if (c >= x0) {
-        if (gs)
-          str_edge(c, bs, es);
+    if constexpr (MODE == 1) {
+      // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+      const int ncol = x1 - xbase;
+      for (int i0 = 0; i0 < ncol; i0 += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int it = i0 + u;
+          if (it >= ncol) break;
+          const int c = xbase + it;
+          if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+          vel_band(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
+          __syncthreads();
+          if (issuer) issue(c + 7);
+          if (c >= x0) str_band(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
+        }
+      }
+    } else {
+      float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)
+      auto vel_edge = [&](int cc, int ib0, int ie0, int ib1, int ie1) {
+        if (!vact) return;
+        const int k = kq, kk = kq + 4, s = slot(cc);
+        const float *pc = ring + s * SL, *v0 = pc + R8;
+        const bool ownc = cc >= x0 && (cc < x1 || lastx);
+        if (kq < TZ) {
+          const bool ownx = ownc && ownr && q <= nz;
+          float vx;
+          if (rxhi && cc >= nx + 2) {
+            vx = cc == nx + 3 ? -vpre : -svx[slot(cc - 1) * R4 + k];  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
+          } else {
+            vx = v0[k];
+            if (vxr && cc >= 4 && cc <= nx) {
+              const float *p3 = ring + slot(cc - 3) * SL, *p2 = ring + slot(cc - 2) * SL,
+                          *p1 = ring + slot(cc - 1) * SL;
+              float D = st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI;
+              const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
+              if (j0 >= 0) D = cpml_p(D, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
+              vx = vx + v0[2 * R4 + k] * D;
+            }
+            if (cc == nx) vpre = vx;
+          }
+          if (rxlo && cc == 4) {
+            // dirichletxmin!: vx[1] = -vx[4] (before its source), vx[2] = -vx[3]
+            const float g1 = -vx, g2 = -svx[slot(3) * R4 + k];
+            svx[slot(1) * R4 + k] = g1;
+            svx[slot(2) * R4 + k] = g2;
+            if (x0 == 1 && ownr && q <= nz) {
+              a.vxB[so + S(q, 1)] = g1;
+              a.vxB[so + S(q, 2)] = g2;
+            }
+          }
+          if (!a.vonly) inject(a.cells, a.amount, ib0, ie0, q, vx);
+          svx[s * R4 + k] = vx;
+          if (ownx) a.vxB[so + S(q, cc)] = vx;
+        }
+        float vz;
+        if (gsrc) {
+          vz = -vz_any(gsrc, cc);  // dirichletzmin!/zmax!
+        } else {
+          vz = v0[R4 + k];
+          if (vzr && cc >= 4 && cc <= nx - 3) {
+            float D = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
+            if (jq1 >= 0) D = cpml_z(D, cq1, PZ(0, cc)[jq1], psB(1) + ZS(cc, jq1), ownc && ownr && cc <= nx);
+            vz = vz + v0[3 * R4 + k] * D;
+          }
+        }
+        if (!a.vonly) inject(a.cells, a.amount, ib1, ie1, q, vz);
+        svz[s * R4 + k] = vz;
+        if (ownc && ownr && cc <= nx && q <= nz + 3) a.vzB[so + S(q, cc)] = vz;
+      };
+      auto str_edge = [&](int c, int bs, int es) {
+        if (!srow) return;
+        const int k = t;
+        const float *pc = ring + slot(c) * SL;
+        float pn = pc[k + 4];
+        if (!a.vonly) {
+          float Dx = st4(svx[slot(c) * R4 + k], svx[slot(c + 1) * R4 + k], svx[slot(c + 2) * R4 + k],
+                         svx[slot(c + 3) * R4 + k]) * a.dxI;
+          const int j2 = pml_slot(c, nx, npml, xlo, xhi);
+          if (j2 >= 0) Dx = cpml_p(Dx, 2, j2, PX(1, c)[r], psB(2) + XS(j2, r), true);
+          const float *w = svz + slot(c) * R4;
+          float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
+          if (jr3 >= 0) Dz = cpml_z(Dz, cr3, PZ(1, c)[jr3], psB(3) + ZS(c, jr3), true);
+          pn = pn + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+          inject(a.cells, a.amount, bs, es, r, pn);  // add_stress_source!
+        }
+        a.pB[so + S(r, c)] = pn;
+      };
+      // one sweep: iterations c < x0 only compute the first velocity columns
+      for (int c = x0 - 3; c < x1; c++) {
+        const int cc = c + 3;
+        int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+        cvx.range(a.cells, cc, ib0, ie0);
+        cvz.range(a.cells, cc, ib1, ie1);
+        if (c >= x0) cst.range(a.cells, c, bs, es);
+        // general code for x edges, mirrors and sources (block-uniform);
+        // otherwise the band code over every row
+        const bool gv = colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
+        const bool gs = colfull_s(c) || bs < es;
+        wait_col(cc);
+        if (gv)
+          vel_edge(cc, ib0, ie0, ib1, ie1);
         else
-          str_band(c);
+          vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc));
+        __syncthreads();
+        if (issuer) issue(c + 7);
+        if (c >= x0) {
+          if (gs)
+            str_edge(c, bs, es);
+          else
+            str_band(c, slot(c), slot(c + 1), slot(c + 2), slot(c + 3));
+        }
       }
     }
   }
@@ -429,14 +480,10 @@ __global__ void __launch_bounds__(A2_THREADS, FAST ? 6 : 4) k_a2(const A2Args a)
 int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   if (mode == GPI_ADJOINT && !vonly) return step_adjoint_acoustic2d(p, it);
   (void)ipw_mask;
-  static int attr_dev[64] = {0};
-  static size_t attr_gen[64] = {0};
+  static size_t attr[3][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !attr_dev[dev]) {
-    GPI_CUDA(p, cudaFuncSetAttribute(k_a2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A2_SMEM));
-    attr_dev[dev] = 1;
-  }
+  if (dev < 0 || dev >= 64) return fail(p, GPI_E_UNSUPPORTED, "device index too large");
   A2Args a;
   a.nz = p->d.nz;
   a.nx = p->d.nx;
@@ -474,29 +521,42 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.tiles = p->d_tiles;
   a.zsw = p->zsw;
   a.pzw = p->pzw;
-  a.psf = a2_psi_floats(*p);
-  const size_t gsmem = a2_smem_general(a.psf);
-  if (dev < 64 && attr_gen[dev] < gsmem) {
-    GPI_CUDA(p, cudaFuncSetAttribute(k_a2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
-    attr_gen[dev] = gsmem;
-  }
-  // the general kernel (longer blocks) goes first, on its own stream, so
-  // that interior blocks fill the SMs around it and its tail
-  const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
-  const bool both = nf && ng;
-  cudaStream_t gstream = fork_general(p, both);
-  if (ng) {
+  // shared memory per block: the ring with the CPML memory each mode stages
+  const bool zf = p->d.pml_faces & (GPI_ZMIN | GPI_ZMAX);
+  const int psf[3] = {0, zf ? 2 * p->pzw : 0, a2_psi_floats(*p)};
+  size_t smem[3];
+  for (int m = 0; m < 3; m++) smem[m] = m == 0 ? A2_SMEM : a2_smem_general(psf[m]);
+  void (*const fn[3])(A2Args) = {k_a2<0>, k_a2<1>, k_a2<2>};
+  for (int m = 0; m < 3; m++)
+    if (attr[m][dev] < smem[m]) {
+      GPI_CUDA(p, cudaFuncSetAttribute(fn[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[m]));
+      attr[m][dev] = smem[m];
+    }
+  auto launch = [&](int m, int first, int n, cudaStream_t st) {
+    if (n <= 0) return;
     A2Args g = a;
-    g.tiles = p->d_tiles + nf;
-    k_a2<false><<<ng, A2_THREADS, gsmem, gstream>>>(g);
+    g.tiles = p->d_tiles + first;
+    g.psf = psf[m];
+    fn[m]<<<n, A2_THREADS, smem[m], st>>>(g);
     p->launches++;
-  }
-  if (nf) {
-    k_a2<true><<<nf, A2_THREADS, A2_SMEM, p->stream>>>(a);
-    p->launches++;
+  };
+  const int nf = p->n_tiles_fast, nb = p->n_tiles_band, ne = p->n_tiles_edge;
+  if (vonly) {
+    // the velocity-only half step runs every tile on the general code
+    launch(2, 0, nf + nb + ne, p->stream);
+  } else {
+    // edge and band blocks (longer) go first, on their own streams, so that
+    // interior blocks fill the SMs around them and their tails
+    const int nside = ((nf > 0) + (nb > 0) + (ne > 0)) > 1 ? 2 : 0;
+    cudaStream_t st[2] = {p->stream, p->stream};
+    if (int rc = fork_side(p, nside, st)) return rc;
+    launch(2, nf + nb, ne, st[0]);
+    launch(1, nf, nb, st[1]);
+    launch(0, 0, nf, p->stream);
+    GPI_CUDA(p, cudaGetLastError());
+    if (int rc = join_side(p, nside)) return rc;
   }
   GPI_CUDA(p, cudaGetLastError());
-  if (int rc = join_general(p, both)) return rc;
   p->cur[0] ^= 1;
   return GPI_OK;
 }

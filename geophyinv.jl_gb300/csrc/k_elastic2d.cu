@@ -66,8 +66,13 @@ inline int e2_psi_floats(const Plan &p) {
 }
 inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (E2_SLOT + psf) + 2 * 8 * E2_R4); }
 
-template <bool FAST>
-__global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a) {
+// MODE 0: interior tiles (no CPML, face or source: straight-line code);
+// MODE 1: tiles that meet only z-strip CPML rows or z faces (the band code
+// over every column); MODE 2: tiles with x-edge, x-strip or source columns
+// (the band code plus the general code per column).
+template <int MODE>
+__global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Args a) {
+  constexpr bool FAST = MODE == 0, XPSI = MODE == 2;
   constexpr int TZ = E2_TZ, R8 = E2_R8, R4 = E2_R4, SLOT = E2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // one mbarrier per ring slot
@@ -115,6 +120,11 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
   auto PX = [&](int i, int cc) -> const float * {
     return ring + slot(cc) * SL + SLOT + 4 * PZW + (i < 2 ? i * R4 : 2 * R4 + (i - 2) * TZ) - z0;
   };
+  // the same by ring slot
+  auto PZs = [&](int i, int s) -> const float * { return ring + s * SL + SLOT + i * PZW - zoff; };
+  auto PXs = [&](int i, int s) -> const float * {
+    return ring + s * SL + SLOT + 4 * PZW + (i < 2 ? i * R4 : 2 * R4 + (i - 2) * TZ) - z0;
+  };
 
   if (t == 0) {
     for (int s = 0; s < 8; s++) mbar_init(&bar[s], 4);  // one arrival per warp
@@ -144,7 +154,7 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       float *v = sl + 3 * R8, *cf = v + 4 * R4;
       float *pz = sl + SLOT, *px = pz + 4 * PZW;
       int jx = -1;
-      if constexpr (!FAST) {
+      if constexpr (XPSI) {
         jx = wq == 0 ? pml_slot(next - 3, nx - 3, npml, xlo, xhi)
            : wq == 1 ? pml_slot(next - 3, nx - 6, npml, xlo, xhi)
            : wq == 2 ? pml_slot(next, nx, npml, xlo, xhi)
@@ -239,6 +249,18 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
     if (own) *dst = psi;
     return D * cf.z + psi;
   };
+  // the same as selects: the memory variable applies where `on`
+  auto cpml_zs = [&](float D, float3 cf, float psi_old, bool on, float *dst, bool own) -> float {
+    const float psi = cf.y * psi_old + cf.x * D;
+    if (on && own) *dst = psi;
+    return on ? D * cf.z + psi : D;
+  };
+  auto cpml_xs = [&](float D, int q8, int j, float psi_old, bool on, float *dst, bool own) -> float {
+    const float *cf = a.pml + q8 * P6;
+    const float psi = __ldg(cf + 2 * npml + j) * psi_old + __ldg(cf + j) * D;
+    if (on && own) *dst = psi;
+    return on ? D * __ldg(cf + 4 * npml + j) + psi : D;
+  };
   // vz at row qq of column cc before its source (source of a mirror row)
   auto vz_any = [&](int qq, int cc) -> float {
     const int kv = qq - z0;
@@ -277,12 +299,14 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
   // unless one of its rows or the current column touches a CPML strip, a
   // rigid or free face, a domain edge or a source cell.
   if constexpr (FAST) {
-    // interior tile: inside every update domain, no CPML, no face, no source
-    auto vel_fast = [&](int cc) {
+    // interior tile: inside every update domain, no CPML, no face, no
+    // source.  The sweep below is unrolled by the ring length, so every ring
+    // and velocity-buffer slot is a compile-time offset.
+    // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
+    auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
       if (!vact) return;
-      const int k = kq, kk = kq + 4, s = slot(cc);
-      const float *b3 = ring + slot(cc - 3) * SLOT, *b2 = ring + slot(cc - 2) * SLOT,
-                  *b1 = ring + slot(cc - 1) * SLOT, *b0 = ring + s * SLOT;
+      const int k = kq, kk = kq + 4;
+      const float *b3 = ring + s3 * SLOT, *b2 = ring + s2 * SLOT, *b1 = ring + s1 * SLOT, *b0 = ring + s0 * SLOT;
       const float *v0 = b0 + 3 * R8, *z3 = b3 + 2 * R8, *zz = b0 + R8;
       const float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
       const float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
@@ -290,22 +314,21 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       const float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
       const float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
       const float vz = v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2);
-      svx[s * R4 + k] = vx;
-      svz[s * R4 + k] = vz;
+      svx[s0 * R4 + k] = vx;
+      svz[s0 * R4 + k] = vz;
       if (cc < x1 && kq < TZ) {
         const int64_t o = so + S(q, cc);
         a.vxB[o] = vx;
         a.vzB[o] = vz;
       }
     };
-    auto str_fast = [&](int c) {
+    // stresses of column c from velocity slots s0..s3 = columns c..c+3
+    auto str_fast = [&](int c, int s0, int s1, int s2, int s3) {
       if (t >= TZ) return;
       const int k = t;
-      const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
-                  *u3 = svx + slot(c + 3) * R4;
-      const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
-                  *w3 = svz + slot(c + 3) * R4;
-      const float *bc = ring + slot(c) * SLOT, *cf = bc + 3 * R8 + 4 * R4;
+      const float *u0 = svx + s0 * R4, *u1 = svx + s1 * R4, *u2 = svx + s2 * R4, *u3 = svx + s3 * R4;
+      const float *w0 = svz + s0 * R4, *w1 = svz + s1 * R4, *w2 = svz + s2 * R4, *w3 = svz + s3 * R4;
+      const float *bc = ring + s0 * SLOT, *cf = bc + 3 * R8 + 4 * R4;
       const float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
       const float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
       const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
@@ -319,13 +342,20 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       a.tzzB[o] = tzz;
       a.txzB[o] = txz;
     };
-    for (int c = x0 - 3; c < x1; c++) {
-      const int cc = c + 3;
-      wait_col(cc);
-      vel_fast(cc);
-      __syncthreads();
-      if (issuer) issue(c + 7);
-      if (c >= x0) str_fast(c);
+    // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+    const int ncol = x1 - xbase;
+    for (int i0 = 0; i0 < ncol; i0 += 8) {
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int it = i0 + u;
+        if (it >= ncol) break;
+        const int c = xbase + it;
+        if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+        vel_fast(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
+        __syncthreads();
+        if (issuer) issue(c + 7);
+        if (c >= x0) str_fast(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
+      }
     }
   } else {
   // columns that need the full general code: x edges and mirrors, sources
@@ -337,6 +367,9 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
   const bool vxb = vact && vxr, vzb = vact && vzr;
   const int jq3v = vxb ? jq3 : -1, jq2v = vzb ? jq2 : -1;
   const int jr5v = srow ? jr5 : -1, jr6v = (srow && xzrow) ? jr6 : -1;
+  // in-window strip slots to read when a row is outside its strip
+  const int jq3c = jq3v >= 0 ? jq3v : zoff, jq2c = jq2v >= 0 ? jq2v : zoff;
+  const int jr5c = jr5v >= 0 ? jr5v : zoff, jr6c = jr6v >= 0 ? jr6v : zoff;
   // ghost rows of vz (dirichletzmin!/zmax!) read their mirror source from
   // the lane that computes it, when that lane is in the same warp
   const int lane = t & 31;
@@ -349,31 +382,29 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
     // Columns away from the x edges and from sources: every row in one
     // pass; rows outside an update domain keep their value, CPML terms where
     // a strip is met (psi staged in the ring slot of the column)
-    auto vel_band = [&](int cc) {
-      const int k = kqc, kk = kqc + 4, s = slot(cc);
-      const int j0 = vxb ? pml_slot(cc - 3, nx - 3, npml, xlo, xhi) : -1;
-      const int j1 = vzb ? pml_slot(cc - 3, nx - 6, npml, xlo, xhi) : -1;
+    // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
+    auto vel_band = [&](int cc, int s3, int s2, int s1, int s0) {
+      const int k = kqc, kk = kqc + 4, s = s0;
       const bool ownc = cc < x1;
       const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && q <= nz + 3;
-      const float *b3 = ring + slot(cc - 3) * SL, *b2 = ring + slot(cc - 2) * SL,
-                  *b1 = ring + slot(cc - 1) * SL, *b0 = ring + s * SL;
+      const float *b3 = ring + s3 * SL, *b2 = ring + s2 * SL, *b1 = ring + s1 * SL, *b0 = ring + s * SL;
       const float *v0 = b0 + 3 * R8, *z3 = b3 + 2 * R8, *zz = b0 + R8;
-      float vx = v0[k];
-      if (vxb) {
-        float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
-        if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
-        float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
-        if (jq3v >= 0) Dz = cpml_z(Dz, cq3, PZ(1, cc)[jq3v], psB(3) + ZS(cc, jq3v), ownx);
-        vx = vx - v0[2 * R4 + k] * (Dx + Dz);
+      // branch-free: every row computes its derivatives; rows outside an
+      // update domain keep their value, rows outside a strip their plain
+      // derivative (selects)
+      float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
+      float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
+      float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
+      float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
+      if constexpr (XPSI) {
+        const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
+        if (j0 >= 0) Dx = cpml_xs(Dx, 0, j0, PXs(0, s)[q], vxb, psB(0) + XS(j0, q), ownx);
+        if (j1 >= 0) Dx2 = cpml_xs(Dx2, 1, j1, PXs(1, s)[q], vzb, psB(1) + XS(j1, q), ownz);
       }
-      float vz = v0[R4 + k];
-      if (vzb) {
-        float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
-        if (j1 >= 0) Dx2 = cpml_p(Dx2, 1, j1, PX(1, cc)[q], psB(1) + XS(j1, q), ownz);
-        float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
-        if (jq2v >= 0) Dz2 = cpml_z(Dz2, cq2, PZ(0, cc)[jq2v], psB(2) + ZS(cc, jq2v), ownz);
-        vz = vz - v0[3 * R4 + k] * (Dx2 + Dz2);
-      }
+      Dz = cpml_zs(Dz, cq3, PZs(1, s)[jq3c], jq3v >= 0, psB(3) + ZS(cc, jq3c), ownx);
+      Dz2 = cpml_zs(Dz2, cq2, PZs(0, s)[jq2c], jq2v >= 0, psB(2) + ZS(cc, jq2c), ownz);
+      const float vx = vxb ? v0[k] - v0[2 * R4 + k] * (Dx + Dz) : v0[k];
+      float vz = vzb ? v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2) : v0[R4 + k];
       if (gany) {
         const float g = __shfl_sync(0xffffffffu, vz, glane);
         if (gsrc) vz = gok ? -g : -vz_any(gsrc, cc);
@@ -386,29 +417,29 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
       if (ownx) a.vxB[o] = vx;
       if (ownz) a.vzB[o] = vz;
     };
-    auto str_band = [&](int c) {
-      if (t >= TZ) return;  // halo lanes
-      const int k = t;
-      const int j4 = srow ? pml_slot(c, nx, npml, xlo, xhi) : -1;
-      const int j7 = (srow && xzrow) ? pml_slot(c, nx - 3, npml, xlo, xhi) : -1;
-      const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
-                  *u3 = svx + slot(c + 3) * R4;
-      const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
-                  *w3 = svz + slot(c + 3) * R4;
-      const float *bc = ring + slot(c) * SL, *cf = bc + 3 * R8 + 4 * R4;
+    // stresses of column c from velocity slots s0..s3 = columns c..c+3;
+    // halo lanes recompute the last row and store nothing
+    auto str_band = [&](int c, int s0, int s1, int s2, int s3) {
+      const int k = t < TZ ? t : TZ - 1, rk = z0 + k;
+      const float *u0 = svx + s0 * R4, *u1 = svx + s1 * R4, *u2 = svx + s2 * R4, *u3 = svx + s3 * R4;
+      const float *w0 = svz + s0 * R4, *w1 = svz + s1 * R4, *w2 = svz + s2 * R4, *w3 = svz + s3 * R4;
+      const float *bc = ring + s0 * SL, *cf = bc + 3 * R8 + 4 * R4;
       float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
-      if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, PX(2, c)[r], psB(4) + XS(j4, r), true);
       float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
-      if (jr5v >= 0) dvzdz = cpml_z(dvzdz, cr5, PZ(2, c)[jr5v], psB(5) + ZS(c, jr5v), true);
+      float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
+      float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
+      if constexpr (XPSI) {
+        const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
+        if (j4 >= 0) dvxdx = cpml_xs(dvxdx, 4, j4, PXs(2, s0)[rk], srow, psB(4) + XS(j4, rk), true);
+        if (j7 >= 0) dvzdx = cpml_xs(dvzdx, 7, j7, PXs(3, s0)[rk], srow && xzrow, psB(7) + XS(j7, rk), true);
+      }
+      dvzdz = cpml_zs(dvzdz, cr5, PZs(2, s0)[jr5c], jr5v >= 0, psB(5) + ZS(c, jr5c), true);
+      dvxdz = cpml_zs(dvxdz, cr6, PZs(3, s0)[jr6c], jr6v >= 0, psB(6) + ZS(c, jr6c), true);
       const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
       const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
       float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
-      float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
-      if (jr6v >= 0) dvxdz = cpml_z(dvxdz, cr6, PZ(3, c)[jr6v], psB(6) + ZS(c, jr6v), true);
-      float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
-      if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, PX(3, c)[r], psB(7) + XS(j7, r), true);
       float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
-      if (fsblk && t < 32) {
+      if (fsblk) {
         // free_surface_mirror!(tauzz), free_surface!(tauxz): tzz[1] = -tzz[2]
         const float t2 = __shfl_down_sync(0xffffffffu, tzz, 1);
         if (fsrow) {
@@ -423,130 +454,148 @@ __global__ void __launch_bounds__(E2_THREADS, FAST ? 4 : 3) k_e2(const E2Args a)
         if (xzrow) a.txzB[o] = txz;
       }
     };
-    // velocities of column cc: update_v! with CPML, mirrors, sources
-    auto vel_edge = [&](int cc, int ib0, int ie0, int ib1, int ie1) {
-      if (!vact) return;
-      const int k = kq, kk = kq + 4, s = slot(cc);
-      const bool vxc = cc >= 4 && cc <= nx, vzc = cc >= 4 && cc <= nx - 3;
-      const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
-      const bool ownc = cc >= x0 && (cc < x1 || lastx);
-      const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && cc <= nx && q <= nz + 3;
-      const float *b3 = ring + slot(cc - 3) * SL, *b2 = ring + slot(cc - 2) * SL,
-                  *b1 = ring + slot(cc - 1) * SL, *bq = ring + s * SL;
-      const float *v0 = bq + 3 * R8, *z3 = b3 + 2 * R8;
-      float vx;
-      if (rxhi && cc >= nx + 2) {
-        vx = cc == nx + 3 ? -vpre : -svx[slot(cc - 1) * R4 + k];  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
-      } else {
-        vx = v0[k];
-        if (vxr && vxc) {
-          float Dx = st4(b3[kk], b2[kk], b1[kk], bq[kk]) * a.dxI;
-          if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
-          float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
-          if (jq3 >= 0) Dz = cpml_z(Dz, cq3, PZ(1, cc)[jq3], psB(3) + ZS(cc, jq3), ownx);
-          vx = vx - v0[2 * R4 + k] * (Dx + Dz);
-        }
-        if (cc == nx) vpre = vx;
-      }
-      if (rxlo && cc == 4) {
-        // dirichletxmin!: vx[1] = -vx[4] (before its source), vx[2] = -vx[3]
-        const float g1 = -vx, g2 = -svx[slot(3) * R4 + k];
-        svx[slot(1) * R4 + k] = g1;
-        svx[slot(2) * R4 + k] = g2;
-        if (x0 == 1 && ownr && q <= nz) {
-          a.vxB[so + S(q, 1)] = g1;
-          a.vxB[so + S(q, 2)] = g2;
+    if constexpr (MODE == 1) {
+      // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+      const int ncol = x1 - xbase;
+      for (int i0 = 0; i0 < ncol; i0 += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int it = i0 + u;
+          if (it >= ncol) break;
+          const int c = xbase + it;
+          if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+          vel_band(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
+          __syncthreads();
+          if (issuer) issue(c + 7);
+          if (c >= x0) str_band(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
         }
       }
-      if (!a.vonly) inject(a.cells, a.amount, ib0, ie0, q, vx);
-      svx[s * R4 + k] = vx;
-      if (ownx) a.vxB[so + S(q, cc)] = vx;
-      float vz;
-      if (gsrc) {
-        vz = -vz_any(gsrc, cc);
-      } else {
-        vz = v0[R4 + k];
-        if (vzr && vzc) {
-          float Dx = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], bq[2 * R8 + kk - 3]) * a.dxI;
-          if (j1 >= 0) Dx = cpml_p(Dx, 1, j1, PX(1, cc)[q], psB(1) + XS(j1, q), ownz);
-          const float *zz = bq + R8;
-          float Dz = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
-          if (jq2 >= 0) Dz = cpml_z(Dz, cq2, PZ(0, cc)[jq2], psB(2) + ZS(cc, jq2), ownz);
-          vz = vz - v0[3 * R4 + k] * (Dx + Dz);
+    } else {
+      // velocities of column cc: update_v! with CPML, mirrors, sources
+      auto vel_edge = [&](int cc, int ib0, int ie0, int ib1, int ie1) {
+        if (!vact) return;
+        const int k = kq, kk = kq + 4, s = slot(cc);
+        const bool vxc = cc >= 4 && cc <= nx, vzc = cc >= 4 && cc <= nx - 3;
+        const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi), j1 = pml_slot(cc - 3, nx - 6, npml, xlo, xhi);
+        const bool ownc = cc >= x0 && (cc < x1 || lastx);
+        const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && cc <= nx && q <= nz + 3;
+        const float *b3 = ring + slot(cc - 3) * SL, *b2 = ring + slot(cc - 2) * SL,
+                    *b1 = ring + slot(cc - 1) * SL, *bq = ring + s * SL;
+        const float *v0 = bq + 3 * R8, *z3 = b3 + 2 * R8;
+        float vx;
+        if (rxhi && cc >= nx + 2) {
+          vx = cc == nx + 3 ? -vpre : -svx[slot(cc - 1) * R4 + k];  // vx[nx+3] = -vx[nx], vx[nx+2] = -vx[nx+1]
+        } else {
+          vx = v0[k];
+          if (vxr && vxc) {
+            float Dx = st4(b3[kk], b2[kk], b1[kk], bq[kk]) * a.dxI;
+            if (j0 >= 0) Dx = cpml_p(Dx, 0, j0, PX(0, cc)[q], psB(0) + XS(j0, q), ownx);
+            float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
+            if (jq3 >= 0) Dz = cpml_z(Dz, cq3, PZ(1, cc)[jq3], psB(3) + ZS(cc, jq3), ownx);
+            vx = vx - v0[2 * R4 + k] * (Dx + Dz);
+          }
+          if (cc == nx) vpre = vx;
         }
-      }
-      if (!a.vonly) inject(a.cells, a.amount, ib1, ie1, q, vz);
-      svz[s * R4 + k] = vz;
-      if (ownz) a.vzB[so + S(q, cc)] = vz;
-    };
-    // stresses of column c: compute_stressii!/ij!, free surface, sources
-    auto str_edge = [&](int c, int bs, int es) {
-      if (!srow) return;
-      const int k = t;
-      const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
-      const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
-                  *u3 = svx + slot(c + 3) * R4;
-      const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
-                  *w3 = svz + slot(c + 3) * R4;
-      const float *bc = ring + slot(c) * SL, *cf = bc + 3 * R8 + 4 * R4;
-      const int64_t o = so + S(r, c);
-      const bool hasxz = xzrow && c <= nx - 3;
-      float txx, tzz, txz = 0.f;
-      if (a.vonly) {
-        txx = bc[k + 4];
-        tzz = bc[R8 + k + 4];
-        txz = bc[2 * R8 + k + 4];
-      } else {
-        float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
-        if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, PX(2, c)[r], psB(4) + XS(j4, r), true);
-        float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
-        if (jr5 >= 0) dvzdz = cpml_z(dvzdz, cr5, PZ(2, c)[jr5], psB(5) + ZS(c, jr5), true);
-        const float M = cf[k], Lm = cf[TZ + k];
-        txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
-        tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
-        if (hasxz) {
-          float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
-          if (jr6 >= 0) dvxdz = cpml_z(dvxdz, cr6, PZ(3, c)[jr6], psB(6) + ZS(c, jr6), true);
-          float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
-          if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, PX(3, c)[r], psB(7) + XS(j7, r), true);
-          txz = bc[2 * R8 + k + 4] - cf[2 * TZ + k] * (dvxdz + dvzdx);
+        if (rxlo && cc == 4) {
+          // dirichletxmin!: vx[1] = -vx[4] (before its source), vx[2] = -vx[3]
+          const float g1 = -vx, g2 = -svx[slot(3) * R4 + k];
+          svx[slot(1) * R4 + k] = g1;
+          svx[slot(2) * R4 + k] = g2;
+          if (x0 == 1 && ownr && q <= nz) {
+            a.vxB[so + S(q, 1)] = g1;
+            a.vxB[so + S(q, 2)] = g2;
+          }
         }
-        if (fsrow) {
-          // free_surface_mirror!(tauzz), free_surface!(tauxz): tzz[1] = -tzz[2]
-          tzz = -tzz_row2(c);
-          txz = 0.f;
+        if (!a.vonly) inject(a.cells, a.amount, ib0, ie0, q, vx);
+        svx[s * R4 + k] = vx;
+        if (ownx) a.vxB[so + S(q, cc)] = vx;
+        float vz;
+        if (gsrc) {
+          vz = -vz_any(gsrc, cc);
+        } else {
+          vz = v0[R4 + k];
+          if (vzr && vzc) {
+            float Dx = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], bq[2 * R8 + kk - 3]) * a.dxI;
+            if (j1 >= 0) Dx = cpml_p(Dx, 1, j1, PX(1, cc)[q], psB(1) + XS(j1, q), ownz);
+            const float *zz = bq + R8;
+            float Dz = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
+            if (jq2 >= 0) Dz = cpml_z(Dz, cq2, PZ(0, cc)[jq2], psB(2) + ZS(cc, jq2), ownz);
+            vz = vz - v0[3 * R4 + k] * (Dx + Dz);
+          }
         }
-        // add_stress_source!: txx += pv dtM; tzz += pv dtM
-        inject(a.cells, a.amount, bs, es, r, txx);
-        inject(a.cells, a.amount, bs, es, r, tzz);
-      }
-      a.txxB[o] = txx;
-      a.tzzB[o] = tzz;
-      if (hasxz) a.txzB[o] = txz;
-    };
-    // one sweep: iterations c < x0 only compute the first velocity columns
-    for (int c = x0 - 3; c < x1; c++) {
-      const int cc = c + 3;
-      int ib0, ie0, ib1, ie1, bs = 0, es = 0;
-      cvx.range(a.cells, cc, ib0, ie0);
-      cvz.range(a.cells, cc, ib1, ie1);
-      if (c >= x0) cst.range(a.cells, c, bs, es);
-      // general code for x edges, mirrors and sources (block-uniform);
-      // otherwise the band code over every row
-      const bool gv = colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
-      const bool gs = colfull_s(c) || bs < es;
-      wait_col(cc);
-      if (gv)
-        vel_edge(cc, ib0, ie0, ib1, ie1);
-      else
-        vel_band(cc);
-      __syncthreads();
-      if (issuer) issue(c + 7);
-      if (c >= x0) {
-        if (gs)
-          str_edge(c, bs, es);
+        if (!a.vonly) inject(a.cells, a.amount, ib1, ie1, q, vz);
+        svz[s * R4 + k] = vz;
+        if (ownz) a.vzB[so + S(q, cc)] = vz;
+      };
+      // stresses of column c: compute_stressii!/ij!, free surface, sources
+      auto str_edge = [&](int c, int bs, int es) {
+        if (!srow) return;
+        const int k = t;
+        const int j4 = pml_slot(c, nx, npml, xlo, xhi), j7 = pml_slot(c, nx - 3, npml, xlo, xhi);
+        const float *u0 = svx + slot(c) * R4, *u1 = svx + slot(c + 1) * R4, *u2 = svx + slot(c + 2) * R4,
+                    *u3 = svx + slot(c + 3) * R4;
+        const float *w0 = svz + slot(c) * R4, *w1 = svz + slot(c + 1) * R4, *w2 = svz + slot(c + 2) * R4,
+                    *w3 = svz + slot(c + 3) * R4;
+        const float *bc = ring + slot(c) * SL, *cf = bc + 3 * R8 + 4 * R4;
+        const int64_t o = so + S(r, c);
+        const bool hasxz = xzrow && c <= nx - 3;
+        float txx, tzz, txz = 0.f;
+        if (a.vonly) {
+          txx = bc[k + 4];
+          tzz = bc[R8 + k + 4];
+          txz = bc[2 * R8 + k + 4];
+        } else {
+          float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
+          if (j4 >= 0) dvxdx = cpml_p(dvxdx, 4, j4, PX(2, c)[r], psB(4) + XS(j4, r), true);
+          float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
+          if (jr5 >= 0) dvzdz = cpml_z(dvzdz, cr5, PZ(2, c)[jr5], psB(5) + ZS(c, jr5), true);
+          const float M = cf[k], Lm = cf[TZ + k];
+          txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
+          tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
+          if (hasxz) {
+            float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
+            if (jr6 >= 0) dvxdz = cpml_z(dvxdz, cr6, PZ(3, c)[jr6], psB(6) + ZS(c, jr6), true);
+            float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
+            if (j7 >= 0) dvzdx = cpml_p(dvzdx, 7, j7, PX(3, c)[r], psB(7) + XS(j7, r), true);
+            txz = bc[2 * R8 + k + 4] - cf[2 * TZ + k] * (dvxdz + dvzdx);
+          }
+          if (fsrow) {
+            // free_surface_mirror!(tauzz), free_surface!(tauxz): tzz[1] = -tzz[2]
+            tzz = -tzz_row2(c);
+            txz = 0.f;
+          }
+          // add_stress_source!: txx += pv dtM; tzz += pv dtM
+          inject(a.cells, a.amount, bs, es, r, txx);
+          inject(a.cells, a.amount, bs, es, r, tzz);
+        }
+        a.txxB[o] = txx;
+        a.tzzB[o] = tzz;
+        if (hasxz) a.txzB[o] = txz;
+      };
+      // one sweep: iterations c < x0 only compute the first velocity columns
+      for (int c = x0 - 3; c < x1; c++) {
+        const int cc = c + 3;
+        int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+        cvx.range(a.cells, cc, ib0, ie0);
+        cvz.range(a.cells, cc, ib1, ie1);
+        if (c >= x0) cst.range(a.cells, c, bs, es);
+        // general code for x edges, mirrors and sources (block-uniform);
+        // otherwise the band code over every row
+        const bool gv = colfull_v(cc) || ib0 < ie0 || ib1 < ie1;
+        const bool gs = colfull_s(c) || bs < es;
+        wait_col(cc);
+        if (gv)
+          vel_edge(cc, ib0, ie0, ib1, ie1);
         else
-          str_band(c);
+          vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc));
+        __syncthreads();
+        if (issuer) issue(c + 7);
+        if (c >= x0) {
+          if (gs)
+            str_edge(c, bs, es);
+          else
+            str_band(c, slot(c), slot(c + 1), slot(c + 2), slot(c + 3));
+        }
       }
     }
   }
@@ -567,14 +616,10 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   (void)ipw_mask;
   (void)it;
   (void)mode;
-  static int attr_dev[64] = {0};
-  static size_t attr_gen[64] = {0};
+  static size_t attr[3][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !attr_dev[dev]) {
-    GPI_CUDA(p, cudaFuncSetAttribute(k_e2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E2_SMEM));
-    attr_dev[dev] = 1;
-  }
+  if (dev < 0 || dev >= 64) return fail(p, GPI_E_UNSUPPORTED, "device index too large");
   E2Args a;
   a.nz = p->d.nz;
   a.nx = p->d.nx;
@@ -619,31 +664,42 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.tiles = p->d_tiles;
   a.zsw = p->zsw;
   a.pzw = p->pzw;
-  a.psf = e2_psi_floats(*p);
-  const size_t gsmem = e2_smem_general(a.psf);
-  if (dev < 64 && attr_gen[dev] < gsmem) {
-    GPI_CUDA(p, cudaFuncSetAttribute(k_e2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
-    attr_gen[dev] = gsmem;
-  }
-  // interior tiles on the straight-line kernel, the rest on the general one;
-  // the velocity-only half step runs every tile on the general kernel
-  // the general kernel (longer blocks) goes first, on its own stream, so
-  // that interior blocks fill the SMs around it and its tail
-  const int nf = vonly ? 0 : p->n_tiles_fast, ng = p->n_tiles_fast + p->n_tiles_gen - nf;
-  const bool both = nf && ng;
-  cudaStream_t gstream = fork_general(p, both);
-  if (ng) {
+  // shared memory per block: the ring with the CPML memory each mode stages
+  const bool zf = p->d.pml_faces & (GPI_ZMIN | GPI_ZMAX);
+  const int psf[3] = {0, zf ? 4 * p->pzw : 0, e2_psi_floats(*p)};
+  size_t smem[3];
+  for (int m = 0; m < 3; m++) smem[m] = m == 0 ? E2_SMEM : e2_smem_general(psf[m]);
+  void (*const fn[3])(E2Args) = {k_e2<0>, k_e2<1>, k_e2<2>};
+  for (int m = 0; m < 3; m++)
+    if (attr[m][dev] < smem[m]) {
+      GPI_CUDA(p, cudaFuncSetAttribute(fn[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[m]));
+      attr[m][dev] = smem[m];
+    }
+  auto launch = [&](int m, int first, int n, cudaStream_t st) {
+    if (n <= 0) return;
     E2Args g = a;
-    g.tiles = p->d_tiles + nf;
-    k_e2<false><<<ng, E2_THREADS, gsmem, gstream>>>(g);
+    g.tiles = p->d_tiles + first;
+    g.psf = psf[m];
+    fn[m]<<<n, E2_THREADS, smem[m], st>>>(g);
     p->launches++;
-  }
-  if (nf) {
-    k_e2<true><<<nf, E2_THREADS, E2_SMEM, p->stream>>>(a);
-    p->launches++;
+  };
+  const int nf = p->n_tiles_fast, nb = p->n_tiles_band, ne = p->n_tiles_edge;
+  if (vonly) {
+    // the velocity-only half step runs every tile on the general code
+    launch(2, 0, nf + nb + ne, p->stream);
+  } else {
+    // edge and band blocks (longer) go first, on their own streams, so that
+    // interior blocks fill the SMs around them and their tails
+    const int nside = ((nf > 0) + (nb > 0) + (ne > 0)) > 1 ? 2 : 0;
+    cudaStream_t st[2] = {p->stream, p->stream};
+    if (int rc = fork_side(p, nside, st)) return rc;
+    launch(2, nf + nb, ne, st[0]);
+    launch(1, nf, nb, st[1]);
+    launch(0, 0, nf, p->stream);
+    GPI_CUDA(p, cudaGetLastError());
+    if (int rc = join_side(p, nside)) return rc;
   }
   GPI_CUDA(p, cudaGetLastError());
-  if (int rc = join_general(p, both)) return rc;
   p->cur[0] ^= 1;
   return GPI_OK;
 }

@@ -256,11 +256,12 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     P.d_group_ptr = (int32_t *)carve(2 * NKIND + 1);
     P.d_wav = (float **)carve(2);
     h_wavptr[0] = (float *)wavelets;
-    int nf = 0;
-    const int ntile = classify_tiles(P, h_cells, h_gptr, h_tiles, kMaxTiles, &nf);
+    int nf = 0, nb = 0;
+    const int ntile = classify_tiles(P, h_cells, h_gptr, h_tiles, kMaxTiles, &nf, &nb);
     if (ntile < 0) return nfail(GPI_E_INVALID, "grid too large for the no-alloc tile table");
     P.n_tiles_fast = nf;
-    P.n_tiles_gen = ntile - nf;
+    P.n_tiles_band = nb;
+    P.n_tiles_edge = ntile - nf - nb;
     P.d_tiles = (int3 *)carve((int64_t)(sizeof(int3) * ntile + 3) / 4);
     if (!room) return nfail(GPI_E_INVALID, "problem exceeds the 64 MiB no-alloc scratch");
     cudaStream_t s = P.stream;
