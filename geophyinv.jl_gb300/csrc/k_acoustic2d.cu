@@ -227,8 +227,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
   // rigid face, a domain edge or a source cell.
   if constexpr (FAST) {
     // interior tile: inside every update domain, no CPML, no face, no
-    // source.  The sweep below is unrolled by the ring length, so every ring
-    // and velocity-buffer slot is a compile-time offset.
+    // source.
     // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
     auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
       if (!vact) return;
@@ -257,20 +256,15 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
       const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
       a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
     };
-    // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
     const int ncol = x1 - xbase;
-    for (int i0 = 0; i0 < ncol; i0 += 8) {
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int it = i0 + u;
-        if (it >= ncol) break;
-        const int c = xbase + it;
-        if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-        vel_fast(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-        __syncthreads();
-        if (issuer) issue(c + 7);
-        if (c >= x0) str_fast(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-      }
+    for (int it = 0; it < ncol; it++) {
+      const int c = xbase + it;
+      if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+      vel_fast(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+      __syncthreads();
+      if (issuer) issue(c + 7);
+      if (c >= x0) str_fast(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
     }
   } else {
   // columns that need the full general code: x edges and mirrors, sources
@@ -282,6 +276,9 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
   const int jq1v = vzb ? jq1 : -1, jr3v = srow ? jr3 : -1;
   // in-window strip slots to read when a row is outside its strip
   const int jq1c = jq1v >= 0 ? jq1v : zoff, jr3c = jr3v >= 0 ? jr3v : zoff;
+  // warps with a z-strip row (velocity / pressure rows): the others skip the
+  // memory-variable code as a whole
+  const bool wzv = __any_sync(0xffffffffu, jq1v >= 0), wzs = __any_sync(0xffffffffu, jr3v >= 0);
   // ghost rows of vz (dirichletzmin!/zmax!) read their mirror source from
   // the lane that computes it, when that lane is in the same warp
   const int lane = t & 31;
@@ -319,7 +316,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
       // derivative (selects)
       float Dz = st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI;
       float Dx = st4(p3[kk], p2[kk], p1s[kk], pc[kk]) * a.dxI;
-      Dz = cpml_zs(Dz, cq1, PZs(0, s)[jq1c], jq1v >= 0, psB(1) + ZS(cc, jq1c), ownc && ownr);
+      if (wzv) Dz = cpml_zs(Dz, cq1, PZs(0, s)[jq1c], jq1v >= 0, psB(1) + ZS(cc, jq1c), ownc && ownr);
       if constexpr (XPSI) {
         const int j0 = pml_slot(cc - 3, nx - 3, npml, xlo, xhi);
         if (j0 >= 0) Dx = cpml_xs(Dx, 0, j0, PXs(0, s)[q], vxr, psB(0) + XS(j0, q), ownx);
@@ -348,25 +345,20 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
         const int j2 = pml_slot(c, nx, npml, xlo, xhi);
         if (j2 >= 0) Dx = cpml_xs(Dx, 2, j2, PXs(1, s0)[rk], srow, psB(2) + XS(j2, rk), true);
       }
-      Dz = cpml_zs(Dz, cr3, PZs(1, s0)[jr3c], jr3v >= 0, psB(3) + ZS(c, jr3c), true);
+      if (wzs) Dz = cpml_zs(Dz, cr3, PZs(1, s0)[jr3c], jr3v >= 0, psB(3) + ZS(c, jr3c), true);
       const float pn = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
       if (srow) a.pB[so + S(r, c)] = pn;
     };
     if constexpr (MODE == 1) {
-      // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+      // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
       const int ncol = x1 - xbase;
-      for (int i0 = 0; i0 < ncol; i0 += 8) {
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-          const int it = i0 + u;
-          if (it >= ncol) break;
-          const int c = xbase + it;
-          if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-          vel_band(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-          __syncthreads();
-          if (issuer) issue(c + 7);
-          if (c >= x0) str_band(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-        }
+      for (int it = 0; it < ncol; it++) {
+        const int c = xbase + it;
+        if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+        vel_band(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+        __syncthreads();
+        if (issuer) issue(c + 7);
+        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
       }
     } else {
       float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)

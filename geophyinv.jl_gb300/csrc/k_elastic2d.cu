@@ -300,8 +300,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
   // rigid or free face, a domain edge or a source cell.
   if constexpr (FAST) {
     // interior tile: inside every update domain, no CPML, no face, no
-    // source.  The sweep below is unrolled by the ring length, so every ring
-    // and velocity-buffer slot is a compile-time offset.
+    // source.
     // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
     auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
       if (!vact) return;
@@ -342,20 +341,15 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
       a.tzzB[o] = tzz;
       a.txzB[o] = txz;
     };
-    // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
     const int ncol = x1 - xbase;
-    for (int i0 = 0; i0 < ncol; i0 += 8) {
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int it = i0 + u;
-        if (it >= ncol) break;
-        const int c = xbase + it;
-        if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-        vel_fast(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-        __syncthreads();
-        if (issuer) issue(c + 7);
-        if (c >= x0) str_fast(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-      }
+    for (int it = 0; it < ncol; it++) {
+      const int c = xbase + it;
+      if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+      vel_fast(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+      __syncthreads();
+      if (issuer) issue(c + 7);
+      if (c >= x0) str_fast(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
     }
   } else {
   // columns that need the full general code: x edges and mirrors, sources
@@ -370,6 +364,10 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
   // in-window strip slots to read when a row is outside its strip
   const int jq3c = jq3v >= 0 ? jq3v : zoff, jq2c = jq2v >= 0 ? jq2v : zoff;
   const int jr5c = jr5v >= 0 ? jr5v : zoff, jr6c = jr6v >= 0 ? jr6v : zoff;
+  // warps with a z-strip row (velocity / stress rows): the others skip the
+  // memory-variable code as a whole
+  const bool wzv = __any_sync(0xffffffffu, jq3v >= 0 || jq2v >= 0);
+  const bool wzs = __any_sync(0xffffffffu, jr5v >= 0 || jr6v >= 0);
   // ghost rows of vz (dirichletzmin!/zmax!) read their mirror source from
   // the lane that computes it, when that lane is in the same warp
   const int lane = t & 31;
@@ -401,8 +399,10 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
         if (j0 >= 0) Dx = cpml_xs(Dx, 0, j0, PXs(0, s)[q], vxb, psB(0) + XS(j0, q), ownx);
         if (j1 >= 0) Dx2 = cpml_xs(Dx2, 1, j1, PXs(1, s)[q], vzb, psB(1) + XS(j1, q), ownz);
       }
-      Dz = cpml_zs(Dz, cq3, PZs(1, s)[jq3c], jq3v >= 0, psB(3) + ZS(cc, jq3c), ownx);
-      Dz2 = cpml_zs(Dz2, cq2, PZs(0, s)[jq2c], jq2v >= 0, psB(2) + ZS(cc, jq2c), ownz);
+      if (wzv) {
+        Dz = cpml_zs(Dz, cq3, PZs(1, s)[jq3c], jq3v >= 0, psB(3) + ZS(cc, jq3c), ownx);
+        Dz2 = cpml_zs(Dz2, cq2, PZs(0, s)[jq2c], jq2v >= 0, psB(2) + ZS(cc, jq2c), ownz);
+      }
       const float vx = vxb ? v0[k] - v0[2 * R4 + k] * (Dx + Dz) : v0[k];
       float vz = vzb ? v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2) : v0[R4 + k];
       if (gany) {
@@ -433,8 +433,10 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
         if (j4 >= 0) dvxdx = cpml_xs(dvxdx, 4, j4, PXs(2, s0)[rk], srow, psB(4) + XS(j4, rk), true);
         if (j7 >= 0) dvzdx = cpml_xs(dvzdx, 7, j7, PXs(3, s0)[rk], srow && xzrow, psB(7) + XS(j7, rk), true);
       }
-      dvzdz = cpml_zs(dvzdz, cr5, PZs(2, s0)[jr5c], jr5v >= 0, psB(5) + ZS(c, jr5c), true);
-      dvxdz = cpml_zs(dvxdz, cr6, PZs(3, s0)[jr6c], jr6v >= 0, psB(6) + ZS(c, jr6c), true);
+      if (wzs) {
+        dvzdz = cpml_zs(dvzdz, cr5, PZs(2, s0)[jr5c], jr5v >= 0, psB(5) + ZS(c, jr5c), true);
+        dvxdz = cpml_zs(dvxdz, cr6, PZs(3, s0)[jr6c], jr6v >= 0, psB(6) + ZS(c, jr6c), true);
+      }
       const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
       const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
       float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
@@ -455,20 +457,15 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
       }
     };
     if constexpr (MODE == 1) {
-      // iteration it handles c = xbase + it: slot(c + m) = (it + m) & 7
+      // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
       const int ncol = x1 - xbase;
-      for (int i0 = 0; i0 < ncol; i0 += 8) {
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-          const int it = i0 + u;
-          if (it >= ncol) break;
-          const int c = xbase + it;
-          if (!mbar_wait(&bar[(u + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-          vel_band(c + 3, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-          __syncthreads();
-          if (issuer) issue(c + 7);
-          if (c >= x0) str_band(c, u & 7, (u + 1) & 7, (u + 2) & 7, (u + 3) & 7);
-        }
+      for (int it = 0; it < ncol; it++) {
+        const int c = xbase + it;
+        if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
+        vel_band(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+        __syncthreads();
+        if (issuer) issue(c + 7);
+        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
       }
     } else {
       // velocities of column cc: update_v! with CPML, mirrors, sources
