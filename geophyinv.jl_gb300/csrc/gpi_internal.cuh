@@ -78,6 +78,7 @@ struct Plan {
   const DerivSpec *ds = nullptr;
   // tiling of the step kernel
   int TZ = 128, TY = 1, L = 128, nzb = 1, nyb = 1, nxb = 1;
+  std::vector<int> xcut;  // 2-D: x-chunk b covers columns [xcut[b], xcut[b + 1])
 
   // device memory
   void *pool = nullptr;
@@ -132,18 +133,19 @@ struct Plan {
 
   int64_t launches = 0;
   int *d_err = nullptr;  // set by a kernel whose pipeline wait gave up
-  // tiles of the 2-D step kernels: interior tiles first (straight-line
-  // kernel), then the tiles that meet a strip, a face or a source
-  int3 *d_tiles = nullptr;
-  int n_tiles_fast = 0, n_tiles_band = 0, n_tiles_edge = 0;
+  // tiles of the 2-D step kernels (z-block, first column, end column, shot),
+  // grouped by class: interior, band, x-band, edge (classify_tiles)
+  int4 *d_tiles = nullptr;
+  int n_tiles[4] = {0, 0, 0, 0};
   // 2-D z-strip CPML memory: column stride and the window of a column that
   // the general step kernel stages per ring slot
   int zsw = 0, pzw = 0;
-  // side streams for the edge and band step kernels, so that their blocks
-  // and the interior kernel's share the SMs (fork and join events on the
-  // plan stream)
-  cudaStream_t side[2] = {nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  // side streams for the edge, x-band and band step kernels, so that their
+  // blocks and the interior kernel's share the SMs (fork and join events on
+  // the plan stream)
+  static constexpr int NSIDE = 3;
+  cudaStream_t side[NSIDE] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[NSIDE] = {};
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 };
 
@@ -194,11 +196,17 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_adjoint_acoustic2d(Plan *p, int it);
-// host: classify the (z-block, x-chunk, shot) tiles of a 2-D plan; writes
-// interior tiles, then band tiles, then edge tiles; returns the tile count
-// (or -1 beyond `cap`)
-int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast,
-                   int *nband);
+// host: x partition of a 2-D grid of nx columns into m interior chunks
+// plus, when the grid is wide enough, one narrow chunk at each x edge (the
+// mirror columns there need the general code); writes nchunks + 1 cut
+// columns, returns nchunks
+int make_xcuts(int nx, int m, int *cuts);
+// host: classify the (z-block, x-chunk, shot) tiles of a 2-D plan and write
+// them grouped by class (0 interior, 1 band, 2 x-band, 3 edge, in that
+// order) with the per-class counts; returns the tile count (or -1 beyond
+// `cap`)
+int classify_tiles(const Plan &p, const int *xcut, const InjCell *cells, const int32_t *gptr, int4 *out, int cap,
+                   int count[4]);
 int aux_step(Plan *p, int it, int mode);
 // nside side streams forked from the plan stream (the plan stream itself
 // when side streams are unavailable); join_side joins them back

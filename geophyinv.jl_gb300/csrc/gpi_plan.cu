@@ -94,22 +94,23 @@ static void choose_tiling(Plan &p) {
     int per_chunk = p.nzb * p.d.nshots;
     int best = 1;
     double best_eff = 0;
-    for (int nxb = 1; nxb <= std::max(1, p.d.nx / 48); nxb++) {
-      int64_t blocks = (int64_t)nxb * per_chunk;
+    for (int m = 1; m <= std::max(1, p.d.nx / 48); m++) {
+      int64_t blocks = (int64_t)m * per_chunk;
       double waves = (double)blocks / resident;
       double eff = waves / std::ceil(waves);
-      int L = (p.d.nx + nxb - 1) / nxb;
+      int L = (p.d.nx + m - 1) / m;
       double halo = 3.0 / L;  // redundant velocity columns
       eff *= (1.0 - halo);
       if (blocks < resident / 2) eff *= (double)blocks / (resident / 2);
       if (eff > best_eff + 1e-9) {
         best_eff = eff;
-        best = nxb;
+        best = m;
       }
     }
-    p.nxb = best;
+    p.xcut.assign(best + 3, 0);
+    p.nxb = make_xcuts(p.d.nx, best, p.xcut.data());
+    p.xcut.resize(p.nxb + 1);
     p.L = (p.d.nx + best - 1) / best;
-    p.nxb = (p.d.nx + p.L - 1) / p.L;
   } else {
     p.TZ = 32;
     p.TY = 8;
@@ -291,14 +292,14 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
     bool ok = cudaEventCreateWithFlags(&p.ev_fork, cudaEventDisableTiming) == cudaSuccess;
-    for (int k = 0; k < 2; k++)
+    for (int k = 0; k < Plan::NSIDE; k++)
       ok = ok && cudaStreamCreateWithPriority(&p.side[k], cudaStreamNonBlocking, hi) == cudaSuccess &&
            cudaEventCreateWithFlags(&p.ev_join[k], cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
       // every step kernel then runs on the plan stream
       cudaGetLastError();
       if (p.ev_fork) cudaEventDestroy(p.ev_fork);
-      for (int k = 0; k < 2; k++) {
+      for (int k = 0; k < Plan::NSIDE; k++) {
         if (p.side[k]) cudaStreamDestroy(p.side[k]);
         if (p.ev_join[k]) cudaEventDestroy(p.ev_join[k]);
         p.side[k] = nullptr;
@@ -364,7 +365,7 @@ void destroy(gpi_plan *pl) {
   cudaGetDevice(&dev);
   cudaSetDevice(p.device);
   if (p.stream) cudaStreamSynchronize(p.stream);
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < Plan::NSIDE; k++) {
     if (p.side[k]) {
       cudaStreamSynchronize(p.side[k]);
       cudaStreamDestroy(p.side[k]);
@@ -706,75 +707,86 @@ static int compile_sources(Plan &p) {
 }
 
 
+int make_xcuts(int nx, int m, int *cuts) {
+  const int E = 8;  // columns of an edge chunk
+  if (nx < 4 * E + m) {
+    const int L = (nx + m - 1) / m;
+    int n = 0;
+    for (int x = 1; x <= nx; x += L) cuts[n++] = x;
+    cuts[n] = nx + 1;
+    return n;
+  }
+  const int lo = 1 + E, hi = nx + 1 - E - 1;  // interior chunks cover [lo, hi)
+  cuts[0] = 1;
+  for (int i = 0; i <= m; i++) cuts[1 + i] = lo + (int)((int64_t)(hi - lo) * i / m);
+  cuts[m + 2] = nx + 1;
+  return m + 2;
+}
+
 // Tile classes of the 2-D step kernels (src/fdtd/cpml.jl:184-211 and
 // src/fdtd/dirichlet.jl:1-79 give the affected rows and columns):
 //   0 interior: every cell it computes lies inside all update domains,
-//     outside every CPML strip and away from mirror rows/columns;
-//   1 band: columns away from the x edges and x strips, rows that may meet
-//     a z strip, a z mirror or the free surface;
-//   2 edge: everything else (x edges, x strips, source cells).
+//     outside every CPML strip, away from mirror rows/columns and sources;
+//   1 band: no x-edge or x-strip column; rows may meet a z strip, a z
+//     mirror, the free surface or a source;
+//   2 x-band: the same with x-strip columns;
+//   3 edge: x-edge columns (domain ends and mirrors).
 // A block computes velocities of rows z0..z0+TZ+2 and columns x0..x1+2 and
 // stresses of rows z0..z0+TZ-1 and columns x0..x1-1 from input columns
 // x0-3..x1+2.
-static int tile_class(const Plan &p, const InjCell *cells, const int32_t *gptr, int zb, int xb, int shot) {
+static int tile_class(const Plan &p, const InjCell *cells, const int32_t *gptr, int zb, int x0, int x1, int shot) {
   const int npml = p.d.npml, nz = p.d.nz, nx = p.d.nx;
-  const int z0 = 1 + zb * p.TZ, x0 = 1 + xb * p.L, x1 = std::min(x0 + p.L, nx + 1);
+  const int z0 = 1 + zb * p.TZ;
+  if (x0 <= 4 || x1 + 2 >= nx - 4) return 3;
+  const bool xpml = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
+  if (xpml && !(x0 > npml + 3 && x1 <= nx - 5 - npml)) return 2;
   for (int ipw = 0; ipw < p.d.npw; ipw++)
     for (int kind = 0; kind < NKIND; kind++) {
       const int gi = (ipw * p.d.nshots + shot) * NKIND + kind;
       for (int c = gptr[gi]; c < gptr[gi + 1]; c++)
         if (cells[c].col >= x0 - 3 && cells[c].col <= x1 + 3 && cells[c].row >= z0 - 1 &&
             cells[c].row <= z0 + p.TZ + 3)
-          return 2;
+          return 1;
     }
-  const bool xpml = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
-  // no x-edge column (mirrors, domain ends) and no x-strip column
-  const bool xin = x0 > 4 && x1 + 2 < nx - 4 && (!xpml || (x0 > npml + 3 && x1 <= nx - 5 - npml));
-  if (!xin) return 2;
   const bool zin = z0 >= npml + 4 && z0 + p.TZ + 2 <= nz - npml - 3;
   return zin && x0 >= npml + 4 && x1 + 2 <= nx - npml - 3 ? 0 : 1;
 }
 
-int classify_tiles(const Plan &p, const InjCell *cells, const int32_t *gptr, int3 *out, int cap, int *nfast,
-                   int *nband) {
+int classify_tiles(const Plan &p, const int *xcut, const InjCell *cells, const int32_t *gptr, int4 *out, int cap,
+                   int count[4]) {
   const int n = p.nzb * p.nxb * p.d.nshots;
   if (n > cap) return -1;
-  int cnt[3] = {0, 0, 0};
+  int cnt[4] = {0, 0, 0, 0};
   for (int pass = 0; pass < 2; pass++) {
-    int at[3] = {0, cnt[0], cnt[0] + cnt[1]};
+    int at[4] = {0, cnt[0], cnt[0] + cnt[1], cnt[0] + cnt[1] + cnt[2]};
     // shots innermost: the blocks of one (z-block, x-chunk) of every shot run
     // together and read the shared coefficient columns once from HBM, then
     // from L2
     for (int xb = 0; xb < p.nxb; xb++)
       for (int zb = 0; zb < p.nzb; zb++)
         for (int shot = 0; shot < p.d.nshots; shot++) {
-          const int k = tile_class(p, cells, gptr, zb, xb, shot);
+          const int k = tile_class(p, cells, gptr, zb, xcut[xb], xcut[xb + 1], shot);
           if (pass == 0)
             cnt[k]++;
           else
-            out[at[k]++] = make_int3(zb, xb, shot);
+            out[at[k]++] = make_int4(zb, xcut[xb], xcut[xb + 1], shot);
         }
   }
-  *nfast = cnt[0];
-  *nband = cnt[1];
+  for (int k = 0; k < 4; k++) count[k] = cnt[k];
   return n;
 }
 
 static int build_tiles(Plan &p) {
   const int n = p.nzb * p.nxb * p.d.nshots;
-  std::vector<int3> t(n);
-  int nf = 0, nb = 0;
+  std::vector<int4> t(n);
   const int32_t *gp = p.group_ptr.empty() ? nullptr : p.group_ptr.data();
   std::vector<int32_t> zero(2 * p.d.nshots * NKIND + 1, 0);
-  if (classify_tiles(p, p.h_cells.data(), gp ? gp : zero.data(), t.data(), n, &nf, &nb) < 0)
+  if (classify_tiles(p, p.xcut.data(), p.h_cells.data(), gp ? gp : zero.data(), t.data(), n, p.n_tiles) < 0)
     return fail(&p, GPI_E_INVALID, "tile list");
   if (p.d_tiles) cudaFree(p.d_tiles);
   p.d_tiles = nullptr;
-  GPI_CUDA(&p, cudaMalloc(&p.d_tiles, n * sizeof(int3)));
-  GPI_CUDA(&p, cudaMemcpy(p.d_tiles, t.data(), n * sizeof(int3), cudaMemcpyHostToDevice));
-  p.n_tiles_fast = nf;
-  p.n_tiles_band = nb;
-  p.n_tiles_edge = n - nf - nb;
+  GPI_CUDA(&p, cudaMalloc(&p.d_tiles, n * sizeof(int4)));
+  GPI_CUDA(&p, cudaMemcpy(p.d_tiles, t.data(), n * sizeof(int4), cudaMemcpyHostToDevice));
   return GPI_OK;
 }
 

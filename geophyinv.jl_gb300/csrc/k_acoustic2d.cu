@@ -31,7 +31,7 @@ struct A2Args {
   int64_t fs;
   int npml, faces, rigid;
   float dxI, dzI;
-  int L, nzb, nxb;
+  int nzb;
   const float *pA, *vxA, *vzA;
   float *pB, *vxB, *vzB;
   const float *psA[4];
@@ -44,7 +44,7 @@ struct A2Args {
   const float *amount;
   int vonly;
   int *err;
-  const int3 *tiles;  // (z-block, x-chunk, shot) per block
+  const int4 *tiles;  // (z-block, first column, end column, shot) per block
   int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
@@ -64,12 +64,13 @@ inline int a2_psi_floats(const Plan &p) {
 inline size_t a2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (A2_SLOT + psf) + 2 * 8 * A2_R4); }
 
 // MODE 0: interior tiles (no CPML, face or source: straight-line code);
-// MODE 1: tiles that meet only z-strip CPML rows or z faces (the band code
-// over every column); MODE 2: tiles with x-edge, x-strip or source columns
-// (the band code plus the general code per column).
+// MODE 1: tiles away from the x edges and x strips (the band code over every
+// column: z strips, z mirrors, sources); MODE 2: the same with x-strip
+// columns; MODE 3: tiles with x-edge columns (the band code plus the general
+// code for the edge and source columns).
 template <int MODE>
 __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Args a) {
-  constexpr bool FAST = MODE == 0, XPSI = MODE == 2;
+  constexpr bool FAST = MODE == 0, XPSI = MODE >= 2;
   constexpr int TZ = A2_TZ, R8 = A2_R8, R4 = A2_R4, SLOT = A2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
@@ -80,12 +81,11 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
   __shared__ int s_rng[3][2];
   __shared__ int s_err;
   const int t = threadIdx.x;
-  const int3 tile = a.tiles[blockIdx.x];
-  const int zb = tile.x, xb = tile.y, shot = tile.z;
-  const int z0 = 1 + zb * TZ, x0 = 1 + xb * a.L;
-  const int x1 = min(x0 + a.L, a.nx + 1);
+  const int4 tile = a.tiles[blockIdx.x];
+  const int zb = tile.x, shot = tile.w;
+  const int z0 = 1 + zb * TZ, x0 = tile.y, x1 = tile.z;
   const int xbase = x0 - 3, xlast = x1 + 2;
-  const bool lastx = xb == a.nxb - 1, lastz = zb == a.nzb - 1;
+  const bool lastx = x1 == a.nx + 1, lastz = zb == a.nzb - 1;
   const int nz = a.nz, nx = a.nx, npml = a.npml, NZP = a.NZP;
   const int64_t so = (int64_t)shot * a.fs;
   const bool xlo = a.faces & GPI_XMIN, xhi = a.faces & GPI_XMAX, zlo = a.faces & GPI_ZMIN, zhi = a.faces & GPI_ZMAX;
@@ -305,7 +305,8 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
     // pass; rows outside an update domain keep their value, CPML terms where
     // a strip is met (psi staged in the ring slot of the column)
     // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
-    auto vel_band = [&](int cc, int s3, int s2, int s1, int s0) {
+    // (cells of the column's vx / vz sources in [ib0, ie0) / [ib1, ie1))
+    auto vel_band = [&](int cc, int s3, int s2, int s1, int s0, int ib0, int ie0, int ib1, int ie1) {
       const int k = kqc, kk = kqc + 4, s = s0;
       const float *pc = ring + s * SL, *v0 = pc + R8;
       const float *p3 = ring + s3 * SL, *p2 = ring + s2 * SL, *p1s = ring + s1 * SL;
@@ -322,11 +323,14 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
         if (j0 >= 0) Dx = cpml_xs(Dx, 0, j0, PXs(0, s)[q], vxr, psB(0) + XS(j0, q), ownx);
       }
       float vz = vzb ? v0[R4 + k] + v0[3 * R4 + k] * Dz : v0[R4 + k];
-      const float vx = vxr ? v0[k] + v0[2 * R4 + k] * Dx : v0[k];
+      float vx = vxr ? v0[k] + v0[2 * R4 + k] * Dx : v0[k];
       if (gany) {
         const float g = __shfl_sync(0xffffffffu, vz, glane);
         if (gsrc) vz = gok ? -g : -vz_any(gsrc, cc);
       }
+      // add_velocity_source! (after the mirrors took their values)
+      if (ib0 < ie0) inject(a.cells, a.amount, ib0, ie0, q, vx);
+      if (ib1 < ie1) inject(a.cells, a.amount, ib1, ie1, q, vz);
       if (vact) svz[s * R4 + k] = vz;
       if (vact && kq < TZ) svx[s * R4 + k] = vx;
       const int64_t o = so + S(q, cc);
@@ -335,7 +339,8 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
     };
     // pressure of column c from velocity slots s0..s3 = columns c..c+3;
     // halo lanes recompute the last row and store nothing
-    auto str_band = [&](int c, int s0, int s1, int s2, int s3) {
+    // (cells of the column's pressure sources in [bs, es))
+    auto str_band = [&](int c, int s0, int s1, int s2, int s3, int bs, int es) {
       const int k = t < TZ ? t : TZ - 1, rk = z0 + k;
       const float *pc = ring + s0 * SL;
       float Dx = st4(svx[s0 * R4 + k], svx[s1 * R4 + k], svx[s2 * R4 + k], svx[s3 * R4 + k]) * a.dxI;
@@ -346,19 +351,24 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
         if (j2 >= 0) Dx = cpml_xs(Dx, 2, j2, PXs(1, s0)[rk], srow, psB(2) + XS(j2, rk), true);
       }
       if (wzs) Dz = cpml_zs(Dz, cr3, PZs(1, s0)[jr3c], jr3v >= 0, psB(3) + ZS(c, jr3c), true);
-      const float pn = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+      float pn = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+      if (bs < es) inject(a.cells, a.amount, bs, es, r, pn);  // add_stress_source!
       if (srow) a.pB[so + S(r, c)] = pn;
     };
-    if constexpr (MODE == 1) {
+    if constexpr (MODE == 1 || MODE == 2) {
       // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
       const int ncol = x1 - xbase;
       for (int it = 0; it < ncol; it++) {
-        const int c = xbase + it;
+        const int c = xbase + it, cc = c + 3;
+        int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+        cvx.range(a.cells, cc, ib0, ie0);
+        cvz.range(a.cells, cc, ib1, ie1);
+        if (c >= x0) cst.range(a.cells, c, bs, es);
         if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-        vel_band(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+        vel_band(cc, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, ib0, ie0, ib1, ie1);
         __syncthreads();
         if (issuer) issue(c + 7);
-        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, bs, es);
       }
     } else {
       float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)
@@ -446,14 +456,14 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
         if (gv)
           vel_edge(cc, ib0, ie0, ib1, ie1);
         else
-          vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc));
+          vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc), ib0, ie0, ib1, ie1);
         __syncthreads();
         if (issuer) issue(c + 7);
         if (c >= x0) {
           if (gs)
             str_edge(c, bs, es);
           else
-            str_band(c, slot(c), slot(c + 1), slot(c + 2), slot(c + 3));
+            str_band(c, slot(c), slot(c + 1), slot(c + 2), slot(c + 3), bs, es);
         }
       }
     }
@@ -472,7 +482,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
 int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   if (mode == GPI_ADJOINT && !vonly) return step_adjoint_acoustic2d(p, it);
   (void)ipw_mask;
-  static size_t attr[3][64] = {};
+  static size_t attr[4][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return fail(p, GPI_E_UNSUPPORTED, "device index too large");
@@ -486,9 +496,7 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.rigid = p->d.rigid_faces;
   a.dxI = (float)(1.0 / (p->d.dx * 24.0));
   a.dzI = (float)(1.0 / (p->d.dz * 24.0));
-  a.L = p->L;
   a.nzb = p->nzb;
-  a.nxb = p->nxb;
   const int A = p->cur[0], B = A ^ 1;
   a.pA = p->state[A][0][GPI_P];
   a.vxA = p->state[A][0][GPI_VX];
@@ -515,11 +523,11 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.pzw = p->pzw;
   // shared memory per block: the ring with the CPML memory each mode stages
   const bool zf = p->d.pml_faces & (GPI_ZMIN | GPI_ZMAX);
-  const int psf[3] = {0, zf ? 2 * p->pzw : 0, a2_psi_floats(*p)};
-  size_t smem[3];
-  for (int m = 0; m < 3; m++) smem[m] = m == 0 ? A2_SMEM : a2_smem_general(psf[m]);
-  void (*const fn[3])(A2Args) = {k_a2<0>, k_a2<1>, k_a2<2>};
-  for (int m = 0; m < 3; m++)
+  const int psf[4] = {0, zf ? 2 * p->pzw : 0, a2_psi_floats(*p), a2_psi_floats(*p)};
+  size_t smem[4];
+  for (int m = 0; m < 4; m++) smem[m] = m == 0 ? A2_SMEM : a2_smem_general(psf[m]);
+  void (*const fn[4])(A2Args) = {k_a2<0>, k_a2<1>, k_a2<2>, k_a2<3>};
+  for (int m = 0; m < 4; m++)
     if (attr[m][dev] < smem[m]) {
       GPI_CUDA(p, cudaFuncSetAttribute(fn[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[m]));
       attr[m][dev] = smem[m];
@@ -532,19 +540,22 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
     fn[m]<<<n, A2_THREADS, smem[m], st>>>(g);
     p->launches++;
   };
-  const int nf = p->n_tiles_fast, nb = p->n_tiles_band, ne = p->n_tiles_edge;
+  const int *n = p->n_tiles;
+  const int ntot = n[0] + n[1] + n[2] + n[3];
   if (vonly) {
     // the velocity-only half step runs every tile on the general code
-    launch(2, 0, nf + nb + ne, p->stream);
+    launch(3, 0, ntot, p->stream);
   } else {
-    // edge and band blocks (longer) go first, on their own streams, so that
-    // interior blocks fill the SMs around them and their tails
-    const int nside = ((nf > 0) + (nb > 0) + (ne > 0)) > 1 ? 2 : 0;
-    cudaStream_t st[2] = {p->stream, p->stream};
+    // edge, x-band and band blocks (longer) go first, on their own streams,
+    // so that interior blocks fill the SMs around them and their tails
+    const int groups = (n[0] > 0) + (n[1] > 0) + (n[2] > 0) + (n[3] > 0);
+    const int nside = groups > 1 ? Plan::NSIDE : 0;
+    cudaStream_t st[Plan::NSIDE] = {p->stream, p->stream, p->stream};
     if (int rc = fork_side(p, nside, st)) return rc;
-    launch(2, nf + nb, ne, st[0]);
-    launch(1, nf, nb, st[1]);
-    launch(0, 0, nf, p->stream);
+    launch(3, n[0] + n[1] + n[2], n[3], st[0]);
+    launch(2, n[0] + n[1], n[2], st[1]);
+    launch(1, n[0], n[1], st[2]);
+    launch(0, 0, n[0], p->stream);
     GPI_CUDA(p, cudaGetLastError());
     if (int rc = join_side(p, nside)) return rc;
   }

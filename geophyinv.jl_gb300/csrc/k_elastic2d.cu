@@ -33,7 +33,7 @@ struct E2Args {
   int64_t fs;
   int npml, faces, rigid, free;
   float dxI, dzI;
-  int L, nzb, nxb;
+  int nzb;
   const float *txxA, *tzzA, *txzA, *vxA, *vzA;
   float *txxB, *tzzB, *txzB, *vxB, *vzB;
   const float *psA[8];
@@ -46,7 +46,7 @@ struct E2Args {
   const float *amount;
   int vonly;
   int *err;  // set when a pipeline wait gives up
-  const int3 *tiles;  // (z-block, x-chunk, shot) per block
+  const int4 *tiles;  // (z-block, first column, end column, shot) per block
   int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
@@ -67,12 +67,13 @@ inline int e2_psi_floats(const Plan &p) {
 inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (E2_SLOT + psf) + 2 * 8 * E2_R4); }
 
 // MODE 0: interior tiles (no CPML, face or source: straight-line code);
-// MODE 1: tiles that meet only z-strip CPML rows or z faces (the band code
-// over every column); MODE 2: tiles with x-edge, x-strip or source columns
-// (the band code plus the general code per column).
+// MODE 1: tiles away from the x edges and x strips (the band code over every
+// column: z strips, z mirrors, the free surface, sources); MODE 2: the same
+// with x-strip columns; MODE 3: tiles with x-edge columns (the band code plus
+// the general code for the edge and source columns).
 template <int MODE>
-__global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Args a) {
-  constexpr bool FAST = MODE == 0, XPSI = MODE == 2;
+__global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Args a) {
+  constexpr bool FAST = MODE == 0, XPSI = MODE >= 2;
   constexpr int TZ = E2_TZ, R8 = E2_R8, R4 = E2_R4, SLOT = E2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // one mbarrier per ring slot
@@ -83,12 +84,11 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
   __shared__ int s_rng[3][2];
   __shared__ int s_err;
   const int t = threadIdx.x;
-  const int3 tile = a.tiles[blockIdx.x];
-  const int zb = tile.x, xb = tile.y, shot = tile.z;
-  const int z0 = 1 + zb * TZ, x0 = 1 + xb * a.L;
-  const int x1 = min(x0 + a.L, a.nx + 1);
+  const int4 tile = a.tiles[blockIdx.x];
+  const int zb = tile.x, shot = tile.w;
+  const int z0 = 1 + zb * TZ, x0 = tile.y, x1 = tile.z;
   const int xbase = x0 - 3, xlast = x1 + 2;  // input columns of this block
-  const bool lastx = xb == a.nxb - 1, lastz = zb == a.nzb - 1;
+  const bool lastx = x1 == a.nx + 1, lastz = zb == a.nzb - 1;
   const int nz = a.nz, nx = a.nx, npml = a.npml, NZP = a.NZP;
   const int64_t so = (int64_t)shot * a.fs;
   const bool xlo = a.faces & GPI_XMIN, xhi = a.faces & GPI_XMAX, zlo = a.faces & GPI_ZMIN, zhi = a.faces & GPI_ZMAX;
@@ -381,7 +381,8 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
     // pass; rows outside an update domain keep their value, CPML terms where
     // a strip is met (psi staged in the ring slot of the column)
     // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
-    auto vel_band = [&](int cc, int s3, int s2, int s1, int s0) {
+    // (cells of the column's vx / vz sources in [ib0, ie0) / [ib1, ie1))
+    auto vel_band = [&](int cc, int s3, int s2, int s1, int s0, int ib0, int ie0, int ib1, int ie1) {
       const int k = kqc, kk = kqc + 4, s = s0;
       const bool ownc = cc < x1;
       const bool ownx = ownc && ownr && q <= nz, ownz = ownc && ownr && q <= nz + 3;
@@ -403,12 +404,15 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
         Dz = cpml_zs(Dz, cq3, PZs(1, s)[jq3c], jq3v >= 0, psB(3) + ZS(cc, jq3c), ownx);
         Dz2 = cpml_zs(Dz2, cq2, PZs(0, s)[jq2c], jq2v >= 0, psB(2) + ZS(cc, jq2c), ownz);
       }
-      const float vx = vxb ? v0[k] - v0[2 * R4 + k] * (Dx + Dz) : v0[k];
+      float vx = vxb ? v0[k] - v0[2 * R4 + k] * (Dx + Dz) : v0[k];
       float vz = vzb ? v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2) : v0[R4 + k];
       if (gany) {
         const float g = __shfl_sync(0xffffffffu, vz, glane);
         if (gsrc) vz = gok ? -g : -vz_any(gsrc, cc);
       }
+      // add_velocity_source! (after the mirrors took their values)
+      if (ib0 < ie0) inject(a.cells, a.amount, ib0, ie0, q, vx);
+      if (ib1 < ie1) inject(a.cells, a.amount, ib1, ie1, q, vz);
       if (vact) {
         svx[s * R4 + k] = vx;
         svz[s * R4 + k] = vz;
@@ -419,7 +423,8 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
     };
     // stresses of column c from velocity slots s0..s3 = columns c..c+3;
     // halo lanes recompute the last row and store nothing
-    auto str_band = [&](int c, int s0, int s1, int s2, int s3) {
+    // (cells of the column's stress sources in [bs, es))
+    auto str_band = [&](int c, int s0, int s1, int s2, int s3, int bs, int es) {
       const int k = t < TZ ? t : TZ - 1, rk = z0 + k;
       const float *u0 = svx + s0 * R4, *u1 = svx + s1 * R4, *u2 = svx + s2 * R4, *u3 = svx + s3 * R4;
       const float *w0 = svz + s0 * R4, *w1 = svz + s1 * R4, *w2 = svz + s2 * R4, *w3 = svz + s3 * R4;
@@ -438,7 +443,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
         dvxdz = cpml_zs(dvxdz, cr6, PZs(3, s0)[jr6c], jr6v >= 0, psB(6) + ZS(c, jr6c), true);
       }
       const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
-      const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
+      float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
       float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
       float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
       if (fsblk) {
@@ -449,6 +454,11 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
           txz = 0.f;
         }
       }
+      // add_stress_source!: txx += pv dtM; tzz += pv dtM
+      if (bs < es) {
+        inject(a.cells, a.amount, bs, es, r, txx);
+        inject(a.cells, a.amount, bs, es, r, tzz);
+      }
       if (srow) {
         const int64_t o = so + S(r, c);
         a.txxB[o] = txx;
@@ -456,16 +466,20 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
         if (xzrow) a.txzB[o] = txz;
       }
     };
-    if constexpr (MODE == 1) {
+    if constexpr (MODE == 1 || MODE == 2) {
       // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
       const int ncol = x1 - xbase;
       for (int it = 0; it < ncol; it++) {
-        const int c = xbase + it;
+        const int c = xbase + it, cc = c + 3;
+        int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+        cvx.range(a.cells, cc, ib0, ie0);
+        cvz.range(a.cells, cc, ib1, ie1);
+        if (c >= x0) cst.range(a.cells, c, bs, es);
         if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-        vel_band(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+        vel_band(cc, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, ib0, ie0, ib1, ie1);
         __syncthreads();
         if (issuer) issue(c + 7);
-        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, bs, es);
       }
     } else {
       // velocities of column cc: update_v! with CPML, mirrors, sources
@@ -584,14 +598,14 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 2 ? 3 : 4) k_e2(const E2Ar
         if (gv)
           vel_edge(cc, ib0, ie0, ib1, ie1);
         else
-          vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc));
+          vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc), ib0, ie0, ib1, ie1);
         __syncthreads();
         if (issuer) issue(c + 7);
         if (c >= x0) {
           if (gs)
             str_edge(c, bs, es);
           else
-            str_band(c, slot(c), slot(c + 1), slot(c + 2), slot(c + 3));
+            str_band(c, slot(c), slot(c + 1), slot(c + 2), slot(c + 3), bs, es);
         }
       }
     }
@@ -613,7 +627,7 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   (void)ipw_mask;
   (void)it;
   (void)mode;
-  static size_t attr[3][64] = {};
+  static size_t attr[4][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return fail(p, GPI_E_UNSUPPORTED, "device index too large");
@@ -628,9 +642,7 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.free = p->d.free_faces;
   a.dxI = (float)(1.0 / (p->d.dx * 24.0));
   a.dzI = (float)(1.0 / (p->d.dz * 24.0));
-  a.L = p->L;
   a.nzb = p->nzb;
-  a.nxb = p->nxb;
   const int A = p->cur[0], B = A ^ 1;
   a.txxA = p->state[A][0][GPI_TAUXX];
   a.tzzA = p->state[A][0][GPI_TAUZZ];
@@ -663,11 +675,11 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.pzw = p->pzw;
   // shared memory per block: the ring with the CPML memory each mode stages
   const bool zf = p->d.pml_faces & (GPI_ZMIN | GPI_ZMAX);
-  const int psf[3] = {0, zf ? 4 * p->pzw : 0, e2_psi_floats(*p)};
-  size_t smem[3];
-  for (int m = 0; m < 3; m++) smem[m] = m == 0 ? E2_SMEM : e2_smem_general(psf[m]);
-  void (*const fn[3])(E2Args) = {k_e2<0>, k_e2<1>, k_e2<2>};
-  for (int m = 0; m < 3; m++)
+  const int psf[4] = {0, zf ? 4 * p->pzw : 0, e2_psi_floats(*p), e2_psi_floats(*p)};
+  size_t smem[4];
+  for (int m = 0; m < 4; m++) smem[m] = m == 0 ? E2_SMEM : e2_smem_general(psf[m]);
+  void (*const fn[4])(E2Args) = {k_e2<0>, k_e2<1>, k_e2<2>, k_e2<3>};
+  for (int m = 0; m < 4; m++)
     if (attr[m][dev] < smem[m]) {
       GPI_CUDA(p, cudaFuncSetAttribute(fn[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[m]));
       attr[m][dev] = smem[m];
@@ -680,19 +692,22 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
     fn[m]<<<n, E2_THREADS, smem[m], st>>>(g);
     p->launches++;
   };
-  const int nf = p->n_tiles_fast, nb = p->n_tiles_band, ne = p->n_tiles_edge;
+  const int *n = p->n_tiles;
+  const int ntot = n[0] + n[1] + n[2] + n[3];
   if (vonly) {
     // the velocity-only half step runs every tile on the general code
-    launch(2, 0, nf + nb + ne, p->stream);
+    launch(3, 0, ntot, p->stream);
   } else {
-    // edge and band blocks (longer) go first, on their own streams, so that
-    // interior blocks fill the SMs around them and their tails
-    const int nside = ((nf > 0) + (nb > 0) + (ne > 0)) > 1 ? 2 : 0;
-    cudaStream_t st[2] = {p->stream, p->stream};
+    // edge, x-band and band blocks (longer) go first, on their own streams,
+    // so that interior blocks fill the SMs around them and their tails
+    const int groups = (n[0] > 0) + (n[1] > 0) + (n[2] > 0) + (n[3] > 0);
+    const int nside = groups > 1 ? Plan::NSIDE : 0;
+    cudaStream_t st[Plan::NSIDE] = {p->stream, p->stream, p->stream};
     if (int rc = fork_side(p, nside, st)) return rc;
-    launch(2, nf + nb, ne, st[0]);
-    launch(1, nf, nb, st[1]);
-    launch(0, 0, nf, p->stream);
+    launch(3, n[0] + n[1] + n[2], n[3], st[0]);
+    launch(2, n[0] + n[1], n[2], st[1]);
+    launch(1, n[0], n[1], st[2]);
+    launch(0, 0, n[0], p->stream);
     GPI_CUDA(p, cudaGetLastError());
     if (int rc = join_side(p, nside)) return rc;
   }

@@ -21,6 +21,7 @@
 // device looks up the device address of the array (cudaGetSymbolAddress)
 // with that device current; make that first call before any stream
 // capture begins.
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -48,8 +49,9 @@ static int32_t h_pj[kMaxPairs];
 static float h_pw[kMaxPairs];
 static int32_t h_gptr[2 * NKIND + 1];
 static float *h_wavptr[1];
-static constexpr int kMaxTiles = 1 << 16;
-static int3 h_tiles[kMaxTiles];
+static constexpr int kMaxTiles = 1 << 16, kMaxCuts = 1 << 13;
+static int4 h_tiles[kMaxTiles];
+static int h_xcut[kMaxCuts];
 static Plan g_plan;  // descriptor filled per call; its pointers point into the scratch
 
 static int nfail(int code, const char *msg) { return fail(nullptr, code, msg); }
@@ -113,7 +115,11 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
   P.TZ = TZ2;
   P.nzb = (d.nz + TZ2 - 1) / TZ2;
   P.L = 128;
-  P.nxb = (d.nx + P.L - 1) / P.L;
+  {
+    const int m = std::max(1, (d.nx - 16 + P.L - 1) / P.L);
+    if (m + 3 > kMaxCuts) return nfail(GPI_E_INVALID, "grid too large for the no-alloc tile table");
+    P.nxb = make_xcuts(d.nx, m, h_xcut);
+  }
   P.nyb = 1;
   P.NZP = (int)(((int64_t)P.nzb * TZ2 + 2 * ZOFF + 4 + 31) / 32 * 32);
   P.NXP = d.nx + 3 + 2 * XOFF + 4;
@@ -256,13 +262,9 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     P.d_group_ptr = (int32_t *)carve(2 * NKIND + 1);
     P.d_wav = (float **)carve(2);
     h_wavptr[0] = (float *)wavelets;
-    int nf = 0, nb = 0;
-    const int ntile = classify_tiles(P, h_cells, h_gptr, h_tiles, kMaxTiles, &nf, &nb);
+    const int ntile = classify_tiles(P, h_xcut, h_cells, h_gptr, h_tiles, kMaxTiles, P.n_tiles);
     if (ntile < 0) return nfail(GPI_E_INVALID, "grid too large for the no-alloc tile table");
-    P.n_tiles_fast = nf;
-    P.n_tiles_band = nb;
-    P.n_tiles_edge = ntile - nf - nb;
-    P.d_tiles = (int3 *)carve((int64_t)(sizeof(int3) * ntile + 3) / 4);
+    P.d_tiles = (int4 *)carve((int64_t)(sizeof(int4) * ntile + 3) / 4);
     if (!room) return nfail(GPI_E_INVALID, "problem exceeds the 64 MiB no-alloc scratch");
     cudaStream_t s = P.stream;
     cudaMemcpyAsync(P.d_cells, h_cells, sizeof(InjCell) * m, cudaMemcpyHostToDevice, s);
@@ -270,7 +272,7 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     cudaMemcpyAsync(P.d_pair_w, h_pw, sizeof(float) * np, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.d_group_ptr, h_gptr, sizeof(h_gptr), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.d_wav, h_wavptr, sizeof(h_wavptr), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.d_tiles, h_tiles, sizeof(int3) * ntile, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.d_tiles, h_tiles, sizeof(int4) * ntile, cudaMemcpyHostToDevice, s);
   }
   if (!room) return nfail(GPI_E_INVALID, "problem exceeds the 64 MiB no-alloc scratch");
   cudaStream_t s = P.stream;
