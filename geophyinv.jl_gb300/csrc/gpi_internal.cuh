@@ -93,6 +93,7 @@ struct Plan {
   float *pml = nullptr;  // [nder][3][2*npml]
   float *grad[2] = {};   // per-shot gradients [shot][storage] (adjoint)
   float *bstore = nullptr;  // boundary store (forward_save -> adjoint)
+  float *bprev = nullptr;   // adjoint: the strip values the forcing replaced, this step
   int64_t bstep = 0;         // floats per step per shot
   int64_t bsnap = 0;         // floats of the final snapshots per shot
   int cur[2] = {0, 0};       // buffer holding the current state, per wavefield
@@ -196,6 +197,7 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_adjoint_acoustic2d(Plan *p, int it);
+int step_a2_wavefield(Plan *p, int ipw, int vonly);
 // host: x partition of a 2-D grid of nx columns into m interior chunks
 // plus, when the grid is wide enough, one narrow chunk at each x edge (the
 // mirror columns there need the general code); writes nchunks + 1 cut

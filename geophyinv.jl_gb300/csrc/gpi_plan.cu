@@ -251,6 +251,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
     }
     p.bsnap += p.fstride * (d.ndim == 3 ? 3 : 2);
     allocs.push_back({&p.bstore, (p.bstep * d.nt + p.bsnap) * d.nshots});
+    allocs.push_back({&p.bprev, p.bstep * d.nshots});
   }
   size_t total = 0;
   for (auto &a : allocs) total += (size_t)round_up(a.second, 64) * sizeof(float);
@@ -586,6 +587,9 @@ static int compile_sources(Plan &p) {
         const Plan::Src &src = p.src[ipw][s][f];
         if (src.ns <= 0) continue;
         const int kind = kind_of(f);
+        // the adjoint wavefield takes velocity sources only: add_stress_source!
+        // injects into wavefield 1 alone (src/fdtd/source.jl:61-77)
+        if (ipw == 1 && kind == 3) continue;
         // spray matrix
         const std::vector<int64_t> *cp, *rows = nullptr;
         const std::vector<float> *w;
@@ -833,7 +837,9 @@ int run(Plan &p, int mode) {
   if (!rc && p.d.ndim == 2 && !p.d_tiles) rc = build_tiles(p);
   if (!rc) rc = zero_state(p);
   p.launches = 0;
-  if (!rc && p.rec_pool) rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
+  // an adjoint run records nothing and keeps the records of the forward run
+  if (!rc && p.rec_pool && mode != GPI_ADJOINT)
+    rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
   if (!rc && mode == GPI_ADJOINT) {
     for (int i = 0; i < 2; i++)
       if (p.grad[i]) rc = cudaMemsetAsync(p.grad[i], 0, p.fstride * p.d.nshots * sizeof(float), p.stream) ? GPI_E_CUDA : rc;
@@ -843,7 +849,8 @@ int run(Plan &p, int mode) {
   const int mask = mode == GPI_ADJOINT ? 3 : 1;
   for (int it = 1; !rc && it <= p.d.nt; it++) {
     rc = aux_step(&p, it, mode);
-    if (!rc && mode == GPI_ADJOINT) rc = boundary_io(&p, p.d.nt - it + 1, 1);
+    // boundary_force! (the replaced values are kept for the gradient)
+    if (!rc && mode == GPI_ADJOINT) rc = boundary_io(&p, p.d.nt - it + 1, 2);
     if (!rc) rc = step(p, mask, it, mode, 0);
     if (!rc && mode == GPI_FORWARD_SAVE) rc = boundary_io(&p, it, 0);
   }

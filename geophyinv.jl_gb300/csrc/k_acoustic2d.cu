@@ -482,6 +482,12 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
 int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   if (mode == GPI_ADJOINT && !vonly) return step_adjoint_acoustic2d(p, it);
   (void)ipw_mask;
+  (void)it;
+  return step_a2_wavefield(p, 0, vonly);
+}
+
+// one time step of wavefield ipw (0 the modelled, 1 the adjoint wavefield)
+int step_a2_wavefield(Plan *p, int ipw, int vonly) {
   static size_t attr[4][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -497,16 +503,16 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.dxI = (float)(1.0 / (p->d.dx * 24.0));
   a.dzI = (float)(1.0 / (p->d.dz * 24.0));
   a.nzb = p->nzb;
-  const int A = p->cur[0], B = A ^ 1;
-  a.pA = p->state[A][0][GPI_P];
-  a.vxA = p->state[A][0][GPI_VX];
-  a.vzA = p->state[A][0][GPI_VZ];
-  a.pB = p->state[B][0][GPI_P];
-  a.vxB = p->state[B][0][GPI_VX];
-  a.vzB = p->state[B][0][GPI_VZ];
+  const int A = p->cur[ipw], B = A ^ 1;
+  a.pA = p->state[A][ipw][GPI_P];
+  a.vxA = p->state[A][ipw][GPI_VX];
+  a.vzA = p->state[A][ipw][GPI_VZ];
+  a.pB = p->state[B][ipw][GPI_P];
+  a.vxB = p->state[B][ipw][GPI_VX];
+  a.vzB = p->state[B][ipw][GPI_VZ];
   for (int q = 0; q < 4; q++) {
-    a.psA[q] = p->psi[A][0][q];
-    a.psB[q] = p->psi[B][0][q];
+    a.psA[q] = p->psi[A][ipw][q];
+    a.psB[q] = p->psi[B][ipw][q];
     a.pss[q] = p->psi_stride[q];
   }
   a.cx = p->coef[0];
@@ -514,7 +520,7 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.dtK = p->coef[2];
   a.pml = p->pml;
   a.cells = p->d_cells;
-  a.gptr = p->d_group_ptr;
+  a.gptr = p->d_group_ptr + (int64_t)ipw * p->d.nshots * NKIND;  // this wavefield's cell groups
   a.amount = p->d_amount;
   a.vonly = vonly;
   a.err = p->d_err;
@@ -560,7 +566,7 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
     if (int rc = join_side(p, nside)) return rc;
   }
   GPI_CUDA(p, cudaGetLastError());
-  p->cur[0] ^= 1;
+  p->cur[ipw] ^= 1;
   return GPI_OK;
 }
 

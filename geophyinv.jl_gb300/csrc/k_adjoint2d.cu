@@ -1,10 +1,121 @@
-// k_adjoint2d.cu -- placeholder of the fused adjoint step (built next).
-#include "gpi_internal.cuh"
+// k_adjoint2d.cu -- adjoint time step and imaging condition, 2-D acoustic.
+//
+// One adjoint step (mod_x_proc! with npw = 2, src/fdtd/propagate.jl:138-261):
+//   save_tp! of both wavefields (src/fdtd/save_tp.jl:5-14)       -- implicit:
+//       the step reads buffer A and writes buffer B, A is the "tp" copy
+//   boundary_force! on wavefield 1 (src/fdtd/boundary.jl:113-170) -- done by
+//       boundary_io before this call; the replaced strip values are kept in
+//       Plan::bprev, since the imaging condition uses the unforced field
+//   update of wavefield 1 (time reversal) and of wavefield 2 (adjoint, fed
+//       through the receiver interpolation) with the fused step kernel
+//   compute_gradient! (src/fdtd/gradient.jl:27-56):
+//       g_invK += p2_prev (p1_prev - p1) dtI                 (every p cell)
+//       bx = vx2_prev (vx1 - vx1_prev) dtI, bz likewise      (velocity grids)
+//       g_rho[iz+h, ix+h] -= (bx[iz+h, ix] + bx[iz+h, ix+1]) / 2
+//                          + (bz[iz, ix+h] + bz[iz+1, ix+h]) / 2,
+//       iz in 1..nz-2h, ix in 1..nx-2h (the averages sit one cell off the
+//       stencil centre, as in the reference)
+// The imaging condition is one streaming pass over both wavefields' old and
+// new states (k_grad_a2); the velocity terms are recomputed at the two
+// neighbours each g_rho cell needs, in the reference's operation order.
+#include "k_stencil.cuh"
 
 namespace gpi {
 
-int step_adjoint_acoustic2d(Plan *p, int) {
-  return fail(p, GPI_E_UNSUPPORTED, "the adjoint step is not part of this build");
+struct GradArgs {
+  int nz, nx, NZP;
+  int64_t fs;
+  int nshots;
+  const float *p1A, *p1B, *p2A;
+  const float *vx1A, *vx1B, *vx2A;
+  const float *vz1A, *vz1B, *vz2A;
+  const float *prev;  // strip values before boundary_force! (x strips, then z strips)
+  int64_t pstride;    // floats per shot in prev
+  int nb, npx, npz;   // strip width and PML offsets of the strips
+  float *gK, *gR;
+  float dtI;
+};
+
+// position of p cell (r, c) in the strip block of boundary_save! (x strips
+// nz x 2nb, then z strips 2nb x nx), -1 when the cell is in no strip
+__device__ __forceinline__ int64_t strip_index(const GradArgs &a, int r, int c) {
+  const int nb = a.nb;
+  int j = -1;
+  if (c > a.npx && c <= a.npx + nb)
+    j = c - a.npx - 1;
+  else if (c > a.nx - a.npx - nb && c <= a.nx - a.npx)
+    j = nb + c - (a.nx - a.npx - nb) - 1;
+  if (j >= 0) return (int64_t)(r - 1) + (int64_t)a.nz * j;
+  if (r > a.npz && r <= a.npz + nb)
+    j = r - a.npz - 1;
+  else if (r > a.nz - a.npz - nb && r <= a.nz - a.npz)
+    j = nb + r - (a.nz - a.npz - nb) - 1;
+  if (j >= 0) return (int64_t)a.nz * 2 * nb + j + (int64_t)2 * nb * (c - 1);
+  return -1;
+}
+
+__global__ void __launch_bounds__(256) k_grad_a2(const GradArgs a) {
+  const int64_t per = (int64_t)a.nz * a.nx;
+  const int64_t total = per * a.nshots;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int shot = (int)(i / per);
+    const int64_t k = i - shot * per;
+    const int r = (int)(k % a.nz) + 1, c = (int)(k / a.nz) + 1;
+    const int64_t so = shot * a.fs;
+    auto S = [&](int rr, int cc) -> int64_t { return so + (int64_t)(cc + XOFF - 1) * a.NZP + (rr + ZOFF - 1); };
+    const int64_t o = S(r, c);
+    // compute_gmodKI!
+    float p1p = a.p1A[o];
+    const int64_t sidx = strip_index(a, r, c);
+    if (sidx >= 0) p1p = a.prev[shot * a.pstride + sidx];
+    a.gK[o] = a.gK[o] + a.p2A[o] * (p1p - a.p1B[o]) * a.dtI;
+    // compute_gmodrho! + combine_gmodrho!
+    if (r >= 4 && r <= a.nz - 3 && c >= 4 && c <= a.nx - 3) {
+      const int64_t x1 = S(r, c - 3), x2 = S(r, c - 2), z1 = S(r - 3, c), z2 = S(r - 2, c);
+      const float bx1 = a.vx2A[x1] * (a.vx1B[x1] - a.vx1A[x1]) * a.dtI;
+      const float bx2 = a.vx2A[x2] * (a.vx1B[x2] - a.vx1A[x2]) * a.dtI;
+      const float bz1 = a.vz2A[z1] * (a.vz1B[z1] - a.vz1A[z1]) * a.dtI;
+      const float bz2 = a.vz2A[z2] * (a.vz1B[z2] - a.vz1A[z2]) * a.dtI;
+      a.gR[o] = a.gR[o] - (bx1 + bx2) * 0.5f - (bz1 + bz2) * 0.5f;
+    }
+  }
+}
+
+int step_adjoint_acoustic2d(Plan *p, int it) {
+  (void)it;
+  if (!p->grad[0] || !p->grad[1] || !p->bprev) return fail(p, GPI_E_STATE, "adjoint step without gradient buffers");
+  const int A1 = p->cur[0], B1 = A1 ^ 1, A2 = p->cur[1];
+  GradArgs g;
+  g.nz = p->d.nz;
+  g.nx = p->d.nx;
+  g.NZP = p->NZP;
+  g.fs = p->fstride;
+  g.nshots = p->d.nshots;
+  g.p1A = p->state[A1][0][GPI_P];
+  g.p1B = p->state[B1][0][GPI_P];
+  g.p2A = p->state[A2][1][GPI_P];
+  g.vx1A = p->state[A1][0][GPI_VX];
+  g.vx1B = p->state[B1][0][GPI_VX];
+  g.vx2A = p->state[A2][1][GPI_VX];
+  g.vz1A = p->state[A1][0][GPI_VZ];
+  g.vz1B = p->state[B1][0][GPI_VZ];
+  g.vz2A = p->state[A2][1][GPI_VZ];
+  g.prev = p->bprev;
+  g.pstride = p->bstep;
+  g.nb = p->d.nbound;
+  g.npx = (p->d.pml_faces & GPI_XMIN) ? p->d.npml : 0;
+  g.npz = (p->d.pml_faces & GPI_ZMIN) ? p->d.npml : 0;
+  g.gK = p->grad[0];
+  g.gR = p->grad[1];
+  g.dtI = (float)(1.0 / p->d.dt);
+  // wavefield 1 (time reversal, boundary already forced), then wavefield 2
+  int rc = step_a2_wavefield(p, 0, 0);
+  if (!rc) rc = step_a2_wavefield(p, 1, 0);
+  if (rc) return rc;
+  k_grad_a2<<<152 * 16, 256, 0, p->stream>>>(g);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
 }
 
 }  // namespace gpi

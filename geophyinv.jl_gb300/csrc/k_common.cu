@@ -163,12 +163,13 @@ __global__ void k_aux(AuxArgs a) {
 }
 
 int aux_step(Plan *p, int it, int mode) {
-  (void)mode;
-  const int n = p->n_rtask + (it <= p->d.nt ? p->n_cells : 0);
+  // an adjoint run records nothing (get_update_parameters, propagate.jl:38-60)
+  const int ntask = mode == GPI_ADJOINT ? 0 : p->n_rtask;
+  const int n = ntask + (it <= p->d.nt ? p->n_cells : 0);
   if (n == 0) return GPI_OK;
   AuxArgs a;
   a.tasks = p->d_rtask;
-  a.ntask = p->n_rtask;
+  a.ntask = ntask;
   a.roff = p->d_roff;
   a.rw = p->d_rw;
   a.rec = p->rec_pool;
@@ -204,8 +205,10 @@ struct StripArgs {
   int64_t sstride;  // floats per shot in the store
   int n1, n2, n3;   // field shape
   int axis, nb, np;
-  int dir;          // 0 save (negated), 1 force
+  int dir;          // 0 save (negated), 1 force, 2 force keeping the replaced values in prev
   int nshots;
+  float *prev;      // dir 2: shot 0, this (field, axis) block, same layout and shot stride pstride
+  int64_t pstride;
 };
 
 __global__ void k_strip(StripArgs a) {
@@ -227,10 +230,12 @@ __global__ void k_strip(StripArgs a) {
     fi[a.axis] = fidx;
     float *f = a.field + shot * a.fs + a.g.off(fi[0], fi[1], fi[2]);
     float *s = a.store + shot * a.sstride + k;
-    if (a.dir == 0)
+    if (a.dir == 0) {
       *s = -*f;
-    else
+    } else {
+      if (a.dir == 2) a.prev[shot * a.pstride + k] = *f;
       *f = *s;
+    }
   }
 }
 
@@ -250,6 +255,7 @@ int boundary_io(Plan *p, int it, int dir) {
   const int nsv = saved_fields(*p, ids);
   const int64_t sstride = p->bstep * p->d.nt + p->bsnap;
   float *st = p->bstore + (int64_t)(it - 1) * p->bstep;
+  float *pv = p->bprev;
   for (int q = 0; q < nsv; q++) {
     int kz, ky, kx;
     field_kinds(ids[q], &kz, &ky, &kx);
@@ -272,12 +278,15 @@ int boundary_io(Plan *p, int it, int dir) {
       a.np = (p->d.pml_faces & fmin) ? p->d.npml : 0;
       a.dir = dir;
       a.nshots = p->d.nshots;
+      a.prev = pv;
+      a.pstride = p->bstep;
       int64_t per = 2 * (int64_t)p->d.nbound * (axis == 0 ? 1 : n1) * (axis == 1 ? 1 : n2) * (axis == 2 ? 1 : n3);
       int blocks = (int)std::min<int64_t>((per * p->d.nshots + 255) / 256, 152 * 16);
       k_strip<<<blocks, 256, 0, p->stream>>>(a);
       p->launches++;
       GPI_CUDA(p, cudaGetLastError());
       st += per;
+      pv += per;
     }
   }
   return GPI_OK;
