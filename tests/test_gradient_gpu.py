@@ -20,17 +20,12 @@ def rel(a, b):
     return np.linalg.norm(np.asarray(a, np.float64) - b) / (nb if nb > 0 else 1.0)
 
 
-def _case(nz, nx, nt, nshots, nrec):
-    true = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=nshots, nrec=nrec, radius=60.0)
-    start = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=nshots, nrec=nrec, anomaly=False)
-    return true, start
-
-
 @pytest.mark.gpu
 @pytest.mark.parametrize("nz,nx,nt,nshots", [(40, 70, 300, 1), (90, 160, 600, 2)])
 def test_acoustic2d_gradient_matches_oracle(engine, nz, nx, nt, nshots):
-    true, start = _case(nz, nx, nt, nshots, nrec=nx // 3)
-    dobs_ref = {f: np.zeros_like(v) for f, v in O.forward(true.as_dict()).items()}
+    nrec = nx // 3
+    start = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=nshots, nrec=nrec, anomaly=False)
+    dobs_ref = {"vz": np.zeros((nshots, nt, nrec), np.float32)}
     loss_o, _, dcal_o, raw_o = O.gradient(start.as_dict(), dobs_ref)
     pa = start.expt(mode="forward_save")
     tg = pa.tgrid
