@@ -1,0 +1,419 @@
+// k_3d.cu -- 3-D acoustic and elastic time steps (order 4).
+//
+// A step is two fused passes over the grid, each updating its fields in place
+// with the derivatives computed on the fly (the reference materialises every
+// derivative field first, src/fdtd/advance_acou.jl:258-313,
+// src/fdtd/advance_elastic.jl:10-230):
+//   velocity pass: stress (or p) derivatives + memory*! + compute_v!
+//   dirichlet{x,y,z}{min,max}! in the reference's face order, velocity sources
+//   stress pass:   velocity derivatives + memory*! + compute_stress*! / compute_p!
+//   free surface (elastic), stress sources
+// Index arithmetic follows the derivative-field tables of the reference
+// (src/fields.jl:92-671, src/fdtd/diff3D.jl:62-134, :303-378): a derivative
+// D(iz, iy, ix) of shape kinds (kz, ky, kx) reads its source field from
+// (iz, iy, ix) (@d_?a) or from (iz, iy, ix) + h on the other two axes
+// (@d_?i), and CPML applies on the first and last npml entries of its own
+// axis.  Every field shares the padded storage index map, so a thread owns
+// the storage cell (r, y, c) of every field it updates.
+#include <algorithm>
+
+#include "k_stencil.cuh"
+
+namespace gpi {
+
+struct G3 {
+  int nz, ny, nx, NZP, NYP;
+  int64_t fs;
+  __device__ __forceinline__ int64_t S(int r, int y, int c) const {
+    return ((int64_t)(c + XOFF - 1) * NYP + (y + YOFF - 1)) * NZP + (r + ZOFF - 1);
+  }
+};
+
+// CPML memory of one derivative field: psi = b psi + a D, D = D kI + psi on
+// the strips of its axis (memory{x,y,z}!, src/fdtd/cpml.jl:158-215).
+struct Mem3 {
+  float *psi[18];
+  int64_t pss[18];
+  const float *pml;  // [q][a | b | kI][2 npml]
+  int npml, w;       // w = 2 npml
+  int faces;
+};
+
+// psi index of derivative index (iz, iy, ix) with strip slot j on `axis`
+__device__ __forceinline__ int64_t psi_index(const G3 &g, const Mem3 &m, int axis, int j, int iz, int iy, int ix) {
+  if (axis == 2) return ((int64_t)j * g.NYP + (iy + YOFF - 1)) * g.NZP + (iz + ZOFF - 1);
+  if (axis == 1) return ((int64_t)(ix + XOFF - 1) * m.w + j) * g.NZP + (iz + ZOFF - 1);
+  return ((int64_t)(ix + XOFF - 1) * g.NYP + (iy + YOFF - 1)) * m.w + j;
+}
+
+// D of derivative q at index (iz, iy, ix); i = index along its axis, nd the
+// derivative field's extent along that axis
+__device__ __forceinline__ float mem3(float D, const G3 &g, const Mem3 &m, int shot, int q, int axis, int i, int nd,
+                                     int iz, int iy, int ix) {
+  const int lo = axis == 0 ? GPI_ZMIN : axis == 1 ? GPI_YMIN : GPI_XMIN;
+  const int hi = axis == 0 ? GPI_ZMAX : axis == 1 ? GPI_YMAX : GPI_XMAX;
+  const int j = pml_slot(i, nd, m.npml, m.faces & lo, m.faces & hi);
+  if (j < 0) return D;
+  const float *cf = m.pml + (int64_t)q * 3 * m.w;
+  float *ps = m.psi[q] + shot * m.pss[q] + psi_index(g, m, axis, j, iz, iy, ix);
+  const float psi = cf[m.w + j] * *ps + cf[j] * D;
+  *ps = psi;
+  return D * cf[2 * m.w + j] + psi;
+}
+
+struct Step3 {
+  G3 g;
+  Mem3 m;
+  float *f[NFIELD];      // fields, shot 0
+  const float *cf[8];    // coefficients (storage layout, shared by shots)
+  float dzI, dyI, dxI;
+  int shot0, nshots;  // shots [shot0, shot0 + nshots) of this launch
+};
+
+// thread -> storage cell (r, y, c) of one shot; extents cover n + h on every axis
+struct Cell3 {
+  int r, y, c, shot;
+  bool ok;
+};
+__device__ __forceinline__ Cell3 cell3(const G3 &g, int shot0, int nshots) {
+  Cell3 e;
+  e.r = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  e.y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int nc = g.nx + 3;
+  e.c = (int)(blockIdx.z % nc) + 1;
+  e.shot = (int)(blockIdx.z / nc);
+  e.ok = e.r <= g.nz + 3 && e.y <= g.ny + 3 && e.shot < nshots;
+  e.shot += shot0;
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+// acoustic (DA3: dpdx dpdy dpdz dvxdx dvydy dvzdz)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k3_vel_a(const Step3 a) {
+  const G3 &g = a.g;
+  const Cell3 e = cell3(g, a.shot0, a.nshots);
+  if (!e.ok) return;
+  const int r = e.r, y = e.y, c = e.c, nz = g.nz, ny = g.ny, nx = g.nx;
+  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c);
+  const float *p = a.f[GPI_P] + so;
+  const int64_t sx = (int64_t)g.NYP * g.NZP, sy = g.NZP;
+  // @inn(vx) += dtinvavxirho * dpdx, dpdx = @d_xi(p) (nz-2h, ny-2h, nx-h)
+  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx) {
+    const int64_t b = g.S(r, y, c - 3);
+    float D = st4(p[b], p[b + sx], p[b + 2 * sx], p[b + 3 * sx]) * a.dxI;
+    D = mem3(D, g, a.m, e.shot, 0, 2, c - 3, nx - 3, r - 3, y - 3, c - 3);
+    a.f[GPI_VX][o] = a.f[GPI_VX][o] + a.cf[0][o - so] * D;
+  }
+  // @inn(vy) += dtinvavyirho * dpdy, dpdy = @d_yi(p) (nz-2h, ny-h, nx-2h)
+  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny && c >= 4 && c <= nx - 3) {
+    const int64_t b = g.S(r, y - 3, c);
+    float D = st4(p[b], p[b + sy], p[b + 2 * sy], p[b + 3 * sy]) * a.dyI;
+    D = mem3(D, g, a.m, e.shot, 1, 1, y - 3, ny - 3, r - 3, y - 3, c - 3);
+    a.f[GPI_VY][o] = a.f[GPI_VY][o] + a.cf[1][o - so] * D;
+  }
+  // @inn(vz) += dtinvavzirho * dpdz, dpdz = @d_zi(p) (nz-h, ny-2h, nx-2h)
+  if (r >= 4 && r <= nz && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx - 3) {
+    const int64_t b = g.S(r - 3, y, c);
+    float D = st4(p[b], p[b + 1], p[b + 2], p[b + 3]) * a.dzI;
+    D = mem3(D, g, a.m, e.shot, 2, 0, r - 3, nz - 3, r - 3, y - 3, c - 3);
+    a.f[GPI_VZ][o] = a.f[GPI_VZ][o] + a.cf[2][o - so] * D;
+  }
+}
+
+__global__ void __launch_bounds__(256) k3_str_a(const Step3 a) {
+  const G3 &g = a.g;
+  const Cell3 e = cell3(g, a.shot0, a.nshots);
+  if (!e.ok) return;
+  const int r = e.r, y = e.y, c = e.c;
+  if (r > g.nz || y > g.ny || c > g.nx) return;
+  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c);
+  const int64_t sx = (int64_t)g.NYP * g.NZP, sy = g.NZP;
+  const float *vx = a.f[GPI_VX] + o, *vy = a.f[GPI_VY] + o, *vz = a.f[GPI_VZ] + o;
+  float Dx = st4(vx[0], vx[sx], vx[2 * sx], vx[3 * sx]) * a.dxI;  // @d_xa(vx)
+  Dx = mem3(Dx, g, a.m, e.shot, 3, 2, c, g.nx, r, y, c);
+  float Dy = st4(vy[0], vy[sy], vy[2 * sy], vy[3 * sy]) * a.dyI;  // @d_ya(vy)
+  Dy = mem3(Dy, g, a.m, e.shot, 4, 1, y, g.ny, r, y, c);
+  float Dz = st4(vz[0], vz[1], vz[2], vz[3]) * a.dzI;  // @d_za(vz)
+  Dz = mem3(Dz, g, a.m, e.shot, 5, 0, r, g.nz, r, y, c);
+  // compute_p!: p += (dvxdx + dvzdz + dvydy) * dtK
+  a.f[GPI_P][o] = a.f[GPI_P][o] + (Dx + Dz + Dy) * a.cf[3][o - so];
+}
+
+// ---------------------------------------------------------------------------
+// elastic (DE3, canonical order: dtauxxdx dtauxydx dtauxzdx dtauyydy
+// dtauxydy dtauyzdy dtauzzdz dtauyzdz dtauxzdz dvxdx dvydy dvzdz dvxdy dvxdz
+// dvydx dvydz dvzdx dvzdy)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k3_vel_e(const Step3 a) {
+  const G3 &g = a.g;
+  const Cell3 e = cell3(g, a.shot0, a.nshots);
+  if (!e.ok) return;
+  const int r = e.r, y = e.y, c = e.c, nz = g.nz, ny = g.ny, nx = g.nx;
+  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c);
+  const int64_t sx = (int64_t)g.NYP * g.NZP, sy = g.NZP;
+  const float *txx = a.f[GPI_TAUXX] + so, *tyy = a.f[GPI_TAUYY] + so, *tzz = a.f[GPI_TAUZZ] + so;
+  const float *txy = a.f[GPI_TAUXY] + so, *txz = a.f[GPI_TAUXZ] + so, *tyz = a.f[GPI_TAUYZ] + so;
+  const int iz = r - 3, iy = y - 3, ix = c - 3;  // derivative index of the @inn velocity cell
+  // vx: @inn(vx) -= dtinvavxirho (dtauxxdx + dtauxydy + dtauxzdz), (nz-2h, ny-2h, nx-h)
+  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx) {
+    int64_t b = g.S(r, y, c - 3);  // @d_xi(tauxx)
+    float D0 = st4(txx[b], txx[b + sx], txx[b + 2 * sx], txx[b + 3 * sx]) * a.dxI;
+    D0 = mem3(D0, g, a.m, e.shot, 0, 2, ix, nx - 3, iz, iy, ix);
+    b = g.S(iz, iy, ix);  // @d_ya(tauxy)
+    float D4 = st4(txy[b], txy[b + sy], txy[b + 2 * sy], txy[b + 3 * sy]) * a.dyI;
+    D4 = mem3(D4, g, a.m, e.shot, 4, 1, iy, ny - 6, iz, iy, ix);
+    float D8 = st4(txz[b], txz[b + 1], txz[b + 2], txz[b + 3]) * a.dzI;  // @d_za(tauxz)
+    D8 = mem3(D8, g, a.m, e.shot, 8, 0, iz, nz - 6, iz, iy, ix);
+    a.f[GPI_VX][o] = a.f[GPI_VX][o] - a.cf[0][o - so] * (D0 + D4 + D8);
+  }
+  // vy: @inn(vy) -= dtinvavyirho (dtauxydx + dtauyydy + dtauyzdz), (nz-2h, ny-h, nx-2h)
+  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny && c >= 4 && c <= nx - 3) {
+    int64_t b = g.S(iz, iy, ix);  // @d_xa(tauxy)
+    float D1 = st4(txy[b], txy[b + sx], txy[b + 2 * sx], txy[b + 3 * sx]) * a.dxI;
+    D1 = mem3(D1, g, a.m, e.shot, 1, 2, ix, nx - 6, iz, iy, ix);
+    b = g.S(r, iy, c);  // @d_yi(tauyy)
+    float D3 = st4(tyy[b], tyy[b + sy], tyy[b + 2 * sy], tyy[b + 3 * sy]) * a.dyI;
+    D3 = mem3(D3, g, a.m, e.shot, 3, 1, iy, ny - 3, iz, iy, ix);
+    b = g.S(iz, iy, ix);  // @d_za(tauyz)
+    float D7 = st4(tyz[b], tyz[b + 1], tyz[b + 2], tyz[b + 3]) * a.dzI;
+    D7 = mem3(D7, g, a.m, e.shot, 7, 0, iz, nz - 6, iz, iy, ix);
+    a.f[GPI_VY][o] = a.f[GPI_VY][o] - a.cf[1][o - so] * (D1 + D3 + D7);
+  }
+  // vz: @inn(vz) -= dtinvavzirho (dtauxzdx + dtauyzdy + dtauzzdz), (nz-h, ny-2h, nx-2h)
+  if (r >= 4 && r <= nz && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx - 3) {
+    int64_t b = g.S(iz, iy, ix);  // @d_xa(tauxz)
+    float D2 = st4(txz[b], txz[b + sx], txz[b + 2 * sx], txz[b + 3 * sx]) * a.dxI;
+    D2 = mem3(D2, g, a.m, e.shot, 2, 2, ix, nx - 6, iz, iy, ix);
+    float D5 = st4(tyz[b], tyz[b + sy], tyz[b + 2 * sy], tyz[b + 3 * sy]) * a.dyI;  // @d_ya(tauyz)
+    D5 = mem3(D5, g, a.m, e.shot, 5, 1, iy, ny - 6, iz, iy, ix);
+    b = g.S(iz, y, c);  // @d_zi(tauzz)
+    float D6 = st4(tzz[b], tzz[b + 1], tzz[b + 2], tzz[b + 3]) * a.dzI;
+    D6 = mem3(D6, g, a.m, e.shot, 6, 0, iz, nz - 3, iz, iy, ix);
+    a.f[GPI_VZ][o] = a.f[GPI_VZ][o] - a.cf[2][o - so] * (D2 + D5 + D6);
+  }
+}
+
+__global__ void __launch_bounds__(256) k3_str_e(const Step3 a) {
+  const G3 &g = a.g;
+  const Cell3 e = cell3(g, a.shot0, a.nshots);
+  if (!e.ok) return;
+  const int r = e.r, y = e.y, c = e.c, nz = g.nz, ny = g.ny, nx = g.nx;
+  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c), oc = o - so;
+  const int64_t sx = (int64_t)g.NYP * g.NZP, sy = g.NZP;
+  const float *vx = a.f[GPI_VX] + so, *vy = a.f[GPI_VY] + so, *vz = a.f[GPI_VZ] + so;
+  // compute_stressii!: full grid
+  if (r <= nz && y <= ny && c <= nx) {
+    const int64_t b = g.S(r, y, c);
+    float D9 = st4(vx[b], vx[b + sx], vx[b + 2 * sx], vx[b + 3 * sx]) * a.dxI;  // @d_xa(vx)
+    D9 = mem3(D9, g, a.m, e.shot, 9, 2, c, nx, r, y, c);
+    float D10 = st4(vy[b], vy[b + sy], vy[b + 2 * sy], vy[b + 3 * sy]) * a.dyI;  // @d_ya(vy)
+    D10 = mem3(D10, g, a.m, e.shot, 10, 1, y, ny, r, y, c);
+    float D11 = st4(vz[b], vz[b + 1], vz[b + 2], vz[b + 3]) * a.dzI;  // @d_za(vz)
+    D11 = mem3(D11, g, a.m, e.shot, 11, 0, r, nz, r, y, c);
+    const float M = a.cf[6][oc], L = a.cf[7][oc];
+    float *txx = a.f[GPI_TAUXX] + o, *tyy = a.f[GPI_TAUYY] + o, *tzz = a.f[GPI_TAUZZ] + o;
+    *txx = *txx - (M * D9) - (L * (D10 + D11));
+    *tyy = *tyy - (M * D10) - (L * (D9 + D11));
+    *tzz = *tzz - (M * D11) - (L * (D10 + D9));
+  }
+  // tauxy (nz-2h, ny-h, nx-h): -= dtavxyimu (dvxdy + dvydx)
+  if (r <= nz - 6 && y <= ny - 3 && c <= nx - 3) {
+    int64_t b = g.S(r + 3, y, c + 3);  // @d_yi(vx)
+    float D12 = st4(vx[b], vx[b + sy], vx[b + 2 * sy], vx[b + 3 * sy]) * a.dyI;
+    D12 = mem3(D12, g, a.m, e.shot, 12, 1, y, ny - 3, r, y, c);
+    b = g.S(r + 3, y + 3, c);  // @d_xi(vy)
+    float D14 = st4(vy[b], vy[b + sx], vy[b + 2 * sx], vy[b + 3 * sx]) * a.dxI;
+    D14 = mem3(D14, g, a.m, e.shot, 14, 2, c, nx - 3, r, y, c);
+    a.f[GPI_TAUXY][o] = a.f[GPI_TAUXY][o] - a.cf[4][oc] * (D12 + D14);
+  }
+  // tauxz (nz-h, ny-2h, nx-h): -= dtavxzimu (dvxdz + dvzdx)
+  if (r <= nz - 3 && y <= ny - 6 && c <= nx - 3) {
+    int64_t b = g.S(r, y + 3, c + 3);  // @d_zi(vx)
+    float D13 = st4(vx[b], vx[b + 1], vx[b + 2], vx[b + 3]) * a.dzI;
+    D13 = mem3(D13, g, a.m, e.shot, 13, 0, r, nz - 3, r, y, c);
+    b = g.S(r + 3, y + 3, c);  // @d_xi(vz)
+    float D16 = st4(vz[b], vz[b + sx], vz[b + 2 * sx], vz[b + 3 * sx]) * a.dxI;
+    D16 = mem3(D16, g, a.m, e.shot, 16, 2, c, nx - 3, r, y, c);
+    a.f[GPI_TAUXZ][o] = a.f[GPI_TAUXZ][o] - a.cf[3][oc] * (D13 + D16);
+  }
+  // tauyz (nz-h, ny-h, nx-2h): -= dtavyzimu (dvydz + dvzdy)
+  if (r <= nz - 3 && y <= ny - 3 && c <= nx - 6) {
+    int64_t b = g.S(r, y + 3, c + 3);  // @d_zi(vy)
+    float D15 = st4(vy[b], vy[b + 1], vy[b + 2], vy[b + 3]) * a.dzI;
+    D15 = mem3(D15, g, a.m, e.shot, 15, 0, r, nz - 3, r, y, c);
+    b = g.S(r + 3, y, c + 3);  // @d_yi(vz)
+    float D17 = st4(vz[b], vz[b + sy], vz[b + 2 * sy], vz[b + 3 * sy]) * a.dyI;
+    D17 = mem3(D17, g, a.m, e.shot, 17, 1, y, ny - 3, r, y, c);
+    a.f[GPI_TAUYZ][o] = a.f[GPI_TAUYZ][o] - a.cf[5][oc] * (D15 + D17);
+  }
+}
+
+// free_surface_mirror!(tauzz), free_surface!(tauxz, tauyz) at z = 1
+__global__ void k3_free(float *tzz, float *txz, float *tyz, G3 g, int nshots) {
+  const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int shot = blockIdx.z;
+  if (y > g.ny || c > g.nx || shot >= nshots) return;
+  const int64_t so = shot * g.fs;
+  tzz[so + g.S(1, y, c)] = -tzz[so + g.S(2, y, c)];
+  if (y <= g.ny - 6 && c <= g.nx - 3) txz[so + g.S(1, y, c)] = 0.f;
+  if (y <= g.ny - 3 && c <= g.nx - 6) tyz[so + g.S(1, y, c)] = 0.f;
+}
+
+// one face of dirichlet{x,y,z}{min,max}! (src/fdtd/dirichlet.jl:1-79): the
+// other velocity components vanish on the face, the normal component is
+// mirrored into the two ghost layers
+__global__ void k3_dirichlet(float *vx, float *vy, float *vz, G3 g, int nshots, int axis, int ismax) {
+  const int n[3] = {g.nz, g.ny, g.nx};
+  const int oa = axis == 0 ? 1 : 0, ob = axis == 2 ? 1 : 2;
+  const int ja = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jb = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int shot = blockIdx.z;
+  if (ja > n[oa] || jb > n[ob] || shot >= nshots) return;
+  const int64_t so = shot * g.fs;
+  float *v[3] = {vz + so, vy + so, vx + so};  // by axis
+  const int nn = n[axis];
+  int idx[3];
+  idx[oa] = ja;
+  idx[ob] = jb;
+  for (int o2 = 0; o2 < 3; o2++) {
+    if (o2 == axis) continue;
+    idx[axis] = ismax ? nn : 1;
+    v[o2][g.S(idx[0], idx[1], idx[2])] = 0.f;
+  }
+  for (int ifd = 1; ifd <= 2; ifd++) {
+    const int gi = ismax ? nn + 4 - ifd : ifd, si = ismax ? nn + ifd - 1 : 5 - ifd;
+    int ig[3] = {idx[0], idx[1], idx[2]}, is[3] = {idx[0], idx[1], idx[2]};
+    ig[axis] = gi;
+    is[axis] = si;
+    v[axis][g.S(ig[0], ig[1], ig[2])] = -v[axis][g.S(is[0], is[1], is[2])];
+  }
+}
+
+// sources of one step: every (shot, kind) group adds its cells' amounts in
+// cell order (add_velocity_source! / add_stress_source!, src/fdtd/source.jl)
+struct Fields3 {
+  float *f[NFIELD];
+};
+__global__ void k3_inject(const InjCell *cells, const int32_t *gptr, const float *amount, Fields3 fld, int64_t fs,
+                          int nshots, int velocity, int physics) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= nshots * NKIND) return;
+  const int shot = gi / NKIND, kind = gi % NKIND;
+  if ((kind < 3) != (velocity != 0)) return;
+  const int64_t so = shot * fs;
+  for (int k = gptr[gi]; k < gptr[gi + 1]; k++) {
+    const InjCell c = cells[k];
+    const float amt = amount[k];
+    if (kind == 0) fld.f[GPI_VX][so + c.off] = fld.f[GPI_VX][so + c.off] + amt;
+    if (kind == 1) fld.f[GPI_VY][so + c.off] = fld.f[GPI_VY][so + c.off] + amt;
+    if (kind == 2) fld.f[GPI_VZ][so + c.off] = fld.f[GPI_VZ][so + c.off] + amt;
+    if (kind == 3) {
+      if (physics == GPI_ACOUSTIC) {
+        fld.f[GPI_P][so + c.off] = fld.f[GPI_P][so + c.off] + amt;
+      } else {
+        fld.f[GPI_TAUXX][so + c.off] = fld.f[GPI_TAUXX][so + c.off] + amt;
+        fld.f[GPI_TAUYY][so + c.off] = fld.f[GPI_TAUYY][so + c.off] + amt;
+        fld.f[GPI_TAUZZ][so + c.off] = fld.f[GPI_TAUZZ][so + c.off] + amt;
+      }
+    }
+  }
+}
+
+static int step3(Plan *p, int vonly) {
+  const bool ac = p->d.physics == GPI_ACOUSTIC;
+  Step3 a;
+  a.g = G3{p->d.nz, p->d.ny, p->d.nx, p->NZP, p->NYP, p->fstride};
+  a.m.pml = p->pml;
+  a.m.npml = p->d.npml;
+  a.m.w = 2 * p->d.npml;
+  a.m.faces = p->d.pml_faces;
+  const int A = p->cur[0];  // 3-D steps update in place
+  for (int q = 0; q < 18; q++) {
+    a.m.psi[q] = q < p->nder ? p->psi[A][0][q] : nullptr;
+    a.m.pss[q] = q < p->nder ? p->psi_stride[q] : 0;
+  }
+  Fields3 fl;
+  for (int f = 0; f < NFIELD; f++) a.f[f] = fl.f[f] = p->state[A][0][f];
+  for (int i = 0; i < 8; i++) a.cf[i] = p->coef[i];
+  a.dzI = (float)(1.0 / (p->d.dz * 24.0));
+  a.dyI = (float)(1.0 / (p->d.dy * 24.0));
+  a.dxI = (float)(1.0 / (p->d.dx * 24.0));
+  const int nc = p->d.nx + 3;
+  if (nc > 65535) return fail(p, GPI_E_UNSUPPORTED, "3-D grids are limited to 65532 columns");
+  const int chunk = 65535 / nc;  // shots per launch (grid z = columns x shots)
+  const dim3 blk(32, 8);
+  auto pass = [&](bool vel) {
+    for (int s0 = 0; s0 < p->d.nshots; s0 += chunk) {
+      Step3 b = a;
+      b.shot0 = s0;
+      b.nshots = std::min(chunk, p->d.nshots - s0);
+      const dim3 grd((p->d.nz + 3 + 31) / 32, (p->d.ny + 3 + 7) / 8, nc * b.nshots);
+      if (vel) {
+        if (ac)
+          k3_vel_a<<<grd, blk, 0, p->stream>>>(b);
+        else
+          k3_vel_e<<<grd, blk, 0, p->stream>>>(b);
+      } else {
+        if (ac)
+          k3_str_a<<<grd, blk, 0, p->stream>>>(b);
+        else
+          k3_str_e<<<grd, blk, 0, p->stream>>>(b);
+      }
+      p->launches++;
+    }
+  };
+  pass(true);
+  // rigid faces in the order x, y, z; min, max (update_v!)
+  const int seq[6][2] = {{2, 0}, {2, 1}, {1, 0}, {1, 1}, {0, 0}, {0, 1}};
+  const int fmask[3][2] = {{GPI_ZMIN, GPI_ZMAX}, {GPI_YMIN, GPI_YMAX}, {GPI_XMIN, GPI_XMAX}};
+  const int n[3] = {p->d.nz, p->d.ny, p->d.nx};
+  const int nsz = std::min(p->d.nshots, 65535);
+  for (int s = 0; s < 6; s++) {
+    const int axis = seq[s][0], ismax = seq[s][1];
+    if (!(p->d.rigid_faces & fmask[axis][ismax])) continue;
+    const int oa = axis == 0 ? 1 : 0, ob = axis == 2 ? 1 : 2;
+    const dim3 db(32, 8), dg((n[oa] + 31) / 32, (n[ob] + 7) / 8, nsz);
+    k3_dirichlet<<<dg, db, 0, p->stream>>>(a.f[GPI_VX], a.f[GPI_VY], a.f[GPI_VZ], a.g, p->d.nshots, axis, ismax);
+    p->launches++;
+  }
+  const int ng = p->d.nshots * NKIND;
+  if (!vonly && p->n_cells) {
+    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, p->d_group_ptr, p->d_amount, fl, p->fstride,
+                                                       p->d.nshots, 1, p->d.physics);
+    p->launches++;
+  }
+  if (vonly) {
+    GPI_CUDA(p, cudaGetLastError());
+    return GPI_OK;
+  }
+  pass(false);
+  if (!ac && (p->d.free_faces & GPI_ZMIN)) {
+    const dim3 fb(32, 8), fg((p->d.nx + 31) / 32, (p->d.ny + 7) / 8, nsz);
+    k3_free<<<fg, fb, 0, p->stream>>>(a.f[GPI_TAUZZ], a.f[GPI_TAUXZ], a.f[GPI_TAUYZ], a.g, p->d.nshots);
+    p->launches++;
+  }
+  if (p->n_cells) {
+    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, p->d_group_ptr, p->d_amount, fl, p->fstride,
+                                                       p->d.nshots, 0, p->d.physics);
+    p->launches++;
+  }
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
+  (void)ipw_mask;
+  (void)it;
+  (void)mode;
+  return step3(p, vonly);
+}
+int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
+  (void)ipw_mask;
+  (void)it;
+  (void)mode;
+  return step3(p, vonly);
+}
+
+}  // namespace gpi

@@ -10,7 +10,11 @@ Gaussian-smoothed random perturbation, wavelets are Ricker wavelets.
                      sigma 15 cells, +-8 %, Ricker 12 Hz explosive)
   acoustic2d_fwi     2-D acoustic gradient, 500 x 1500 at 10 m, 32 shots,
                      3000 steps (layers + 200 m Gaussian anomaly of +10 %)
-  elastic3d          3-D elastic forward, 600^3 at 10 m, 20-cell CPML, 2500 steps
+  elastic3d          3-D elastic forward, 600^3 at 10 m, 20-cell CPML (npml 23),
+                     2500 steps (linear vp 2000->5000, vs = vp/1.75, Gardner rho,
+                     sigma 10 cells, +-5 %, Ricker 10 Hz explosive at 50 m,
+                     121 x 121 surface receivers)
+  acoustic3d         the same medium, acoustic, p source
 
 Every builder accepts overrides (sizes, steps, shot count) so tests can run
 reduced versions with the same shapes of inputs.
@@ -58,7 +62,8 @@ class Workload:
     def nt(self):
         return len(self.tgrid)
 
-    def cells(self, npml=43):
+    def cells(self, npml=None):
+        npml = npml if npml is not None else (self.npml if self.npml is not None else 43)
         n = 1
         for g in self.grid:
             n *= len(g) + 2 * npml
@@ -97,6 +102,8 @@ class Workload:
         from .fdtd import FdtdAcoustic, FdtdElastic, SeisForwExpt
 
         attrib = (FdtdAcoustic if self.physics == "acoustic" else FdtdElastic)(mode)
+        if self.npml is not None:
+            kw.setdefault("npml", self.npml)
         return SeisForwExpt(attrib, medium=self.medium(), ageom=self.ageom(), srcwav=self.srcwav(),
                             tgrid=self.tgrid, rfields=self.rfields, pml_faces=self.pml_faces,
                             stressfree_faces=self.stressfree_faces, **kw)
@@ -117,6 +124,8 @@ class Workload:
              "dt": self.tgrid.step, "nt": self.nt, "shots": shots, "rfields": self.rfields}
         if self.vs is not None:
             d["vs"] = self.vs
+        if self.npml is not None:
+            d["npml"] = int(self.npml)
         return d
 
 
@@ -192,3 +201,41 @@ def acoustic2d_fwi(nz=500, nx=1500, d=10.0, nt=3000, dt=0.001, nshots=32, nrec=N
     shots = [(np.array([[min(2 * d, grid[0].last), x]]), rec) for x in xs]
     return Workload("acoustic2d_fwi", "acoustic", grid, vp, rho, shots=shots, tgrid=tgrid,
                     wavelet=ricker(f0, tgrid), rfields=("vz",), src_field="vz")
+
+
+def _media3d(nz, ny, nx, d, seed, vp0=2000.0, vp1=5000.0, pert=0.05, sigma=10.0, vsr=1.75):
+    z = np.linspace(0.0, 1.0, nz)[:, None, None]
+    vp = np.broadcast_to(vp0 + (vp1 - vp0) * z, (nz, ny, nx)).astype(np.float32)
+    vp = (vp * (1 + pert * smooth_noise((nz, ny, nx), sigma, seed))).astype(np.float32)
+    return vp, (vp / vsr).astype(np.float32), gardner(vp)
+
+
+def _surface_receivers(grid, nside):
+    ym, xm = grid[1].last, grid[2].last
+    yy, xx = np.meshgrid(np.linspace(0.0, ym, nside), np.linspace(0.0, xm, nside), indexing="ij")
+    return np.stack([np.zeros(yy.size), yy.ravel(), xx.ravel()], 1)
+
+
+def elastic3d(nz=600, ny=600, nx=600, d=10.0, nt=2500, dt=0.0008, npml=23, nrec_side=121, seed=3, f0=10.0,
+              zsrc=50.0, rfields=("vz",), src_field="tauxx"):
+    """3-D elastic forward: explosive source centred at zsrc, surface grid of
+    receivers."""
+    vp, vs, rho = _media3d(nz, ny, nx, d, seed)
+    grid = [Grid(0.0, d, nz), Grid(0.0, d, ny), Grid(0.0, d, nx)]
+    tgrid = Grid(0.0, dt, nt)
+    src = np.array([[min(zsrc, grid[0].last), 0.5 * grid[1].last, 0.5 * grid[2].last]])
+    rec = _surface_receivers(grid, nrec_side)
+    return Workload("elastic3d", "elastic", grid, vp, rho, vs=vs, shots=[(src, rec)], tgrid=tgrid,
+                    wavelet=ricker(f0, tgrid), rfields=rfields, src_field=src_field, npml=npml)
+
+
+def acoustic3d(nz=600, ny=600, nx=600, d=10.0, nt=2500, dt=0.0008, npml=23, nrec_side=121, seed=3, f0=10.0,
+               zsrc=50.0, rfields=("p", "vz"), src_field="p"):
+    """3-D acoustic forward on the medium of elastic3d."""
+    vp, _, rho = _media3d(nz, ny, nx, d, seed)
+    grid = [Grid(0.0, d, nz), Grid(0.0, d, ny), Grid(0.0, d, nx)]
+    tgrid = Grid(0.0, dt, nt)
+    src = np.array([[min(zsrc, grid[0].last), 0.5 * grid[1].last, 0.5 * grid[2].last]])
+    rec = _surface_receivers(grid, nrec_side)
+    return Workload("acoustic3d", "acoustic", grid, vp, rho, shots=[(src, rec)], tgrid=tgrid,
+                    wavelet=ricker(f0, tgrid), rfields=rfields, src_field=src_field, npml=npml)

@@ -126,13 +126,16 @@ class SeisForwExpt:
     """PFdtd (src/fdtd/fdtd.jl:61-297) driving one libgpi_fdtd plan."""
 
     def __init__(self, attrib, *, medium, ageom, srcwav, tgrid, rfields=("vz",), pml_faces=ALL_FACES,
-                 rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False):
+                 rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False,
+                 npml=None):
         L = _lib.load()
         self.L = L
         self.attrib = attrib
         self.order = order
         self.h = order - 1
-        self.npml = 40 + self.h
+        # the reference pads by 40 + h cells (_fd_npml, GeoPhyInv.jl:90); a smaller CPML
+        # (npml = n + h) may be asked for explicitly
+        self.npml = int(npml) if npml is not None else 40 + self.h
         self.nbound = 3
         N = medium.ndim
         self.ndim = N

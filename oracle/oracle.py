@@ -89,7 +89,7 @@ class Prepared:
         self.ndim = ex["ndim"]
         self.order = ex.get("order", 4)
         self.h = self.order - 1
-        self.npml = S.npml_of(self.order)
+        self.npml = int(ex["npml"]) if ex.get("npml") is not None else S.npml_of(self.order)
         self.faces = ex["pml_faces"]
         self.rigid = ex.get("rigid_faces", self.faces) | self.faces
         self.free = ex.get("free_faces", 0)
