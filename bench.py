@@ -13,6 +13,10 @@ One bench step is one full forward modelling of the batch (update!(pa)).
   cpu_baseline  the CPU oracle (C restatement of the reference, OpenMP on
          all host cores) on a bounded sample of the same workload
 
+Other workloads (--workload): acoustic2d (201 x 301 at 5 m, 2000 steps, 36 B
+per cell update), elastic3d (600^3 at 10 m, npml 23, 2500 steps, 104 B) and
+acoustic3d (48 B); the default line is the elastic 2-D batch.
+
 --impl reference times the CPU restatement of the reference on the host
 cores (the reference is Julia and cannot run here).  Multi-GPU: one process
 per GPU, each rank models its own batch of shots (shots are independent,
@@ -35,7 +39,18 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "Gcell-updates/s"
-BYTES_PER_CELL = 60  # elastic 2-D: 4 B x (2 x 5 state + 5 coefficient arrays)
+
+# algorithmic bytes per cell update: 4 B x (2 x state arrays + coefficient arrays)
+WORKLOADS = {
+    "elastic2d": {"name": "elastic2d_psv_1000x3000_5m_16shots_4000steps", "bpc": 60, "nshots": 16, "nt": 4000,
+                  "kernel": "k_e2 (fused elastic step), algorithmic 60 B/cell, launch time = run time / nt"},
+    "acoustic2d": {"name": "acoustic2d_layers_201x301_5m_2000steps", "bpc": 36, "nshots": 1, "nt": 2000,
+                   "kernel": "k_a2 (fused acoustic step), algorithmic 36 B/cell, launch time = run time / nt"},
+    "elastic3d": {"name": "elastic3d_600x600x600_10m_npml23_2500steps", "bpc": 104, "nshots": 1, "nt": 2500,
+                  "kernel": "k3_vel_e + k3_str_e (two fused passes), algorithmic 104 B/cell"},
+    "acoustic3d": {"name": "acoustic3d_600x600x600_10m_npml23_2500steps", "bpc": 48, "nshots": 1, "nt": 2500,
+                   "kernel": "k3_vel_a + k3_str_a (two fused passes), algorithmic 48 B/cell"},
+}
 
 
 def parse():
@@ -44,8 +59,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--nt", type=int, default=4000)
-    ap.add_argument("--nshots", type=int, default=16)
+    ap.add_argument("--workload", default="elastic2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--nt", type=int, default=None)
+    ap.add_argument("--nshots", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -57,20 +73,36 @@ def dist_env():
     return rank, world, local
 
 
-def workload(nt, nshots):
+def workload(kind, nt=None, nshots=None, side=None):
+    """The workload; `side` shrinks a 3-D grid to side^3 (CPU samples)."""
     from geophyinv_gb300 import configs
 
-    return configs.elastic2d_batch(nt=nt, nshots=nshots)
+    kw = {} if nt is None else {"nt": nt}
+    if side and kind.endswith("3d"):
+        kw.update(nz=side, ny=side, nx=side)
+    if kind == "elastic2d":
+        return configs.elastic2d_batch(nshots=nshots or 16, **kw)
+    if kind == "acoustic2d":
+        wl = configs.acoustic2d_layers(**kw)
+    elif kind == "elastic3d":
+        wl = configs.elastic3d(**kw)
+    else:
+        wl = configs.acoustic3d(**kw)
+    if nshots and nshots > 1:
+        wl.shots = wl.shots * nshots
+    return wl
 
 
-def config_json(wl, n_gpus):
-    return {"workload": "elastic2d_psv_1000x3000_5m_16shots_4000steps",
-            "grid": [len(g) for g in wl.grid], "extended_grid": [len(g) + 86 for g in wl.grid],
+def config_json(kind, wl, n_gpus):
+    npml = wl.npml if wl.npml is not None else 43
+    state = {"elastic2d": 5, "acoustic2d": 3, "elastic3d": 9, "acoustic3d": 4}[kind]
+    return {"workload": WORKLOADS[kind]["name"],
+            "grid": [len(g) for g in wl.grid], "extended_grid": [len(g) + 2 * npml for g in wl.grid],
             "shots_per_gpu": len(wl.shots), "nt": wl.nt, "dt": wl.tgrid.step, "order": 4,
             "receivers_per_shot": len(wl.shots[0][1]), "rfields": wl.rfields,
             "parallelism": "shot replicas x%d" % n_gpus,
             "l2": "not flushed: per-step working set %.2f GB >> 129 MB L2" % (
-                2 * 5 * wl.cells() * len(wl.shots) * 4 / 1e9)}
+                2 * state * wl.cells() * len(wl.shots) * 4 / 1e9)}
 
 
 class Clocks:
@@ -136,15 +168,17 @@ def traffic_per_cell():
         return None
 
 
-def cpu_sample(nt_cap=None, target_s=12.0):
+def cpu_sample(kind, nt_cap=None, target_s=12.0):
     """The CPU oracle (all host threads) on one shot of the workload for a
     bounded number of time steps; returns (Gcell-updates/s, threads, sample)."""
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
 
+    side = 160 if kind.endswith("3d") else None  # 3-D: a 160^3 sub-grid (+ CPML) of the 600^3 model
+
     def run(nt):
-        wl = workload(nt, 1)
+        wl = workload(kind, nt, 1, side)
         ex = wl.as_dict()
         prep = O.Prepared(ex, np.float32)
         orc = O.Oracle(prep, nthreads=threads)
@@ -161,7 +195,8 @@ def cpu_sample(nt_cap=None, target_s=12.0):
     nt = int(max(8, min(nt_cap or 400, target_s / max(per_step, 1e-6))))
     cells, t = run(nt)
     rate = cells * nt / t / 1e9
-    return rate, threads, "1 of 16 shots, %d of 4000 steps, %d extended cells, %.1f s" % (nt, cells, t)
+    return rate, threads, "1 of %d shots, %d of %d steps, %d extended cells%s, %.1f s" % (
+        WORKLOADS[kind]["nshots"], nt, WORKLOADS[kind]["nt"], cells, " (160^3 sub-grid)" if side else "", t)
 
 
 def engine_arm(args, rank, world, local):
@@ -176,7 +211,7 @@ def engine_arm(args, rank, world, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    wl = workload(args.nt, args.nshots)
+    wl = workload(args.workload, args.nt, args.nshots)
     pa = wl.expt(stream=stream.cuda_stream)
     medium = wl.medium()
     srcwav = wl.srcwav()
@@ -233,19 +268,20 @@ def engine_arm(args, rank, world, local):
     d2h = sum(pa.data[0][i].d[f].size * 4 for i in range(pa.nss) for f in pa.rfields)
 
     peak, peak_kind = peaks()
-    achieved = BYTES_PER_CELL * cells / (ms * 1e-3 / pa.nt) / 1e9  # per launch, all time charged to it
-    tpc = traffic_per_cell()
+    W = WORKLOADS[args.workload]
+    achieved = W["bpc"] * cells / (ms * 1e-3 / pa.nt) / 1e9  # per launch, all time charged to it
+    tpc = traffic_per_cell() if args.workload == "elastic2d" else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded gradient + smoothed perturbation model)",
-        "config": config_json(wl, world),
+        "config": config_json(args.workload, wl, world),
         "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": None if tpc is None else round(tpc * cells),
-                     "kernel": "k_e2 (fused elastic step), algorithmic 60 B/cell, launch time = run time / nt",
+                     "kernel": W["kernel"],
                      "peak_source": peak_kind + " hbm_gbs"},
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -259,14 +295,14 @@ def reference_arm(args):
     sample = ""
     threads = os.cpu_count() or 1
     for i in range(args.warmup + args.steps):
-        rate, threads, sample = cpu_sample(nt_cap=60, target_s=6.0)
+        rate, threads, sample = cpu_sample(args.workload, nt_cap=60, target_s=6.0)
         if i >= args.warmup:
             rates.append(rate)
     v = float(np.mean(rates))
     return {"metric": METRIC, "value": round(v, 4), "unit": "Gcell/s", "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "elastic2d_psv_1000x3000_5m_16shots_4000steps", "sample": sample},
+            "config": {"workload": WORKLOADS[args.workload]["name"], "sample": sample},
             "cpu_baseline": {"value": round(v, 4), "unit": "Gcell/s", "cores": threads, "kind": "port",
                              "sample": sample + "; C restatement of the reference time loop (Julia is absent)"},
             "e2e": {"value": round(v, 4), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -282,7 +318,7 @@ def main():
     line, dist = engine_arm(args, rank, world, local)
     if rank == 0:
         if not args.no_cpu_baseline:
-            rate, threads, sample = cpu_sample()
+            rate, threads, sample = cpu_sample(args.workload)
             line["cpu_baseline"] = {"value": round(rate, 4), "unit": "Gcell/s", "cores": threads, "kind": "port",
                                     "sample": sample}
         print(json.dumps(line))
