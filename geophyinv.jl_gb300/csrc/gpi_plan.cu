@@ -94,7 +94,8 @@ static void choose_tiling(Plan &p) {
     int per_chunk = p.nzb * p.d.nshots;
     int best = 1;
     double best_eff = 0;
-    for (int m = 1; m <= std::max(1, p.d.nx / 48); m++) {
+    // chunks of at least 16 columns (3 of them recomputed halo)
+    for (int m = 1; m <= std::max(1, p.d.nx / 16); m++) {
       int64_t blocks = (int64_t)m * per_chunk;
       double waves = (double)blocks / resident;
       double eff = waves / std::ceil(waves);
