@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--workload", default="elastic2d", choices=sorted(WORKLOADS))
     ap.add_argument("--nt", type=int, default=None)
     ap.add_argument("--nshots", type=int, default=None)
+    ap.add_argument("--side", type=int, default=None, help="3-D workloads: a side^3 sub-grid (profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -211,7 +212,7 @@ def engine_arm(args, rank, world, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    wl = workload(args.workload, args.nt, args.nshots)
+    wl = workload(args.workload, args.nt, args.nshots, args.side)
     pa = wl.expt(stream=stream.cuda_stream)
     medium = wl.medium()
     srcwav = wl.srcwav()
