@@ -193,7 +193,7 @@ def cpu_sample(kind, nt_cap=None, target_s=12.0):
 
     cells, t = run(4)
     per_step = t / 4
-    nt = int(max(8, min(nt_cap or 400, target_s / max(per_step, 1e-6))))
+    nt = int(max(8, min(nt_cap or WORKLOADS[kind]["nt"], target_s / max(per_step, 1e-6))))
     cells, t = run(nt)
     rate = cells * nt / t / 1e9
     return rate, threads, "1 of %d shots, %d of %d steps, %d extended cells%s, %.1f s" % (
