@@ -108,8 +108,8 @@ static void choose_tiling(Plan &p) {
         best = m;
       }
     }
-    p.xcut.assign(best + 3, 0);
-    p.nxb = make_xcuts(p.d.nx, best, p.xcut.data());
+    p.xcut.assign(best + 6, 0);
+    p.nxb = make_xcuts(p.d.nx, best, p.d.npml, p.d.pml_faces & GPI_XMIN, p.d.pml_faces & GPI_XMAX, p.xcut.data());
     p.xcut.resize(p.nxb + 1);
     p.L = (p.d.nx + best - 1) / best;
   } else {
@@ -712,20 +712,27 @@ static int compile_sources(Plan &p) {
 }
 
 
-int make_xcuts(int nx, int m, int *cuts) {
+int make_xcuts(int nx, int m, int npml, bool xlo, bool xhi, int *cuts) {
   const int E = 8;  // columns of an edge chunk
-  if (nx < 4 * E + m) {
+  // x-strip chunks: [E + 1, npml + 4) and [nx - npml - 5, nx - E), so that
+  // the chunks between them meet no x strip (tile_class)
+  const bool sl = xlo && npml + 4 > E + 1, sh = xhi && nx - npml - 5 < nx - E;
+  const int lo = sl ? npml + 4 : E + 1, hi = sh ? nx - npml - 5 : nx - E;  // interior chunks cover [lo, hi)
+  if (hi - lo < 2 * m || hi - lo < 16) {
     const int L = (nx + m - 1) / m;
     int n = 0;
     for (int x = 1; x <= nx; x += L) cuts[n++] = x;
     cuts[n] = nx + 1;
     return n;
   }
-  const int lo = 1 + E, hi = nx + 1 - E - 1;  // interior chunks cover [lo, hi)
-  cuts[0] = 1;
-  for (int i = 0; i <= m; i++) cuts[1 + i] = lo + (int)((int64_t)(hi - lo) * i / m);
-  cuts[m + 2] = nx + 1;
-  return m + 2;
+  int n = 0;
+  cuts[n++] = 1;
+  if (sl) cuts[n++] = E + 1;
+  for (int i = 0; i < m; i++) cuts[n++] = lo + (int)((int64_t)(hi - lo) * i / m);
+  cuts[n++] = hi;
+  if (sh) cuts[n++] = nx - E;
+  cuts[n] = nx + 1;
+  return n;
 }
 
 // Tile classes of the 2-D step kernels (src/fdtd/cpml.jl:184-211 and
