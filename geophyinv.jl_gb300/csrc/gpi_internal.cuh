@@ -201,7 +201,8 @@ int step_a2_wavefield(Plan *p, int ipw, int vonly);
 // host: x partition of a 2-D grid of nx columns into m interior chunks
 // plus, when the grid is wide enough, one narrow chunk at each x edge (the
 // mirror columns there need the general code) and one chunk over each x
-// CPML strip; writes nchunks + 1 cut columns (at most m + 5), returns nchunks
+// CPML strip (split to the interior chunk width); writes nchunks + 1 cut
+// columns (at most m + 2 npml + 8), returns nchunks
 int make_xcuts(int nx, int m, int npml, bool xlo, bool xhi, int *cuts);
 // host: classify the (z-block, x-chunk, shot) tiles of a 2-D plan and write
 // them grouped by class (0 interior, 1 band, 2 x-band, 3 edge, in that

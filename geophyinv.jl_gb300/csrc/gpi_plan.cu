@@ -88,9 +88,9 @@ static void choose_tiling(Plan &p) {
     p.TY = 1;
     p.nzb = (p.d.nz + p.TZ - 1) / p.TZ;
     p.nyb = 1;
-    // blocks resident at once (128 threads; shared memory: acoustic 33 KB,
-    // elastic 49 KB per block)
-    int resident = sms * (p.d.physics == GPI_ACOUSTIC ? 6 : 4);
+    // interior blocks resident at once (128 threads; shared memory:
+    // acoustic 33 KB, elastic 37 KB per block)
+    int resident = sms * 6;
     int per_chunk = p.nzb * p.d.nshots;
     int best = 1;
     double best_eff = 0;
@@ -108,7 +108,7 @@ static void choose_tiling(Plan &p) {
         best = m;
       }
     }
-    p.xcut.assign(best + 6, 0);
+    p.xcut.assign(best + 2 * p.d.npml + 8, 0);
     p.nxb = make_xcuts(p.d.nx, best, p.d.npml, p.d.pml_faces & GPI_XMIN, p.d.pml_faces & GPI_XMAX, p.xcut.data());
     p.xcut.resize(p.nxb + 1);
     p.L = (p.d.nx + best - 1) / best;
@@ -725,12 +725,20 @@ int make_xcuts(int nx, int m, int npml, bool xlo, bool xhi, int *cuts) {
     cuts[n] = nx + 1;
     return n;
   }
+  // strip chunks no wider than the interior chunks (short column sweeps on
+  // small grids)
+  const int L = (hi - lo + m - 1) / m;
+  auto split = [&](int a, int b, int *out) -> int {
+    const int k = (b - a + L - 1) / L;
+    for (int i = 0; i < k; i++) out[i] = a + (int)((int64_t)(b - a) * i / k);
+    return k;
+  };
   int n = 0;
   cuts[n++] = 1;
-  if (sl) cuts[n++] = E + 1;
+  if (sl) n += split(E + 1, lo, cuts + n);
   for (int i = 0; i < m; i++) cuts[n++] = lo + (int)((int64_t)(hi - lo) * i / m);
-  cuts[n++] = hi;
-  if (sh) cuts[n++] = nx - E;
+  if (sh) n += split(hi, nx - E, cuts + n);
+  cuts[n++] = nx - E;  // the right edge chunk (hi itself without a right strip)
   cuts[n] = nx + 1;
   return n;
 }

@@ -48,12 +48,15 @@ struct A2Args {
   int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
+// slots of the shared-memory column ring: 4 columns in use by the stencils
+// plus 4 in flight (deep prefetch for the latency-bound small grids)
+constexpr int RING = 8;
 constexpr int A2_TZ = TZ2;                             // pressure rows per block
 constexpr int A2_THREADS = 128;                        // TZ + 3 velocity rows, one per thread
 constexpr int A2_R8 = A2_TZ + 8;                       // p rows z0-4 .. z0+TZ+3
 constexpr int A2_R4 = A2_TZ + 4;                       // velocity-input rows z0 .. z0+TZ+3
 constexpr int A2_SLOT = A2_R8 + 4 * A2_R4 + A2_TZ;     // floats per ring slot
-constexpr size_t A2_SMEM = 128 + sizeof(float) * (8 * A2_SLOT + 2 * 8 * A2_R4);
+constexpr size_t A2_SMEM = 128 + sizeof(float) * (RING * A2_SLOT + 2 * RING * A2_R4);
 
 // CPML floats per ring slot of the general kernel: two z-strip windows
 // (dpdz, dvzdz) and the x-strip columns of dpdx and dvxdx
@@ -61,7 +64,7 @@ inline int a2_psi_floats(const Plan &p) {
   const bool zf = p.d.pml_faces & (GPI_ZMIN | GPI_ZMAX), xf = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
   return (zf ? 2 * p.pzw : 0) + (xf ? 2 * A2_TZ : 0);
 }
-inline size_t a2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (A2_SLOT + psf) + 2 * 8 * A2_R4); }
+inline size_t a2_smem_general(int psf) { return 128 + sizeof(float) * (RING * (A2_SLOT + psf) + 2 * RING * A2_R4); }
 
 // MODE 0: interior tiles (no CPML, face or source: straight-line code);
 // MODE 1: tiles away from the x edges and x strips (the band code over every
@@ -69,15 +72,15 @@ inline size_t a2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (A2_S
 // columns; MODE 3: tiles with x-edge columns (the band code plus the general
 // code for the edge and source columns).
 template <int MODE>
-__global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Args a) {
+__global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4) k_a2(const A2Args a) {
   constexpr bool FAST = MODE == 0, XPSI = MODE >= 2;
   constexpr int TZ = A2_TZ, R8 = A2_R8, R4 = A2_R4, SLOT = A2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-  float *ring = reinterpret_cast<float *>(smem + 128);  // [8][SLOT]: p | vx vz cx cz | dtK
+  float *ring = reinterpret_cast<float *>(smem + 128);  // [RING][SLOT]: p | vx vz cx cz | dtK
   const int SL = FAST ? SLOT : SLOT + a.psf;            // floats per ring slot
-  float *svx = ring + 8 * SL;                            // [8][R4] new velocities
-  float *svz = svx + 8 * R4;
+  float *svx = ring + RING * SL;                         // [RING][R4] new velocities
+  float *svz = svx + RING * R4;
   __shared__ int s_rng[3][2];
   __shared__ int s_err;
   const int t = threadIdx.x;
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
   auto ZS = [&](int cc, int j) -> int64_t { return (int64_t)(cc + XOFF - 1) * a.zsw + j; };
   auto psA = [&](int i) -> const float * { return a.psA[i] + shot * a.pss[i]; };
   auto psB = [&](int i) -> float * { return a.psB[i] + shot * a.pss[i]; };
-  auto slot = [&](int cc) -> int { return (cc - xbase) & 7; };
+  auto slot = [&](int cc) -> int { return (cc - xbase) % RING; };
   // General kernel: the CPML memory of each column travels in its ring slot
   // (z-strip windows of dpdz and dvzdz, x-strip columns of dpdx and dvxdx).
   const int zt = FAST ? 0 : zstrip_touch(z0, TZ, nz, npml, zlo, zhi);
@@ -111,7 +114,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
   auto PXs = [&](int i, int s) -> const float * { return ring + s * SL + SLOT + 2 * PZW + i * TZ - z0; };
 
   if (t == 0) {
-    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 4);  // one arrival per warp
+    for (int s = 0; s < RING; s++) mbar_init(&bar[s], 4);  // one arrival per warp
     mbar_fence_init();
     s_err = 0;
   }
@@ -164,10 +167,10 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
       }
     }
   };
-  if (issuer) issue(xbase + 7);
+  if (issuer) issue(xbase + RING - 1);
   auto wait_col = [&](int cc) {
     const int j = cc - xbase;
-    if (!mbar_wait(&bar[j & 7], (j >> 3) & 1)) s_err = 1;
+    if (!mbar_wait(&bar[j % RING], (j / RING) & 1)) s_err = 1;
   };
 
   InjCursor cvx, cvz, cst;
@@ -256,15 +259,15 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
       const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
       a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
     };
-    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
+    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
     const int ncol = x1 - xbase;
     for (int it = 0; it < ncol; it++) {
       const int c = xbase + it;
-      if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-      vel_fast(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+      if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
+      vel_fast(c + 3, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
       __syncthreads();
-      if (issuer) issue(c + 7);
-      if (c >= x0) str_fast(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+      if (issuer) issue(c + RING - 1);
+      if (c >= x0) str_fast(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
     }
   } else {
   // columns that need the full general code: x edges and mirrors, sources
@@ -356,7 +359,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
       if (srow) a.pB[so + S(r, c)] = pn;
     };
     if constexpr (MODE == 1 || MODE == 2) {
-      // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
+      // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
       const int ncol = x1 - xbase;
       for (int it = 0; it < ncol; it++) {
         const int c = xbase + it, cc = c + 3;
@@ -364,11 +367,11 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
         cvx.range(a.cells, cc, ib0, ie0);
         cvz.range(a.cells, cc, ib1, ie1);
         if (c >= x0) cst.range(a.cells, c, bs, es);
-        if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-        vel_band(cc, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, ib0, ie0, ib1, ie1);
+        if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
+        vel_band(cc, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, ib0, ie0, ib1, ie1);
         __syncthreads();
-        if (issuer) issue(c + 7);
-        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, bs, es);
+        if (issuer) issue(c + RING - 1);
+        if (c >= x0) str_band(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, bs, es);
       }
     } else {
       float vpre = 0.f;  // vx[r, nx] before its source (xmax mirror)
@@ -458,7 +461,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
         else
           vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc), ib0, ie0, ib1, ie1);
         __syncthreads();
-        if (issuer) issue(c + 7);
+        if (issuer) issue(c + RING - 1);
         if (c >= x0) {
           if (gs)
             str_edge(c, bs, es);
@@ -471,9 +474,9 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : 4) k_a2(const A2Ar
   }
   __syncthreads();
   if (s_err && t == 0) {
-    for (int cc = max(xbase, xlast - 7); cc <= xlast; cc++) {
+    for (int cc = max(xbase, xlast - (RING - 1)); cc <= xlast; cc++) {
       const int j = cc - xbase;
-      mbar_wait(&bar[j & 7], (j >> 3) & 1);
+      mbar_wait(&bar[j % RING], (j / RING) & 1);
     }
     atomicExch(a.err, 1);
   }

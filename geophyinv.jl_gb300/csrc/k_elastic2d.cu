@@ -50,12 +50,15 @@ struct E2Args {
   int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
 };
 
+// slots of the shared-memory column ring: 4 columns in use by the stencils
+// plus 2 in flight; 6 keeps an interior block at 37 KB (6 blocks per SM)
+constexpr int RING = 6;
 constexpr int E2_TZ = TZ2;                                      // stress rows per block
 constexpr int E2_THREADS = 128;                                 // TZ + 3 velocity rows, one per thread
 constexpr int E2_R8 = E2_TZ + 8;                                // stress rows z0-4 .. z0+TZ+3
 constexpr int E2_R4 = E2_TZ + 4;                                // velocity-input rows z0 .. z0+TZ+3
 constexpr int E2_SLOT = 3 * E2_R8 + 4 * E2_R4 + 3 * E2_TZ;      // floats per ring slot
-constexpr size_t E2_SMEM = 128 + sizeof(float) * (8 * E2_SLOT + 2 * 8 * E2_R4);
+constexpr size_t E2_SMEM = 128 + sizeof(float) * (RING * E2_SLOT + 2 * RING * E2_R4);
 
 // CPML floats per ring slot of the general kernel: four z-strip windows
 // (derivatives 2, 3, 5, 6) and the x-strip columns of derivatives 0, 1
@@ -64,7 +67,7 @@ inline int e2_psi_floats(const Plan &p) {
   const bool zf = p.d.pml_faces & (GPI_ZMIN | GPI_ZMAX), xf = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
   return (zf ? 4 * p.pzw : 0) + (xf ? 2 * E2_R4 + 2 * E2_TZ : 0);
 }
-inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (E2_SLOT + psf) + 2 * 8 * E2_R4); }
+inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (RING * (E2_SLOT + psf) + 2 * RING * E2_R4); }
 
 // MODE 0: interior tiles (no CPML, face or source: straight-line code);
 // MODE 1: tiles away from the x edges and x strips (the band code over every
@@ -72,15 +75,15 @@ inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (8 * (E2_S
 // with x-strip columns; MODE 3: tiles with x-edge columns (the band code plus
 // the general code for the edge and source columns).
 template <int MODE>
-__global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Args a) {
+__global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : MODE == 2 ? 4 : 3) k_e2(const E2Args a) {
   constexpr bool FAST = MODE == 0, XPSI = MODE >= 2;
   constexpr int TZ = E2_TZ, R8 = E2_R8, R4 = E2_R4, SLOT = E2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // one mbarrier per ring slot
-  float *ring = reinterpret_cast<float *>(smem + 128);  // [8][SLOT]
+  float *ring = reinterpret_cast<float *>(smem + 128);  // [RING][SLOT]
   const int SL = FAST ? SLOT : SLOT + a.psf;            // floats per ring slot
-  float *svx = ring + 8 * SL;                            // [8][R4] new velocities
-  float *svz = svx + 8 * R4;
+  float *svx = ring + RING * SL;                         // [RING][R4] new velocities
+  float *svz = svx + RING * R4;
   __shared__ int s_rng[3][2];
   __shared__ int s_err;
   const int t = threadIdx.x;
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
   const int zoff = FAST ? 0 : zstrip_off(zt, a.zsw, a.pzw);
   const int PZW = FAST ? 0 : a.pzw;
   // ring views of input column cc
-  auto slot = [&](int cc) -> int { return (cc - xbase) & 7; };
+  auto slot = [&](int cc) -> int { return (cc - xbase) % RING; };
   auto T = [&](int f, int cc) -> const float * { return ring + slot(cc) * SL + f * R8; };           // txx tzz txz
   auto V = [&](int f, int cc) -> const float * { return ring + slot(cc) * SL + 3 * R8 + f * R4; };  // vx vz cx cz
   auto C = [&](int f, int cc) -> const float * {
@@ -127,7 +130,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
   };
 
   if (t == 0) {
-    for (int s = 0; s < 8; s++) mbar_init(&bar[s], 4);  // one arrival per warp
+    for (int s = 0; s < RING; s++) mbar_init(&bar[s], 4);  // one arrival per warp
     mbar_fence_init();
     s_err = 0;
   }
@@ -199,10 +202,10 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
       }
     }
   };
-  if (issuer) issue(xbase + 7);
+  if (issuer) issue(xbase + RING - 1);
   auto wait_col = [&](int cc) {
     const int j = cc - xbase;
-    if (!mbar_wait(&bar[j & 7], (j >> 3) & 1)) s_err = 1;
+    if (!mbar_wait(&bar[j % RING], (j / RING) & 1)) s_err = 1;
   };
 
   InjCursor cvx, cvz, cst;
@@ -341,15 +344,15 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
       a.tzzB[o] = tzz;
       a.txzB[o] = txz;
     };
-    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
+    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
     const int ncol = x1 - xbase;
     for (int it = 0; it < ncol; it++) {
       const int c = xbase + it;
-      if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-      vel_fast(c + 3, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+      if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
+      vel_fast(c + 3, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
       __syncthreads();
-      if (issuer) issue(c + 7);
-      if (c >= x0) str_fast(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7);
+      if (issuer) issue(c + RING - 1);
+      if (c >= x0) str_fast(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
     }
   } else {
   // columns that need the full general code: x edges and mirrors, sources
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
       }
     };
     if constexpr (MODE == 1 || MODE == 2) {
-      // iteration it handles column c = xbase + it: slot(c + m) = (it + m) & 7
+      // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
       const int ncol = x1 - xbase;
       for (int it = 0; it < ncol; it++) {
         const int c = xbase + it, cc = c + 3;
@@ -475,11 +478,11 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
         cvx.range(a.cells, cc, ib0, ie0);
         cvz.range(a.cells, cc, ib1, ie1);
         if (c >= x0) cst.range(a.cells, c, bs, es);
-        if (!mbar_wait(&bar[(it + 3) & 7], ((it + 3) >> 3) & 1)) s_err = 1;
-        vel_band(cc, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, ib0, ie0, ib1, ie1);
+        if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
+        vel_band(cc, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, ib0, ie0, ib1, ie1);
         __syncthreads();
-        if (issuer) issue(c + 7);
-        if (c >= x0) str_band(c, it & 7, (it + 1) & 7, (it + 2) & 7, (it + 3) & 7, bs, es);
+        if (issuer) issue(c + RING - 1);
+        if (c >= x0) str_band(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, bs, es);
       }
     } else {
       // velocities of column cc: update_v! with CPML, mirrors, sources
@@ -600,7 +603,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
         else
           vel_band(cc, slot(cc - 3), slot(cc - 2), slot(cc - 1), slot(cc), ib0, ie0, ib1, ie1);
         __syncthreads();
-        if (issuer) issue(c + 7);
+        if (issuer) issue(c + RING - 1);
         if (c >= x0) {
           if (gs)
             str_edge(c, bs, es);
@@ -615,9 +618,9 @@ __global__ void __launch_bounds__(E2_THREADS, MODE <= 1 ? 4 : 3) k_e2(const E2Ar
   if (s_err && t == 0) {
     // a wait gave up: let the copies still in flight land before the block's
     // shared memory is released, then report
-    for (int cc = max(xbase, xlast - 7); cc <= xlast; cc++) {
+    for (int cc = max(xbase, xlast - (RING - 1)); cc <= xlast; cc++) {
       const int j = cc - xbase;
-      mbar_wait(&bar[j & 7], (j >> 3) & 1);
+      mbar_wait(&bar[j % RING], (j / RING) & 1);
     }
     atomicExch(a.err, 1);
   }

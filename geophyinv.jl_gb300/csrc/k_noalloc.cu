@@ -117,7 +117,7 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
   P.L = 128;
   {
     const int m = std::max(1, (d.nx - 16 + P.L - 1) / P.L);
-    if (m + 6 > kMaxCuts) return nfail(GPI_E_INVALID, "grid too large for the no-alloc tile table");
+    if (m + 2 * d.npml + 8 > kMaxCuts) return nfail(GPI_E_INVALID, "grid too large for the no-alloc tile table");
     P.nxb = make_xcuts(d.nx, m, d.npml, d.pml_faces & GPI_XMIN, d.pml_faces & GPI_XMAX, h_xcut);
   }
   P.nyb = 1;
