@@ -75,12 +75,12 @@ struct Cell3 {
   int r, y, c, shot;
   bool ok;
 };
-__device__ __forceinline__ Cell3 cell3(const G3 &g, int shot0, int nshots) {
+__device__ __forceinline__ Cell3 cell3(const G3 &g, int shot0, int nshots, int base = 1) {
   Cell3 e;
-  e.r = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  e.y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int nc = g.nx + 3;
-  e.c = (int)(blockIdx.z % nc) + 1;
+  e.r = blockIdx.x * blockDim.x + threadIdx.x + base;
+  e.y = blockIdx.y * blockDim.y + threadIdx.y + base;
+  const int nc = g.nx + 4 - base;
+  e.c = (int)(blockIdx.z % nc) + base;
   e.shot = (int)(blockIdx.z / nc);
   e.ok = e.r <= g.nz + 3 && e.y <= g.ny + 3 && e.shot < nshots;
   e.shot += shot0;
@@ -147,105 +147,101 @@ __global__ void __launch_bounds__(256) k3_str_a(const Step3 a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k3_vel_e(const Step3 a) {
   const G3 &g = a.g;
-  const Cell3 e = cell3(g, a.shot0, a.nshots);
+  const Cell3 e = cell3(g, a.shot0, a.nshots, 4);
   if (!e.ok) return;
   const int r = e.r, y = e.y, c = e.c, nz = g.nz, ny = g.ny, nx = g.nx;
-  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c);
+  if (r > nz || y > ny || c > nx) return;
+  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c), oc = o - so;
   const int64_t sx = (int64_t)g.NYP * g.NZP, sy = g.NZP;
   const float *txx = a.f[GPI_TAUXX] + so, *tyy = a.f[GPI_TAUYY] + so, *tzz = a.f[GPI_TAUZZ] + so;
   const float *txy = a.f[GPI_TAUXY] + so, *txz = a.f[GPI_TAUXZ] + so, *tyz = a.f[GPI_TAUYZ] + so;
   const int iz = r - 3, iy = y - 3, ix = c - 3;  // derivative index of the @inn velocity cell
+  // every stencil read first (all in the padded storage for r, y, c >= 4),
+  // so that the loads of the three components are in flight together
+  const int64_t bx = g.S(r, y, c - 3), bi = g.S(iz, iy, ix), by = g.S(r, iy, c), bz = g.S(iz, y, c);
+  float D0 = st4(txx[bx], txx[bx + sx], txx[bx + 2 * sx], txx[bx + 3 * sx]) * a.dxI;  // @d_xi(tauxx)
+  float D4 = st4(txy[bi], txy[bi + sy], txy[bi + 2 * sy], txy[bi + 3 * sy]) * a.dyI;  // @d_ya(tauxy)
+  float D8 = st4(txz[bi], txz[bi + 1], txz[bi + 2], txz[bi + 3]) * a.dzI;              // @d_za(tauxz)
+  float D1 = st4(txy[bi], txy[bi + sx], txy[bi + 2 * sx], txy[bi + 3 * sx]) * a.dxI;  // @d_xa(tauxy)
+  float D3 = st4(tyy[by], tyy[by + sy], tyy[by + 2 * sy], tyy[by + 3 * sy]) * a.dyI;  // @d_yi(tauyy)
+  float D7 = st4(tyz[bi], tyz[bi + 1], tyz[bi + 2], tyz[bi + 3]) * a.dzI;              // @d_za(tauyz)
+  float D2 = st4(txz[bi], txz[bi + sx], txz[bi + 2 * sx], txz[bi + 3 * sx]) * a.dxI;  // @d_xa(tauxz)
+  float D5 = st4(tyz[bi], tyz[bi + sy], tyz[bi + 2 * sy], tyz[bi + 3 * sy]) * a.dyI;  // @d_ya(tauyz)
+  float D6 = st4(tzz[bz], tzz[bz + 1], tzz[bz + 2], tzz[bz + 3]) * a.dzI;              // @d_zi(tauzz)
+  const float cx = a.cf[0][oc], cy = a.cf[1][oc], cz = a.cf[2][oc];
+  float *vx = a.f[GPI_VX] + o, *vy = a.f[GPI_VY] + o, *vz = a.f[GPI_VZ] + o;
+  const float vx0 = *vx, vy0 = *vy, vz0 = *vz;
   // vx: @inn(vx) -= dtinvavxirho (dtauxxdx + dtauxydy + dtauxzdz), (nz-2h, ny-2h, nx-h)
-  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx) {
-    int64_t b = g.S(r, y, c - 3);  // @d_xi(tauxx)
-    float D0 = st4(txx[b], txx[b + sx], txx[b + 2 * sx], txx[b + 3 * sx]) * a.dxI;
+  if (r <= nz - 3 && y <= ny - 3) {
     D0 = mem3(D0, g, a.m, e.shot, 0, 2, ix, nx - 3, iz, iy, ix);
-    b = g.S(iz, iy, ix);  // @d_ya(tauxy)
-    float D4 = st4(txy[b], txy[b + sy], txy[b + 2 * sy], txy[b + 3 * sy]) * a.dyI;
     D4 = mem3(D4, g, a.m, e.shot, 4, 1, iy, ny - 6, iz, iy, ix);
-    float D8 = st4(txz[b], txz[b + 1], txz[b + 2], txz[b + 3]) * a.dzI;  // @d_za(tauxz)
     D8 = mem3(D8, g, a.m, e.shot, 8, 0, iz, nz - 6, iz, iy, ix);
-    a.f[GPI_VX][o] = a.f[GPI_VX][o] - a.cf[0][o - so] * (D0 + D4 + D8);
+    *vx = vx0 - cx * (D0 + D4 + D8);
   }
   // vy: @inn(vy) -= dtinvavyirho (dtauxydx + dtauyydy + dtauyzdz), (nz-2h, ny-h, nx-2h)
-  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny && c >= 4 && c <= nx - 3) {
-    int64_t b = g.S(iz, iy, ix);  // @d_xa(tauxy)
-    float D1 = st4(txy[b], txy[b + sx], txy[b + 2 * sx], txy[b + 3 * sx]) * a.dxI;
+  if (r <= nz - 3 && c <= nx - 3) {
     D1 = mem3(D1, g, a.m, e.shot, 1, 2, ix, nx - 6, iz, iy, ix);
-    b = g.S(r, iy, c);  // @d_yi(tauyy)
-    float D3 = st4(tyy[b], tyy[b + sy], tyy[b + 2 * sy], tyy[b + 3 * sy]) * a.dyI;
     D3 = mem3(D3, g, a.m, e.shot, 3, 1, iy, ny - 3, iz, iy, ix);
-    b = g.S(iz, iy, ix);  // @d_za(tauyz)
-    float D7 = st4(tyz[b], tyz[b + 1], tyz[b + 2], tyz[b + 3]) * a.dzI;
     D7 = mem3(D7, g, a.m, e.shot, 7, 0, iz, nz - 6, iz, iy, ix);
-    a.f[GPI_VY][o] = a.f[GPI_VY][o] - a.cf[1][o - so] * (D1 + D3 + D7);
+    *vy = vy0 - cy * (D1 + D3 + D7);
   }
   // vz: @inn(vz) -= dtinvavzirho (dtauxzdx + dtauyzdy + dtauzzdz), (nz-h, ny-2h, nx-2h)
-  if (r >= 4 && r <= nz && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx - 3) {
-    int64_t b = g.S(iz, iy, ix);  // @d_xa(tauxz)
-    float D2 = st4(txz[b], txz[b + sx], txz[b + 2 * sx], txz[b + 3 * sx]) * a.dxI;
+  if (y <= ny - 3 && c <= nx - 3) {
     D2 = mem3(D2, g, a.m, e.shot, 2, 2, ix, nx - 6, iz, iy, ix);
-    float D5 = st4(tyz[b], tyz[b + sy], tyz[b + 2 * sy], tyz[b + 3 * sy]) * a.dyI;  // @d_ya(tauyz)
     D5 = mem3(D5, g, a.m, e.shot, 5, 1, iy, ny - 6, iz, iy, ix);
-    b = g.S(iz, y, c);  // @d_zi(tauzz)
-    float D6 = st4(tzz[b], tzz[b + 1], tzz[b + 2], tzz[b + 3]) * a.dzI;
     D6 = mem3(D6, g, a.m, e.shot, 6, 0, iz, nz - 3, iz, iy, ix);
-    a.f[GPI_VZ][o] = a.f[GPI_VZ][o] - a.cf[2][o - so] * (D2 + D5 + D6);
+    *vz = vz0 - cz * (D2 + D5 + D6);
   }
 }
 
 __global__ void __launch_bounds__(256) k3_str_e(const Step3 a) {
   const G3 &g = a.g;
-  const Cell3 e = cell3(g, a.shot0, a.nshots);
+  const Cell3 e = cell3(g, a.shot0, a.nshots, 1);
   if (!e.ok) return;
   const int r = e.r, y = e.y, c = e.c, nz = g.nz, ny = g.ny, nx = g.nx;
+  if (r > nz || y > ny || c > nx) return;
   const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c), oc = o - so;
   const int64_t sx = (int64_t)g.NYP * g.NZP, sy = g.NZP;
   const float *vx = a.f[GPI_VX] + so, *vy = a.f[GPI_VY] + so, *vz = a.f[GPI_VZ] + so;
+  // every stencil read first (in the padded storage for r, y, c <= n)
+  const int64_t b = g.S(r, y, c), bxy = g.S(r + 3, y, c + 3), bxz = g.S(r, y + 3, c + 3), byx = g.S(r + 3, y + 3, c);
+  float D9 = st4(vx[b], vx[b + sx], vx[b + 2 * sx], vx[b + 3 * sx]) * a.dxI;            // @d_xa(vx)
+  float D10 = st4(vy[b], vy[b + sy], vy[b + 2 * sy], vy[b + 3 * sy]) * a.dyI;           // @d_ya(vy)
+  float D11 = st4(vz[b], vz[b + 1], vz[b + 2], vz[b + 3]) * a.dzI;                      // @d_za(vz)
+  float D12 = st4(vx[bxy], vx[bxy + sy], vx[bxy + 2 * sy], vx[bxy + 3 * sy]) * a.dyI;   // @d_yi(vx)
+  float D14 = st4(vy[byx], vy[byx + sx], vy[byx + 2 * sx], vy[byx + 3 * sx]) * a.dxI;   // @d_xi(vy)
+  float D13 = st4(vx[bxz], vx[bxz + 1], vx[bxz + 2], vx[bxz + 3]) * a.dzI;              // @d_zi(vx)
+  float D16 = st4(vz[byx], vz[byx + sx], vz[byx + 2 * sx], vz[byx + 3 * sx]) * a.dxI;   // @d_xi(vz)
+  float D15 = st4(vy[bxz], vy[bxz + 1], vy[bxz + 2], vy[bxz + 3]) * a.dzI;              // @d_zi(vy)
+  float D17 = st4(vz[bxy], vz[bxy + sy], vz[bxy + 2 * sy], vz[bxy + 3 * sy]) * a.dyI;   // @d_yi(vz)
+  const float M = a.cf[6][oc], L = a.cf[7][oc], mxz = a.cf[3][oc], mxy = a.cf[4][oc], myz = a.cf[5][oc];
+  float *txx = a.f[GPI_TAUXX] + o, *tyy = a.f[GPI_TAUYY] + o, *tzz = a.f[GPI_TAUZZ] + o;
+  float *txy = a.f[GPI_TAUXY] + o, *txz = a.f[GPI_TAUXZ] + o, *tyz = a.f[GPI_TAUYZ] + o;
+  const float txx0 = *txx, tyy0 = *tyy, tzz0 = *tzz, txy0 = *txy, txz0 = *txz, tyz0 = *tyz;
   // compute_stressii!: full grid
-  if (r <= nz && y <= ny && c <= nx) {
-    const int64_t b = g.S(r, y, c);
-    float D9 = st4(vx[b], vx[b + sx], vx[b + 2 * sx], vx[b + 3 * sx]) * a.dxI;  // @d_xa(vx)
-    D9 = mem3(D9, g, a.m, e.shot, 9, 2, c, nx, r, y, c);
-    float D10 = st4(vy[b], vy[b + sy], vy[b + 2 * sy], vy[b + 3 * sy]) * a.dyI;  // @d_ya(vy)
-    D10 = mem3(D10, g, a.m, e.shot, 10, 1, y, ny, r, y, c);
-    float D11 = st4(vz[b], vz[b + 1], vz[b + 2], vz[b + 3]) * a.dzI;  // @d_za(vz)
-    D11 = mem3(D11, g, a.m, e.shot, 11, 0, r, nz, r, y, c);
-    const float M = a.cf[6][oc], L = a.cf[7][oc];
-    float *txx = a.f[GPI_TAUXX] + o, *tyy = a.f[GPI_TAUYY] + o, *tzz = a.f[GPI_TAUZZ] + o;
-    *txx = *txx - (M * D9) - (L * (D10 + D11));
-    *tyy = *tyy - (M * D10) - (L * (D9 + D11));
-    *tzz = *tzz - (M * D11) - (L * (D10 + D9));
-  }
+  D9 = mem3(D9, g, a.m, e.shot, 9, 2, c, nx, r, y, c);
+  D10 = mem3(D10, g, a.m, e.shot, 10, 1, y, ny, r, y, c);
+  D11 = mem3(D11, g, a.m, e.shot, 11, 0, r, nz, r, y, c);
+  *txx = txx0 - (M * D9) - (L * (D10 + D11));
+  *tyy = tyy0 - (M * D10) - (L * (D9 + D11));
+  *tzz = tzz0 - (M * D11) - (L * (D10 + D9));
   // tauxy (nz-2h, ny-h, nx-h): -= dtavxyimu (dvxdy + dvydx)
   if (r <= nz - 6 && y <= ny - 3 && c <= nx - 3) {
-    int64_t b = g.S(r + 3, y, c + 3);  // @d_yi(vx)
-    float D12 = st4(vx[b], vx[b + sy], vx[b + 2 * sy], vx[b + 3 * sy]) * a.dyI;
     D12 = mem3(D12, g, a.m, e.shot, 12, 1, y, ny - 3, r, y, c);
-    b = g.S(r + 3, y + 3, c);  // @d_xi(vy)
-    float D14 = st4(vy[b], vy[b + sx], vy[b + 2 * sx], vy[b + 3 * sx]) * a.dxI;
     D14 = mem3(D14, g, a.m, e.shot, 14, 2, c, nx - 3, r, y, c);
-    a.f[GPI_TAUXY][o] = a.f[GPI_TAUXY][o] - a.cf[4][oc] * (D12 + D14);
+    *txy = txy0 - mxy * (D12 + D14);
   }
   // tauxz (nz-h, ny-2h, nx-h): -= dtavxzimu (dvxdz + dvzdx)
   if (r <= nz - 3 && y <= ny - 6 && c <= nx - 3) {
-    int64_t b = g.S(r, y + 3, c + 3);  // @d_zi(vx)
-    float D13 = st4(vx[b], vx[b + 1], vx[b + 2], vx[b + 3]) * a.dzI;
     D13 = mem3(D13, g, a.m, e.shot, 13, 0, r, nz - 3, r, y, c);
-    b = g.S(r + 3, y + 3, c);  // @d_xi(vz)
-    float D16 = st4(vz[b], vz[b + sx], vz[b + 2 * sx], vz[b + 3 * sx]) * a.dxI;
     D16 = mem3(D16, g, a.m, e.shot, 16, 2, c, nx - 3, r, y, c);
-    a.f[GPI_TAUXZ][o] = a.f[GPI_TAUXZ][o] - a.cf[3][oc] * (D13 + D16);
+    *txz = txz0 - mxz * (D13 + D16);
   }
   // tauyz (nz-h, ny-h, nx-2h): -= dtavyzimu (dvydz + dvzdy)
   if (r <= nz - 3 && y <= ny - 3 && c <= nx - 6) {
-    int64_t b = g.S(r, y + 3, c + 3);  // @d_zi(vy)
-    float D15 = st4(vy[b], vy[b + 1], vy[b + 2], vy[b + 3]) * a.dzI;
     D15 = mem3(D15, g, a.m, e.shot, 15, 0, r, nz - 3, r, y, c);
-    b = g.S(r + 3, y, c + 3);  // @d_yi(vz)
-    float D17 = st4(vz[b], vz[b + sy], vz[b + 2 * sy], vz[b + 3 * sy]) * a.dyI;
     D17 = mem3(D17, g, a.m, e.shot, 17, 1, y, ny - 3, r, y, c);
-    a.f[GPI_TAUYZ][o] = a.f[GPI_TAUYZ][o] - a.cf[5][oc] * (D15 + D17);
+    *tyz = tyz0 - myz * (D15 + D17);
   }
 }
 
@@ -340,16 +336,19 @@ static int step3(Plan *p, int vonly) {
   a.dzI = (float)(1.0 / (p->d.dz * 24.0));
   a.dyI = (float)(1.0 / (p->d.dy * 24.0));
   a.dxI = (float)(1.0 / (p->d.dx * 24.0));
-  const int nc = p->d.nx + 3;
-  if (nc > 65535) return fail(p, GPI_E_UNSUPPORTED, "3-D grids are limited to 65532 columns");
-  const int chunk = 65535 / nc;  // shots per launch (grid z = columns x shots)
+  if (p->d.nx + 3 > 65535) return fail(p, GPI_E_UNSUPPORTED, "3-D grids are limited to 65532 columns");
   const dim3 blk(32, 8);
+  // the elastic velocity pass covers cells from (4, 4, 4) (its update
+  // domains), every other pass from (1, 1, 1)
   auto pass = [&](bool vel) {
+    const int base = (vel && !ac) ? 4 : 1;
+    const int nc = p->d.nx + 4 - base;
+    const int chunk = 65535 / nc;  // shots per launch (grid z = columns x shots)
     for (int s0 = 0; s0 < p->d.nshots; s0 += chunk) {
       Step3 b = a;
       b.shot0 = s0;
       b.nshots = std::min(chunk, p->d.nshots - s0);
-      const dim3 grd((p->d.nz + 3 + 31) / 32, (p->d.ny + 3 + 7) / 8, nc * b.nshots);
+      const dim3 grd((p->d.nz + 4 - base + 31) / 32, (p->d.ny + 4 - base + 7) / 8, nc * b.nshots);
       if (vel) {
         if (ac)
           k3_vel_a<<<grd, blk, 0, p->stream>>>(b);
