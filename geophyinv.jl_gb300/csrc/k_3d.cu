@@ -92,32 +92,35 @@ __device__ __forceinline__ Cell3 cell3(const G3 &g, int shot0, int nshots, int b
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k3_vel_a(const Step3 a) {
   const G3 &g = a.g;
-  const Cell3 e = cell3(g, a.shot0, a.nshots);
+  const Cell3 e = cell3(g, a.shot0, a.nshots, 4);
   if (!e.ok) return;
   const int r = e.r, y = e.y, c = e.c, nz = g.nz, ny = g.ny, nx = g.nx;
-  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c);
+  if (r > nz || y > ny || c > nx) return;
+  const int64_t so = e.shot * g.fs, o = so + g.S(r, y, c), oc = o - so;
   const float *p = a.f[GPI_P] + so;
   const int64_t sx = (int64_t)g.NYP * g.NZP, sy = g.NZP;
-  // @inn(vx) += dtinvavxirho * dpdx, dpdx = @d_xi(p) (nz-2h, ny-2h, nx-h)
-  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx) {
-    const int64_t b = g.S(r, y, c - 3);
-    float D = st4(p[b], p[b + sx], p[b + 2 * sx], p[b + 3 * sx]) * a.dxI;
-    D = mem3(D, g, a.m, e.shot, 0, 2, c - 3, nx - 3, r - 3, y - 3, c - 3);
-    a.f[GPI_VX][o] = a.f[GPI_VX][o] + a.cf[0][o - so] * D;
+  // every stencil read first (all in the padded storage for r, y, c >= 4)
+  const int64_t bx = g.S(r, y, c - 3), by = g.S(r, y - 3, c), bz = g.S(r - 3, y, c);
+  float Dx = st4(p[bx], p[bx + sx], p[bx + 2 * sx], p[bx + 3 * sx]) * a.dxI;  // @d_xi(p)
+  float Dy = st4(p[by], p[by + sy], p[by + 2 * sy], p[by + 3 * sy]) * a.dyI;  // @d_yi(p)
+  float Dz = st4(p[bz], p[bz + 1], p[bz + 2], p[bz + 3]) * a.dzI;              // @d_zi(p)
+  const float cx = a.cf[0][oc], cy = a.cf[1][oc], cz = a.cf[2][oc];
+  float *vx = a.f[GPI_VX] + o, *vy = a.f[GPI_VY] + o, *vz = a.f[GPI_VZ] + o;
+  const float vx0 = *vx, vy0 = *vy, vz0 = *vz;
+  // @inn(vx) += dtinvavxirho * dpdx (nz-2h, ny-2h, nx-h)
+  if (r <= nz - 3 && y <= ny - 3) {
+    Dx = mem3(Dx, g, a.m, e.shot, 0, 2, c - 3, nx - 3, r - 3, y - 3, c - 3);
+    *vx = vx0 + cx * Dx;
   }
-  // @inn(vy) += dtinvavyirho * dpdy, dpdy = @d_yi(p) (nz-2h, ny-h, nx-2h)
-  if (r >= 4 && r <= nz - 3 && y >= 4 && y <= ny && c >= 4 && c <= nx - 3) {
-    const int64_t b = g.S(r, y - 3, c);
-    float D = st4(p[b], p[b + sy], p[b + 2 * sy], p[b + 3 * sy]) * a.dyI;
-    D = mem3(D, g, a.m, e.shot, 1, 1, y - 3, ny - 3, r - 3, y - 3, c - 3);
-    a.f[GPI_VY][o] = a.f[GPI_VY][o] + a.cf[1][o - so] * D;
+  // @inn(vy) += dtinvavyirho * dpdy (nz-2h, ny-h, nx-2h)
+  if (r <= nz - 3 && c <= nx - 3) {
+    Dy = mem3(Dy, g, a.m, e.shot, 1, 1, y - 3, ny - 3, r - 3, y - 3, c - 3);
+    *vy = vy0 + cy * Dy;
   }
-  // @inn(vz) += dtinvavzirho * dpdz, dpdz = @d_zi(p) (nz-h, ny-2h, nx-2h)
-  if (r >= 4 && r <= nz && y >= 4 && y <= ny - 3 && c >= 4 && c <= nx - 3) {
-    const int64_t b = g.S(r - 3, y, c);
-    float D = st4(p[b], p[b + 1], p[b + 2], p[b + 3]) * a.dzI;
-    D = mem3(D, g, a.m, e.shot, 2, 0, r - 3, nz - 3, r - 3, y - 3, c - 3);
-    a.f[GPI_VZ][o] = a.f[GPI_VZ][o] + a.cf[2][o - so] * D;
+  // @inn(vz) += dtinvavzirho * dpdz (nz-h, ny-2h, nx-2h)
+  if (y <= ny - 3 && c <= nx - 3) {
+    Dz = mem3(Dz, g, a.m, e.shot, 2, 0, r - 3, nz - 3, r - 3, y - 3, c - 3);
+    *vz = vz0 + cz * Dz;
   }
 }
 
@@ -171,30 +174,36 @@ __global__ void __launch_bounds__(256) k3_vel_e(const Step3 a) {
   const float cx = a.cf[0][oc], cy = a.cf[1][oc], cz = a.cf[2][oc];
   float *vx = a.f[GPI_VX] + o, *vy = a.f[GPI_VY] + o, *vz = a.f[GPI_VZ] + o;
   const float vx0 = *vx, vy0 = *vy, vz0 = *vz;
+  const bool inx = r <= nz - 3 && y <= ny - 3, iny = r <= nz - 3 && c <= nx - 3, inz = y <= ny - 3 && c <= nx - 3;
+  // CPML memory only where a derivative index can fall into a strip
+  // (strips of extent-(n-6) .. extent-(n-3) derivative fields)
+  const int np = a.m.npml;
+  if (ix <= np || ix > nx - 6 - np || iy <= np || iy > ny - 6 - np || iz <= np || iz > nz - 6 - np) {
+    if (inx) {
+      D0 = mem3(D0, g, a.m, e.shot, 0, 2, ix, nx - 3, iz, iy, ix);
+      D4 = mem3(D4, g, a.m, e.shot, 4, 1, iy, ny - 6, iz, iy, ix);
+      D8 = mem3(D8, g, a.m, e.shot, 8, 0, iz, nz - 6, iz, iy, ix);
+    }
+    if (iny) {
+      D1 = mem3(D1, g, a.m, e.shot, 1, 2, ix, nx - 6, iz, iy, ix);
+      D3 = mem3(D3, g, a.m, e.shot, 3, 1, iy, ny - 3, iz, iy, ix);
+      D7 = mem3(D7, g, a.m, e.shot, 7, 0, iz, nz - 6, iz, iy, ix);
+    }
+    if (inz) {
+      D2 = mem3(D2, g, a.m, e.shot, 2, 2, ix, nx - 6, iz, iy, ix);
+      D5 = mem3(D5, g, a.m, e.shot, 5, 1, iy, ny - 6, iz, iy, ix);
+      D6 = mem3(D6, g, a.m, e.shot, 6, 0, iz, nz - 3, iz, iy, ix);
+    }
+  }
   // vx: @inn(vx) -= dtinvavxirho (dtauxxdx + dtauxydy + dtauxzdz), (nz-2h, ny-2h, nx-h)
-  if (r <= nz - 3 && y <= ny - 3) {
-    D0 = mem3(D0, g, a.m, e.shot, 0, 2, ix, nx - 3, iz, iy, ix);
-    D4 = mem3(D4, g, a.m, e.shot, 4, 1, iy, ny - 6, iz, iy, ix);
-    D8 = mem3(D8, g, a.m, e.shot, 8, 0, iz, nz - 6, iz, iy, ix);
-    *vx = vx0 - cx * (D0 + D4 + D8);
-  }
+  if (inx) *vx = vx0 - cx * (D0 + D4 + D8);
   // vy: @inn(vy) -= dtinvavyirho (dtauxydx + dtauyydy + dtauyzdz), (nz-2h, ny-h, nx-2h)
-  if (r <= nz - 3 && c <= nx - 3) {
-    D1 = mem3(D1, g, a.m, e.shot, 1, 2, ix, nx - 6, iz, iy, ix);
-    D3 = mem3(D3, g, a.m, e.shot, 3, 1, iy, ny - 3, iz, iy, ix);
-    D7 = mem3(D7, g, a.m, e.shot, 7, 0, iz, nz - 6, iz, iy, ix);
-    *vy = vy0 - cy * (D1 + D3 + D7);
-  }
+  if (iny) *vy = vy0 - cy * (D1 + D3 + D7);
   // vz: @inn(vz) -= dtinvavzirho (dtauxzdx + dtauyzdy + dtauzzdz), (nz-h, ny-2h, nx-2h)
-  if (y <= ny - 3 && c <= nx - 3) {
-    D2 = mem3(D2, g, a.m, e.shot, 2, 2, ix, nx - 6, iz, iy, ix);
-    D5 = mem3(D5, g, a.m, e.shot, 5, 1, iy, ny - 6, iz, iy, ix);
-    D6 = mem3(D6, g, a.m, e.shot, 6, 0, iz, nz - 3, iz, iy, ix);
-    *vz = vz0 - cz * (D2 + D5 + D6);
-  }
+  if (inz) *vz = vz0 - cz * (D2 + D5 + D6);
 }
 
-__global__ void __launch_bounds__(256) k3_str_e(const Step3 a) {
+__global__ void __launch_bounds__(256, 5) k3_str_e(const Step3 a) {
   const G3 &g = a.g;
   const Cell3 e = cell3(g, a.shot0, a.nshots, 1);
   if (!e.ok) return;
@@ -218,31 +227,38 @@ __global__ void __launch_bounds__(256) k3_str_e(const Step3 a) {
   float *txx = a.f[GPI_TAUXX] + o, *tyy = a.f[GPI_TAUYY] + o, *tzz = a.f[GPI_TAUZZ] + o;
   float *txy = a.f[GPI_TAUXY] + o, *txz = a.f[GPI_TAUXZ] + o, *tyz = a.f[GPI_TAUYZ] + o;
   const float txx0 = *txx, tyy0 = *tyy, tzz0 = *tzz, txy0 = *txy, txz0 = *txz, tyz0 = *tyz;
+  const bool ixy = r <= nz - 6 && y <= ny - 3 && c <= nx - 3, ixz = r <= nz - 3 && y <= ny - 6 && c <= nx - 3,
+             iyz = r <= nz - 3 && y <= ny - 3 && c <= nx - 6;
+  // CPML memory only where a derivative index can fall into a strip
+  // (strips of extent-(n-3) .. extent-n derivative fields)
+  const int np = a.m.npml;
+  if (c <= np || c > nx - 3 - np || y <= np || y > ny - 3 - np || r <= np || r > nz - 3 - np) {
+    D9 = mem3(D9, g, a.m, e.shot, 9, 2, c, nx, r, y, c);
+    D10 = mem3(D10, g, a.m, e.shot, 10, 1, y, ny, r, y, c);
+    D11 = mem3(D11, g, a.m, e.shot, 11, 0, r, nz, r, y, c);
+    if (ixy) {
+      D12 = mem3(D12, g, a.m, e.shot, 12, 1, y, ny - 3, r, y, c);
+      D14 = mem3(D14, g, a.m, e.shot, 14, 2, c, nx - 3, r, y, c);
+    }
+    if (ixz) {
+      D13 = mem3(D13, g, a.m, e.shot, 13, 0, r, nz - 3, r, y, c);
+      D16 = mem3(D16, g, a.m, e.shot, 16, 2, c, nx - 3, r, y, c);
+    }
+    if (iyz) {
+      D15 = mem3(D15, g, a.m, e.shot, 15, 0, r, nz - 3, r, y, c);
+      D17 = mem3(D17, g, a.m, e.shot, 17, 1, y, ny - 3, r, y, c);
+    }
+  }
   // compute_stressii!: full grid
-  D9 = mem3(D9, g, a.m, e.shot, 9, 2, c, nx, r, y, c);
-  D10 = mem3(D10, g, a.m, e.shot, 10, 1, y, ny, r, y, c);
-  D11 = mem3(D11, g, a.m, e.shot, 11, 0, r, nz, r, y, c);
   *txx = txx0 - (M * D9) - (L * (D10 + D11));
   *tyy = tyy0 - (M * D10) - (L * (D9 + D11));
   *tzz = tzz0 - (M * D11) - (L * (D10 + D9));
   // tauxy (nz-2h, ny-h, nx-h): -= dtavxyimu (dvxdy + dvydx)
-  if (r <= nz - 6 && y <= ny - 3 && c <= nx - 3) {
-    D12 = mem3(D12, g, a.m, e.shot, 12, 1, y, ny - 3, r, y, c);
-    D14 = mem3(D14, g, a.m, e.shot, 14, 2, c, nx - 3, r, y, c);
-    *txy = txy0 - mxy * (D12 + D14);
-  }
+  if (ixy) *txy = txy0 - mxy * (D12 + D14);
   // tauxz (nz-h, ny-2h, nx-h): -= dtavxzimu (dvxdz + dvzdx)
-  if (r <= nz - 3 && y <= ny - 6 && c <= nx - 3) {
-    D13 = mem3(D13, g, a.m, e.shot, 13, 0, r, nz - 3, r, y, c);
-    D16 = mem3(D16, g, a.m, e.shot, 16, 2, c, nx - 3, r, y, c);
-    *txz = txz0 - mxz * (D13 + D16);
-  }
+  if (ixz) *txz = txz0 - mxz * (D13 + D16);
   // tauyz (nz-h, ny-h, nx-2h): -= dtavyzimu (dvydz + dvzdy)
-  if (r <= nz - 3 && y <= ny - 3 && c <= nx - 6) {
-    D15 = mem3(D15, g, a.m, e.shot, 15, 0, r, nz - 3, r, y, c);
-    D17 = mem3(D17, g, a.m, e.shot, 17, 1, y, ny - 3, r, y, c);
-    *tyz = tyz0 - myz * (D15 + D17);
-  }
+  if (iyz) *tyz = tyz0 - myz * (D15 + D17);
 }
 
 // free_surface_mirror!(tauzz), free_surface!(tauxz, tauyz) at z = 1
@@ -338,10 +354,10 @@ static int step3(Plan *p, int vonly) {
   a.dxI = (float)(1.0 / (p->d.dx * 24.0));
   if (p->d.nx + 3 > 65535) return fail(p, GPI_E_UNSUPPORTED, "3-D grids are limited to 65532 columns");
   const dim3 blk(32, 8);
-  // the elastic velocity pass covers cells from (4, 4, 4) (its update
-  // domains), every other pass from (1, 1, 1)
+  // the velocity passes cover cells from (4, 4, 4) (their update domains),
+  // the stress passes from (1, 1, 1)
   auto pass = [&](bool vel) {
-    const int base = (vel && !ac) ? 4 : 1;
+    const int base = vel ? 4 : 1;
     const int nc = p->d.nx + 4 - base;
     const int chunk = 65535 / nc;  // shots per launch (grid z = columns x shots)
     for (int s0 = 0; s0 < p->d.nshots; s0 += chunk) {
