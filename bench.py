@@ -50,6 +50,11 @@ WORKLOADS = {
                   "kernel": "k3_vel_e + k3_str_e (two fused passes), algorithmic 104 B/cell"},
     "acoustic3d": {"name": "acoustic3d_600x600x600_10m_npml23_2500steps", "bpc": 48, "nshots": 1, "nt": 2500,
                    "kernel": "k3_vel_a + k3_str_a (two fused passes), algorithmic 48 B/cell"},
+    # one bench step = one gradient!: forward_save (36 B) + adjoint step with
+    # the imaging condition (76 B fused) per cell and time step
+    "acoustic2d_grad": {"name": "acoustic2d_fwi_gradient_500x1500_10m_32shots_3000steps", "bpc": 112, "nshots": 32,
+                        "nt": 3000,
+                        "kernel": "forward_save + adjoint (k_a2 x 3 + k_grad_a2), algorithmic 36 + 76 B/cell"},
 }
 
 
@@ -83,6 +88,8 @@ def workload(kind, nt=None, nshots=None, side=None):
         kw.update(nz=side, ny=side, nx=side)
     if kind == "elastic2d":
         return configs.elastic2d_batch(nshots=nshots or 16, **kw)
+    if kind == "acoustic2d_grad":
+        return configs.acoustic2d_fwi(nshots=nshots or 32, anomaly=False, **kw)
     if kind == "acoustic2d":
         wl = configs.acoustic2d_layers(**kw)
     elif kind == "elastic3d":
@@ -96,7 +103,7 @@ def workload(kind, nt=None, nshots=None, side=None):
 
 def config_json(kind, wl, n_gpus):
     npml = wl.npml if wl.npml is not None else 43
-    state = {"elastic2d": 5, "acoustic2d": 3, "elastic3d": 9, "acoustic3d": 4}[kind]
+    state = {"elastic2d": 5, "acoustic2d": 3, "elastic3d": 9, "acoustic3d": 4, "acoustic2d_grad": 6}[kind]
     return {"workload": WORKLOADS[kind]["name"],
             "grid": [len(g) for g in wl.grid], "extended_grid": [len(g) + 2 * npml for g in wl.grid],
             "shots_per_gpu": len(wl.shots), "nt": wl.nt, "dt": wl.tgrid.step, "order": 4,
@@ -290,6 +297,58 @@ def engine_arm(args, rank, world, local):
     return line, dist
 
 
+def gradient_arm(args, world, local):
+    """One bench step = gradient!(g, m, L2DistLoss(), dobs, pa) over all shots:
+    forward_save, adjoint sources, adjoint run with the imaging condition.
+    The observed data are modelled once (not timed) on the model with the
+    Gaussian anomaly; the starting model omits it."""
+    import torch
+
+    from geophyinv_gb300 import L2DistLoss, Recs, configs, get_modelvector, gradient, update
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    kw = {} if args.nt is None else {"nt": args.nt}
+    nsh = args.nshots or 32
+    true = configs.acoustic2d_fwi(nshots=nsh, **kw)
+    pt = true.expt(stream=stream.cuda_stream)
+    update(pt)
+    dobs = [Recs(r.n, r.grid, r.fields, {f: r.d[f].copy() for f in r.fields}) for r in pt.data[0]]
+    del pt
+    wl = workload("acoustic2d_grad", args.nt, nsh)
+    pa = wl.expt(mode="forward_save", stream=stream.cuda_stream)
+    cells = pa.nss * int(np.prod([len(g) for g in pa.exgrid]))
+    units = cells * pa.nt
+    m0 = get_modelvector(pa, ["invK", "rho"])
+    g = np.zeros_like(m0)
+    for _ in range(args.warmup):
+        gradient(g, m0, L2DistLoss(), dobs, pa)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    launches = 0
+    for _ in range(args.steps):
+        gradient(g, m0, L2DistLoss(), dobs, pa)
+        launches += pa.launches()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    clk = clocks.stop()
+    value = world * units / (ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    W = WORKLOADS["acoustic2d_grad"]
+    achieved = W["bpc"] * cells / (ms * 1e-3 / pa.nt) / 1e9
+    return {"metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (layered + Gaussian anomaly, zero-anomaly start)",
+            "config": config_json("acoustic2d_grad", wl, world),
+            "e2e": {"value": round(value, 3), "unit": "Gcell/s", "note": "gradient! is the public call; host buffers"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "kernel": W["kernel"],
+                         "peak_source": peak_kind + " hbm_gbs"},
+            "gpu_launches": int(launches), "clocks": clk}
+
+
 def reference_arm(args):
     """CPU restatement of the reference (the oracle) on all host cores."""
     rates = []
@@ -316,7 +375,10 @@ def main():
         if rank == 0:
             print(json.dumps(reference_arm(args)))
         return
-    line, dist = engine_arm(args, rank, world, local)
+    if args.workload == "acoustic2d_grad":
+        line, dist = gradient_arm(args, world, local), None
+    else:
+        line, dist = engine_arm(args, rank, world, local)
     if rank == 0:
         if not args.no_cpu_baseline:
             rate, threads, sample = cpu_sample(args.workload)
