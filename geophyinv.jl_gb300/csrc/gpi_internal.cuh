@@ -147,6 +147,11 @@ struct Plan {
   static constexpr int NSIDE = 3;
   cudaStream_t side[NSIDE] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[NSIDE] = {};
+  // whole-run CUDA graphs per mode (gpi_set_graph)
+  bool use_graph = false;
+  cudaStream_t own_stream = nullptr;  // created for graphs when no stream was given
+  cudaGraphExec_t gexec[3] = {};
+  int64_t glaunches[3] = {};
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 };
 
@@ -211,6 +216,7 @@ int make_xcuts(int nx, int m, int npml, bool xlo, bool xhi, int *cuts);
 int classify_tiles(const Plan &p, const int *xcut, const InjCell *cells, const int32_t *gptr, int4 *out, int cap,
                    int count[4]);
 int aux_step(Plan *p, int it, int mode);
+void drop_graphs(Plan &p);
 // nside side streams forked from the plan stream (the plan stream itself
 // when side streams are unavailable); join_side joins them back
 int fork_side(Plan *p, int nside, cudaStream_t *out);

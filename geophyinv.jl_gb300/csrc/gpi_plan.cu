@@ -367,6 +367,8 @@ void destroy(gpi_plan *pl) {
   cudaGetDevice(&dev);
   cudaSetDevice(p.device);
   if (p.stream) cudaStreamSynchronize(p.stream);
+  drop_graphs(p);
+  if (p.own_stream) cudaStreamDestroy(p.own_stream);
   for (int k = 0; k < Plan::NSIDE; k++) {
     if (p.side[k]) {
       cudaStreamSynchronize(p.side[k]);
@@ -833,6 +835,8 @@ static int zero_state(Plan &p) {
   return GPI_OK;
 }
 
+static int run_body(Plan &p, int mode);
+
 int run(Plan &p, int mode) {
   if (mode != GPI_FORWARD && mode != GPI_FORWARD_SAVE && mode != GPI_ADJOINT) return fail(&p, GPI_E_INVALID, "mode");
   if (mode != GPI_FORWARD && p.d.npw != 2) return fail(&p, GPI_E_INVALID, "forward_save/adjoint need npw = 2");
@@ -845,13 +849,54 @@ int run(Plan &p, int mode) {
   cudaGetDevice(&dev);
   if (dev != p.device) GPI_CUDA(&p, cudaSetDevice(p.device));
   int rc = GPI_OK;
+  const bool recompile = p.rec_dirty || p.src_dirty || (p.d.ndim == 2 && !p.d_tiles);
   if (p.rec_dirty) rc = compile_receivers(p);
   if (!rc && p.src_dirty) {
     rc = compile_sources(p);
     if (!rc && p.d.ndim == 2) rc = build_tiles(p);
   }
   if (!rc && p.d.ndim == 2 && !p.d_tiles) rc = build_tiles(p);
-  if (!rc) rc = zero_state(p);
+  if (!rc && recompile) drop_graphs(p);
+  if (!rc && p.use_graph) {
+    // the whole run as one CUDA graph: captured on first use per mode,
+    // replayed afterwards (the tables and buffers it uses keep their
+    // addresses until the sources or receivers change)
+    if (!p.gexec[mode]) {
+      GPI_CUDA(&p, cudaStreamBeginCapture(p.stream, cudaStreamCaptureModeThreadLocal));
+      rc = run_body(p, mode);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(p.stream, &graph);
+      if (!rc && e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+      if (!rc && cudaGraphInstantiate(&p.gexec[mode], graph, 0) != cudaSuccess) {
+        p.gexec[mode] = nullptr;
+        rc = fail(&p, GPI_E_CUDA, "graph instantiation failed");
+      }
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      p.glaunches[mode] = p.launches;
+    }
+    if (!rc) {
+      GPI_CUDA(&p, cudaGraphLaunch(p.gexec[mode], p.stream));
+      p.launches = p.glaunches[mode];
+      if (mode == GPI_FORWARD_SAVE) p.have_save = 1;
+    }
+  } else if (!rc) {
+    rc = run_body(p, mode);
+  }
+  if (dev != p.device) cudaSetDevice(dev);
+  return rc;
+}
+
+void drop_graphs(Plan &p) {
+  for (int m = 0; m < 3; m++) {
+    if (p.gexec[m]) cudaGraphExecDestroy(p.gexec[m]);
+    p.gexec[m] = nullptr;
+  }
+}
+
+// the device work of one run: state reset, the time loop, the final half step
+static int run_body(Plan &p, int mode) {
+  int rc = zero_state(p);
   p.launches = 0;
   // an adjoint run records nothing and keeps the records of the forward run
   if (!rc && p.rec_pool && mode != GPI_ADJOINT)
@@ -879,7 +924,6 @@ int run(Plan &p, int mode) {
     if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));
   }
   if (!rc && mode == GPI_FORWARD_SAVE) p.have_save = 1;
-  if (dev != p.device) cudaSetDevice(dev);
   return rc;
 }
 
@@ -963,6 +1007,7 @@ const char *gpi_last_error(const gpi_plan *plan) { return plan ? plan->p.err.c_s
 int gpi_set_stream(gpi_plan *plan, void *stream) {
   if (!plan) return GPI_E_INVALID;
   plan->p.stream = (cudaStream_t)stream;
+  if (!stream && plan->p.use_graph) plan->p.stream = plan->p.own_stream;
   return GPI_OK;
 }
 int gpi_plan_bytes(const gpi_plan *plan, size_t *bytes) {
@@ -994,6 +1039,28 @@ int gpi_get_gradient(gpi_plan *plan, int param, float *out, int on_device) {
 }
 int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int on_device) {
   return plan ? gpi::get_field(plan->p, ipw, shot, field, out, on_device) : GPI_E_INVALID;
+}
+int gpi_set_graph(gpi_plan *plan, int enable) {
+  if (!plan) return GPI_E_INVALID;
+  // a graph cannot be captured on the legacy default stream: give the plan
+  // a stream of its own
+  if (enable && !plan->p.stream) {
+    GPI_CUDA(&plan->p, cudaStreamCreateWithFlags(&plan->p.own_stream, cudaStreamNonBlocking));
+    plan->p.stream = plan->p.own_stream;
+  }
+  plan->p.use_graph = enable != 0;
+  if (!enable) gpi::drop_graphs(plan->p);
+  return GPI_OK;
+}
+int gpi_query(gpi_plan *plan, int *done) {
+  if (!plan || !done) return GPI_E_INVALID;
+  const cudaError_t e = cudaStreamQuery(plan->p.stream);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return GPI_OK;
+  }
+  *done = 1;
+  return e == cudaSuccess ? GPI_OK : gpi::fail(&plan->p, GPI_E_CUDA, cudaGetErrorString(e));
 }
 int gpi_last_launches(const gpi_plan *plan, int64_t *launches) {
   if (!plan || !launches) return GPI_E_INVALID;

@@ -296,6 +296,16 @@ class SeisForwExpt:
     def run(self, mode):
         self._check(self.L.gpi_run(self.plan, mode))
 
+    def set_graph(self, enable=True):
+        """Replay each run as one CUDA graph (captured on first use)."""
+        self._check(self.L.gpi_set_graph(self.plan, int(bool(enable))))
+
+    def done(self):
+        """True when every run issued so far has finished on the device."""
+        v = ctypes.c_int32()
+        self._check(self.L.gpi_query(self.plan, ctypes.byref(v)))
+        return bool(v.value)
+
     def records(self, iss, field):
         out = np.zeros((self.nt, self.ageom[iss].nr), np.float32, order="F")
         self._check(self.L.gpi_get_records(self.plan, iss, _lib.FIELD[field], _ptr(out), 0))

@@ -124,6 +124,16 @@ int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int 
 /* Number of engine kernel launches issued by the last gpi_run. */
 int gpi_last_launches(const gpi_plan *plan, int64_t *launches);
 
+/* Run every later gpi_run of this plan as one CUDA graph per mode: the time
+ * loop is captured on its first run (after the sources and receivers are
+ * compiled) and replayed, which removes the per-launch host cost of small
+ * grids.  Changing the sources or receivers drops the graphs.  No
+ * counterpart in the reference (its time loop launches every kernel). */
+int gpi_set_graph(gpi_plan *plan, int enable);
+/* Non-blocking completion test of the plan's stream (1 when all work
+ * issued so far has finished).  No counterpart in the reference. */
+int gpi_query(gpi_plan *plan, int *done);
+
 /* Size of the device scratch array used by gpi_forward_acoustic2d_noalloc. */
 #define GPI_NOALLOC_SCRATCH_BYTES (64u << 20)
 
