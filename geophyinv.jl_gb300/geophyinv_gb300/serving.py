@@ -1,0 +1,244 @@
+"""Continuous-batching serving loop for forward and gradient shot requests.
+
+Requests of uneven grid sizes, step counts and shot counts arrive over time.
+The server admits a request as soon as an in-flight slot is free and its
+plan fits the HBM budget, gives it a plan of its own (all of its shots in one
+multi-shot launch per step, its own CUDA stream, the whole time loop as one
+CUDA graph) and keeps its wavefields, boundary store and records resident
+until it completes; requests on the GPU overlap, and the host work of one
+request (plan set-up, adjoint sources, record reads) overlaps the device work
+of the others.  A gradient request runs forward_save, builds its adjoint
+sources from the residuals and runs the adjoint (gradient!,
+src/fdtd/func_grad.jl:11-49).
+
+The baseline (`serve_plain`) models the same stream one request at a time
+with plain launches (no graphs, no overlap).  Results do not depend on what
+else runs: every request's arithmetic is its own and deterministic.
+"""
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib, configs
+from .fdtd import L2DistLoss, Recs, Srcs, update
+
+KINDS = ("acoustic_forward", "elastic_forward", "acoustic_gradient")
+
+
+@dataclass
+class Request:
+    """One modelling request: `kind` in KINDS, grid nz x nx, nt steps, nshots
+    supersources, arrival time in seconds from the start of the stream."""
+    rid: int
+    kind: str
+    nz: int
+    nx: int
+    nt: int
+    nshots: int
+    arrival: float = 0.0
+    seed: int = 0
+
+    def workload(self):
+        nrec = max(8, self.nx // 4)
+        if self.kind == "acoustic_forward":
+            wl = configs.acoustic2d_layers(nz=self.nz, nx=self.nx, nt=self.nt, nrec=nrec, seed=self.seed,
+                                           rfields=("p", "vz"))
+            src, rec = wl.shots[0]
+            xm = wl.grid[1].last
+            wl.shots = [(np.array([[src[0, 0], x]]), rec) for x in np.linspace(0.0, xm, self.nshots + 2)[1:-1]]
+            return wl
+        if self.kind == "elastic_forward":
+            return configs.elastic2d_batch(nz=self.nz, nx=self.nx, nt=self.nt, nshots=self.nshots, nrec=nrec,
+                                           seed=self.seed)
+        return configs.acoustic2d_fwi(nz=self.nz, nx=self.nx, nt=self.nt, nshots=self.nshots, nrec=nrec,
+                                      seed=self.seed, anomaly=False)
+
+    def cells(self):
+        return (self.nz + 86) * (self.nx + 86) * self.nshots * self.nt
+
+
+def make_stream(n, rate, seed=4, sides=(200, 2000), steps=(1000, 6000), shots=(1, 8), mix=(0.5, 0.3, 0.2)):
+    """A seeded request stream: Poisson arrivals at `rate` requests/s, grid
+    sides and step counts uniform in the given ranges, 50 / 30 / 20 %
+    acoustic forward / elastic forward / acoustic gradient."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        kind = KINDS[int(rng.choice(3, p=np.asarray(mix) / np.sum(mix)))]
+        out.append(Request(i, kind, int(rng.integers(sides[0], sides[1] + 1)), int(rng.integers(sides[0], sides[1] + 1)),
+                           int(rng.integers(steps[0], steps[1] + 1)), int(rng.integers(shots[0], shots[1] + 1)), t,
+                           seed=int(rng.integers(0, 1 << 30))))
+    return out
+
+
+def plan_bytes_estimate(req):
+    """Device bytes of a request's plan (state, CPML strips, coefficients,
+    records, boundary store), from the layout of the engine."""
+    nz, nx = req.nz + 86, req.nx + 86
+    nzp = (nz + 124 + 12 + 31) // 32 * 32
+    f = nzp * (nx + 15) * 4
+    ela = req.kind == "elastic_forward"
+    npw = 2 if req.kind == "acoustic_gradient" else 1
+    state = (5 if ela else 3) * 2 * npw * req.nshots * f
+    coef = ((5 if ela else 3) + 3) * f
+    psi = (8 if ela else 4) * 2 * npw * req.nshots * 88 * max(nzp, nx + 15) * 4
+    rec = req.nt * (req.nx // 4 + 8) * 2 * req.nshots * 4
+    store = (req.nt * 6 * (nz + nx) + 3 * nzp * (nx + 15)) * 4 * req.nshots if npw == 2 else 0
+    return state + coef + psi + rec + store + npw * 2 * req.nshots * f
+
+
+@dataclass
+class Result:
+    rid: int
+    kind: str
+    records: list = field(default_factory=list)
+    gradient: dict = None
+    loss: float = None
+    t_admit: float = 0.0
+    t_done: float = 0.0
+
+
+class _Job:
+    """The life of one request on the server (a small state machine)."""
+
+    def __init__(self, req, graphs, stream):
+        self.req = req
+        self.wl = req.workload()
+        mode = "forward_save" if req.kind == "acoustic_gradient" else "forward"
+        self.pa = self.wl.expt(mode=mode, stream=stream)
+        if graphs:
+            self.pa.set_graph(True)
+        self.res = Result(req.rid, req.kind)
+        self.phase = 0
+
+    def launch(self):
+        pa = self.pa
+        if self.req.kind == "acoustic_gradient":
+            if self.phase == 0:
+                update(pa, pa.srcwav, [1, 0])
+                pa.run(_lib.FORWARD_SAVE)
+            else:
+                pa.run(_lib.ADJOINT)
+        else:
+            pa.run(_lib.FORWARD)
+
+    def finish_phase(self):
+        """Called when the device work of the current phase is done; returns
+        True when the request is complete."""
+        pa = self.pa
+        recs = [{f: pa.records(i, f) for f in pa.rfields} for i in range(pa.nss)]
+        if self.req.kind != "acoustic_gradient":
+            self.res.records = recs
+            return True
+        if self.phase == 0:
+            # adjoint sources: deriv(L2DistLoss(), dobs, dcal) reversed in time,
+            # with zero observed data (func_grad.jl:19-31)
+            loss = L2DistLoss()
+            adj = []
+            total = 0.0
+            for i in range(pa.nss):
+                s = Srcs(pa.ageom[i].nr, pa.tgrid, pa.rfields)
+                for f in pa.rfields:
+                    obs = np.zeros_like(recs[i][f])
+                    total += loss.value(obs, recs[i][f])
+                    s.d[f] = loss.deriv(obs, recs[i][f])[::-1].copy()
+                adj.append(s)
+            self.res.records = recs
+            self.res.loss = total
+            pa.srcwav[1] = adj
+            update(pa, pa.srcwav, [-1, 1])
+            self.phase = 1
+            self.launch()
+            return False
+        self.res.gradient = {"invK": pa.gradient_raw(0), "rho": pa.gradient_raw(1)}
+        return True
+
+    def close(self):
+        self.pa.close() if hasattr(self.pa, "close") else None
+        self.pa = None
+
+
+def _streams(n):
+    import torch
+
+    return [torch.cuda.Stream() for _ in range(n)]
+
+
+def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=True):
+    """Continuous batching: admit arrived requests while slots and HBM budget
+    allow, poll the in-flight ones, launch their next phase or collect their
+    results.  Returns (results by id, stats)."""
+    import torch
+
+    streams = _streams(max_inflight)
+    free = list(range(max_inflight))
+    pending = sorted(requests, key=lambda r: r.arrival)
+    inflight = {}
+    results = {}
+    used = 0
+    t0 = time.perf_counter()
+    while pending or inflight:
+        now = time.perf_counter() - t0
+        # admission: arrival order, HBM budget, a free stream
+        while pending and free and (not realtime or pending[0].arrival <= now):
+            need = plan_bytes_estimate(pending[0])
+            if inflight and used + need > hbm_budget:
+                break
+            req = pending.pop(0)
+            slot = free.pop()
+            job = _Job(req, graphs, streams[slot].cuda_stream)
+            job.res.t_admit = time.perf_counter() - t0
+            job.launch()
+            inflight[req.rid] = (job, slot, need)
+            used += need
+        done_any = False
+        for rid in list(inflight):
+            job, slot, need = inflight[rid]
+            if job.pa.done():
+                done_any = True
+                if job.finish_phase():
+                    job.res.t_done = time.perf_counter() - t0
+                    results[rid] = job.res
+                    job.close()
+                    del inflight[rid]
+                    free.append(slot)
+                    used -= need
+        if not done_any:
+            time.sleep(0.0002)
+    torch.cuda.synchronize()
+    return results, _stats(requests, results, time.perf_counter() - t0)
+
+
+def serve_plain(requests, realtime=True):
+    """One request at a time, plain launches, each to completion."""
+    import torch
+
+    results = {}
+    t0 = time.perf_counter()
+    for req in sorted(requests, key=lambda r: r.arrival):
+        if realtime:
+            wait = req.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+        job = _Job(req, False, None)
+        job.res.t_admit = time.perf_counter() - t0
+        job.launch()
+        while True:
+            torch.cuda.synchronize()
+            if job.finish_phase():
+                break
+        job.res.t_done = time.perf_counter() - t0
+        results[req.rid] = job.res
+        job.close()
+    return results, _stats(requests, results, time.perf_counter() - t0)
+
+
+def _stats(requests, results, wall):
+    lat = np.array([results[r.rid].t_done - r.arrival for r in requests])
+    shots = sum(r.nshots for r in requests)
+    return {"requests": len(requests), "shots": shots, "wall_s": wall, "shots_per_s": shots / wall,
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "gcells_per_s": sum(r.cells() for r in requests) / wall / 1e9}
