@@ -64,7 +64,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="elastic2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="elastic2d", choices=sorted(WORKLOADS) + ["serving"])
+    ap.add_argument("--requests", type=int, default=64, help="serving: requests in the stream")
+    ap.add_argument("--rate", type=float, default=32.0, help="serving: arrival rate, requests/s")
     ap.add_argument("--nt", type=int, default=None)
     ap.add_argument("--nshots", type=int, default=None)
     ap.add_argument("--side", type=int, default=None, help="3-D workloads: a side^3 sub-grid (profiling)")
@@ -349,6 +351,37 @@ def gradient_arm(args, world, local):
             "gpu_launches": int(launches), "clocks": clk}
 
 
+def serving_arm(args):
+    """The mixed request stream (50 % acoustic forward, 30 % elastic forward,
+    20 % acoustic gradient; Poisson arrivals) through the continuous-batching
+    loop and one request at a time with plain launches.  The stream is a
+    scaled version of the 2000-request one (sides 200-800 instead of
+    200-2000, 500-2000 steps instead of 1000-6000) so that both arms finish
+    in minutes."""
+    from geophyinv_gb300 import serving
+
+    reqs = serving.make_stream(args.requests, rate=args.rate, seed=4, sides=(200, 800), steps=(500, 2000),
+                               shots=(1, 8))
+    warm = serving.make_stream(6, rate=1000.0, seed=5, sides=(100, 150), steps=(50, 60), shots=(1, 2))
+    serving.serve(warm, realtime=False)
+    serving.serve_plain(warm, realtime=False)
+    clocks = Clocks(0)
+    clocks.start()
+    _, st = serving.serve(reqs, max_inflight=8)
+    clk = clocks.stop()
+    _, pl = serving.serve_plain(reqs)
+    return {"metric": "shots/s", "value": round(st["shots_per_s"], 3), "unit": "shots/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic request stream (seed 4)",
+            "config": {"workload": "serving_stream_%d_requests_%g_per_s" % (len(reqs), args.rate),
+                       "sides": [200, 800], "steps": [500, 2000], "shots": [1, 8],
+                       "mix": "50 % acoustic forward, 30 % elastic forward, 20 % acoustic gradient",
+                       "max_inflight": 8},
+            "serving": {k: round(v, 4) if isinstance(v, float) else v for k, v in st.items()},
+            "plain": {k: round(v, 4) if isinstance(v, float) else v for k, v in pl.items()},
+            "speedup_shots_per_s": round(st["shots_per_s"] / pl["shots_per_s"], 3), "clocks": clk}
+
+
 def reference_arm(args):
     """CPU restatement of the reference (the oracle) on all host cores."""
     rates = []
@@ -374,6 +407,9 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(reference_arm(args)))
+        return
+    if args.workload == "serving":
+        print(json.dumps(serving_arm(args)))
         return
     if args.workload == "acoustic2d_grad":
         line, dist = gradient_arm(args, world, local), None

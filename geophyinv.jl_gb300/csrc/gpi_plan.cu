@@ -26,6 +26,13 @@ int fail(Plan *p, int code, const std::string &msg) {
   return code;
 }
 
+// Stream-ordered device allocations and uploads on the plan's stream: no
+// device-wide synchronisation, so plans of other requests keep running.
+static cudaError_t dalloc(Plan &p, void **ptr, size_t bytes) { return cudaMallocAsync(ptr, bytes, p.stream); }
+static cudaError_t h2d(Plan &p, void *dst, const void *src, size_t bytes) {
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, p.stream);
+}
+
 // ---------------------------------------------------------------------------
 // derivative-field tables (get_mgrid shapes, src/fields.jl:92-671)
 // ---------------------------------------------------------------------------
@@ -256,11 +263,19 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   }
   size_t total = 0;
   for (auto &a : allocs) total += (size_t)round_up(a.second, 64) * sizeof(float);
-  cudaError_t e = cudaMalloc(&p.pool, total);
-  if (e != cudaSuccess) {
+  // one stream-ordered allocation (set-up stream, synchronised below)
+  cudaStream_t cs = nullptr;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
     delete pl;
     cudaGetLastError();
-    return fail(nullptr, GPI_E_NOMEM, "cudaMalloc of " + std::to_string(total) + " bytes failed");
+    return fail(nullptr, GPI_E_CUDA, "stream creation failed");
+  }
+  cudaError_t e = cudaMallocAsync(&p.pool, total, cs);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(cs);
+    delete pl;
+    cudaGetLastError();
+    return fail(nullptr, GPI_E_NOMEM, "allocation of " + std::to_string(total) + " bytes failed");
   }
   p.pool_bytes = total;
   char *c = (char *)p.pool;
@@ -268,22 +283,24 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
     *a.first = (float *)c;
     c += (size_t)round_up(a.second, 64) * sizeof(float);
   }
-  e = cudaMemset(p.pool, 0, total);
+  // zeroed state, identity PML (kI = 1) until gpi_set_pml is called
+  std::vector<float> pm((size_t)p.nder * 3 * 2 * d.npml, 0.f);
+  for (int q = 0; q < p.nder; q++)
+    for (int i = 0; i < 2 * d.npml; i++) {
+      pm[((size_t)q * 3 + 1) * 2 * d.npml + i] = 1.f;
+      pm[((size_t)q * 3 + 2) * 2 * d.npml + i] = 1.f;
+    }
+  e = cudaMemsetAsync(p.pool, 0, total, cs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(p.pml, pm.data(), pm.size() * sizeof(float), cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
   if (e != cudaSuccess) {
-    cudaFree(p.pool);
+    cudaFreeAsync(p.pool, cs);
+    cudaStreamSynchronize(cs);
+    cudaStreamDestroy(cs);
     delete pl;
     return fail(nullptr, GPI_E_CUDA, cudaGetErrorString(e));
   }
-  // identity PML (kI = 1) until gpi_set_pml is called
-  {
-    std::vector<float> pm((size_t)p.nder * 3 * 2 * d.npml, 0.f);
-    for (int q = 0; q < p.nder; q++)
-      for (int i = 0; i < 2 * d.npml; i++) {
-        pm[((size_t)q * 3 + 1) * 2 * d.npml + i] = 1.f;
-        pm[((size_t)q * 3 + 2) * 2 * d.npml + i] = 1.f;
-      }
-    cudaMemcpy(p.pml, pm.data(), pm.size() * sizeof(float), cudaMemcpyHostToDevice);
-  }
+  cudaStreamDestroy(cs);
   p.rec_n.assign(d.nshots, std::vector<int>(NFIELD, 0));
   p.rec_cp.assign(d.nshots, std::vector<std::vector<int64_t>>(NFIELD));
   p.rec_off.assign(d.nshots, std::vector<std::vector<int64_t>>(NFIELD));
@@ -333,30 +350,30 @@ int join_side(Plan *p, int nside) {
   return GPI_OK;
 }
 
-static void free_dev(void *&x) {
-  if (x) cudaFree(x);
+static void free_dev(Plan &p, void *&x) {
+  if (x) cudaFreeAsync(x, p.stream);
   x = nullptr;
 }
 
 static void free_sources(Plan &p) {
-  free_dev((void *&)p.d_cells);
-  free_dev((void *&)p.d_pair_j);
-  free_dev((void *&)p.d_pair_w);
-  free_dev((void *&)p.d_wav);
-  free_dev((void *&)p.d_wav_ns);
-  free_dev((void *&)p.d_amount);
-  free_dev((void *&)p.d_group_ptr);
-  free_dev((void *&)p.d_tiles);
+  free_dev(p, (void *&)p.d_cells);
+  free_dev(p, (void *&)p.d_pair_j);
+  free_dev(p, (void *&)p.d_pair_w);
+  free_dev(p, (void *&)p.d_wav);
+  free_dev(p, (void *&)p.d_wav_ns);
+  free_dev(p, (void *&)p.d_amount);
+  free_dev(p, (void *&)p.d_group_ptr);
+  free_dev(p, (void *&)p.d_tiles);
   p.h_cells.clear();
-  for (auto b : p.wav_bufs) cudaFree(b);
+  for (auto b : p.wav_bufs) cudaFreeAsync(b, p.stream);
   p.wav_bufs.clear();
   p.n_cells = 0;
 }
 static void free_receivers(Plan &p) {
-  free_dev((void *&)p.rec_pool);
-  free_dev((void *&)p.d_rtask);
-  free_dev((void *&)p.d_roff);
-  free_dev((void *&)p.d_rw);
+  free_dev(p, (void *&)p.rec_pool);
+  free_dev(p, (void *&)p.d_rtask);
+  free_dev(p, (void *&)p.d_roff);
+  free_dev(p, (void *&)p.d_rw);
   p.n_rtask = 0;
 }
 
@@ -368,7 +385,6 @@ void destroy(gpi_plan *pl) {
   cudaSetDevice(p.device);
   if (p.stream) cudaStreamSynchronize(p.stream);
   drop_graphs(p);
-  if (p.own_stream) cudaStreamDestroy(p.own_stream);
   for (int k = 0; k < Plan::NSIDE; k++) {
     if (p.side[k]) {
       cudaStreamSynchronize(p.side[k]);
@@ -377,9 +393,11 @@ void destroy(gpi_plan *pl) {
     if (p.ev_join[k]) cudaEventDestroy(p.ev_join[k]);
   }
   if (p.ev_fork) cudaEventDestroy(p.ev_fork);
+  // stream-ordered frees on the plan's stream, then its own stream if any
   free_sources(p);
   free_receivers(p);
-  free_dev(p.pool);
+  free_dev(p, p.pool);
+  if (p.own_stream) cudaStreamDestroy(p.own_stream);
   cudaSetDevice(dev);
   delete pl;
 }
@@ -554,16 +572,16 @@ static int compile_receivers(Plan &p) {
     }
   p.rec_pool_floats = pool;
   p.n_rtask = (int)tasks.size();
-  if (pool) GPI_CUDA(&p, cudaMalloc(&p.rec_pool, pool * sizeof(float)));
+  if (pool) GPI_CUDA(&p, dalloc(p, (void **)&p.rec_pool, pool * sizeof(float)));
   if (!tasks.empty()) {
-    GPI_CUDA(&p, cudaMalloc(&p.d_rtask, tasks.size() * sizeof(RecTask)));
-    GPI_CUDA(&p, cudaMemcpy(p.d_rtask, tasks.data(), tasks.size() * sizeof(RecTask), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_rtask, tasks.size() * sizeof(RecTask)));
+    GPI_CUDA(&p, h2d(p, p.d_rtask, tasks.data(), tasks.size() * sizeof(RecTask)));
   }
   if (!offs.empty()) {
-    GPI_CUDA(&p, cudaMalloc(&p.d_roff, offs.size() * sizeof(int64_t)));
-    GPI_CUDA(&p, cudaMalloc(&p.d_rw, ws.size() * sizeof(float)));
-    GPI_CUDA(&p, cudaMemcpy(p.d_roff, offs.data(), offs.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
-    GPI_CUDA(&p, cudaMemcpy(p.d_rw, ws.data(), ws.size() * sizeof(float), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_roff, offs.size() * sizeof(int64_t)));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_rw, ws.size() * sizeof(float)));
+    GPI_CUDA(&p, h2d(p, p.d_roff, offs.data(), offs.size() * sizeof(int64_t)));
+    GPI_CUDA(&p, h2d(p, p.d_rw, ws.data(), ws.size() * sizeof(float)));
   }
   p.rec_dirty = false;
   return GPI_OK;
@@ -609,8 +627,8 @@ static int compile_sources(Plan &p) {
           lin.clear();
         }
         float *dw = nullptr;
-        GPI_CUDA(&p, cudaMalloc(&dw, src.wav.size() * sizeof(float)));
-        GPI_CUDA(&p, cudaMemcpy(dw, src.wav.data(), src.wav.size() * sizeof(float), cudaMemcpyHostToDevice));
+        GPI_CUDA(&p, dalloc(p, (void **)&dw, src.wav.size() * sizeof(float)));
+        GPI_CUDA(&p, h2d(p, dw, src.wav.data(), src.wav.size() * sizeof(float)));
         p.wav_bufs.push_back(dw);
         const int widx = (int)wavptr.size();
         wavptr.push_back(dw);
@@ -692,22 +710,22 @@ static int compile_sources(Plan &p) {
   p.group_ptr[groups.size()] = (int32_t)cells.size();
   p.n_cells = (int)cells.size();
   p.h_cells = cells;
-  GPI_CUDA(&p, cudaMalloc(&p.d_group_ptr, p.group_ptr.size() * sizeof(int32_t)));
-  GPI_CUDA(&p, cudaMemcpy(p.d_group_ptr, p.group_ptr.data(), p.group_ptr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  GPI_CUDA(&p, dalloc(p, (void **)&p.d_group_ptr, p.group_ptr.size() * sizeof(int32_t)));
+  GPI_CUDA(&p, h2d(p, p.d_group_ptr, p.group_ptr.data(), p.group_ptr.size() * sizeof(int32_t)));
   if (p.n_cells) {
-    GPI_CUDA(&p, cudaMalloc(&p.d_cells, cells.size() * sizeof(InjCell)));
-    GPI_CUDA(&p, cudaMemcpy(p.d_cells, cells.data(), cells.size() * sizeof(InjCell), cudaMemcpyHostToDevice));
-    GPI_CUDA(&p, cudaMalloc(&p.d_pair_j, pj.size() * sizeof(int32_t)));
-    GPI_CUDA(&p, cudaMalloc(&p.d_pair_w, pw.size() * sizeof(float)));
-    GPI_CUDA(&p, cudaMemcpy(p.d_pair_j, pj.data(), pj.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-    GPI_CUDA(&p, cudaMemcpy(p.d_pair_w, pw.data(), pw.size() * sizeof(float), cudaMemcpyHostToDevice));
-    GPI_CUDA(&p, cudaMalloc(&p.d_amount, cells.size() * sizeof(float)));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_cells, cells.size() * sizeof(InjCell)));
+    GPI_CUDA(&p, h2d(p, p.d_cells, cells.data(), cells.size() * sizeof(InjCell)));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_pair_j, pj.size() * sizeof(int32_t)));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_pair_w, pw.size() * sizeof(float)));
+    GPI_CUDA(&p, h2d(p, p.d_pair_j, pj.data(), pj.size() * sizeof(int32_t)));
+    GPI_CUDA(&p, h2d(p, p.d_pair_w, pw.data(), pw.size() * sizeof(float)));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_amount, cells.size() * sizeof(float)));
   }
   if (!wavptr.empty()) {
-    GPI_CUDA(&p, cudaMalloc(&p.d_wav, wavptr.size() * sizeof(float *)));
-    GPI_CUDA(&p, cudaMalloc(&p.d_wav_ns, wavns.size() * sizeof(int32_t)));
-    GPI_CUDA(&p, cudaMemcpy(p.d_wav, wavptr.data(), wavptr.size() * sizeof(float *), cudaMemcpyHostToDevice));
-    GPI_CUDA(&p, cudaMemcpy(p.d_wav_ns, wavns.data(), wavns.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_wav, wavptr.size() * sizeof(float *)));
+    GPI_CUDA(&p, dalloc(p, (void **)&p.d_wav_ns, wavns.size() * sizeof(int32_t)));
+    GPI_CUDA(&p, h2d(p, p.d_wav, wavptr.data(), wavptr.size() * sizeof(float *)));
+    GPI_CUDA(&p, h2d(p, p.d_wav_ns, wavns.data(), wavns.size() * sizeof(int32_t)));
   }
   p.src_dirty = false;
   return GPI_OK;
@@ -805,10 +823,10 @@ static int build_tiles(Plan &p) {
   std::vector<int32_t> zero(2 * p.d.nshots * NKIND + 1, 0);
   if (classify_tiles(p, p.xcut.data(), p.h_cells.data(), gp ? gp : zero.data(), t.data(), n, p.n_tiles) < 0)
     return fail(&p, GPI_E_INVALID, "tile list");
-  if (p.d_tiles) cudaFree(p.d_tiles);
+  if (p.d_tiles) cudaFreeAsync(p.d_tiles, p.stream);
   p.d_tiles = nullptr;
-  GPI_CUDA(&p, cudaMalloc(&p.d_tiles, n * sizeof(int4)));
-  GPI_CUDA(&p, cudaMemcpy(p.d_tiles, t.data(), n * sizeof(int4), cudaMemcpyHostToDevice));
+  GPI_CUDA(&p, dalloc(p, (void **)&p.d_tiles, n * sizeof(int4)));
+  GPI_CUDA(&p, h2d(p, p.d_tiles, t.data(), n * sizeof(int4)));
   return GPI_OK;
 }
 
@@ -930,9 +948,10 @@ static int run_body(Plan &p, int mode) {
 // a kernel reports a pipeline wait that gave up through d_err
 static int check_err(Plan &p) {
   int h = 0;
-  GPI_CUDA(&p, cudaMemcpy(&h, p.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  GPI_CUDA(&p, cudaMemcpyAsync(&h, p.d_err, sizeof(int), cudaMemcpyDeviceToHost, p.stream));
+  GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
   if (h) {
-    cudaMemset(p.d_err, 0, sizeof(int));
+    cudaMemsetAsync(p.d_err, 0, sizeof(int), p.stream);
     return fail(&p, GPI_E_CUDA, "a kernel's copy pipeline timed out; results of the last run are invalid");
   }
   return GPI_OK;

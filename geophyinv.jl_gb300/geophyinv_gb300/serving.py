@@ -2,12 +2,14 @@
 
 Requests of uneven grid sizes, step counts and shot counts arrive over time.
 The server admits a request as soon as an in-flight slot is free and its
-plan fits the HBM budget, gives it a plan of its own (all of its shots in one
-multi-shot launch per step, its own CUDA stream, the whole time loop as one
-CUDA graph) and keeps its wavefields, boundary store and records resident
-until it completes; requests on the GPU overlap, and the host work of one
-request (plan set-up, adjoint sources, record reads) overlaps the device work
-of the others.  A gradient request runs forward_save, builds its adjoint
+plan fits the HBM budget, prepares it on a host worker thread (model, CPML
+profiles, projections, a plan of its own with stream-ordered device
+allocations) while other requests run, then launches it on its own CUDA
+stream (all of its shots in one multi-shot launch per step; optionally the
+whole time loop as one CUDA graph, worth it for plans that run more than
+once) and keeps its wavefields, boundary store and records resident until it
+completes.  Requests on the GPU overlap, and the host work of one request
+overlaps the device work of the others.  A gradient request runs forward_save, builds its adjoint
 sources from the residuals and runs the adjoint (gradient!,
 src/fdtd/func_grad.jl:11-49).
 
@@ -167,33 +169,44 @@ def _streams(n):
     return [torch.cuda.Stream() for _ in range(n)]
 
 
-def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=True):
+def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=False, realtime=True, prep_threads=4):
     """Continuous batching: admit arrived requests while slots and HBM budget
-    allow, poll the in-flight ones, launch their next phase or collect their
-    results.  Returns (results by id, stats)."""
+    allow, prepare them on host threads, launch them when ready, poll the
+    in-flight ones, launch their next phase or collect their results.
+    Returns (results by id, stats)."""
+    from concurrent.futures import ThreadPoolExecutor
+
     import torch
 
     streams = _streams(max_inflight)
     free = list(range(max_inflight))
     pending = sorted(requests, key=lambda r: r.arrival)
+    preparing = {}
     inflight = {}
     results = {}
     used = 0
+    pool = ThreadPoolExecutor(max_workers=prep_threads)
     t0 = time.perf_counter()
-    while pending or inflight:
+    while pending or preparing or inflight:
         now = time.perf_counter() - t0
         # admission: arrival order, HBM budget, a free stream
         while pending and free and (not realtime or pending[0].arrival <= now):
             need = plan_bytes_estimate(pending[0])
-            if inflight and used + need > hbm_budget:
+            if (inflight or preparing) and used + need > hbm_budget:
                 break
             req = pending.pop(0)
             slot = free.pop()
-            job = _Job(req, graphs, streams[slot].cuda_stream)
-            job.res.t_admit = time.perf_counter() - t0
-            job.launch()
-            inflight[req.rid] = (job, slot, need)
+            preparing[req.rid] = (pool.submit(_Job, req, graphs, streams[slot].cuda_stream), slot, need,
+                                  time.perf_counter() - t0)
             used += need
+        for rid in list(preparing):
+            fut, slot, need, t_admit = preparing[rid]
+            if fut.done():
+                job = fut.result()
+                job.res.t_admit = t_admit
+                job.launch()
+                inflight[rid] = (job, slot, need)
+                del preparing[rid]
         done_any = False
         for rid in list(inflight):
             job, slot, need = inflight[rid]
@@ -208,6 +221,7 @@ def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=T
                     used -= need
         if not done_any:
             time.sleep(0.0002)
+    pool.shutdown()
     torch.cuda.synchronize()
     return results, _stats(requests, results, time.perf_counter() - t0)
 
