@@ -354,22 +354,27 @@ def gradient_arm(args, world, local):
 def serving_arm(args):
     """The mixed request stream (50 % acoustic forward, 30 % elastic forward,
     20 % acoustic gradient; Poisson arrivals) through the continuous-batching
-    loop and one request at a time with plain launches.  The stream is a
-    scaled version of the 2000-request one (sides 200-800 instead of
-    200-2000, 500-2000 steps instead of 1000-6000) so that both arms finish
-    in minutes."""
+    loop, one shot at a time with plain launches (the baseline the serving
+    target is quoted against) and one request at a time with its shots
+    batched.  The stream is a scaled version of the 2000-request one (sides
+    200-800 instead of 200-2000, 500-2000 steps instead of 1000-6000) so that
+    all arms finish in minutes.  Request payloads (models, geometry) are
+    built before the clock starts: they arrive with the request."""
     from geophyinv_gb300 import serving
 
     reqs = serving.make_stream(args.requests, rate=args.rate, seed=4, sides=(200, 800), steps=(500, 2000),
                                shots=(1, 8))
+    for r in reqs:
+        r.payload()
     warm = serving.make_stream(6, rate=1000.0, seed=5, sides=(100, 150), steps=(50, 60), shots=(1, 2))
     serving.serve(warm, realtime=False)
-    serving.serve_plain(warm, realtime=False)
+    serving.serve_plain(warm, realtime=False, per_shot=True)
     clocks = Clocks(0)
     clocks.start()
     _, st = serving.serve(reqs, max_inflight=8)
     clk = clocks.stop()
-    _, pl = serving.serve_plain(reqs)
+    _, pl = serving.serve_plain(reqs, per_shot=True)
+    _, pr = serving.serve_plain(reqs)
     return {"metric": "shots/s", "value": round(st["shots_per_s"], 3), "unit": "shots/s", "n_gpus": 1,
             "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic request stream (seed 4)",
@@ -378,8 +383,10 @@ def serving_arm(args):
                        "mix": "50 % acoustic forward, 30 % elastic forward, 20 % acoustic gradient",
                        "max_inflight": 8},
             "serving": {k: round(v, 4) if isinstance(v, float) else v for k, v in st.items()},
-            "plain": {k: round(v, 4) if isinstance(v, float) else v for k, v in pl.items()},
-            "speedup_shots_per_s": round(st["shots_per_s"] / pl["shots_per_s"], 3), "clocks": clk}
+            "plain_one_shot_at_a_time": {k: round(v, 4) if isinstance(v, float) else v for k, v in pl.items()},
+            "plain_one_request_at_a_time": {k: round(v, 4) if isinstance(v, float) else v for k, v in pr.items()},
+            "speedup_shots_per_s": round(st["shots_per_s"] / pl["shots_per_s"], 3),
+            "speedup_vs_request_at_a_time": round(st["shots_per_s"] / pr["shots_per_s"], 3), "clocks": clk}
 
 
 def reference_arm(args):

@@ -101,8 +101,11 @@ static void choose_tiling(Plan &p) {
     int per_chunk = p.nzb * p.d.nshots;
     int best = 1;
     double best_eff = 0;
-    // chunks of at least 16 columns (3 of them recomputed halo)
-    for (int m = 1; m <= std::max(1, p.d.nx / 16); m++) {
+    // chunks of at least 16 columns (3 of them recomputed halo); grids too
+    // small to fill the GPU with such chunks take chunks down to 8 columns,
+    // which halves the column march a step waits for
+    const int minw = (int64_t)std::max(1, p.d.nx / 16) * per_chunk < resident ? 8 : 16;
+    for (int m = 1; m <= std::max(1, p.d.nx / minw); m++) {
       int64_t blocks = (int64_t)m * per_chunk;
       double waves = (double)blocks / resident;
       double eff = waves / std::ceil(waves);

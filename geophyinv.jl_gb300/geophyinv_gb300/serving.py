@@ -13,10 +13,14 @@ overlaps the device work of the others.  A gradient request runs forward_save, b
 sources from the residuals and runs the adjoint (gradient!,
 src/fdtd/func_grad.jl:11-49).
 
-The baseline (`serve_plain`) models the same stream one request at a time
-with plain launches (no graphs, no overlap).  Results do not depend on what
-else runs: every request's arithmetic is its own and deterministic.
+A request carries its payload (model, geometry, wavelets: `Request.payload`,
+built by the client before it is sent); the server's own work starts at
+admission.  The baselines (`serve_plain`) take the same stream one shot at a
+time (a single-shot plan per shot, plain launches, no overlap), or one
+request at a time with its shots batched.  Results do not depend on what else
+runs: every request's arithmetic is its own and deterministic.
 """
+import copy
 import time
 from dataclasses import dataclass, field
 
@@ -40,6 +44,13 @@ class Request:
     nshots: int
     arrival: float = 0.0
     seed: int = 0
+    _payload: object = field(default=None, repr=False, compare=False)
+
+    def payload(self):
+        """The request's workload (built once, then kept)."""
+        if self._payload is None:
+            self._payload = self.workload()
+        return self._payload
 
     def workload(self):
         nrec = max(8, self.nx // 4)
@@ -106,15 +117,20 @@ class Result:
 class _Job:
     """The life of one request on the server (a small state machine)."""
 
-    def __init__(self, req, graphs, stream):
+    def __init__(self, req, graphs, stream, shot=None):
         self.req = req
-        self.wl = req.workload()
+        self.wl = req.payload()
+        if shot is not None:
+            self.wl = copy.copy(self.wl)
+            self.wl.shots = [self.wl.shots[shot]]
         mode = "forward_save" if req.kind == "acoustic_gradient" else "forward"
         self.pa = self.wl.expt(mode=mode, stream=stream)
         if graphs:
             self.pa.set_graph(True)
         self.res = Result(req.rid, req.kind)
         self.phase = 0
+        self.busy = None  # a launch still being issued on a worker thread
+        self.error = None
 
     def launch(self):
         pa = self.pa
@@ -127,9 +143,10 @@ class _Job:
         else:
             pa.run(_lib.FORWARD)
 
-    def finish_phase(self):
+    def finish_phase(self, pool=None):
         """Called when the device work of the current phase is done; returns
-        True when the request is complete."""
+        True when the request is complete.  The next phase is issued on a
+        worker thread of `pool` when one is given."""
         pa = self.pa
         recs = [{f: pa.records(i, f) for f in pa.rfields} for i in range(pa.nss)]
         if self.req.kind != "acoustic_gradient":
@@ -153,14 +170,28 @@ class _Job:
             pa.srcwav[1] = adj
             update(pa, pa.srcwav, [-1, 1])
             self.phase = 1
-            self.launch()
+            if pool is None:
+                self.launch()
+            else:
+                self.busy = pool.submit(self.launch)
+                self.busy.add_done_callback(self._issued)
             return False
         self.res.gradient = {"invK": pa.gradient_raw(0), "rho": pa.gradient_raw(1)}
         return True
 
+    def _issued(self, fut):
+        self.error = fut.exception()
+        self.busy = None
+
     def close(self):
         self.pa.close() if hasattr(self.pa, "close") else None
         self.pa = None
+
+
+def _prepare(req, graphs, stream):
+    job = _Job(req, graphs, stream)
+    job.launch()
+    return job
 
 
 def _streams(n):
@@ -196,7 +227,7 @@ def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=False, realtime=
                 break
             req = pending.pop(0)
             slot = free.pop()
-            preparing[req.rid] = (pool.submit(_Job, req, graphs, streams[slot].cuda_stream), slot, need,
+            preparing[req.rid] = (pool.submit(_prepare, req, graphs, streams[slot].cuda_stream), slot, need,
                                   time.perf_counter() - t0)
             used += need
         for rid in list(preparing):
@@ -204,15 +235,16 @@ def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=False, realtime=
             if fut.done():
                 job = fut.result()
                 job.res.t_admit = t_admit
-                job.launch()
                 inflight[rid] = (job, slot, need)
                 del preparing[rid]
         done_any = False
         for rid in list(inflight):
             job, slot, need = inflight[rid]
-            if job.pa.done():
+            if job.error is not None:
+                raise job.error
+            if job.busy is None and job.pa.done():
                 done_any = True
-                if job.finish_phase():
+                if job.finish_phase(pool):
                     job.res.t_done = time.perf_counter() - t0
                     results[rid] = job.res
                     job.close()
@@ -226,10 +258,24 @@ def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=False, realtime=
     return results, _stats(requests, results, time.perf_counter() - t0)
 
 
-def serve_plain(requests, realtime=True):
-    """One request at a time, plain launches, each to completion."""
+def _run_plain(job):
     import torch
 
+    job.launch()
+    while True:
+        torch.cuda.synchronize()
+        if job.finish_phase():
+            break
+    res = job.res
+    job.close()
+    return res
+
+
+def serve_plain(requests, realtime=True, per_shot=False):
+    """The baseline: one request at a time, or with `per_shot` one shot at a
+    time (a single-shot plan per shot), plain launches, each to completion.
+    A request's result collects its shots' records in order (and sums their
+    gradients and losses)."""
     results = {}
     t0 = time.perf_counter()
     for req in sorted(requests, key=lambda r: r.arrival):
@@ -237,16 +283,21 @@ def serve_plain(requests, realtime=True):
             wait = req.arrival - (time.perf_counter() - t0)
             if wait > 0:
                 time.sleep(wait)
-        job = _Job(req, False, None)
-        job.res.t_admit = time.perf_counter() - t0
-        job.launch()
-        while True:
-            torch.cuda.synchronize()
-            if job.finish_phase():
-                break
-        job.res.t_done = time.perf_counter() - t0
-        results[req.rid] = job.res
-        job.close()
+        t_admit = time.perf_counter() - t0
+        if not per_shot:
+            res = _run_plain(_Job(req, False, None))
+        else:
+            res = Result(req.rid, req.kind)
+            for i in range(req.nshots):
+                one = _run_plain(_Job(req, False, None, shot=i))
+                res.records += one.records
+                if one.gradient is not None:
+                    res.loss = one.loss if res.loss is None else res.loss + one.loss
+                    res.gradient = one.gradient if res.gradient is None else \
+                        {k: res.gradient[k] + one.gradient[k] for k in one.gradient}
+        res.t_admit = t_admit
+        res.t_done = time.perf_counter() - t0
+        results[req.rid] = res
     return results, _stats(requests, results, time.perf_counter() - t0)
 
 

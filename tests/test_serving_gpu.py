@@ -39,3 +39,24 @@ def test_admission_respects_the_hbm_budget(engine):
     res, stats = serving.serve(reqs, hbm_budget=budget, max_inflight=4, realtime=False)
     order = sorted(res.values(), key=lambda r: r.t_admit)
     assert all(b.t_admit >= a.t_done for a, b in zip(order, order[1:]))
+
+
+@pytest.mark.gpu
+def test_one_shot_at_a_time_baseline_gives_the_same_results(engine):
+    """The baseline's single-shot plans give the same records as the batched
+    multi-shot plans of the server (bit for bit), and the same summed
+    gradient up to the order of the shot sum."""
+    reqs = serving.make_stream(6, rate=1000.0, seed=11, sides=(60, 120), steps=(60, 150), shots=(2, 3))
+    mixed, _ = serving.serve(reqs, max_inflight=4, realtime=False)
+    single, _ = serving.serve_plain(reqs, realtime=False, per_shot=True)
+    for r in reqs:
+        a, b = mixed[r.rid], single[r.rid]
+        assert len(a.records) == len(b.records) == r.nshots
+        for ra, rb in zip(a.records, b.records):
+            for f in ra:
+                assert np.array_equal(ra[f], rb[f]), (r.rid, f)
+        if a.gradient is not None:
+            for k in a.gradient:
+                ga, gb = a.gradient[k].astype(np.float64), b.gradient[k].astype(np.float64)
+                assert np.linalg.norm(ga - gb) <= 1e-6 * np.linalg.norm(gb), (r.rid, k)
+            assert abs(a.loss - b.loss) <= 1e-6 * abs(b.loss)
