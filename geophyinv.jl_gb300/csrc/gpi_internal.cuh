@@ -153,6 +153,16 @@ struct Plan {
   cudaGraphExec_t gexec[3] = {};
   int64_t glaunches[3] = {};
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
+
+  // checkpointed adjoint (gpi_plan_desc.checkpoints > 0): full states of
+  // wavefield 1 (fields and CPML memory) in ck_slots device slots instead of
+  // the boundary store; the adjoint run recomputes forward states from them
+  // on a binomial schedule
+  int ck_slots = 0;
+  float *ck_pool = nullptr;
+  int64_t ck_floats = 0;                     // floats per slot
+  std::vector<std::pair<int, int>> ck_first;  // (state, slot) the forward_save run stores
+  std::vector<std::vector<Src>> ck_src;      // wavefield-1 sources of the forward_save run
 };
 
 // error helpers
@@ -203,6 +213,12 @@ int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_adjoint_acoustic2d(Plan *p, int it);
 int step_a2_wavefield(Plan *p, int ipw, int vonly);
+int step3_wavefield(Plan *p, int ipw, int vonly);
+// checkpointed adjoint (gpi_ckpt.cu)
+int64_t ckpt_slot_floats(const Plan &p);
+int ckpt_forward_store(Plan *p, int it);  // after forward_save step it
+int ckpt_adjoint(Plan *p);                 // the whole adjoint run
+int aux_step2(Plan *p, int it1, int it2);
 // host: x partition of a 2-D grid of nx columns into m interior chunks
 // plus, when the grid is wide enough, one narrow chunk at each x edge (the
 // mirror columns there need the general code) and one chunk over each x

@@ -176,6 +176,10 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   if (d.ndim != 2 && d.ndim != 3) return fail(nullptr, GPI_E_INVALID, "ndim must be 2 or 3");
   if (d.order != 4) return fail(nullptr, GPI_E_UNSUPPORTED, "the engine implements order 4 only");
   if (d.nt < 1 || d.nshots < 1 || (d.npw != 1 && d.npw != 2)) return fail(nullptr, GPI_E_INVALID, "nt/nshots/npw");
+  if (d.checkpoints < 0 || (d.checkpoints > 0 && d.npw != 2))
+    return fail(nullptr, GPI_E_INVALID, "checkpoints: > 0 only with npw = 2");
+  if (d.checkpoints > 0 && d.physics != GPI_ACOUSTIC)
+    return fail(nullptr, GPI_E_UNSUPPORTED, "checkpointed gradients: acoustic media only");
   if (d.npml < 1 || d.nbound < 1) return fail(nullptr, GPI_E_INVALID, "npml/nbound");
   if (!(d.dt > 0) || !(d.dz > 0) || !(d.dx > 0) || (d.ndim == 3 && !(d.dy > 0)))
     return fail(nullptr, GPI_E_INVALID, "dt and grid steps must be positive");
@@ -242,7 +246,13 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   for (int i = 0; i < p.ncoef; i++) allocs.push_back({&p.coef[i], p.fstride});
   allocs.push_back({&p.pml, (int64_t)p.nder * 3 * 2 * d.npml});
   allocs.push_back({(float **)&p.d_err, 64});
-  if (d.npw == 2) {
+  if (d.npw == 2 && d.checkpoints > 0) {
+    // checkpointed adjoint: state slots instead of the boundary store
+    for (int i = 0; i < p.nmod && i < 2; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
+    p.ck_slots = d.checkpoints;
+    p.ck_floats = ckpt_slot_floats(p);
+    allocs.push_back({&p.ck_pool, p.ck_floats * p.ck_slots});
+  } else if (d.npw == 2) {
     for (int i = 0; i < p.nmod && i < 2; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
     int ids[3];
     int ns = nsaved(p, ids);
@@ -858,18 +868,45 @@ static int zero_state(Plan &p) {
 
 static int run_body(Plan &p, int mode);
 
+static bool same_sources(const std::vector<std::vector<Plan::Src>> &a, const std::vector<std::vector<Plan::Src>> &b) {
+  if (a.size() != b.size()) return false;
+  for (size_t s = 0; s < a.size(); s++) {
+    if (a[s].size() != b[s].size()) return false;
+    for (size_t f = 0; f < a[s].size(); f++) {
+      const Plan::Src &x = a[s][f], &y = b[s][f];
+      if (x.ns != y.ns || x.cp != y.cp || x.rv != y.rv || x.nz != y.nz || x.wav != y.wav) return false;
+    }
+  }
+  return true;
+}
+
+void ckpt_prepare_forward(Plan *p);  // gpi_ckpt.cu
+
 int run(Plan &p, int mode) {
   if (mode != GPI_FORWARD && mode != GPI_FORWARD_SAVE && mode != GPI_ADJOINT) return fail(&p, GPI_E_INVALID, "mode");
   if (mode != GPI_FORWARD && p.d.npw != 2) return fail(&p, GPI_E_INVALID, "forward_save/adjoint need npw = 2");
   if (mode == GPI_ADJOINT && !p.have_save) return fail(&p, GPI_E_STATE, "adjoint run needs a forward_save run first");
-  if (mode == GPI_ADJOINT && !(p.d.physics == GPI_ACOUSTIC && p.d.ndim == 2))
-    return fail(&p, GPI_E_UNSUPPORTED, "the reference computes gradients for 2-D acoustic media only");
+  if (mode == GPI_ADJOINT && !(p.d.physics == GPI_ACOUSTIC && (p.d.ndim == 2 || p.ck_slots > 0)))
+    return fail(&p, GPI_E_UNSUPPORTED,
+                "gradients: acoustic media only, 3-D with a checkpointed plan (the reference: 2-D acoustic)");
   if (mode == GPI_FORWARD_SAVE && p.d.ndim == 3 && p.d.physics == GPI_ELASTIC)
     return fail(&p, GPI_E_UNSUPPORTED, "the reference defines no boundary store for 3-D elastic media");
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev != p.device) GPI_CUDA(&p, cudaSetDevice(p.device));
   int rc = GPI_OK;
+  // a checkpointed adjoint recomputes wavefield 1 with the sources of its
+  // forward_save run, whatever the caller set for the time-reversed run
+  // (update!(pa, srcwav, [-1, 1]) in gradient!, func_grad.jl:33)
+  const bool swap_src = p.ck_slots > 0 && mode == GPI_ADJOINT && !same_sources(p.src[0], p.ck_src);
+  if (swap_src) {
+    std::swap(p.src[0], p.ck_src);
+    p.src_dirty = true;
+  }
+  if (p.ck_slots > 0 && mode == GPI_FORWARD_SAVE) {
+    ckpt_prepare_forward(&p);
+    p.ck_src = p.src[0];
+  }
   const bool recompile = p.rec_dirty || p.src_dirty || (p.d.ndim == 2 && !p.d_tiles);
   if (p.rec_dirty) rc = compile_receivers(p);
   if (!rc && p.src_dirty) {
@@ -904,6 +941,10 @@ int run(Plan &p, int mode) {
   } else if (!rc) {
     rc = run_body(p, mode);
   }
+  if (swap_src) {
+    std::swap(p.src[0], p.ck_src);
+    p.src_dirty = true;
+  }
   if (dev != p.device) cudaSetDevice(dev);
   return rc;
 }
@@ -917,6 +958,15 @@ void drop_graphs(Plan &p) {
 
 // the device work of one run: state reset, the time loop, the final half step
 static int run_body(Plan &p, int mode) {
+  if (mode == GPI_ADJOINT && p.ck_slots > 0) {
+    p.launches = 0;
+    int rc = ckpt_adjoint(&p);
+    if (!rc) {
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));
+    }
+    return rc;
+  }
   int rc = zero_state(p);
   p.launches = 0;
   // an adjoint run records nothing and keeps the records of the forward run
@@ -934,12 +984,13 @@ static int run_body(Plan &p, int mode) {
     // boundary_force! (the replaced values are kept for the gradient)
     if (!rc && mode == GPI_ADJOINT) rc = boundary_io(&p, p.d.nt - it + 1, 2);
     if (!rc) rc = step(p, mask, it, mode, 0);
-    if (!rc && mode == GPI_FORWARD_SAVE) rc = boundary_io(&p, it, 0);
+    if (!rc && mode == GPI_FORWARD_SAVE) rc = p.ck_slots > 0 ? ckpt_forward_store(&p, it) : boundary_io(&p, it, 0);
   }
+  const bool snaps = mode == GPI_FORWARD_SAVE && p.ck_slots == 0;
   if (!rc) rc = aux_step(&p, p.d.nt + 1, mode);  // velocity records of the last step
-  if (!rc && mode == GPI_FORWARD_SAVE) rc = snap_io(&p, 1, 0);
+  if (!rc && snaps) rc = snap_io(&p, 1, 0);
   if (!rc) rc = step(p, 1, p.d.nt + 1, mode, 1);  // the extra velocity half step (propagate.jl:254-255)
-  if (!rc && mode == GPI_FORWARD_SAVE) rc = snap_io(&p, 0, 0);
+  if (!rc && snaps) rc = snap_io(&p, 0, 0);
   if (!rc) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));

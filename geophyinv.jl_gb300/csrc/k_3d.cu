@@ -333,7 +333,9 @@ __global__ void k3_inject(const InjCell *cells, const int32_t *gptr, const float
   }
 }
 
-static int step3(Plan *p, int vonly) {
+// one step of wavefield ipw (vonly: bit 0 velocity half step only, bit 1
+// with the velocity sources)
+int step3_wavefield(Plan *p, int ipw, int vonly) {
   const bool ac = p->d.physics == GPI_ACOUSTIC;
   Step3 a;
   a.g = G3{p->d.nz, p->d.ny, p->d.nx, p->NZP, p->NYP, p->fstride};
@@ -341,13 +343,14 @@ static int step3(Plan *p, int vonly) {
   a.m.npml = p->d.npml;
   a.m.w = 2 * p->d.npml;
   a.m.faces = p->d.pml_faces;
-  const int A = p->cur[0];  // 3-D steps update in place
+  const int A = p->cur[ipw];  // 3-D steps update in place
   for (int q = 0; q < 18; q++) {
-    a.m.psi[q] = q < p->nder ? p->psi[A][0][q] : nullptr;
+    a.m.psi[q] = q < p->nder ? p->psi[A][ipw][q] : nullptr;
     a.m.pss[q] = q < p->nder ? p->psi_stride[q] : 0;
   }
   Fields3 fl;
-  for (int f = 0; f < NFIELD; f++) a.f[f] = fl.f[f] = p->state[A][0][f];
+  for (int f = 0; f < NFIELD; f++) a.f[f] = fl.f[f] = p->state[A][ipw][f];
+  const int32_t *gptr = p->d_group_ptr + (int64_t)ipw * p->d.nshots * NKIND;  // this wavefield's cell groups
   for (int i = 0; i < 8; i++) a.cf[i] = p->coef[i];
   a.dzI = (float)(1.0 / (p->d.dz * 24.0));
   a.dyI = (float)(1.0 / (p->d.dy * 24.0));
@@ -394,8 +397,8 @@ static int step3(Plan *p, int vonly) {
     p->launches++;
   }
   const int ng = p->d.nshots * NKIND;
-  if (!vonly && p->n_cells) {
-    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, p->d_group_ptr, p->d_amount, fl, p->fstride,
+  if ((!vonly || (vonly & 2)) && p->n_cells) {
+    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride,
                                                        p->d.nshots, 1, p->d.physics);
     p->launches++;
   }
@@ -410,7 +413,7 @@ static int step3(Plan *p, int vonly) {
     p->launches++;
   }
   if (p->n_cells) {
-    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, p->d_group_ptr, p->d_amount, fl, p->fstride,
+    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride,
                                                        p->d.nshots, 0, p->d.physics);
     p->launches++;
   }
@@ -422,13 +425,13 @@ int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   (void)ipw_mask;
   (void)it;
   (void)mode;
-  return step3(p, vonly);
+  return step3_wavefield(p, 0, vonly);
 }
 int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   (void)ipw_mask;
   (void)it;
   (void)mode;
-  return step3(p, vonly);
+  return step3_wavefield(p, 0, vonly);
 }
 
 }  // namespace gpi

@@ -42,7 +42,8 @@ struct A2Args {
   const InjCell *cells;
   const int32_t *gptr;
   const float *amount;
-  int vonly;
+  int vonly;  // bit 0: velocity half step only; bit 1: with the velocity
+              // sources; bit 2: leave the target p unwritten
   int *err;
   const int4 *tiles;  // (z-block, first column, end column, shot) per block
   int zsw, pzw, psf;  // z-strip column stride, staged window, CPML floats per ring slot
@@ -272,6 +273,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
   } else {
   // columns that need the full general code: x edges and mirrors, sources
   auto colfull_v = [&](int cc) { return a.vonly || cc <= 4 || cc >= nx - 4; };
+  const bool vsrc = !(a.vonly & 1) || (a.vonly & 2);
   auto colfull_s = [&](int c) { return a.vonly || c >= nx - 4; };
   // per-row constants of the band path (vxr already excludes the halo rows)
   const int kqc = vact ? kq : 0;
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
               a.vxB[so + S(q, 2)] = g2;
             }
           }
-          if (!a.vonly) inject(a.cells, a.amount, ib0, ie0, q, vx);
+          if (vsrc) inject(a.cells, a.amount, ib0, ie0, q, vx);
           svx[s * R4 + k] = vx;
           if (ownx) a.vxB[so + S(q, cc)] = vx;
         }
@@ -422,7 +424,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
             vz = vz + v0[3 * R4 + k] * D;
           }
         }
-        if (!a.vonly) inject(a.cells, a.amount, ib1, ie1, q, vz);
+        if (vsrc) inject(a.cells, a.amount, ib1, ie1, q, vz);
         svz[s * R4 + k] = vz;
         if (ownc && ownr && cc <= nx && q <= nz + 3) a.vzB[so + S(q, cc)] = vz;
       };
@@ -442,7 +444,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
           pn = pn + (Dx + Dz) * pc[R8 + 4 * R4 + k];
           inject(a.cells, a.amount, bs, es, r, pn);  // add_stress_source!
         }
-        a.pB[so + S(r, c)] = pn;
+        if (!(a.vonly & 4)) a.pB[so + S(r, c)] = pn;
       };
       // one sweep: iterations c < x0 only compute the first velocity columns
       for (int c = x0 - 3; c < x1; c++) {

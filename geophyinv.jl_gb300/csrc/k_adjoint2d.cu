@@ -81,6 +81,39 @@ __global__ void __launch_bounds__(256) k_grad_a2(const GradArgs a) {
   }
 }
 
+// the imaging condition with wavefield 1's old (A) and new (B) states given
+// explicitly and no strip values (the checkpointed adjoint)
+int grad_a2_launch(Plan *p, const float *p1A, const float *p1B, const float *vx1A, const float *vx1B,
+                   const float *vz1A, const float *vz1B) {
+  GradArgs g;
+  g.nz = p->d.nz;
+  g.nx = p->d.nx;
+  g.NZP = p->NZP;
+  g.fs = p->fstride;
+  g.nshots = p->d.nshots;
+  g.p1A = p1A;
+  g.p1B = p1B;
+  const int A2 = p->cur[1];
+  g.p2A = p->state[A2][1][GPI_P];
+  g.vx1A = vx1A;
+  g.vx1B = vx1B;
+  g.vx2A = p->state[A2][1][GPI_VX];
+  g.vz1A = vz1A;
+  g.vz1B = vz1B;
+  g.vz2A = p->state[A2][1][GPI_VZ];
+  g.prev = nullptr;
+  g.pstride = 0;
+  g.nb = 0;  // no strip replaces a value
+  g.npx = g.npz = 0;
+  g.gK = p->grad[0];
+  g.gR = p->grad[1];
+  g.dtI = (float)(1.0 / p->d.dt);
+  k_grad_a2<<<152 * 16, 256, 0, p->stream>>>(g);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
 int step_adjoint_acoustic2d(Plan *p, int it) {
   (void)it;
   if (!p->grad[0] || !p->grad[1] || !p->bprev) return fail(p, GPI_E_STATE, "adjoint step without gradient buffers");

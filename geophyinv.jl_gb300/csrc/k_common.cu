@@ -117,6 +117,8 @@ struct AuxArgs {
   const float *rw;
   float *rec;
   int it, nt;
+  int it2, split;  // cells from `split` on (the adjoint wavefield's) take step it2
+  int zero;        // write 0 for cells whose step is out of range
   const float *field[NFIELD];  // wavefield 1, current buffer, shot 0
   int64_t fs;
   const InjCell *cells;
@@ -149,9 +151,14 @@ __global__ void k_aux(AuxArgs a) {
     return;
   }
   i -= a.ntask;
-  if (i >= a.ncells || a.it > a.nt) return;
+  if (i >= a.ncells) return;
+  const int itc = i < a.split ? a.it : a.it2;
+  if (itc < 1 || itc > a.nt) {
+    if (a.zero) a.amount[i] = 0.f;
+    return;
+  }
   const InjCell c = a.cells[i];
-  const float *w = a.wav[c.wav] + (a.it - 1);
+  const float *w = a.wav[c.wav] + (itc - 1);
   float pv = 0.f;
   for (int e = c.e0; e < c.e1; e++) pv = pv + a.pw[e] * w[(int64_t)a.pj[e] * a.nt];
   float amt;
@@ -160,6 +167,32 @@ __global__ void k_aux(AuxArgs a) {
   else
     amt = pv * a.kcoef[c.off];  // muladd_tauii!
   a.amount[i] = amt;
+}
+
+// source amounts of wavefield 1 at step it1 and of the adjoint wavefield at
+// step it2 (0: none), no records (the checkpointed adjoint)
+int aux_step2(Plan *p, int it1, int it2) {
+  if (!p->n_cells) return GPI_OK;
+  AuxArgs a = {};
+  a.ntask = 0;
+  a.it = it1;
+  a.it2 = it2;
+  a.nt = p->d.nt;
+  a.split = p->d.npw == 2 ? p->group_ptr[(size_t)p->d.nshots * NKIND] : p->n_cells;
+  a.zero = 1;
+  a.cells = p->d_cells;
+  a.ncells = p->n_cells;
+  a.pj = p->d_pair_j;
+  a.pw = p->d_pair_w;
+  a.wav = p->d_wav;
+  a.amount = p->d_amount;
+  a.rho = p->mod[p->d.physics == GPI_ACOUSTIC ? 1 : 2];
+  a.kcoef = p->d.physics == GPI_ACOUSTIC ? p->coef[p->ncoef - 1] : p->coef[p->ncoef - 2];
+  a.dt = (float)p->d.dt;
+  k_aux<<<(p->n_cells + 127) / 128, 128, 0, p->stream>>>(a);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
 }
 
 int aux_step(Plan *p, int it, int mode) {
@@ -175,6 +208,9 @@ int aux_step(Plan *p, int it, int mode) {
   a.rec = p->rec_pool;
   a.it = it;
   a.nt = p->d.nt;
+  a.it2 = it;
+  a.split = p->n_cells;
+  a.zero = 0;
   for (int f = 0; f < NFIELD; f++) a.field[f] = p->state[p->cur[0]][0][f];
   a.fs = p->fstride;
   a.cells = p->d_cells;

@@ -20,7 +20,7 @@ FIELD = {"p": 0, "vx": 1, "vy": 2, "vz": 3, "tauxx": 4, "tauyy": 5, "tauzz": 6, 
 EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_stream", "gpi_plan_bytes",
            "gpi_set_medium", "gpi_set_pml", "gpi_set_sources", "gpi_clear_sources", "gpi_set_receivers",
            "gpi_run", "gpi_get_records", "gpi_get_gradient", "gpi_get_field", "gpi_last_launches",
-           "gpi_set_graph", "gpi_query", "gpi_forward_acoustic2d_noalloc"]
+           "gpi_set_graph", "gpi_query", "gpi_checkpoint_schedule", "gpi_forward_acoustic2d_noalloc"]
 
 
 class PlanDesc(ctypes.Structure):
@@ -28,7 +28,8 @@ class PlanDesc(ctypes.Structure):
                 ("nz", ctypes.c_int32), ("ny", ctypes.c_int32), ("nx", ctypes.c_int32),
                 ("npml", ctypes.c_int32), ("nbound", ctypes.c_int32), ("pml_faces", ctypes.c_int32),
                 ("rigid_faces", ctypes.c_int32), ("free_faces", ctypes.c_int32), ("nt", ctypes.c_int32),
-                ("nshots", ctypes.c_int32), ("npw", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4),
+                ("nshots", ctypes.c_int32), ("npw", ctypes.c_int32), ("checkpoints", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 3),
                 ("dt", ctypes.c_double), ("dz", ctypes.c_double), ("dy", ctypes.c_double), ("dx", ctypes.c_double)]
 
 
@@ -73,6 +74,8 @@ def load():
     L.gpi_last_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.gpi_set_graph.argtypes = [vp, i32]
     L.gpi_query.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
+    L.gpi_checkpoint_schedule.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                          ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]
     L.gpi_forward_acoustic2d_noalloc.argtypes = [ctypes.POINTER(PlanDesc), fp, fp, fp, i32, i32, i64p, i64p, fp, fp,
                                                  i32, vp, vp, vp, vp, vp, vp, vp]
     _LIB = L

@@ -127,7 +127,7 @@ class SeisForwExpt:
 
     def __init__(self, attrib, *, medium, ageom, srcwav, tgrid, rfields=("vz",), pml_faces=ALL_FACES,
                  rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False,
-                 npml=None):
+                 npml=None, checkpoints=0):
         L = _lib.load()
         self.L = L
         self.attrib = attrib
@@ -184,6 +184,10 @@ class SeisForwExpt:
         d.nt = self.nt
         d.nshots = self.nss
         d.npw = attrib.npw
+        # checkpointed adjoint (no counterpart in the reference): this many
+        # device slots of wavefield-1 states replace the boundary store
+        d.checkpoints = int(checkpoints) if attrib.npw == 2 else 0
+        self.checkpoints = d.checkpoints
         d.dt = self.dt
         self.desc = d
         plan = ctypes.c_void_p()
@@ -482,7 +486,9 @@ def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
             s.d[f] = loss.deriv(o.d[f], c.d[f])[::-1].copy()  # reverse!(srcwav[2])
         adj.append(s)
     pa.srcwav[1] = adj
-    update(pa, pa.srcwav, [-1, 1])
+    # a checkpointed plan recomputes wavefield 1 forward in time, with the
+    # sources of its forward_save run (no time-reversed copy is needed)
+    update(pa, pa.srcwav, [1 if pa.checkpoints else -1, 1])
     pa.attrib.mode = "adjoint"
     update(pa)
     inn = _inner(pa)

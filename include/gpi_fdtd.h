@@ -67,7 +67,13 @@ typedef struct {
   int32_t nt;          /* time steps */
   int32_t nshots;      /* supersources held by the plan */
   int32_t npw;         /* propagating wavefields: 1 (forward) or 2 (forward_save + adjoint) */
-  int32_t reserved[4];
+  /* > 0 (acoustic, npw = 2): a checkpointed adjoint instead of the boundary
+   * store (boundary.jl): forward_save keeps this many full states of
+   * wavefield 1 on the device and the adjoint run recomputes forward states
+   * from them on a binomial schedule; 3-D acoustic gradients too.  No
+   * counterpart in the reference.  0: the reference's boundary store. */
+  int32_t checkpoints;
+  int32_t reserved[3];
   double dt, dz, dy, dx; /* time step and grid steps (dy ignored in 2-D) */
 } gpi_plan_desc;
 
@@ -133,6 +139,11 @@ int gpi_set_graph(gpi_plan *plan, int enable);
 /* Non-blocking completion test of the plan's stream (1 when all work
  * issued so far has finished).  No counterpart in the reference. */
 int gpi_query(gpi_plan *plan, int *done);
+/* The binomial checkpoint schedule of a checkpointed adjoint over nt steps
+ * with `slots` state slots (host only, no device needed): forward steps it
+ * recomputes besides its turns, turns (= nt), slots the forward_save run
+ * fills.  No counterpart in the reference. */
+int gpi_checkpoint_schedule(int nt, int slots, int64_t *advances, int64_t *turns, int *stored);
 
 /* Size of the device scratch array used by gpi_forward_acoustic2d_noalloc. */
 #define GPI_NOALLOC_SCRATCH_BYTES (64u << 20)

@@ -121,6 +121,8 @@ typedef struct gpo_ctx {
   size_t pvlen;
   int nshots;
   REAL **bstore; /* boundary store per shot */
+  REAL **hist;   /* forward history per shot (GPO_FORWARD_HIST) */
+  size_t hstep;  /* REALs per step in the history: p, vx, [vy,] vz */
   size_t bstep;  /* REALs per time step in the store */
   size_t bsnap;  /* REALs of the final snapshots */
 } ctx;
@@ -697,24 +699,66 @@ static void compute_gradient(ctx *c, REAL *gK, REAL *gR) {
   /* compute_gmodKI!: g += pa_prev * (pf_prev - pf) * dtI */
   for (size_t i = 0; i < alen(p1); i++) gK[i] = gK[i] + p2p.a[i] * (p1p.a[i] - p1.a[i]) * dtI;
   /* compute_gmodrho!: buffer = va_prev * (vf - vf_prev) * dtI */
-  const int vids[2] = {GPO_VX, GPO_VZ};
-  for (int q = 0; q < 2; q++) {
+  const int three = c->d.ndim == 3;
+  const int vids[3] = {GPO_VX, GPO_VZ, GPO_VY};
+  for (int q = 0; q < 2 + three; q++) {
     arr vf = c->w[0][vids[q]], vfp = c->wp[0][vids[q]], vap = c->wp[1][vids[q]], bf = c->vbuf[q];
     for (size_t i = 0; i < alen(vf); i++) bf.a[i] = vap.a[i] * (vf.a[i] - vfp.a[i]) * dtI;
   }
-  /* combine_gmodrho!: @inn(g) = @inn(g) - @av_xi(vxbuf) - @av_zi(vzbuf) */
+  /* combine_gmodrho!: @inn(g) = @inn(g) - @av_xi(vxbuf) - @av_zi(vzbuf).
+   * 3-D (no reference counterpart): the same with the y average between
+   * them, g - avx - avy - avz, each average one cell off the stencil centre
+   * along its axis as in 2-D. */
   arr g;
   g.a = gR;
   g.n1 = c->d.nz;
-  g.n2 = 1;
+  g.n2 = c->d.ny;
   g.n3 = c->d.nx;
-  arr bx = c->vbuf[0], bz = c->vbuf[1];
+  arr bx = c->vbuf[0], bz = c->vbuf[1], by = c->vbuf[2];
+  const int hy = three ? h : 0;
   for (int ix = 1; ix <= g.n3 - 2 * h; ix++)
-    for (int iz = 1; iz <= g.n1 - 2 * h; iz++) {
-      REAL avx = (AT(bx, iz + h, 1, ix) + AT(bx, iz + h, 1, ix + 1)) * (REAL)0.5;
-      REAL avz = (AT(bz, iz, 1, ix + h) + AT(bz, iz + 1, 1, ix + h)) * (REAL)0.5;
-      AT(g, iz + h, 1, ix + h) = AT(g, iz + h, 1, ix + h) - avx - avz;
+    for (int iy = 1; iy <= g.n2 - 2 * hy; iy++)
+      for (int iz = 1; iz <= g.n1 - 2 * h; iz++) {
+        REAL avx = (AT(bx, iz + h, iy + hy, ix) + AT(bx, iz + h, iy + hy, ix + 1)) * (REAL)0.5;
+        REAL avz = (AT(bz, iz, iy + hy, ix + h) + AT(bz, iz + 1, iy + hy, ix + h)) * (REAL)0.5;
+        REAL gv = AT(g, iz + h, iy + hy, ix + h) - avx;
+        if (three) gv = gv - (AT(by, iz + h, iy, ix + h) + AT(by, iz + h, iy + 1, ix + h)) * (REAL)0.5;
+        AT(g, iz + h, iy + hy, ix + h) = gv - avz;
+      }
+}
+
+static void save_tp(ctx *c, int ipw);
+
+/* forward history (GPO_FORWARD_HIST): slot s holds p after step s and the
+ * velocities after step s (s = nt + 1: after the extra half step) */
+static void hist_io(ctx *c, int ishot, int s, int dir, int with_p) {
+  REAL *b = c->hist[ishot] + (size_t)s * c->hstep;
+  const int ids[4] = {GPO_P, GPO_VX, GPO_VY, GPO_VZ};
+  for (int q = 0; q < 4; q++) {
+    if (!c->present[ids[q]]) continue;
+    arr f = c->w[0][ids[q]];
+    if (q > 0 || with_p) {
+      if (dir == 0)
+        memcpy(b, f.a, alen(f) * sizeof(REAL));
+      else
+        memcpy(f.a, b, alen(f) * sizeof(REAL));
     }
+    b += alen(f);
+  }
+}
+/* wavefield 1 of adjoint step it from the history: tp = (-p_s, v_{s+1}),
+ * t = (-p_{s-1}, v_s) with s = nt - it + 1, as the time-reversed run holds
+ * them (p reversed in sign, velocities not) */
+static void hist_states(ctx *c, int ishot, int it) {
+  const int s = c->d.nt - it + 1;
+  arr p = c->w[0][GPO_P];
+  hist_io(c, ishot, s, 1, 1);
+  for (size_t i = 0; i < alen(p); i++) p.a[i] = -p.a[i];
+  hist_io(c, ishot, s + 1, 1, 0);
+  save_tp(c, 0);
+  hist_io(c, ishot, s - 1, 1, 1);
+  for (size_t i = 0; i < alen(p); i++) p.a[i] = -p.a[i];
+  hist_io(c, ishot, s, 1, 0);
 }
 
 /* ------------------------------------------------------------------ */
@@ -798,6 +842,11 @@ gpo_ctx *SFX(gpo_create)(const gpo_desc *d, const void *const *mod, const void *
   }
   c->vbuf[0] = field_arr(c, GPO_VX);
   c->vbuf[1] = field_arr(c, GPO_VZ);
+  if (d->ndim == 3) c->vbuf[2] = field_arr(c, GPO_VY);
+  c->hstep = 0;
+  if (c->present[GPO_P])
+    for (int f = 0; f < 4; f++)
+      if (c->present[f]) c->hstep += alen(c->w[0][f]);
   c->pvlen = maxlen;
   c->pv = (REAL *)calloc(maxlen, sizeof(REAL));
   c->pvflag = (unsigned char *)calloc(maxlen, 1);
@@ -817,6 +866,7 @@ gpo_ctx *SFX(gpo_create)(const gpo_desc *d, const void *const *mod, const void *
   if (d->ndim == 3) c->bsnap += alen(c->w[0][GPO_VY]);
   c->nshots = nshots;
   c->bstore = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
+  c->hist = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
   return (gpo_ctx *)c;
 }
 
@@ -849,29 +899,40 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
   if (c->d.nthreads > 0) omp_set_num_threads(c->d.nthreads);
 #endif
   const int nt = c->d.nt;
-  const int adjoint = mode == GPO_ADJOINT;
-  if (mode != GPO_FORWARD && !c->bstore[ishot])
+  const int hist = mode == GPO_FORWARD_HIST || mode == GPO_ADJOINT_HIST;
+  const int adjoint = mode == GPO_ADJOINT || mode == GPO_ADJOINT_HIST;
+  if ((mode == GPO_FORWARD_SAVE || mode == GPO_ADJOINT) && !c->bstore[ishot])
     c->bstore[ishot] = (REAL *)calloc((size_t)nt * c->bstep + c->bsnap, sizeof(REAL));
-  if (adjoint && (c->d.physics != GPO_ACOUSTIC || c->d.ndim != 2) && (grad_invK || grad_rho)) return -2;
+  if (hist && (c->d.physics != GPO_ACOUSTIC || !c->hstep)) return -2;
+  if (mode == GPO_FORWARD_HIST && !c->hist[ishot])
+    c->hist[ishot] = (REAL *)calloc((size_t)(nt + 2) * c->hstep, sizeof(REAL));
+  if (mode == GPO_ADJOINT_HIST && !c->hist[ishot]) return -3;
+  if (mode == GPO_ADJOINT && (c->d.physics != GPO_ACOUSTIC || c->d.ndim != 2) && (grad_invK || grad_rho)) return -2;
   reset_w(c);
-  if (adjoint) {
+  if (mode == GPO_ADJOINT) {
     snap_io(c, ishot, 1, 1); /* boundary_force_snap_tau! */
     snap_io(c, ishot, 0, 1); /* boundary_force_snap_v! */
   }
+  /* the history run propagates the adjoint wavefield alone */
+  const int pw0 = mode == GPO_ADJOINT_HIST ? 1 : 0;
   const int npw = adjoint ? 2 : 1;
   for (int it = 1; it <= nt; it++) {
     /* record! [:p] */
     for (int r = 0; r < nrec; r++)
       if (rec[r].field == GPO_P) record(c, c->w[0], &rec[r], it - 1);
-    if (adjoint) {
+    if (mode == GPO_ADJOINT) {
       save_tp(c, 0);
       save_tp(c, 1);
       boundary_force(c, ishot, nt - it + 1);
     }
-    for (int ipw = 0; ipw < npw; ipw++) update_dstress(c, ipw);
-    for (int ipw = 0; ipw < npw; ipw++) update_v(c, ipw);
+    if (mode == GPO_ADJOINT_HIST) {
+      save_tp(c, 1);
+      hist_states(c, ishot, it);
+    }
+    for (int ipw = pw0; ipw < npw; ipw++) update_dstress(c, ipw);
+    for (int ipw = pw0; ipw < npw; ipw++) update_v(c, ipw);
     /* add_velocity_source! (wavefield 1, then the adjoint wavefield) */
-    for (int s = 0; s < nsrc; s++)
+    for (int s = 0; s < nsrc && !pw0; s++)
       if (is_velocity(src[s].field)) add_velocity_source(c, c->w[0], &src[s], it - 1);
     if (adjoint)
       for (int s = 0; s < nadj; s++)
@@ -879,18 +940,21 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
     /* record! [:vx, :vy, :vz] */
     for (int r = 0; r < nrec; r++)
       if (is_velocity(rec[r].field)) record(c, c->w[0], &rec[r], it - 1);
-    for (int ipw = 0; ipw < npw; ipw++) update_dv(c, ipw);
-    for (int ipw = 0; ipw < npw; ipw++) update_stress(c, ipw);
+    for (int ipw = pw0; ipw < npw; ipw++) update_dv(c, ipw);
+    for (int ipw = pw0; ipw < npw; ipw++) update_stress(c, ipw);
     /* add_stress_source! (wavefield 1 only) */
-    for (int s = 0; s < nsrc; s++)
+    for (int s = 0; s < nsrc && !pw0; s++)
       if (is_stress_src(src[s].field)) add_stress_source(c, c->w[0], &src[s], it - 1);
     if (mode == GPO_FORWARD_SAVE) boundary_save(c, ishot, it);
+    if (mode == GPO_FORWARD_HIST) hist_io(c, ishot, it, 0, 1);
     if (adjoint && (grad_invK || grad_rho)) compute_gradient(c, (REAL *)grad_invK, (REAL *)grad_rho);
   }
+  if (mode == GPO_ADJOINT_HIST) return 0;
   if (mode == GPO_FORWARD_SAVE) snap_io(c, ishot, 1, 0); /* boundary_save_snap_tau! */
   update_dstress(c, 0);
   update_v(c, 0);
   if (mode == GPO_FORWARD_SAVE) snap_io(c, ishot, 0, 0); /* boundary_save_snap_v! */
+  if (mode == GPO_FORWARD_HIST) hist_io(c, ishot, nt + 1, 0, 0);
   return 0;
 }
 
@@ -924,6 +988,9 @@ void SFX(gpo_destroy)(gpo_ctx *cc) {
   }
   free(c->vbuf[0].a);
   free(c->vbuf[1].a);
+  free(c->vbuf[2].a);
+  for (int i = 0; i < c->nshots; i++) free(c->hist[i]);
+  free(c->hist);
   free(c->pv);
   free(c->pvflag);
   for (int i = 0; i < c->nshots; i++) free(c->bstore[i]);

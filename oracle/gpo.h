@@ -29,7 +29,13 @@ extern "C" {
 #endif
 
 enum { GPO_ACOUSTIC = 0, GPO_ELASTIC = 1 };
-enum { GPO_FORWARD = 0, GPO_FORWARD_SAVE = 1, GPO_ADJOINT = 2 };
+enum { GPO_FORWARD = 0, GPO_FORWARD_SAVE = 1, GPO_ADJOINT = 2, GPO_FORWARD_HIST = 3, GPO_ADJOINT_HIST = 4 };
+/* GPO_FORWARD_HIST / GPO_ADJOINT_HIST (acoustic, 2-D and 3-D): the same
+ * gradient as forward_save -> adjoint, but wavefield 1 is not rebuilt by
+ * time reversal: the forward run keeps its whole history (p and v after
+ * every step, and v after the extra half step) and the adjoint run takes
+ * wavefield 1's old and new states from it.  This is the gradient that a
+ * checkpointed adjoint computes (forward states recomputed, not reversed). */
 /* face bits, in the reference's naming (:zmin, :zmax, :ymin, ...) */
 enum { GPO_ZMIN = 1, GPO_ZMAX = 2, GPO_YMIN = 4, GPO_YMAX = 8, GPO_XMIN = 16, GPO_XMAX = 32 };
 /* wavefield ids (the reference's Fields symbols, non-derivative part) */
@@ -80,8 +86,9 @@ typedef struct gpo_ctx gpo_ctx;
 gpo_ctx *gpo_create_f32(const gpo_desc *d, const void *const *mod, const void *const *pml, int nshots);
 gpo_ctx *gpo_create_f64(const gpo_desc *d, const void *const *mod, const void *const *pml, int nshots);
 /* Run one supersource (shot) in the given mode.  rec data are written
- * (records), src/adj data are read.  grad (acoustic 2-D adjoint only): two
- * extended-grid arrays {invK, rho} that the shot's gradient is ADDED to. */
+ * (records), src/adj data are read.  grad (acoustic adjoint only; 3-D only
+ * with GPO_ADJOINT_HIST): two extended-grid arrays {invK, rho} that the
+ * shot's gradient is ADDED to. */
 int gpo_shot_f32(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec,
                  gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho);
 int gpo_shot_f64(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec,

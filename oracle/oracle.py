@@ -263,11 +263,15 @@ def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=Fal
     return res
 
 
-def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True):
+def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=False):
     """gradient!(g, m, L2DistLoss(), dobs, pa) for 2-D acoustic
     (src/fdtd/func_grad.jl:11-49).  Returns (loss, {"invK": g, "rho": g},
     dcal) with g the chain-ruled gradient on the inner (non-PML) grid and the
-    raw per-cell accumulations on the extended grid."""
+    raw per-cell accumulations on the extended grid.
+
+    history=True takes wavefield 1 from the stored forward history instead
+    of rebuilding it by time reversal (GPO_FORWARD_HIST / GPO_ADJOINT_HIST):
+    the gradient of a checkpointed adjoint; 2-D and 3-D acoustic."""
     prep = Prepared(ex, dtype, ref_compat)
     orc = Oracle(prep, nthreads)
     shape = prep.shape
@@ -277,7 +281,7 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True):
     # forward_save with src_types [1, 0]
     for i, shot in enumerate(ex["shots"]):
         src, rec = _shot_inputs(prep, shot, 1)
-        r = orc.shot(i, 1, src, rec)
+        r = orc.shot(i, 3 if history else 1, src, rec)
         for f in ex["rfields"]:
             dcal[f].append(r[f])
     dcal = {f: np.stack(v) for f, v in dcal.items()}
@@ -289,7 +293,7 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True):
         for f in ex["rfields"]:
             a = S.l2_deriv(dobs[f][i], dcal[f][i])[::-1].copy()
             adj.append((f, prep.proj(f, shot["rec"]), a))
-        orc.shot(i, 2, src, [], adj, (gK, gR))
+        orc.shot(i, 4 if history else 2, src, [], adj, (gK, gR))
     orc.close()
     raw = {"invK": gK.copy(), "rho": gR.copy()}
     inner = []
