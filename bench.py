@@ -55,6 +55,22 @@ WORKLOADS = {
     "acoustic2d_grad": {"name": "acoustic2d_fwi_gradient_500x1500_10m_32shots_3000steps", "bpc": 112, "nshots": 32,
                         "nt": 3000,
                         "kernel": "forward_save + adjoint (k_a2 x 3 + k_grad_a2), algorithmic 36 + 76 B/cell"},
+    # the same gradient through the checkpointed adjoint, a checkpoint every
+    # 100 steps (30 state slots): forward_save (36 B) + the schedule's
+    # recomputed steps (36 B each) + per step a turn: forward step (36 B),
+    # velocity half step (20 B), imaging condition (52 B), adjoint step (36 B)
+    "acoustic2d_grad_ckpt": {"name": "acoustic2d_fwi_gradient_checkpointed_500x1500_10m_32shots_3000steps_30slots",
+                             "bpc": None, "nshots": 32, "nt": 3000, "slots": 30,
+                             "kernel": "checkpointed gradient (k_a2 forward, recompute and turns, k_grad_a2), "
+                                       "algorithmic 36 x (2 + recomputed/nt) + 108 B/cell"},
+    # 3-D acoustic gradient on the 3-D workload's grid (646^3 extended), 500
+    # of its 2500 steps, 8 state slots (5.1 GB each): forward_save (48 B) +
+    # recomputed steps (48 B) + turns: copies (32 B), forward step (48 B),
+    # velocity half step (40 B), imaging condition (64 B), adjoint step (48 B)
+    "acoustic3d_grad_ckpt": {"name": "acoustic3d_gradient_checkpointed_600x600x600_10m_npml23_500steps_8slots",
+                             "bpc": None, "nshots": 1, "nt": 500, "slots": 8,
+                             "kernel": "checkpointed gradient (k3 passes, recompute and turns, k_grad_a3), "
+                                       "algorithmic 48 x (2 + recomputed/nt) + 184 B/cell"},
 }
 
 
@@ -86,12 +102,15 @@ def workload(kind, nt=None, nshots=None, side=None):
     from geophyinv_gb300 import configs
 
     kw = {} if nt is None else {"nt": nt}
-    if side and kind.endswith("3d"):
+    if side and "3d" in kind:
         kw.update(nz=side, ny=side, nx=side)
     if kind == "elastic2d":
         return configs.elastic2d_batch(nshots=nshots or 16, **kw)
-    if kind == "acoustic2d_grad":
+    if kind in ("acoustic2d_grad", "acoustic2d_grad_ckpt"):
         return configs.acoustic2d_fwi(nshots=nshots or 32, anomaly=False, **kw)
+    if kind == "acoustic3d_grad_ckpt":
+        kw.setdefault("nt", WORKLOADS[kind]["nt"])
+        return configs.acoustic3d(rfields=("vz",), src_field="p", **kw)
     if kind == "acoustic2d":
         wl = configs.acoustic2d_layers(**kw)
     elif kind == "elastic3d":
@@ -105,7 +124,8 @@ def workload(kind, nt=None, nshots=None, side=None):
 
 def config_json(kind, wl, n_gpus):
     npml = wl.npml if wl.npml is not None else 43
-    state = {"elastic2d": 5, "acoustic2d": 3, "elastic3d": 9, "acoustic3d": 4, "acoustic2d_grad": 6}[kind]
+    state = {"elastic2d": 5, "acoustic2d": 3, "elastic3d": 9, "acoustic3d": 4, "acoustic2d_grad": 6,
+             "acoustic2d_grad_ckpt": 6, "acoustic3d_grad_ckpt": 8}[kind]
     return {"workload": WORKLOADS[kind]["name"],
             "grid": [len(g) for g in wl.grid], "extended_grid": [len(g) + 2 * npml for g in wl.grid],
             "shots_per_gpu": len(wl.shots), "nt": wl.nt, "dt": wl.tgrid.step, "order": 4,
@@ -180,23 +200,35 @@ def traffic_per_cell():
 
 def cpu_sample(kind, nt_cap=None, target_s=12.0):
     """The CPU oracle (all host threads) on one shot of the workload for a
-    bounded number of time steps; returns (Gcell-updates/s, threads, sample)."""
+    bounded number of time steps; returns (Gcell-updates/s, threads, sample).
+    Gradient workloads time the whole gradient (forward_save and adjoint;
+    the 3-D one through the oracle's history mode, the reference having no
+    3-D gradient)."""
     from oracle import oracle as O
 
     threads = os.cpu_count() or 1
 
-    side = 160 if kind.endswith("3d") else None  # 3-D: a 160^3 sub-grid (+ CPML) of the 600^3 model
+    grad = "grad" in kind
+    # 3-D: a 160^3 sub-grid (+ CPML) of the 600^3 model; 96^3 for the 3-D
+    # gradient, whose oracle keeps the whole forward history in memory
+    side = (96 if grad else 160) if "3d" in kind else None
 
     def run(nt):
         wl = workload(kind, nt, 1, side)
         ex = wl.as_dict()
         prep = O.Prepared(ex, np.float32)
+        cells = int(np.prod(prep.shape))
+        if grad:
+            nr = len(wl.shots[0][1])
+            dobs = {f: np.zeros((1, nt, nr), np.float32) for f in wl.rfields}
+            t0 = time.perf_counter()
+            O.gradient(ex, dobs, nthreads=threads, history="3d" in kind)
+            return cells, time.perf_counter() - t0
         orc = O.Oracle(prep, nthreads=threads)
         src, rec = O._shot_inputs(prep, ex["shots"][0])
         t0 = time.perf_counter()
         orc.shot(0, 0, src, rec)
         t = time.perf_counter() - t0
-        cells = int(np.prod(prep.shape))
         orc.close()
         return cells, t
 
@@ -205,8 +237,9 @@ def cpu_sample(kind, nt_cap=None, target_s=12.0):
     nt = int(max(8, min(nt_cap or WORKLOADS[kind]["nt"], target_s / max(per_step, 1e-6))))
     cells, t = run(nt)
     rate = cells * nt / t / 1e9
-    return rate, threads, "1 of %d shots, %d of %d steps, %d extended cells%s, %.1f s" % (
-        WORKLOADS[kind]["nshots"], nt, WORKLOADS[kind]["nt"], cells, " (160^3 sub-grid)" if side else "", t)
+    return rate, threads, "1 of %d shots, %d of %d steps, %d extended cells%s, %.1f s%s" % (
+        WORKLOADS[kind]["nshots"], nt, WORKLOADS[kind]["nt"], cells, " (%d^3 sub-grid)" % side if side else "", t,
+        ", whole gradient (forward_save + adjoint)" if grad else "")
 
 
 def engine_arm(args, rank, world, local):
@@ -299,26 +332,36 @@ def engine_arm(args, rank, world, local):
     return line, dist
 
 
-def gradient_arm(args, world, local):
+def gradient_arm(args, world, local, kind="acoustic2d_grad"):
     """One bench step = gradient!(g, m, L2DistLoss(), dobs, pa) over all shots:
     forward_save, adjoint sources, adjoint run with the imaging condition.
-    The observed data are modelled once (not timed) on the model with the
-    Gaussian anomaly; the starting model omits it."""
+    2-D: the observed data are modelled once (not timed) on the model with
+    the Gaussian anomaly; the starting model omits it.  3-D: zero observed
+    data (the misfit is the energy of the records).  The checkpointed kinds
+    run the same gradient through a plan with state slots."""
+    import ctypes
+
     import torch
 
-    from geophyinv_gb300 import L2DistLoss, Recs, configs, get_modelvector, gradient, update
+    from geophyinv_gb300 import L2DistLoss, Recs, _lib, configs, get_modelvector, gradient, update
 
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
+    W = WORKLOADS[kind]
     kw = {} if args.nt is None else {"nt": args.nt}
-    nsh = args.nshots or 32
-    true = configs.acoustic2d_fwi(nshots=nsh, **kw)
-    pt = true.expt(stream=stream.cuda_stream)
-    update(pt)
-    dobs = [Recs(r.n, r.grid, r.fields, {f: r.d[f].copy() for f in r.fields}) for r in pt.data[0]]
-    del pt
-    wl = workload("acoustic2d_grad", args.nt, nsh)
-    pa = wl.expt(mode="forward_save", stream=stream.cuda_stream)
+    nsh = args.nshots or W["nshots"]
+    wl = workload(kind, args.nt, nsh, args.side)
+    if kind.startswith("acoustic2d"):
+        true = configs.acoustic2d_fwi(nshots=nsh, **kw)
+        pt = true.expt(stream=stream.cuda_stream)
+        update(pt)
+        dobs = [Recs(r.n, r.grid, r.fields, {f: r.d[f].copy() for f in r.fields}) for r in pt.data[0]]
+        del pt
+    else:
+        dobs = [Recs(len(s[1]), wl.tgrid, list(wl.rfields),
+                     {f: np.zeros((wl.nt, len(s[1])), np.float32) for f in wl.rfields}) for s in wl.shots]
+    slots = W.get("slots", 0)
+    pa = wl.expt(mode="forward_save", stream=stream.cuda_stream, checkpoints=slots)
     cells = pa.nss * int(np.prod([len(g) for g in pa.exgrid]))
     units = cells * pa.nt
     m0 = get_modelvector(pa, ["invK", "rho"])
@@ -338,12 +381,22 @@ def gradient_arm(args, world, local):
     clk = clocks.stop()
     value = world * units / (ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    W = WORKLOADS["acoustic2d_grad"]
-    achieved = W["bpc"] * cells / (ms * 1e-3 / pa.nt) / 1e9
+    bpc = W["bpc"]
+    sched = None
+    if slots:
+        adv, turns, stored = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+        _lib.load().gpi_checkpoint_schedule(pa.nt, slots, ctypes.byref(adv), ctypes.byref(turns), ctypes.byref(stored))
+        sched = {"slots": slots, "recomputed_steps": adv.value, "turns": turns.value,
+                 "slot_gb": round(pa.plan_bytes() / 1e9, 2) if hasattr(pa, "plan_bytes") else None}
+        base, turn = (36, 108) if kind.startswith("acoustic2d") else (48, 184)
+        bpc = base * (2 + adv.value / pa.nt) + turn
+    achieved = bpc * cells / (ms * 1e-3 / pa.nt) / 1e9
     return {"metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (layered + Gaussian anomaly, zero-anomaly start)",
-            "config": config_json("acoustic2d_grad", wl, world),
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (layered + Gaussian anomaly, zero-anomaly start)" if kind.startswith("acoustic2d")
+            else "synthetic (linear-gradient medium with a smoothed perturbation; zero observed data)",
+            "config": dict(config_json(kind, wl, world), checkpoints=sched),
             "e2e": {"value": round(value, 3), "unit": "Gcell/s", "note": "gradient! is the public call; host buffers"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None, "kernel": W["kernel"],
@@ -418,8 +471,8 @@ def main():
     if args.workload == "serving":
         print(json.dumps(serving_arm(args)))
         return
-    if args.workload == "acoustic2d_grad":
-        line, dist = gradient_arm(args, world, local), None
+    if args.workload in ("acoustic2d_grad", "acoustic2d_grad_ckpt", "acoustic3d_grad_ckpt"):
+        line, dist = gradient_arm(args, world, local, args.workload), None
     else:
         line, dist = engine_arm(args, rank, world, local)
     if rank == 0:

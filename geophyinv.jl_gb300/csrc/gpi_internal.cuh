@@ -130,6 +130,7 @@ struct Plan {
   std::vector<float *> wav_bufs;
   float *d_amount = nullptr;               // per cell, current step
   std::vector<int32_t> group_ptr;          // [(ipw*nshots + shot)*NKIND + kind] -> cell range
+  bool inj_shared = false;                 // some group holds one storage cell twice
   int32_t *d_group_ptr = nullptr;
 
   int64_t launches = 0;

@@ -722,6 +722,15 @@ static int compile_sources(Plan &p) {
   }
   p.group_ptr[groups.size()] = (int32_t)cells.size();
   p.n_cells = (int)cells.size();
+  // a cell twice in a group (two stress source fields on one cell) needs
+  // the in-order injection
+  p.inj_shared = false;
+  for (size_t g = 0; g + 1 < p.group_ptr.size() && !p.inj_shared; g++) {
+    std::vector<int64_t> offs;
+    for (int32_t k = p.group_ptr[g]; k < p.group_ptr[g + 1]; k++) offs.push_back(cells[k].off);
+    std::sort(offs.begin(), offs.end());
+    p.inj_shared = std::adjacent_find(offs.begin(), offs.end()) != offs.end();
+  }
   p.h_cells = cells;
   GPI_CUDA(&p, dalloc(p, (void **)&p.d_group_ptr, p.group_ptr.size() * sizeof(int32_t)));
   GPI_CUDA(&p, h2d(p, p.d_group_ptr, p.group_ptr.data(), p.group_ptr.size() * sizeof(int32_t)));

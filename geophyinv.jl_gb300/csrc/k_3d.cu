@@ -308,29 +308,54 @@ __global__ void k3_dirichlet(float *vx, float *vy, float *vz, G3 g, int nshots, 
 struct Fields3 {
   float *f[NFIELD];
 };
-__global__ void k3_inject(const InjCell *cells, const int32_t *gptr, const float *amount, Fields3 fld, int64_t fs,
-                          int nshots, int velocity, int physics) {
+__device__ __forceinline__ void inject_cell(const InjCell &c, float amt, int kind, int64_t so, Fields3 &fld,
+                                            int physics) {
+  if (kind == 0) fld.f[GPI_VX][so + c.off] = fld.f[GPI_VX][so + c.off] + amt;
+  if (kind == 1) fld.f[GPI_VY][so + c.off] = fld.f[GPI_VY][so + c.off] + amt;
+  if (kind == 2) fld.f[GPI_VZ][so + c.off] = fld.f[GPI_VZ][so + c.off] + amt;
+  if (kind == 3) {
+    if (physics == GPI_ACOUSTIC) {
+      fld.f[GPI_P][so + c.off] = fld.f[GPI_P][so + c.off] + amt;
+    } else {
+      fld.f[GPI_TAUXX][so + c.off] = fld.f[GPI_TAUXX][so + c.off] + amt;
+      fld.f[GPI_TAUYY][so + c.off] = fld.f[GPI_TAUYY][so + c.off] + amt;
+      fld.f[GPI_TAUZZ][so + c.off] = fld.f[GPI_TAUZZ][so + c.off] + amt;
+    }
+  }
+}
+
+// add_stress_source! / add_velocity_source! of one wavefield, one thread per
+// (shot, kind) group, cells in order: for groups where two source fields
+// reach the same cell (stress sources on several fields)
+__global__ void k3_inject_groups(const InjCell *cells, const int32_t *gptr, const float *amount, Fields3 fld,
+                                 int64_t fs, int nshots, int velocity, int physics) {
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= nshots * NKIND) return;
   const int shot = gi / NKIND, kind = gi % NKIND;
   if ((kind < 3) != (velocity != 0)) return;
-  const int64_t so = shot * fs;
-  for (int k = gptr[gi]; k < gptr[gi + 1]; k++) {
-    const InjCell c = cells[k];
-    const float amt = amount[k];
-    if (kind == 0) fld.f[GPI_VX][so + c.off] = fld.f[GPI_VX][so + c.off] + amt;
-    if (kind == 1) fld.f[GPI_VY][so + c.off] = fld.f[GPI_VY][so + c.off] + amt;
-    if (kind == 2) fld.f[GPI_VZ][so + c.off] = fld.f[GPI_VZ][so + c.off] + amt;
-    if (kind == 3) {
-      if (physics == GPI_ACOUSTIC) {
-        fld.f[GPI_P][so + c.off] = fld.f[GPI_P][so + c.off] + amt;
-      } else {
-        fld.f[GPI_TAUXX][so + c.off] = fld.f[GPI_TAUXX][so + c.off] + amt;
-        fld.f[GPI_TAUYY][so + c.off] = fld.f[GPI_TAUYY][so + c.off] + amt;
-        fld.f[GPI_TAUZZ][so + c.off] = fld.f[GPI_TAUZZ][so + c.off] + amt;
-      }
-    }
+  for (int k = gptr[gi]; k < gptr[gi + 1]; k++) inject_cell(cells[k], amount[k], kind, shot * fs, fld, physics);
+}
+
+// the same, one thread per injection cell, when the cells of every group
+// are distinct (compile_sources merges the contributions of one source
+// field to a cell), so that the adds commute
+__global__ void k3_inject(const InjCell *cells, const int32_t *gptr, const float *amount, Fields3 fld, int64_t fs,
+                          int nshots, int velocity, int physics) {
+  const int ng = nshots * NKIND;
+  const int k = gptr[0] + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= gptr[ng]) return;
+  // the group of cell k: the last g with gptr[g] <= k
+  int lo = 0, hi = ng - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (gptr[mid] <= k)
+      lo = mid;
+    else
+      hi = mid - 1;
   }
+  const int shot = lo / NKIND, kind = lo % NKIND;
+  if ((kind < 3) != (velocity != 0)) return;
+  inject_cell(cells[k], amount[k], kind, shot * fs, fld, physics);
 }
 
 // one step of wavefield ipw (vonly: bit 0 velocity half step only, bit 1
@@ -397,11 +422,18 @@ int step3_wavefield(Plan *p, int ipw, int vonly) {
     p->launches++;
   }
   const int ng = p->d.nshots * NKIND;
-  if ((!vonly || (vonly & 2)) && p->n_cells) {
-    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride,
-                                                       p->d.nshots, 1, p->d.physics);
+  const size_t g0 = (size_t)ipw * ng;
+  const int ncw = p->group_ptr.empty() ? 0 : p->group_ptr[g0 + ng] - p->group_ptr[g0];  // cells of this wavefield
+  auto inject = [&](int velocity) {
+    if (p->inj_shared)
+      k3_inject_groups<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride,
+                                                                p->d.nshots, velocity, p->d.physics);
+    else
+      k3_inject<<<(ncw + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride,
+                                                          p->d.nshots, velocity, p->d.physics);
     p->launches++;
-  }
+  };
+  if ((!vonly || (vonly & 2)) && ncw > 0) inject(1);
   if (vonly) {
     GPI_CUDA(p, cudaGetLastError());
     return GPI_OK;
@@ -412,11 +444,7 @@ int step3_wavefield(Plan *p, int ipw, int vonly) {
     k3_free<<<fg, fb, 0, p->stream>>>(a.f[GPI_TAUZZ], a.f[GPI_TAUXZ], a.f[GPI_TAUYZ], a.g, p->d.nshots);
     p->launches++;
   }
-  if (p->n_cells) {
-    k3_inject<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride,
-                                                       p->d.nshots, 0, p->d.physics);
-    p->launches++;
-  }
+  if (ncw > 0) inject(0);
   GPI_CUDA(p, cudaGetLastError());
   return GPI_OK;
 }

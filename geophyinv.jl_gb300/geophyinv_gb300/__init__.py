@@ -7,8 +7,9 @@ reference's Julia API (SeisForwExpt, update!, gradient!, lossvalue).
 """
 from .fdtd import (AGeomss, AcousticMedium, ElasticMedium, FdtdAcoustic, FdtdElastic, Fields, L2DistLoss,  # noqa
                    Recs, SeisForwExpt, Srcs, get_modelvector, gradient, lossvalue, update)
+from .rrule import NoTangent, misfit, rrule  # noqa
 from .setup import Grid, findfreq_peak, ricker  # noqa
 
 __all__ = ["AGeomss", "AcousticMedium", "ElasticMedium", "FdtdAcoustic", "FdtdElastic", "Fields", "Grid",
-           "L2DistLoss", "Recs", "SeisForwExpt", "Srcs", "findfreq_peak", "get_modelvector", "gradient",
-           "lossvalue", "ricker", "update"]
+           "L2DistLoss", "NoTangent", "Recs", "SeisForwExpt", "Srcs", "findfreq_peak", "get_modelvector",
+           "gradient", "lossvalue", "misfit", "ricker", "rrule", "update"]

@@ -473,12 +473,30 @@ def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
     """gradient!(g, m, loss, dobs, pa, mparams) (src/fdtd/func_grad.jl:11-49):
     forward_save, adjoint sources deriv(loss, dobs, dcal) reversed in time,
     adjoint run with src_types [-1, 1], chain rule g * exp(m) * ref."""
-    mparams = list(mparams)
-    update(pa, m, mparams)
+    _forward_save(pa, m, mparams)
+    gv = _adjoint(pa, m, loss, dobs, mparams)
+    if g is not None:
+        g[:] = gv
+    return _loss(loss, dobs, pa.data[0])
+
+
+def _forward_save(pa, m, mparams):
+    """The first half of gradient!: update!(pa, m), forward_save run (the
+    boundary store, or the checkpoints of a checkpointed plan, stay on the
+    device)."""
+    update(pa, m, list(mparams))
     mode_save = pa.attrib.mode
     pa.attrib.mode = "forward_save"
     update(pa, pa.srcwav, [1, 0])
     update(pa)
+    pa.attrib.mode = mode_save
+
+
+def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
+    """The second half of gradient!: adjoint sources from the records of the
+    last forward_save run, the adjoint run, the chain rule onto m (times
+    `scale`)."""
+    mparams = list(mparams)
     adj = []
     for o, c in zip(dobs, pa.data[0]):
         s = Srcs(o.n, pa.tgrid, pa.rfields)
@@ -489,8 +507,10 @@ def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
     # a checkpointed plan recomputes wavefield 1 forward in time, with the
     # sources of its forward_save run (no time-reversed copy is needed)
     update(pa, pa.srcwav, [1 if pa.checkpoints else -1, 1])
+    mode_save = pa.attrib.mode
     pa.attrib.mode = "adjoint"
     update(pa)
+    pa.attrib.mode = mode_save
     inn = _inner(pa)
     chunks = np.split(np.asarray(m, np.float32), len(mparams))
     out = []
@@ -502,9 +522,6 @@ def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
         gm = gr[inn]
         gm = gm * np.exp(x.reshape(gm.shape, order="F")) * pa.ref_mod[k]
         out.append(gm.astype(np.float32).ravel(order="F"))
-    gv = np.concatenate(out)
-    if g is not None:
-        g[:] = gv
     pa.gradients = raw
-    pa.attrib.mode = mode_save
-    return _loss(loss, dobs, pa.data[0])
+    gv = np.concatenate(out)
+    return gv if scale == 1.0 else (gv * np.float32(scale)).astype(np.float32)
