@@ -7,9 +7,10 @@ reference's Julia API (SeisForwExpt, update!, gradient!, lossvalue).
 """
 from .fdtd import (AGeomss, AcousticMedium, ElasticMedium, FdtdAcoustic, FdtdElastic, Fields, L2DistLoss,  # noqa
                    Recs, SeisForwExpt, Srcs, get_modelvector, gradient, lossvalue, update)
+from . import fwi  # noqa
 from .rrule import NoTangent, misfit, rrule  # noqa
 from .setup import Grid, findfreq_peak, ricker  # noqa
 
 __all__ = ["AGeomss", "AcousticMedium", "ElasticMedium", "FdtdAcoustic", "FdtdElastic", "Fields", "Grid",
-           "L2DistLoss", "NoTangent", "Recs", "SeisForwExpt", "Srcs", "findfreq_peak", "get_modelvector",
+           "L2DistLoss", "NoTangent", "fwi", "Recs", "SeisForwExpt", "Srcs", "findfreq_peak", "get_modelvector",
            "gradient", "lossvalue", "misfit", "ricker", "rrule", "update"]
