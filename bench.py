@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--nshots", type=int, default=None)
     ap.add_argument("--side", type=int, default=None, help="3-D workloads: a side^3 sub-grid (profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--graph", type=int, default=2, choices=[0, 1, 2],
+                    help="forward workloads: CUDA graphs (0 plain, 1 whole run, 2 replayed 16-step chunks)")
     return ap.parse_args()
 
 
@@ -248,14 +250,17 @@ def engine_arm(args, rank, world, local):
     from geophyinv_gb300 import _lib, update
 
     torch.cuda.set_device(local)
-    stream = torch.cuda.current_stream()
     dist = None
     if world > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    # a stream of the plan's own (graphs cannot be captured on the legacy
+    # default stream); the CUDA events below are recorded on it
+    stream = torch.cuda.Stream()
     wl = workload(args.workload, args.nt, args.nshots, args.side)
     pa = wl.expt(stream=stream.cuda_stream)
+    pa.set_graph(args.graph)
     medium = wl.medium()
     srcwav = wl.srcwav()
     cells = pa.nss * int(np.prod([len(g) for g in pa.exgrid]))
@@ -318,7 +323,8 @@ def engine_arm(args, rank, world, local):
         "metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded gradient + smoothed perturbation model)",
-        "config": config_json(args.workload, wl, world),
+        "config": dict(config_json(args.workload, wl, world),
+                       cuda_graphs={0: "off", 1: "whole run", 2: "replayed 16-step chunks"}[args.graph]),
         "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

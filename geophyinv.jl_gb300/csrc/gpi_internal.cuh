@@ -148,11 +148,17 @@ struct Plan {
   static constexpr int NSIDE = 3;
   cudaStream_t side[NSIDE] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[NSIDE] = {};
-  // whole-run CUDA graphs per mode (gpi_set_graph)
+  // CUDA graphs (gpi_set_graph): 1 the whole run per mode, 2 forward runs
+  // as replays of one captured chunk of kChunkSteps steps that read the
+  // step from d_it
   bool use_graph = false;
+  int graph_kind = 0;
   cudaStream_t own_stream = nullptr;  // created for graphs when no stream was given
   cudaGraphExec_t gexec[3] = {};
   int64_t glaunches[3] = {};
+  cudaGraphExec_t cexec = nullptr;
+  int64_t claunches = 0;
+  int *d_it = nullptr;
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 
   // checkpointed adjoint (gpi_plan_desc.checkpoints > 0): full states of
@@ -220,6 +226,9 @@ int64_t ckpt_slot_floats(const Plan &p);
 int ckpt_forward_store(Plan *p, int it);  // after forward_save step it
 int ckpt_adjoint(Plan *p);                 // the whole adjoint run
 int aux_step2(Plan *p, int it1, int it2);
+int aux_step_dev(Plan *p, int off, int mode);  // step *d_it + off
+int set_step(Plan *p, int v, int add);         // *d_it = v, or += v
+constexpr int kChunkSteps = 16;                // steps per replayed chunk (even: ping-pong)
 // host: x partition of a 2-D grid of nx columns into m interior chunks
 // plus, when the grid is wide enough, one narrow chunk at each x edge (the
 // mirror columns there need the general code) and one chunk over each x

@@ -246,6 +246,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   for (int i = 0; i < p.ncoef; i++) allocs.push_back({&p.coef[i], p.fstride});
   allocs.push_back({&p.pml, (int64_t)p.nder * 3 * 2 * d.npml});
   allocs.push_back({(float **)&p.d_err, 64});
+  allocs.push_back({(float **)&p.d_it, 64});
   if (d.npw == 2 && d.checkpoints > 0) {
     // checkpointed adjoint: state slots instead of the boundary store
     for (int i = 0; i < p.nmod && i < 2; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
@@ -876,6 +877,7 @@ static int zero_state(Plan &p) {
 }
 
 static int run_body(Plan &p, int mode);
+static int run_chunked(Plan &p);
 
 static bool same_sources(const std::vector<std::vector<Plan::Src>> &a, const std::vector<std::vector<Plan::Src>> &b) {
   if (a.size() != b.size()) return false;
@@ -924,7 +926,9 @@ int run(Plan &p, int mode) {
   }
   if (!rc && p.d.ndim == 2 && !p.d_tiles) rc = build_tiles(p);
   if (!rc && recompile) drop_graphs(p);
-  if (!rc && p.use_graph) {
+  if (!rc && p.graph_kind == 2 && mode == GPI_FORWARD) {
+    rc = run_chunked(p);
+  } else if (!rc && p.graph_kind == 1) {
     // the whole run as one CUDA graph: captured on first use per mode,
     // replayed afterwards (the tables and buffers it uses keep their
     // addresses until the sources or receivers change)
@@ -963,6 +967,60 @@ void drop_graphs(Plan &p) {
     if (p.gexec[m]) cudaGraphExecDestroy(p.gexec[m]);
     p.gexec[m] = nullptr;
   }
+  if (p.cexec) cudaGraphExecDestroy(p.cexec);
+  p.cexec = nullptr;
+}
+
+// a forward run as replays of one captured chunk of kChunkSteps steps (the
+// chunk's k_aux launches read the step from the device counter, which the
+// chunk advances at its end), the remainder and the final half step plain:
+// the per-step host cost of small grids goes, one capture serves every run
+static int run_chunked(Plan &p) {
+  const int mode = GPI_FORWARD, K = kChunkSteps;
+  int rc = zero_state(p);
+  p.launches = 0;
+  if (!rc && p.rec_pool) rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
+  const int nchunks = p.d.nt / K;
+  if (!rc && nchunks > 0 && !p.cexec) {
+    const int64_t l0 = p.launches;
+    GPI_CUDA(&p, cudaStreamBeginCapture(p.stream, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < K && !rc; k++) {
+      rc = aux_step_dev(&p, k, mode);
+      if (!rc) rc = step(p, 1, 0, mode, 0);
+    }
+    if (!rc) rc = set_step(&p, K, 1);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(p.stream, &graph);
+    if (!rc && e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    if (!rc && cudaGraphInstantiate(&p.cexec, graph, 0) != cudaSuccess) {
+      p.cexec = nullptr;
+      rc = fail(&p, GPI_E_CUDA, "graph instantiation failed");
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    p.claunches = p.launches - l0;
+    p.launches = l0;
+  }
+  int it = 1;
+  if (!rc && nchunks > 0) {
+    rc = set_step(&p, 1, 0);
+    for (int c = 0; c < nchunks && !rc; c++) {
+      if (cudaGraphLaunch(p.cexec, p.stream) != cudaSuccess) rc = fail(&p, GPI_E_CUDA, "graph launch failed");
+      p.launches += p.claunches;
+    }
+    it = nchunks * K + 1;
+  }
+  for (; !rc && it <= p.d.nt; it++) {
+    rc = aux_step(&p, it, mode);
+    if (!rc) rc = step(p, 1, it, mode, 0);
+  }
+  if (!rc) rc = aux_step(&p, p.d.nt + 1, mode);
+  if (!rc) rc = step(p, 1, p.d.nt + 1, mode, 1);
+  if (!rc) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));
+  }
+  return rc;
 }
 
 // the device work of one run: state reset, the time loop, the final half step
@@ -1130,8 +1188,10 @@ int gpi_set_graph(gpi_plan *plan, int enable) {
     GPI_CUDA(&plan->p, cudaStreamCreateWithFlags(&plan->p.own_stream, cudaStreamNonBlocking));
     plan->p.stream = plan->p.own_stream;
   }
+  if (enable < 0 || enable > 2) return GPI_E_INVALID;
+  if (enable != plan->p.graph_kind) gpi::drop_graphs(plan->p);
   plan->p.use_graph = enable != 0;
-  if (!enable) gpi::drop_graphs(plan->p);
+  plan->p.graph_kind = enable;
   return GPI_OK;
 }
 int gpi_query(gpi_plan *plan, int *done) {

@@ -119,6 +119,8 @@ struct AuxArgs {
   int it, nt;
   int it2, split;  // cells from `split` on (the adjoint wavefield's) take step it2
   int zero;        // write 0 for cells whose step is out of range
+  const int *it_dev;  // when set: the step is *it_dev + it_off (graph-replayed step chunks)
+  int it_off;
   const float *field[NFIELD];  // wavefield 1, current buffer, shot 0
   int64_t fs;
   const InjCell *cells;
@@ -134,6 +136,11 @@ struct AuxArgs {
 
 __global__ void k_aux(AuxArgs a) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a.it_dev) {
+    const int itd = *a.it_dev + a.it_off;
+    a.it = itd;
+    a.it2 = itd;
+  }
   if (i < a.ntask) {
     // record!: p is sampled before step it, velocities after step it-1
     const RecTask t = a.tasks[i];
@@ -211,6 +218,8 @@ int aux_step(Plan *p, int it, int mode) {
   a.it2 = it;
   a.split = p->n_cells;
   a.zero = 0;
+  a.it_dev = nullptr;
+  a.it_off = 0;
   for (int f = 0; f < NFIELD; f++) a.field[f] = p->state[p->cur[0]][0][f];
   a.fs = p->fstride;
   a.cells = p->d_cells;
@@ -223,6 +232,53 @@ int aux_step(Plan *p, int it, int mode) {
   a.kcoef = p->d.physics == GPI_ACOUSTIC ? p->coef[p->ncoef - 1] : p->coef[p->ncoef - 2];
   a.dt = (float)p->d.dt;
   k_aux<<<(n + 127) / 128, 128, 0, p->stream>>>(a);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+// aux_step for step *d_it + off (the step chunks a CUDA graph replays)
+int aux_step_dev(Plan *p, int off, int mode) {
+  const int it = 1;  // cells are always launched; the kernel reads the step
+  // an adjoint run records nothing (get_update_parameters, propagate.jl:38-60)
+  const int ntask = mode == GPI_ADJOINT ? 0 : p->n_rtask;
+  const int n = ntask + (it <= p->d.nt ? p->n_cells : 0);
+  if (n == 0) return GPI_OK;
+  AuxArgs a;
+  a.tasks = p->d_rtask;
+  a.ntask = ntask;
+  a.roff = p->d_roff;
+  a.rw = p->d_rw;
+  a.rec = p->rec_pool;
+  a.it = it;
+  a.nt = p->d.nt;
+  a.it2 = it;
+  a.split = p->n_cells;
+  a.zero = 0;
+  a.it_dev = p->d_it;
+  a.it_off = off;
+  for (int f = 0; f < NFIELD; f++) a.field[f] = p->state[p->cur[0]][0][f];
+  a.fs = p->fstride;
+  a.cells = p->d_cells;
+  a.ncells = p->n_cells;
+  a.pj = p->d_pair_j;
+  a.pw = p->d_pair_w;
+  a.wav = p->d_wav;
+  a.amount = p->d_amount;
+  a.rho = p->mod[p->d.physics == GPI_ACOUSTIC ? 1 : 2];
+  a.kcoef = p->d.physics == GPI_ACOUSTIC ? p->coef[p->ncoef - 1] : p->coef[p->ncoef - 2];
+  a.dt = (float)p->d.dt;
+  k_aux<<<(n + 127) / 128, 128, 0, p->stream>>>(a);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+__global__ void k_set_step(int *it, int v, int add) { *it = add ? *it + v : v; }
+
+// the device step counter of the chunked runs: set (add = 0) or advance
+int set_step(Plan *p, int v, int add) {
+  k_set_step<<<1, 1, 0, p->stream>>>(p->d_it, v, add);
   p->launches++;
   GPI_CUDA(p, cudaGetLastError());
   return GPI_OK;

@@ -301,8 +301,11 @@ class SeisForwExpt:
         self._check(self.L.gpi_run(self.plan, mode))
 
     def set_graph(self, enable=True):
-        """Replay each run as one CUDA graph (captured on first use)."""
-        self._check(self.L.gpi_set_graph(self.plan, int(bool(enable))))
+        """CUDA graphs: True / 1 replays each run as one graph (captured on
+        first use); 2 replays forward runs as chunks of 16 captured steps
+        (pays off for a plan that runs once); False / 0 plain launches."""
+        kind = int(enable) if not isinstance(enable, bool) else int(enable)
+        self._check(self.L.gpi_set_graph(self.plan, kind))
 
     def done(self):
         """True when every run issued so far has finished on the device."""

@@ -126,7 +126,9 @@ class _Job:
         mode = "forward_save" if req.kind == "acoustic_gradient" else "forward"
         self.pa = self.wl.expt(mode=mode, stream=stream)
         if graphs:
-            self.pa.set_graph(True)
+            # forward runs as replays of one captured 16-step chunk; a
+            # whole-run graph would cost more to capture than one run saves
+            self.pa.set_graph(2)
         self.res = Result(req.rid, req.kind)
         self.phase = 0
         self.busy = None  # a launch still being issued on a worker thread
@@ -200,7 +202,7 @@ def _streams(n):
     return [torch.cuda.Stream() for _ in range(n)]
 
 
-def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=False, realtime=True, prep_threads=4):
+def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=True, prep_threads=4):
     """Continuous batching: admit arrived requests while slots and HBM budget
     allow, prepare them on host threads, launch them when ready, poll the
     in-flight ones, launch their next phase or collect their results.

@@ -130,11 +130,15 @@ int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int 
 /* Number of engine kernel launches issued by the last gpi_run. */
 int gpi_last_launches(const gpi_plan *plan, int64_t *launches);
 
-/* Run every later gpi_run of this plan as one CUDA graph per mode: the time
- * loop is captured on its first run (after the sources and receivers are
- * compiled) and replayed, which removes the per-launch host cost of small
- * grids.  Changing the sources or receivers drops the graphs.  No
- * counterpart in the reference (its time loop launches every kernel). */
+/* CUDA graphs for later gpi_run calls of this plan.  enable = 1: each run
+ * as one graph per mode, captured on its first run (after the sources and
+ * receivers are compiled) and replayed, which removes the per-launch host
+ * cost of small grids for plans that run repeatedly.  enable = 2: forward
+ * runs as replays of one captured chunk of 16 steps that reads the step
+ * from a device counter, so that a plan that runs once gains too (other
+ * modes run plain).  0: plain launches.  Changing the sources or receivers
+ * drops the graphs.  No counterpart in the reference (its time loop
+ * launches every kernel). */
 int gpi_set_graph(gpi_plan *plan, int enable);
 /* Non-blocking completion test of the plan's stream (1 when all work
  * issued so far has finished).  No counterpart in the reference. */

@@ -1,6 +1,8 @@
-"""Whole-run CUDA graphs (gpi_set_graph): a captured and replayed run gives
-the same records, fields and gradients as plain launches, bit for bit, and
-changing the sources drops and re-captures the graph."""
+"""CUDA graphs (gpi_set_graph): a captured and replayed run (1: the whole
+run; 2: replays of a captured 16-step chunk that reads the step from a
+device counter, remainder steps plain) gives the same records, fields and
+gradients as plain launches, bit for bit, and changing the sources drops
+and re-captures the graph."""
 import numpy as np
 import pytest
 
@@ -12,24 +14,27 @@ def _records(pa, wl):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["acoustic", "elastic"])
-def test_graph_runs_match_plain_runs(engine, kind):
+@pytest.mark.parametrize("gkind", [1, 2])
+@pytest.mark.parametrize("kind", ["acoustic", "elastic", "acoustic3d"])
+def test_graph_runs_match_plain_runs(engine, kind, gkind):
     if kind == "acoustic":
         wl = configs.acoustic2d_layers(nz=101, nx=131, nt=300, nrec=21)
-    else:
+    elif kind == "elastic":
         wl = configs.elastic2d_batch(nz=110, nx=190, nt=300, nshots=3, nrec=31)
+    else:
+        wl = configs.acoustic3d(nz=20, ny=18, nx=22, nt=75, npml=10, nrec_side=4, rfields=("p", "vz"))
     plain = wl.expt()
     update(plain)
     want = _records(plain, wl)
     pa = wl.expt()
-    pa.set_graph(True)
+    pa.set_graph(gkind)
     for _ in range(2):  # capture, then replay
         update(pa)
         got = _records(pa, wl)
         for a, b in zip(got, want):
             for f in wl.rfields:
                 assert np.array_equal(a[f], b[f]), f
-    f0 = "p" if kind == "acoustic" else "vz"
+    f0 = "vz" if kind == "elastic" else "p"
     assert np.array_equal(pa.field(f0, iss=len(wl.shots) - 1), plain.field(f0, iss=len(wl.shots) - 1))
     # new wavelets: the graph is dropped and captured again
     sw = wl.srcwav()
