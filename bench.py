@@ -352,7 +352,7 @@ def gradient_arm(args, world, local, kind="acoustic2d_grad"):
     from geophyinv_gb300 import L2DistLoss, Recs, _lib, configs, get_modelvector, gradient, update
 
     torch.cuda.set_device(local)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
     W = WORKLOADS[kind]
     kw = {} if args.nt is None else {"nt": args.nt}
     nsh = args.nshots or W["nshots"]
@@ -368,6 +368,7 @@ def gradient_arm(args, world, local, kind="acoustic2d_grad"):
                      {f: np.zeros((wl.nt, len(s[1])), np.float32) for f in wl.rfields}) for s in wl.shots]
     slots = W.get("slots", 0)
     pa = wl.expt(mode="forward_save", stream=stream.cuda_stream, checkpoints=slots)
+    pa.set_graph(args.graph)
     cells = pa.nss * int(np.prod([len(g) for g in pa.exgrid]))
     units = cells * pa.nt
     m0 = get_modelvector(pa, ["invK", "rho"])
@@ -402,7 +403,8 @@ def gradient_arm(args, world, local, kind="acoustic2d_grad"):
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (layered + Gaussian anomaly, zero-anomaly start)" if kind.startswith("acoustic2d")
             else "synthetic (linear-gradient medium with a smoothed perturbation; zero observed data)",
-            "config": dict(config_json(kind, wl, world), checkpoints=sched),
+            "config": dict(config_json(kind, wl, world), checkpoints=sched,
+                           cuda_graphs={0: "off", 1: "whole run", 2: "replayed 16-step chunks"}[args.graph]),
             "e2e": {"value": round(value, 3), "unit": "Gcell/s", "note": "gradient! is the public call; host buffers"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None, "kernel": W["kernel"],

@@ -156,8 +156,8 @@ struct Plan {
   cudaStream_t own_stream = nullptr;  // created for graphs when no stream was given
   cudaGraphExec_t gexec[3] = {};
   int64_t glaunches[3] = {};
-  cudaGraphExec_t cexec = nullptr;
-  int64_t claunches = 0;
+  cudaGraphExec_t cexec[3] = {};
+  int64_t claunches[3] = {};
   int *d_it = nullptr;
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 
@@ -249,6 +249,7 @@ int fork_side(Plan *p, int nside, cudaStream_t *out);
 int join_side(Plan *p, int nside);
 int compute_coefficients(Plan *p);
 int boundary_io(Plan *p, int it, int dir);
+int boundary_io_dev(Plan *p, int off, int dir);  // step *d_it + off
 int snap_io(Plan *p, int tau, int dir);
 
 }  // namespace gpi

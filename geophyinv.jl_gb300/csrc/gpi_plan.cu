@@ -876,8 +876,7 @@ static int zero_state(Plan &p) {
   return GPI_OK;
 }
 
-static int run_body(Plan &p, int mode);
-static int run_chunked(Plan &p);
+static int run_body(Plan &p, int mode, bool chunked = false);
 
 static bool same_sources(const std::vector<std::vector<Plan::Src>> &a, const std::vector<std::vector<Plan::Src>> &b) {
   if (a.size() != b.size()) return false;
@@ -926,8 +925,8 @@ int run(Plan &p, int mode) {
   }
   if (!rc && p.d.ndim == 2 && !p.d_tiles) rc = build_tiles(p);
   if (!rc && recompile) drop_graphs(p);
-  if (!rc && p.graph_kind == 2 && mode == GPI_FORWARD) {
-    rc = run_chunked(p);
+  if (!rc && p.graph_kind == 2) {
+    rc = run_body(p, mode, true);
   } else if (!rc && p.graph_kind == 1) {
     // the whole run as one CUDA graph: captured on first use per mode,
     // replayed afterwards (the tables and buffers it uses keep their
@@ -967,64 +966,64 @@ void drop_graphs(Plan &p) {
     if (p.gexec[m]) cudaGraphExecDestroy(p.gexec[m]);
     p.gexec[m] = nullptr;
   }
-  if (p.cexec) cudaGraphExecDestroy(p.cexec);
-  p.cexec = nullptr;
+  for (int m = 0; m < 3; m++) {
+    if (p.cexec[m]) cudaGraphExecDestroy(p.cexec[m]);
+    p.cexec[m] = nullptr;
+  }
 }
 
-// a forward run as replays of one captured chunk of kChunkSteps steps (the
-// chunk's k_aux launches read the step from the device counter, which the
-// chunk advances at its end), the remainder and the final half step plain:
-// the per-step host cost of small grids goes, one capture serves every run
-static int run_chunked(Plan &p) {
-  const int mode = GPI_FORWARD, K = kChunkSteps;
-  int rc = zero_state(p);
-  p.launches = 0;
-  if (!rc && p.rec_pool) rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
-  const int nchunks = p.d.nt / K;
-  if (!rc && nchunks > 0 && !p.cexec) {
+
+// the device work of one run: state reset, the time loop, the final half step
+// one time step of the loop of mod_x_proc!; with `dev` its step index is
+// the device counter plus `off` (inside a captured chunk)
+static int step_body(Plan &p, int mode, int it, bool dev, int off) {
+  const int mask = mode == GPI_ADJOINT ? 3 : 1;
+  int rc = dev ? aux_step_dev(&p, off, mode) : aux_step(&p, it, mode);
+  // boundary_force! (the replaced values are kept for the gradient)
+  if (!rc && mode == GPI_ADJOINT) rc = dev ? boundary_io_dev(&p, off, 2) : boundary_io(&p, p.d.nt - it + 1, 2);
+  if (!rc) rc = step(p, mask, it, mode, 0);
+  if (!rc && mode == GPI_FORWARD_SAVE)
+    rc = p.ck_slots > 0 ? ckpt_forward_store(&p, it) : dev ? boundary_io_dev(&p, off, 0) : boundary_io(&p, it, 0);
+  return rc;
+}
+
+// the steps [1, nchunks * K] as replays of one captured chunk of K steps
+// (its aux and strip kernels read the step from the device counter, which
+// the chunk advances at its end); returns the next plain step
+static int run_chunks(Plan &p, int mode, int *next) {
+  const int K = kChunkSteps, nchunks = p.d.nt / K;
+  *next = 1;
+  if (nchunks == 0) return GPI_OK;
+  int rc = GPI_OK;
+  if (!p.cexec[mode]) {
     const int64_t l0 = p.launches;
+    const int c0 = p.cur[0], c1 = p.cur[1];
     GPI_CUDA(&p, cudaStreamBeginCapture(p.stream, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < K && !rc; k++) {
-      rc = aux_step_dev(&p, k, mode);
-      if (!rc) rc = step(p, 1, 0, mode, 0);
-    }
+    for (int k = 0; k < K && !rc; k++) rc = step_body(p, mode, 0, true, k);
     if (!rc) rc = set_step(&p, K, 1);
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(p.stream, &graph);
     if (!rc && e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    if (!rc && cudaGraphInstantiate(&p.cexec, graph, 0) != cudaSuccess) {
-      p.cexec = nullptr;
+    if (!rc && cudaGraphInstantiate(&p.cexec[mode], graph, 0) != cudaSuccess) {
+      p.cexec[mode] = nullptr;
       rc = fail(&p, GPI_E_CUDA, "graph instantiation failed");
     }
     if (graph) cudaGraphDestroy(graph);
     cudaGetLastError();
-    p.claunches = p.launches - l0;
+    p.claunches[mode] = p.launches - l0;
     p.launches = l0;
+    if (!rc && (p.cur[0] != c0 || p.cur[1] != c1)) rc = fail(&p, GPI_E_CUDA, "chunk does not end on its first buffers");
   }
-  int it = 1;
-  if (!rc && nchunks > 0) {
-    rc = set_step(&p, 1, 0);
-    for (int c = 0; c < nchunks && !rc; c++) {
-      if (cudaGraphLaunch(p.cexec, p.stream) != cudaSuccess) rc = fail(&p, GPI_E_CUDA, "graph launch failed");
-      p.launches += p.claunches;
-    }
-    it = nchunks * K + 1;
+  if (!rc) rc = set_step(&p, 1, 0);
+  for (int c = 0; c < nchunks && !rc; c++) {
+    if (cudaGraphLaunch(p.cexec[mode], p.stream) != cudaSuccess) rc = fail(&p, GPI_E_CUDA, "graph launch failed");
+    p.launches += p.claunches[mode];
   }
-  for (; !rc && it <= p.d.nt; it++) {
-    rc = aux_step(&p, it, mode);
-    if (!rc) rc = step(p, 1, it, mode, 0);
-  }
-  if (!rc) rc = aux_step(&p, p.d.nt + 1, mode);
-  if (!rc) rc = step(p, 1, p.d.nt + 1, mode, 1);
-  if (!rc) {
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));
-  }
+  *next = nchunks * K + 1;
   return rc;
 }
 
-// the device work of one run: state reset, the time loop, the final half step
-static int run_body(Plan &p, int mode) {
+static int run_body(Plan &p, int mode, bool chunked) {
   if (mode == GPI_ADJOINT && p.ck_slots > 0) {
     p.launches = 0;
     int rc = ckpt_adjoint(&p);
@@ -1045,14 +1044,10 @@ static int run_body(Plan &p, int mode) {
     if (!rc) rc = snap_io(&p, 1, 1);
     if (!rc) rc = snap_io(&p, 0, 1);
   }
-  const int mask = mode == GPI_ADJOINT ? 3 : 1;
-  for (int it = 1; !rc && it <= p.d.nt; it++) {
-    rc = aux_step(&p, it, mode);
-    // boundary_force! (the replaced values are kept for the gradient)
-    if (!rc && mode == GPI_ADJOINT) rc = boundary_io(&p, p.d.nt - it + 1, 2);
-    if (!rc) rc = step(p, mask, it, mode, 0);
-    if (!rc && mode == GPI_FORWARD_SAVE) rc = p.ck_slots > 0 ? ckpt_forward_store(&p, it) : boundary_io(&p, it, 0);
-  }
+  int first = 1;
+  // a checkpointed forward_save stores states at host-chosen steps: plain
+  if (!rc && chunked && !(mode == GPI_FORWARD_SAVE && p.ck_slots > 0)) rc = run_chunks(p, mode, &first);
+  for (int it = first; !rc && it <= p.d.nt; it++) rc = step_body(p, mode, it, false, 0);
   const bool snaps = mode == GPI_FORWARD_SAVE && p.ck_slots == 0;
   if (!rc) rc = aux_step(&p, p.d.nt + 1, mode);  // velocity records of the last step
   if (!rc && snaps) rc = snap_io(&p, 1, 0);

@@ -301,6 +301,11 @@ struct StripArgs {
   int nshots;
   float *prev;      // dir 2: shot 0, this (field, axis) block, same layout and shot stride pstride
   int64_t pstride;
+  // when set: the store block of step idx = *it_dev + it_off (dir 0) or
+  // nt - (*it_dev + it_off) + 1 (dir 2), at store + (idx - 1) * bstep
+  const int *it_dev;
+  int it_off, nt;
+  int64_t bstep;
 };
 
 __global__ void k_strip(StripArgs a) {
@@ -322,6 +327,10 @@ __global__ void k_strip(StripArgs a) {
     fi[a.axis] = fidx;
     float *f = a.field + shot * a.fs + a.g.off(fi[0], fi[1], fi[2]);
     float *s = a.store + shot * a.sstride + k;
+    if (a.it_dev) {
+      const int it = *a.it_dev + a.it_off;
+      s += (int64_t)((a.dir == 0 ? it : a.nt - it + 1) - 1) * a.bstep;
+    }
     if (a.dir == 0) {
       *s = -*f;
     } else {
@@ -342,11 +351,11 @@ static int saved_fields(const Plan &p, int *ids) {
   return 3;
 }
 
-int boundary_io(Plan *p, int it, int dir) {
+static int boundary_impl(Plan *p, int it, int dir, bool dev, int off) {
   int ids[3];
   const int nsv = saved_fields(*p, ids);
   const int64_t sstride = p->bstep * p->d.nt + p->bsnap;
-  float *st = p->bstore + (int64_t)(it - 1) * p->bstep;
+  float *st = p->bstore + (dev ? 0 : (int64_t)(it - 1) * p->bstep);
   float *pv = p->bprev;
   for (int q = 0; q < nsv; q++) {
     int kz, ky, kx;
@@ -372,6 +381,10 @@ int boundary_io(Plan *p, int it, int dir) {
       a.nshots = p->d.nshots;
       a.prev = pv;
       a.pstride = p->bstep;
+      a.it_dev = dev ? p->d_it : nullptr;
+      a.it_off = off;
+      a.nt = p->d.nt;
+      a.bstep = p->bstep;
       int64_t per = 2 * (int64_t)p->d.nbound * (axis == 0 ? 1 : n1) * (axis == 1 ? 1 : n2) * (axis == 2 ? 1 : n3);
       int blocks = (int)std::min<int64_t>((per * p->d.nshots + 255) / 256, 152 * 16);
       k_strip<<<blocks, 256, 0, p->stream>>>(a);
@@ -383,6 +396,9 @@ int boundary_io(Plan *p, int it, int dir) {
   }
   return GPI_OK;
 }
+
+int boundary_io(Plan *p, int it, int dir) { return boundary_impl(p, it, dir, false, 0); }
+int boundary_io_dev(Plan *p, int off, int dir) { return boundary_impl(p, 0, dir, true, off); }
 
 // final snapshots: -tau (or -p) at nt and v after the extra half step, kept
 // in storage layout after the strips of the last step

@@ -133,10 +133,10 @@ int gpi_last_launches(const gpi_plan *plan, int64_t *launches);
 /* CUDA graphs for later gpi_run calls of this plan.  enable = 1: each run
  * as one graph per mode, captured on its first run (after the sources and
  * receivers are compiled) and replayed, which removes the per-launch host
- * cost of small grids for plans that run repeatedly.  enable = 2: forward
- * runs as replays of one captured chunk of 16 steps that reads the step
- * from a device counter, so that a plan that runs once gains too (other
- * modes run plain).  0: plain launches.  Changing the sources or receivers
+ * cost of small grids for plans that run repeatedly.  enable = 2: each run
+ * as replays of one captured chunk of 16 steps that reads the step from a
+ * device counter, so that a plan that runs once gains too (the checkpointed
+ * forward_save and adjoint runs stay plain).  0: plain launches.  Changing the sources or receivers
  * drops the graphs.  No counterpart in the reference (its time loop
  * launches every kernel). */
 int gpi_set_graph(gpi_plan *plan, int enable);

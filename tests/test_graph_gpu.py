@@ -55,7 +55,7 @@ def test_graph_gradient_matches_plain_gradient(engine):
     nz, nx, nt, nrec = 40, 70, 300, 23
     wl = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=2, nrec=nrec, anomaly=False)
     out = []
-    for graph in (False, True):
+    for graph in (0, 1, 2):
         pa = wl.expt(mode="forward_save")
         pa.set_graph(graph)
         dobs = [Recs(nrec, pa.tgrid, ["vz"], {"vz": np.zeros((nt, nrec), np.float32)}) for _ in range(2)]
@@ -63,5 +63,6 @@ def test_graph_gradient_matches_plain_gradient(engine):
         g = np.zeros_like(m)
         loss = gradient(g, m, L2DistLoss(), dobs, pa)
         out.append((loss, g.copy()))
-    assert out[0][0] == out[1][0]
-    assert np.array_equal(out[0][1], out[1][1])
+    for loss, g in out[1:]:
+        assert loss == out[0][0]
+        assert np.array_equal(g, out[0][1])
