@@ -143,6 +143,132 @@ __global__ void __launch_bounds__(256) k3_str_a(const Step3 a) {
   a.f[GPI_P][o] = a.f[GPI_P][o] + (Dx + Dz + Dy) * a.cf[3][o - so];
 }
 
+// The acoustic stress pass marching along x: a block owns a 32 x 8 (z, y)
+// tile of one shot over a run of columns; vx travels in a register queue
+// (c .. c+3), the vy and vz planes of column c in shared memory with their
+// +3 halos, and the loads of column c+1 are issued before column c is
+// computed.  Same arithmetic as k3_str_a.
+constexpr int XM_Z = 32, XM_Y = 8;
+__global__ void __launch_bounds__(256) k3_str_a_xm(const Step3 a, int ncx) {
+  const G3 &g = a.g;
+  __shared__ float svy[2][XM_Y + 3][XM_Z];
+  __shared__ float svz[2][XM_Y][XM_Z + 3];
+  const int tz = threadIdx.x, ty = threadIdx.y;
+  const int z0 = 1 + blockIdx.x * XM_Z, y0 = 1 + blockIdx.y * XM_Y;
+  const int xc = (int)(blockIdx.z % ncx), shot = a.shot0 + (int)(blockIdx.z / ncx);
+  const int c0 = 1 + (int)((int64_t)g.nx * xc / ncx), c1 = 1 + (int)((int64_t)g.nx * (xc + 1) / ncx);
+  const int r = z0 + tz, y = y0 + ty;
+  const bool own = r <= g.nz && y <= g.ny;
+  const int64_t so = shot * g.fs, sx = (int64_t)g.NYP * g.NZP;
+  const float *vx = a.f[GPI_VX] + so, *vy = a.f[GPI_VY] + so, *vz = a.f[GPI_VZ] + so;
+  float *p = a.f[GPI_P] + so;
+  // rows of this thread (clamped into the padded storage: cells past the
+  // grid are never used by an owner)
+  const int rr = min(r, g.nz + 3), yy = min(y, g.ny + 3);
+  const int64_t o0 = g.S(rr, yy, c0);
+  // halo rows: vy at y0+8+ty (ty < 3), vz at z0+32+tz (tz < 3)
+  const bool hy = ty < 3, hz = tz < 3;
+  const int64_t oy = g.S(rr, min(y0 + XM_Y + ty, g.ny + 3), c0) - o0;
+  const int64_t oz = g.S(min(z0 + XM_Z + tz, g.nz + 3), yy, c0) - o0;
+  // x queue: vx(c .. c+3)
+  float q0 = vx[o0], q1 = vx[o0 + sx], q2 = vx[o0 + 2 * sx], q3;
+  float ny_vy = vy[o0], ny_h = hy ? vy[o0 + oy] : 0.f, nz_vz = vz[o0], nz_h = hz ? vz[o0 + oz] : 0.f;
+  float nq3 = vx[o0 + 3 * sx];
+  for (int c = c0, b = 0; c < c1; c++, b ^= 1) {
+    const int64_t o = o0 + (int64_t)(c - c0) * sx;
+    q3 = nq3;
+    svy[b][ty][tz] = ny_vy;
+    if (hy) svy[b][XM_Y + ty][tz] = ny_h;
+    svz[b][ty][tz] = nz_vz;
+    if (hz) svz[b][ty][XM_Z + tz] = nz_h;
+    const float p0 = p[o], k0 = a.cf[3][o - so];
+    // the next column's loads, in flight while this one is computed
+    if (c + 1 < c1) {
+      const int64_t on = o + sx;
+      nq3 = vx[on + 3 * sx];
+      ny_vy = vy[on];
+      if (hy) ny_h = vy[on + oy];
+      nz_vz = vz[on];
+      if (hz) nz_h = vz[on + oz];
+    }
+    __syncthreads();
+    if (own) {
+      float Dx = st4(q0, q1, q2, q3) * a.dxI;  // @d_xa(vx)
+      Dx = mem3(Dx, g, a.m, shot, 3, 2, c, g.nx, r, y, c);
+      float Dy = st4(svy[b][ty][tz], svy[b][ty + 1][tz], svy[b][ty + 2][tz], svy[b][ty + 3][tz]) * a.dyI;  // @d_ya(vy)
+      Dy = mem3(Dy, g, a.m, shot, 4, 1, y, g.ny, r, y, c);
+      float Dz = st4(svz[b][ty][tz], svz[b][ty][tz + 1], svz[b][ty][tz + 2], svz[b][ty][tz + 3]) * a.dzI;  // @d_za(vz)
+      Dz = mem3(Dz, g, a.m, shot, 5, 0, r, g.nz, r, y, c);
+      p[o] = p0 + (Dx + Dz + Dy) * k0;
+    }
+    q0 = q1;
+    q1 = q2;
+    q2 = q3;
+  }
+}
+
+// The acoustic velocity pass marching along x (cells from (4, 4, 4), as
+// k3_vel_a): p travels in a register queue (c-3 .. c) and its plane c in
+// shared memory with the -3 halos in y and z.  Same arithmetic as k3_vel_a.
+__global__ void __launch_bounds__(256) k3_vel_a_xm(const Step3 a, int ncx) {
+  const G3 &g = a.g;
+  __shared__ float sp[2][XM_Y + 3][XM_Z + 3];
+  const int tz = threadIdx.x, ty = threadIdx.y;
+  const int nz = g.nz, ny = g.ny, nx = g.nx;
+  const int z0 = 4 + blockIdx.x * XM_Z, y0 = 4 + blockIdx.y * XM_Y;
+  const int xc = (int)(blockIdx.z % ncx), shot = a.shot0 + (int)(blockIdx.z / ncx);
+  const int span = nx - 3;
+  const int c0 = 4 + (int)((int64_t)span * xc / ncx), c1 = 4 + (int)((int64_t)span * (xc + 1) / ncx);
+  const int r = z0 + tz, y = y0 + ty;
+  const bool own = r <= nz && y <= ny;
+  const int64_t so = shot * g.fs, sx = (int64_t)g.NYP * g.NZP;
+  const float *p = a.f[GPI_P] + so;
+  const int rr = min(r, nz + 3), yy = min(y, ny + 3);
+  const int64_t o0 = g.S(rr, yy, c0);
+  const bool hy = ty < 3, hz = tz < 3;
+  const int64_t oy = g.S(rr, y0 - 3 + ty, c0) - o0;  // p(r, y0-3+ty, c)
+  const int64_t oz = g.S(z0 - 3 + tz, yy, c0) - o0;  // p(z0-3+tz, y, c)
+  float q0 = p[o0 - 3 * sx], q1 = p[o0 - 2 * sx], q2 = p[o0 - sx], q3;
+  float n3 = p[o0], nh_y = hy ? p[o0 + oy] : 0.f, nh_z = hz ? p[o0 + oz] : 0.f;
+  for (int c = c0, b = 0; c < c1; c++, b ^= 1) {
+    const int64_t o = o0 + (int64_t)(c - c0) * sx, oc = o - so;
+    q3 = n3;
+    sp[b][ty + 3][tz + 3] = q3;
+    if (hy) sp[b][ty][tz + 3] = nh_y;
+    if (hz) sp[b][ty + 3][tz] = nh_z;
+    const float cx = a.cf[0][oc], cy = a.cf[1][oc], cz = a.cf[2][oc];
+    float *vx = a.f[GPI_VX] + o, *vy = a.f[GPI_VY] + o, *vz = a.f[GPI_VZ] + o;
+    const float vx0 = *vx, vy0 = *vy, vz0 = *vz;
+    if (c + 1 < c1) {
+      const int64_t on = o + sx;
+      n3 = p[on];
+      if (hy) nh_y = p[on + oy];
+      if (hz) nh_z = p[on + oz];
+    }
+    __syncthreads();
+    if (own) {
+      float Dx = st4(q0, q1, q2, q3) * a.dxI;  // @d_xi(p)
+      float Dy = st4(sp[b][ty][tz + 3], sp[b][ty + 1][tz + 3], sp[b][ty + 2][tz + 3], sp[b][ty + 3][tz + 3]) * a.dyI;
+      float Dz = st4(sp[b][ty + 3][tz], sp[b][ty + 3][tz + 1], sp[b][ty + 3][tz + 2], sp[b][ty + 3][tz + 3]) * a.dzI;
+      if (r <= nz - 3 && y <= ny - 3) {
+        Dx = mem3(Dx, g, a.m, shot, 0, 2, c - 3, nx - 3, r - 3, y - 3, c - 3);
+        *vx = vx0 + cx * Dx;
+      }
+      if (r <= nz - 3 && c <= nx - 3) {
+        Dy = mem3(Dy, g, a.m, shot, 1, 1, y - 3, ny - 3, r - 3, y - 3, c - 3);
+        *vy = vy0 + cy * Dy;
+      }
+      if (y <= ny - 3 && c <= nx - 3) {
+        Dz = mem3(Dz, g, a.m, shot, 2, 0, r - 3, nz - 3, r - 3, y - 3, c - 3);
+        *vz = vz0 + cz * Dz;
+      }
+    }
+    q0 = q1;
+    q1 = q2;
+    q2 = q3;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // elastic (DE3, canonical order: dtauxxdx dtauxydx dtauxzdx dtauyydy
 // dtauxydy dtauyzdy dtauzzdz dtauyzdz dtauxzdz dvxdx dvydy dvzdz dvxdy dvxdz
@@ -384,6 +510,15 @@ int step3_wavefield(Plan *p, int ipw, int vonly) {
   const dim3 blk(32, 8);
   // the velocity passes cover cells from (4, 4, 4) (their update domains),
   // the stress passes from (1, 1, 1)
+  // x-marching launch (acoustic): (z, y) tiles of the cells from `base`,
+  // the columns split into runs so that about four waves of blocks start
+  auto xm_grid = [&](int base, int nsh, dim3 *g2, int *ncx) -> bool {
+    const int nzt = (p->d.nz + 1 - base + XM_Z - 1) / XM_Z, nyt = (p->d.ny + 1 - base + XM_Y - 1) / XM_Y;
+    const int tiles = nzt * nyt * nsh;
+    *ncx = std::max(1, std::min((p->d.nx + 1 - base) / 16, (4 * 152 * 8 + tiles - 1) / tiles));
+    *g2 = dim3(nzt, nyt, *ncx * nsh);
+    return (int64_t)*ncx * nsh <= 65535;
+  };
   auto pass = [&](bool vel) {
     const int base = vel ? 4 : 1;
     const int nc = p->d.nx + 4 - base;
@@ -393,13 +528,20 @@ int step3_wavefield(Plan *p, int ipw, int vonly) {
       b.shot0 = s0;
       b.nshots = std::min(chunk, p->d.nshots - s0);
       const dim3 grd((p->d.nz + 4 - base + 31) / 32, (p->d.ny + 4 - base + 7) / 8, nc * b.nshots);
+      dim3 g2;
+      int ncx = 1;
+      const bool xm = ac && xm_grid(base, b.nshots, &g2, &ncx);
       if (vel) {
-        if (ac)
+        if (xm)
+          k3_vel_a_xm<<<g2, dim3(XM_Z, XM_Y), 0, p->stream>>>(b, ncx);
+        else if (ac)
           k3_vel_a<<<grd, blk, 0, p->stream>>>(b);
         else
           k3_vel_e<<<grd, blk, 0, p->stream>>>(b);
       } else {
-        if (ac)
+        if (xm)
+          k3_str_a_xm<<<g2, dim3(XM_Z, XM_Y), 0, p->stream>>>(b, ncx);
+        else if (ac)
           k3_str_a<<<grd, blk, 0, p->stream>>>(b);
         else
           k3_str_e<<<grd, blk, 0, p->stream>>>(b);
@@ -407,6 +549,7 @@ int step3_wavefield(Plan *p, int ipw, int vonly) {
       p->launches++;
     }
   };
+
   pass(true);
   // rigid faces in the order x, y, z; min, max (update_v!)
   const int seq[6][2] = {{2, 0}, {2, 1}, {1, 0}, {1, 1}, {0, 0}, {0, 1}};
