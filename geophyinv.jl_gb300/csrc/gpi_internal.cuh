@@ -161,6 +161,12 @@ struct Plan {
   int *d_it = nullptr;
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 
+  // snapshots (gpi_set_snapshots): field, steps, device copies
+  // [ipw][k][shot][storage]
+  int snap_field = -1;
+  std::vector<int> snap_its;
+  float *snap_buf = nullptr;
+
   // checkpointed adjoint (gpi_plan_desc.checkpoints > 0): full states of
   // wavefield 1 (fields and CPML memory) in ck_slots device slots instead of
   // the boundary store; the adjoint run recomputes forward states from them

@@ -410,6 +410,11 @@ void destroy(gpi_plan *pl) {
   // stream-ordered frees on the plan's stream, then its own stream if any
   free_sources(p);
   free_receivers(p);
+  {
+    void *sb = p.snap_buf;
+    free_dev(p, sb);
+    p.snap_buf = nullptr;
+  }
   free_dev(p, p.pool);
   if (p.own_stream) cudaStreamDestroy(p.own_stream);
   cudaSetDevice(dev);
@@ -976,6 +981,22 @@ void drop_graphs(Plan &p) {
 // the device work of one run: state reset, the time loop, the final half step
 // one time step of the loop of mod_x_proc!; with `dev` its step index is
 // the device counter plus `off` (inside a captured chunk)
+// snaps_save! (src/fdtd/propagate.jl:238-245, src/fdtd/fdtd.jl:586-591):
+// the snapshot field of every active wavefield after step it
+static int save_snapshots(Plan &p, int mode, int it) {
+  const int64_t n = p.fstride * p.d.nshots;
+  const int npw = mode == GPI_ADJOINT ? 2 : 1;
+  for (size_t k = 0; k < p.snap_its.size(); k++) {
+    if (p.snap_its[k] != it) continue;
+    for (int ipw = 0; ipw < npw; ipw++) {
+      float *dst = p.snap_buf + ((int64_t)ipw * p.snap_its.size() + k) * n;
+      GPI_CUDA(&p, cudaMemcpyAsync(dst, p.state[p.cur[ipw]][ipw][p.snap_field], n * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, p.stream));
+    }
+  }
+  return GPI_OK;
+}
+
 static int step_body(Plan &p, int mode, int it, bool dev, int off) {
   const int mask = mode == GPI_ADJOINT ? 3 : 1;
   int rc = dev ? aux_step_dev(&p, off, mode) : aux_step(&p, it, mode);
@@ -984,6 +1005,7 @@ static int step_body(Plan &p, int mode, int it, bool dev, int off) {
   if (!rc) rc = step(p, mask, it, mode, 0);
   if (!rc && mode == GPI_FORWARD_SAVE)
     rc = p.ck_slots > 0 ? ckpt_forward_store(&p, it) : dev ? boundary_io_dev(&p, off, 0) : boundary_io(&p, it, 0);
+  if (!rc && !dev && p.snap_buf) rc = save_snapshots(p, mode, it);
   return rc;
 }
 
@@ -1045,8 +1067,9 @@ static int run_body(Plan &p, int mode, bool chunked) {
     if (!rc) rc = snap_io(&p, 0, 1);
   }
   int first = 1;
-  // a checkpointed forward_save stores states at host-chosen steps: plain
-  if (!rc && chunked && !(mode == GPI_FORWARD_SAVE && p.ck_slots > 0)) rc = run_chunks(p, mode, &first);
+  // a checkpointed forward_save stores states and snapshots are taken at
+  // host-chosen steps: plain
+  if (!rc && chunked && !(mode == GPI_FORWARD_SAVE && p.ck_slots > 0) && !p.snap_buf) rc = run_chunks(p, mode, &first);
   for (int it = first; !rc && it <= p.d.nt; it++) rc = step_body(p, mode, it, false, 0);
   const bool snaps = mode == GPI_FORWARD_SAVE && p.ck_slots == 0;
   if (!rc) rc = aux_step(&p, p.d.nt + 1, mode);  // velocity records of the last step
@@ -1093,6 +1116,46 @@ int get_records(Plan &p, int shot, int field, float *out, int on_device) {
   if (rc) return rc;
   GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
   return check_err(p);
+}
+
+int set_snapshots(Plan &p, int field, int n, const int *its) {
+  if (p.snap_buf) cudaFreeAsync(p.snap_buf, p.stream);
+  p.snap_buf = nullptr;
+  p.snap_its.clear();
+  p.snap_field = -1;
+  if (field < 0 || n <= 0) return GPI_OK;
+  if (field >= NFIELD || !p.present[field]) return fail(&p, GPI_E_INVALID, "snapshot field not in this physics");
+  if (!its) return fail(&p, GPI_E_INVALID, "snapshot steps");
+  for (int k = 0; k < n; k++)
+    if (its[k] < 1 || its[k] > p.d.nt) return fail(&p, GPI_E_INVALID, "snapshot step outside 1..nt");
+  p.snap_its.assign(its, its + n);
+  p.snap_field = field;
+  const size_t bytes = (size_t)p.d.npw * n * p.fstride * p.d.nshots * sizeof(float);
+  if (cudaMallocAsync((void **)&p.snap_buf, bytes, p.stream) != cudaSuccess) {
+    cudaGetLastError();
+    p.snap_buf = nullptr;
+    p.snap_its.clear();
+    return fail(&p, GPI_E_NOMEM, "snapshot buffer of " + std::to_string(bytes) + " bytes");
+  }
+  GPI_CUDA(&p, cudaMemsetAsync(p.snap_buf, 0, bytes, p.stream));
+  drop_graphs(p);
+  return GPI_OK;
+}
+
+int get_snapshot(Plan &p, int ipw, int k, int shot, float *out, int on_device) {
+  if (!p.snap_buf) return fail(&p, GPI_E_STATE, "no snapshots configured");
+  if (ipw < 1 || ipw > p.d.npw || k < 0 || k >= (int)p.snap_its.size() || shot < 0 || shot >= p.d.nshots)
+    return fail(&p, GPI_E_INVALID, "ipw/snapshot/shot");
+  int n[3];
+  field_shape(p, p.snap_field, n);
+  const float *src = p.snap_buf + (((int64_t)(ipw - 1) * p.snap_its.size() + k) * p.d.nshots + shot) * p.fstride;
+  int rc = from_storage(p, out, src, n[0], n[1], n[2], on_device);
+  if (rc) return rc;
+  if (!on_device) {
+    GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+    return check_err(p);
+  }
+  return GPI_OK;
 }
 
 int get_field(Plan &p, int ipw, int shot, int field, float *out, int on_device) {
@@ -1171,6 +1234,12 @@ int gpi_get_records(gpi_plan *plan, int shot, int field, float *out, int on_devi
 }
 int gpi_get_gradient(gpi_plan *plan, int param, float *out, int on_device) {
   return plan ? gpi::get_gradient(plan->p, param, out, on_device) : GPI_E_INVALID;
+}
+int gpi_set_snapshots(gpi_plan *plan, int field, int n, const int *its) {
+  return plan ? gpi::set_snapshots(plan->p, field, n, its) : GPI_E_INVALID;
+}
+int gpi_get_snapshot(gpi_plan *plan, int ipw, int k, int shot, float *out, int on_device) {
+  return plan ? gpi::get_snapshot(plan->p, ipw, k, shot, out, on_device) : GPI_E_INVALID;
 }
 int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int on_device) {
   return plan ? gpi::get_field(plan->p, ipw, shot, field, out, on_device) : GPI_E_INVALID;

@@ -20,7 +20,8 @@ FIELD = {"p": 0, "vx": 1, "vy": 2, "vz": 3, "tauxx": 4, "tauyy": 5, "tauzz": 6, 
 EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_stream", "gpi_plan_bytes",
            "gpi_set_medium", "gpi_set_pml", "gpi_set_sources", "gpi_clear_sources", "gpi_set_receivers",
            "gpi_run", "gpi_get_records", "gpi_get_gradient", "gpi_get_field", "gpi_last_launches",
-           "gpi_set_graph", "gpi_query", "gpi_checkpoint_schedule", "gpi_forward_acoustic2d_noalloc"]
+           "gpi_set_graph", "gpi_query", "gpi_checkpoint_schedule", "gpi_set_snapshots", "gpi_get_snapshot",
+           "gpi_forward_acoustic2d_noalloc"]
 
 
 class PlanDesc(ctypes.Structure):
@@ -74,6 +75,8 @@ def load():
     L.gpi_last_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.gpi_set_graph.argtypes = [vp, i32]
     L.gpi_query.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
+    L.gpi_set_snapshots.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_int32)]
+    L.gpi_get_snapshot.argtypes = [vp, i32, i32, i32, fp, i32]
     L.gpi_checkpoint_schedule.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
                                           ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]
     L.gpi_forward_acoustic2d_noalloc.argtypes = [ctypes.POINTER(PlanDesc), fp, fp, fp, i32, i32, i64p, i64p, fp, fp,

@@ -127,7 +127,7 @@ class SeisForwExpt:
 
     def __init__(self, attrib, *, medium, ageom, srcwav, tgrid, rfields=("vz",), pml_faces=ALL_FACES,
                  rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False,
-                 npml=None, checkpoints=0):
+                 npml=None, checkpoints=0, tsnaps=None, snaps_field=None):
         L = _lib.load()
         self.L = L
         self.attrib = attrib
@@ -206,6 +206,18 @@ class SeisForwExpt:
         self.check_stability(verbose)
         self.data = [[Recs(a.nr, tgrid, self.rfields) for a in ageom] for _ in range(attrib.npw)]
         self.gradients = None
+        # snapshots at the steps nearest to tsnaps (fdtd.jl:179-187; default
+        # time: the middle of tgrid)
+        self.snaps_field = snaps_field
+        self.itsnaps = []
+        if snaps_field is not None:
+            assert snaps_field in fields, "snapshot field %s not in %s" % (snaps_field, fields)
+            t = tgrid.values()
+            ts = [0.5 * (t[0] + t[-1])] if tsnaps is None else list(tsnaps)
+            self.tsnaps = ts
+            self.itsnaps = [int(np.argmin(np.abs(t - x))) + 1 for x in ts]
+            its = (ctypes.c_int32 * len(self.itsnaps))(*self.itsnaps)
+            self._check(L.gpi_set_snapshots(self.plan, _lib.FIELD[snaps_field], len(self.itsnaps), its))
 
     # ------------------------------------------------------------------
     def _check(self, rc):
@@ -290,6 +302,10 @@ class SeisForwExpt:
             warnings.warn("decrease time sampling (%.2e) below %.2e" % (self.dt, dtmax))
 
     def __getitem__(self, key):
+        if isinstance(key, tuple) and key[0] == "snaps":
+            return self.snaps(key[1] if len(key) > 1 else 0)
+        if key == "snaps":
+            return self.snaps(0)
         if key == "data":
             return self.data[0]
         if key == "srcwav":
@@ -312,6 +328,23 @@ class SeisForwExpt:
         v = ctypes.c_int32()
         self._check(self.L.gpi_query(self.plan, ctypes.byref(v)))
         return bool(v.value)
+
+    def snaps(self, iss=0, ipw=1):
+        """pa[:snaps, iss] (getprop.jl:10-29): the snapshots of the last run,
+        in the order of tsnaps (0-based shot index)."""
+        name = self.snaps_field
+        n = [len(g) for g in self.exgrid]
+        kinds = S.FIELD_KINDS[name]
+        shape = []
+        for ax, g in enumerate(n):
+            k = kinds[ax if self.ndim == 3 else (0 if ax == 0 else 2)]
+            shape.append(g + self.h if k == S.KV else g - self.h if k == S.KH else g - 2 * self.h if k == S.KI else g)
+        out = []
+        for k in range(len(self.itsnaps)):
+            a = np.zeros(shape, np.float32, order="F")
+            self._check(self.L.gpi_get_snapshot(self.plan, ipw, k, iss, _ptr(a), 0))
+            out.append(a)
+        return out
 
     def records(self, iss, field):
         out = np.zeros((self.nt, self.ageom[iss].nr), np.float32, order="F")

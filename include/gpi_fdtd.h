@@ -127,6 +127,16 @@ int gpi_get_gradient(gpi_plan *plan, int param, float *out, int on_device);
 /* Final state of a field of wavefield ipw for one shot (w1[:t]) in its
  * reference shape. */
 int gpi_get_field(gpi_plan *plan, int ipw, int shot, int field, float *out, int on_device);
+/* Snapshots (tsnaps / snaps_field of PFdtd, src/fdtd/fdtd.jl:179-187;
+ * snaps_save!, src/fdtd/fdtd.jl:586-591, called at the end of step it,
+ * src/fdtd/propagate.jl:238-245): every later run keeps, after step its[k]
+ * (1-based) of the time loop, the field `field` of each active wavefield on
+ * the device.  field < 0 or n = 0 turns them off.  A checkpointed adjoint
+ * run takes none. */
+int gpi_set_snapshots(gpi_plan *plan, int field, int n, const int *its);
+/* Snapshot k (order of `its`) of wavefield ipw (1 or 2) for one shot, in
+ * the field's reference shape (pa[:snaps, iss]). */
+int gpi_get_snapshot(gpi_plan *plan, int ipw, int k, int shot, float *out, int on_device);
 /* Number of engine kernel launches issued by the last gpi_run. */
 int gpi_last_launches(const gpi_plan *plan, int64_t *launches);
 

@@ -122,6 +122,8 @@ typedef struct gpo_ctx {
   int nshots;
   REAL **bstore; /* boundary store per shot */
   REAL **hist;   /* forward history per shot (GPO_FORWARD_HIST) */
+  int snap_field, nsnap, snap_its[64]; /* snaps_save! (fdtd.jl:586-591) */
+  REAL **snaps;  /* per shot: nsnap copies of wavefield 1's snap_field */
   size_t hstep;  /* REALs per step in the history: p, vx, [vy,] vz */
   size_t bstep;  /* REALs per time step in the store */
   size_t bsnap;  /* REALs of the final snapshots */
@@ -867,6 +869,8 @@ gpo_ctx *SFX(gpo_create)(const gpo_desc *d, const void *const *mod, const void *
   c->nshots = nshots;
   c->bstore = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
   c->hist = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
+  c->snaps = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
+  c->snap_field = -1;
   return (gpo_ctx *)c;
 }
 
@@ -948,6 +952,13 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
     if (mode == GPO_FORWARD_SAVE) boundary_save(c, ishot, it);
     if (mode == GPO_FORWARD_HIST) hist_io(c, ishot, it, 0, 1);
     if (adjoint && (grad_invK || grad_rho)) compute_gradient(c, (REAL *)grad_invK, (REAL *)grad_rho);
+    /* snaps_save! for wavefield 1 at the end of step it (propagate.jl:238-245) */
+    for (int k = 0; k < c->nsnap; k++)
+      if (c->snap_its[k] == it) {
+        arr f = c->w[0][c->snap_field];
+        if (!c->snaps[ishot]) c->snaps[ishot] = (REAL *)calloc((size_t)c->nsnap * alen(f), sizeof(REAL));
+        memcpy(c->snaps[ishot] + (size_t)k * alen(f), f.a, alen(f) * sizeof(REAL));
+      }
   }
   if (mode == GPO_ADJOINT_HIST) return 0;
   if (mode == GPO_FORWARD_SAVE) snap_io(c, ishot, 1, 0); /* boundary_save_snap_tau! */
@@ -955,6 +966,23 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
   update_v(c, 0);
   if (mode == GPO_FORWARD_SAVE) snap_io(c, ishot, 0, 0); /* boundary_save_snap_v! */
   if (mode == GPO_FORWARD_HIST) hist_io(c, ishot, nt + 1, 0, 0);
+  return 0;
+}
+
+int SFX(gpo_set_snaps)(gpo_ctx *cc, int field, int n, const int *its) {
+  ctx *c = (ctx *)cc;
+  if (n < 0 || n > 64 || (n > 0 && (field < 0 || field >= GPO_NFIELD || !c->present[field]))) return -1;
+  c->snap_field = field;
+  c->nsnap = n;
+  for (int k = 0; k < n; k++) c->snap_its[k] = its[k];
+  return 0;
+}
+
+int SFX(gpo_get_snap)(gpo_ctx *cc, int ishot, int k, void *out) {
+  ctx *c = (ctx *)cc;
+  if (ishot < 0 || ishot >= c->nshots || k < 0 || k >= c->nsnap || !c->snaps[ishot]) return -1;
+  arr f = c->w[0][c->snap_field];
+  memcpy(out, c->snaps[ishot] + (size_t)k * alen(f), alen(f) * sizeof(REAL));
   return 0;
 }
 
@@ -991,6 +1019,8 @@ void SFX(gpo_destroy)(gpo_ctx *cc) {
   free(c->vbuf[2].a);
   for (int i = 0; i < c->nshots; i++) free(c->hist[i]);
   free(c->hist);
+  for (int i = 0; i < c->nshots; i++) free(c->snaps[i]);
+  free(c->snaps);
   free(c->pv);
   free(c->pvflag);
   for (int i = 0; i < c->nshots; i++) free(c->bstore[i]);

@@ -93,6 +93,12 @@ int gpo_shot_f32(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src,
                  gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho);
 int gpo_shot_f64(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec,
                  gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho);
+/* snaps_save! (src/fdtd/fdtd.jl:586-591): keep wavefield 1's `field` at
+ * the end of steps its[0..n) of later shots; read them per shot and k. */
+int gpo_set_snaps_f32(gpo_ctx *c, int field, int n, const int *its);
+int gpo_set_snaps_f64(gpo_ctx *c, int field, int n, const int *its);
+int gpo_get_snap_f32(gpo_ctx *c, int ishot, int k, void *out);
+int gpo_get_snap_f64(gpo_ctx *c, int ishot, int k, void *out);
 /* Copy the current (last shot's final) state of a field of wavefield ipw (1 or 2). */
 int gpo_get_field_f32(gpo_ctx *c, int ipw, int field, void *out);
 int gpo_get_field_f64(gpo_ctx *c, int ipw, int field, void *out);

@@ -246,10 +246,18 @@ def _shot_inputs(prep, shot, src_types=1):
     return src, rec
 
 
-def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=False):
-    """update!(pa) in :forward mode: records[field] of shape (nshots, nt, nr)."""
+def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=False, snaps=None):
+    """update!(pa) in :forward mode: records[field] of shape (nshots, nt, nr).
+    snaps = (field, [steps]) also returns res["snaps"][shot][k], the field at
+    the end of step steps[k] (1-based; snaps_save!)."""
     prep = Prepared(ex, dtype, ref_compat)
     orc = Oracle(prep, nthreads)
+    if snaps is not None:
+        its = (ctypes.c_int * len(snaps[1]))(*snaps[1])
+        sfx = orc.sfx
+        fn = getattr(orc.L, "gpo_set_snaps_" + sfx)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        assert fn(orc.ctx, S.FIELD_ID[snaps[0]], len(snaps[1]), its) == 0
     out = {f: [] for f in ex["rfields"]}
     for i, shot in enumerate(ex["shots"]):
         src, rec = _shot_inputs(prep, shot)
@@ -257,6 +265,18 @@ def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=Fal
         for f in ex["rfields"]:
             out[f].append(r[f])
     res = {f: np.stack(v) for f, v in out.items()}
+    if snaps is not None:
+        shape = orc.field(snaps[0]).shape
+        get = getattr(orc.L, "gpo_get_snap_" + orc.sfx)
+        get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        res["snaps"] = []
+        for i in range(len(ex["shots"])):
+            per = []
+            for k in range(len(snaps[1])):
+                a = np.zeros(int(np.prod(shape)), dtype=prep.dtype)
+                assert get(orc.ctx, i, k, a.ctypes.data) == 0
+                per.append(a.reshape(shape, order="F"))
+            res["snaps"].append(per)
     if return_oracle:
         return res, orc
     orc.close()
