@@ -1,0 +1,42 @@
+"""The engine against the 2-D Green's function (the reference's accuracy
+test, test/fdtd/accuracy2D.jl:6-82): pressure of a point pressure source in
+a homogeneous medium, FP32 on the GPU, against rho dA w / 4 H0^(2)(w r / c)
+W(w) in absolute amplitude and phase (the reference asks a normalised
+misfit below 1e-2)."""
+import numpy as np
+import pytest
+from scipy.special import hankel2
+
+from geophyinv_gb300 import Grid, configs, ricker, update
+
+
+@pytest.mark.gpu
+def test_green_function_on_the_engine(engine):
+    nz = nx = 161
+    d, nt, dt = 5.0, 600, 0.0005
+    vp, rho, f0 = 2000.0, 2000.0, 15.0
+    sz = sx = 400.0
+    offs = np.array([100.0, 150.0, 200.0])
+    tgrid = Grid(0.0, dt, nt)
+    w = ricker(f0, tgrid)
+    wl = configs.Workload("homogeneous", "acoustic", [Grid(0.0, d, nz), Grid(0.0, d, nx)],
+                          np.full((nz, nx), vp, np.float32), np.full((nz, nx), rho, np.float32),
+                          shots=[(np.array([[sz, sx]]), np.array([[sz, sx + o] for o in offs]))],
+                          tgrid=tgrid, wavelet=w, rfields=("p",), pml_faces=("zmin", "zmax", "xmin", "xmax"),
+                          src_field="p")
+    pa = wl.expt()
+    update(pa)
+    r = pa.data[0][0].d["p"].astype(np.float64)
+    nf = 8 * nt
+    om = 2 * np.pi * np.fft.rfftfreq(nf, dt)
+    # the spray adds K dt w to one cell of area dA; the leapfrog places the
+    # injected sample half a step late
+    W = np.fft.rfft(np.asarray(w, np.float64), nf) * np.exp(-1j * om * 0.5 * dt)
+    err = []
+    for i, o in enumerate(offs):
+        H = np.zeros_like(W)
+        H[1:] = rho * d * d * om[1:] / 4.0 * hankel2(0, om[1:] * o / vp)
+        p_an = np.fft.irfft(H * W, nf)[:nt]
+        err.append(np.sum((r[:, i] - p_an) ** 2) / np.sum(p_an ** 2))
+    assert max(err) < 1e-2, err  # the reference's bound
+    assert max(err) < 1e-4, err
