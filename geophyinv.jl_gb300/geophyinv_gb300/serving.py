@@ -256,7 +256,8 @@ def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=T
         if not done_any:
             time.sleep(0.0002)
     pool.shutdown()
-    torch.cuda.synchronize()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
     return results, _stats(requests, results, time.perf_counter() - t0)
 
 
