@@ -232,6 +232,9 @@ int64_t ckpt_slot_floats(const Plan &p);
 int ckpt_forward_store(Plan *p, int it);  // after forward_save step it
 int ckpt_adjoint(Plan *p);                 // the whole adjoint run
 int aux_step2(Plan *p, int it1, int it2);
+// raise a kernel's dynamic shared-memory limit on the current device to
+// `bytes` once (thread-safe: plans on several host threads share it)
+int ensure_smem_attr(Plan *p, const void *fn, int slot, size_t bytes);
 int aux_step_dev(Plan *p, int off, int mode);  // step *d_it + off
 int set_step(Plan *p, int v, int add);         // *d_it = v, or += v
 constexpr int kChunkSteps = 16;                // steps per replayed chunk (even: ping-pong)

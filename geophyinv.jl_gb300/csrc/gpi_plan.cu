@@ -6,6 +6,7 @@
 // (src/fdtd/types.jl:8-22, :81-88).  Shots are batched inside each launch
 // instead of being looped over by Distributed workers.
 #include <algorithm>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -964,6 +965,19 @@ int run(Plan &p, int mode) {
   }
   if (dev != p.device) cudaSetDevice(dev);
   return rc;
+}
+
+int ensure_smem_attr(Plan *p, const void *fn, int slot, size_t bytes) {
+  static std::mutex mu;
+  static size_t done[16][64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || slot < 0 || slot >= 16) return fail(p, GPI_E_UNSUPPORTED, "kernel slot or device index");
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[slot][dev] >= bytes) return GPI_OK;
+  GPI_CUDA(p, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  done[slot][dev] = bytes;
+  return GPI_OK;
 }
 
 void drop_graphs(Plan &p) {

@@ -493,10 +493,6 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
 
 // one time step of wavefield ipw (0 the modelled, 1 the adjoint wavefield)
 int step_a2_wavefield(Plan *p, int ipw, int vonly) {
-  static size_t attr[4][64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) return fail(p, GPI_E_UNSUPPORTED, "device index too large");
   A2Args a;
   a.nz = p->d.nz;
   a.nx = p->d.nx;
@@ -539,10 +535,7 @@ int step_a2_wavefield(Plan *p, int ipw, int vonly) {
   for (int m = 0; m < 4; m++) smem[m] = m == 0 ? A2_SMEM : a2_smem_general(psf[m]);
   void (*const fn[4])(A2Args) = {k_a2<0>, k_a2<1>, k_a2<2>, k_a2<3>};
   for (int m = 0; m < 4; m++)
-    if (attr[m][dev] < smem[m]) {
-      GPI_CUDA(p, cudaFuncSetAttribute(fn[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[m]));
-      attr[m][dev] = smem[m];
-    }
+    if (int rc = ensure_smem_attr(p, (const void *)fn[m], 0 + m, smem[m])) return rc;
   auto launch = [&](int m, int first, int n, cudaStream_t st) {
     if (n <= 0) return;
     A2Args g = a;

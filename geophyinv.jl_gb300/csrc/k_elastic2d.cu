@@ -630,10 +630,6 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   (void)ipw_mask;
   (void)it;
   (void)mode;
-  static size_t attr[4][64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) return fail(p, GPI_E_UNSUPPORTED, "device index too large");
   E2Args a;
   a.nz = p->d.nz;
   a.nx = p->d.nx;
@@ -683,10 +679,7 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   for (int m = 0; m < 4; m++) smem[m] = m == 0 ? E2_SMEM : e2_smem_general(psf[m]);
   void (*const fn[4])(E2Args) = {k_e2<0>, k_e2<1>, k_e2<2>, k_e2<3>};
   for (int m = 0; m < 4; m++)
-    if (attr[m][dev] < smem[m]) {
-      GPI_CUDA(p, cudaFuncSetAttribute(fn[m], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[m]));
-      attr[m][dev] = smem[m];
-    }
+    if (int rc = ensure_smem_attr(p, (const void *)fn[m], 4 + m, smem[m])) return rc;
   auto launch = [&](int m, int first, int n, cudaStream_t st) {
     if (n <= 0) return;
     E2Args g = a;
