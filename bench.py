@@ -83,6 +83,7 @@ def parse():
     ap.add_argument("--workload", default="elastic2d", choices=sorted(WORKLOADS) + ["serving"])
     ap.add_argument("--requests", type=int, default=64, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=32.0, help="serving: arrival rate, requests/s")
+    ap.add_argument("--rates", default="", help="serving: also sweep these arrival rates (comma list)")
     ap.add_argument("--nt", type=int, default=None)
     ap.add_argument("--nshots", type=int, default=None)
     ap.add_argument("--side", type=int, default=None, help="3-D workloads: a side^3 sub-grid (profiling)")
@@ -447,7 +448,24 @@ def serving_arm(args):
             "plain_one_shot_at_a_time": {k: round(v, 4) if isinstance(v, float) else v for k, v in pl.items()},
             "plain_one_request_at_a_time": {k: round(v, 4) if isinstance(v, float) else v for k, v in pr.items()},
             "speedup_shots_per_s": round(st["shots_per_s"] / pl["shots_per_s"], 3),
-            "speedup_vs_request_at_a_time": round(st["shots_per_s"] / pr["shots_per_s"], 3), "clocks": clk}
+            "speedup_vs_request_at_a_time": round(st["shots_per_s"] / pr["shots_per_s"], 3), "clocks": clk,
+            "sweep": [rate_point(float(r)) for r in args.rates.split(",") if r] or None}
+
+
+def rate_point(rate):
+    """Serving against one shot at a time at one arrival rate: 8 s of
+    arrivals (16 to 48 requests), shots/s, p50 and p99 of both."""
+    from geophyinv_gb300 import serving
+
+    n = int(max(16, min(48, 8 * rate)))
+    reqs = serving.make_stream(n, rate=rate, seed=6, sides=(200, 800), steps=(500, 2000), shots=(1, 8))
+    for r in reqs:
+        r.payload()
+    _, st = serving.serve(reqs, max_inflight=8)
+    _, pl = serving.serve_plain(reqs, per_shot=True)
+    keep = ("shots_per_s", "p50_s", "p99_s")
+    return {"rate": rate, "requests": n, "serving": {k: round(st[k], 4) for k in keep},
+            "plain_one_shot_at_a_time": {k: round(pl[k], 4) for k in keep}}
 
 
 def reference_arm(args):
