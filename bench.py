@@ -470,6 +470,8 @@ def rate_point(rate):
 
 def reference_arm(args):
     """CPU restatement of the reference (the oracle) on all host cores."""
+    if args.workload not in WORKLOADS:
+        return {"impl": "reference", "unavailable": "the serving loop has no counterpart in the reference"}
     rates = []
     sample = ""
     threads = os.cpu_count() or 1
