@@ -5,6 +5,7 @@ uses it to drive the engine.  Loading fails loudly when the library has not
 been built: there is no CPU fallback.
 """
 import ctypes
+import threading
 import os
 
 from . import _build
@@ -39,6 +40,7 @@ class EngineError(RuntimeError):
 
 
 _LIB = None
+_LOAD_LOCK = threading.Lock()
 
 
 def lib_path():
@@ -46,7 +48,15 @@ def lib_path():
 
 
 def load():
-    """Load the engine; raises if it is missing (build it with _build.build())."""
+    """Load the engine; raises if it is missing (build it with _build.build()).
+    Thread-safe: plans are created on the serving loop's worker threads."""
+    if _LIB is not None:
+        return _LIB
+    with _LOAD_LOCK:
+        return _load()
+
+
+def _load():
     global _LIB
     if _LIB is not None:
         return _LIB
