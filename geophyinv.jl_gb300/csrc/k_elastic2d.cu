@@ -51,8 +51,11 @@ struct E2Args {
 };
 
 // slots of the shared-memory column ring: 4 columns in use by the stencils
-// plus 2 in flight; 6 keeps an interior block at 37 KB (6 blocks per SM)
+// plus 2 in flight; 6 keeps an interior block at 37 KB (6 blocks per SM).
+// The band tiles take 5 (one column in flight) so that six of their blocks
+// fit an SM as well (80 registers, about 35 KB)
 constexpr int RING = 6;
+__host__ __device__ constexpr int e2_ring(int mode) { return mode == 1 ? 5 : RING; }
 constexpr int E2_TZ = TZ2;                                      // stress rows per block
 constexpr int E2_THREADS = 128;                                 // TZ + 3 velocity rows, one per thread
 constexpr int E2_R8 = E2_TZ + 8;                                // stress rows z0-4 .. z0+TZ+3
@@ -67,7 +70,9 @@ inline int e2_psi_floats(const Plan &p) {
   const bool zf = p.d.pml_faces & (GPI_ZMIN | GPI_ZMAX), xf = p.d.pml_faces & (GPI_XMIN | GPI_XMAX);
   return (zf ? 4 * p.pzw : 0) + (xf ? 2 * E2_R4 + 2 * E2_TZ : 0);
 }
-inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (RING * (E2_SLOT + psf) + 2 * RING * E2_R4); }
+inline size_t e2_smem_general(int psf, int ring) {
+  return 128 + sizeof(float) * (ring * (E2_SLOT + psf) + 2 * ring * E2_R4);
+}
 
 // MODE 0: interior tiles (no CPML, face or source: straight-line code);
 // MODE 1: tiles away from the x edges and x strips (the band code over every
@@ -75,8 +80,9 @@ inline size_t e2_smem_general(int psf) { return 128 + sizeof(float) * (RING * (E
 // with x-strip columns; MODE 3: tiles with x-edge columns (the band code plus
 // the general code for the edge and source columns).
 template <int MODE>
-__global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : MODE == 2 ? 4 : 3) k_e2(const E2Args a) {
+__global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MODE == 2 ? 4 : 3) k_e2(const E2Args a) {
   constexpr bool FAST = MODE == 0, XPSI = MODE >= 2;
+  constexpr int RING = e2_ring(MODE);
   constexpr int TZ = E2_TZ, R8 = E2_R8, R4 = E2_R4, SLOT = E2_SLOT;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);  // one mbarrier per ring slot
@@ -676,7 +682,7 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   const bool zf = p->d.pml_faces & (GPI_ZMIN | GPI_ZMAX);
   const int psf[4] = {0, zf ? 4 * p->pzw : 0, e2_psi_floats(*p), e2_psi_floats(*p)};
   size_t smem[4];
-  for (int m = 0; m < 4; m++) smem[m] = m == 0 ? E2_SMEM : e2_smem_general(psf[m]);
+  for (int m = 0; m < 4; m++) smem[m] = m == 0 ? E2_SMEM : e2_smem_general(psf[m], e2_ring(m));
   void (*const fn[4])(E2Args) = {k_e2<0>, k_e2<1>, k_e2<2>, k_e2<3>};
   for (int m = 0; m < 4; m++)
     if (int rc = ensure_smem_attr(p, (const void *)fn[m], 4 + m, smem[m])) return rc;
