@@ -290,16 +290,38 @@ class SeisForwExpt:
             self._check(self.L.gpi_set_pml(self.plan, q, _ptr(a), _ptr(b), _ptr(k)))
 
     def check_stability(self, verbose=False):
-        """check_stability (src/fdtd/stability.jl:8-60): warnings only."""
+        """check_stability (src/fdtd/stability.jl:8-60): warnings only.
+        Spatial sampling: at least H = 20 / order points per minimum
+        wavelength at the highest source frequency (vmin: the smallest
+        non-zero vs for elastic media, the lower vp bound otherwise); time
+        sampling: the Courant limit dt <= d_min / (sqrt(ndim) vmax), vmax
+        = sqrt(vp_max^2 + vs_max^2) for elastic media.  As in the reference,
+        the limits are compared as %0.2e strings first."""
+        H = 20 // self.order
         _, vb = S.ref_bounds(self.medium.vp)
-        vmax = float(vb[1])
+        vmin, vmax = float(vb[0]), float(vb[1])
         if self.attrib.physics == "elastic":
             _, vsb = S.ref_bounds(self.medium.vs)
+            vs = np.asarray(self.medium.vs)
+            vmin = float(vs[vs != 0].min())
             vmax = float(np.sqrt(vb[1] ** 2 + vsb[1] ** 2))
-        dmin = min(g.step for g in self.medium.grid)
-        dtmax = (1.0 / np.sqrt(self.ndim)) * dmin / vmax
-        if self.dt > dtmax:
-            warnings.warn("decrease time sampling (%.2e) below %.2e" % (self.dt, dtmax))
+        steps = [g.step for g in self.medium.grid]
+        fmax = getattr(self, "freqmax", None)
+        if fmax and np.isfinite(fmax) and fmax > 0:
+            ds_temp = round(vmin / H / fmax, 2)
+            s1, s2 = "%0.2e" % max(steps), "%0.2e" % ds_temp
+            if s1 != s2:
+                if max(steps) > ds_temp:
+                    warnings.warn("decrease maximum spatial sampling (%s) below %s" % (s1, s2))
+                elif verbose:
+                    print("spatial sampling (%s) can be as high as %s" % (s1, s2))
+        dtmax = (1.0 / np.sqrt(self.ndim)) * min(steps) / vmax
+        s1, s2 = "%0.2e" % self.dt, "%0.2e" % dtmax
+        if s1 != s2:
+            if self.dt > dtmax:
+                warnings.warn("decrease time sampling (%s) below %s" % (s1, s2))
+            elif verbose:
+                print("time sampling (%s) can be as high as %s" % (s1, s2))
 
     def __getitem__(self, key):
         if isinstance(key, tuple) and key[0] == "snaps":
@@ -424,6 +446,7 @@ def _update_srcwav(pa, srcwav, src_types=None):
     for ipw, sw in enumerate(srcwav):
         pa.srcwav[ipw] = [s.copy() for s in sw]
     peaks = []
+    fmaxs = []
     for ipw in range(pa.attrib.npw):
         st = src_types[ipw] if ipw < len(src_types) else 0
         pa._check(pa.L.gpi_clear_sources(pa.plan, ipw + 1, -1))
@@ -441,6 +464,8 @@ def _update_srcwav(pa, srcwav, src_types=None):
                 if np.all(w == 0):
                     continue
                 fpeaks.append(S.findfreq_peak(w, pa.dt))
+                if ipw == 0:
+                    fmaxs.append(S.findfreq(w, pa.dt, "max"))
                 wf = np.asfortranarray(w, np.float32)
                 if ipw == 0:
                     cp, rv, nz = pa._proj(f, pa.ageom[iss].points("s", pa.ndim))
@@ -451,6 +476,8 @@ def _update_srcwav(pa, srcwav, src_types=None):
                                                    _ptr(wf)))
             if fpeaks and ipw == 0:
                 peaks.append(np.mean(fpeaks))
+    if fmaxs:
+        pa.freqmax = float(min(fmaxs))  # fill_wavelets! (src/fdtd/source.jl:46-53)
     if peaks:
         pa.freqpeak = np.float32(np.mean(peaks))
     elif not hasattr(pa, "freqpeak"):

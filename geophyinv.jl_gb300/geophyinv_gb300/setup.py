@@ -241,6 +241,28 @@ def findfreq_peak(w, dt):
     return np.fft.rfftfreq(w.shape[0], dt)[i % ax.shape[0]]
 
 
+def findfreq(w, dt, attrib="peak", threshold=-50.0):
+    """findfreq (src/Utils/freq.jl:28-57): on the power spectrum of all
+    columns, normalised to its maximum in dB, the frequency of the maximum
+    ("peak"), of the last ("max") or first ("min") sample at or above
+    `threshold`, in the column-major order of the spectra."""
+    w = np.asarray(w, np.float64)
+    w = w[:, None] if w.ndim == 1 else w
+    ax = np.abs(np.fft.rfft(w, axis=0)) ** 2
+    f = np.fft.rfftfreq(w.shape[0], dt)
+    if ax.max() == 0.0:
+        return 0.0
+    db = 10.0 * np.log10(np.maximum(ax / ax.max(), 1e-300))
+    flat = db.T.reshape(-1)  # column-major order of (frequency, column)
+    if attrib == "peak":
+        i = int(np.argmax(flat))
+    elif attrib == "max":
+        i = int(np.nonzero(flat >= threshold)[0][-1])
+    else:
+        i = int(np.nonzero(flat >= threshold)[0][0])
+    return float(f[i % ax.shape[0]])
+
+
 def reverse_source(w):
     """Source of the time-reversed wavefield (get_source(..., Val{-1}),
     src/fdtd/source.jl:8-19): -w shifted by one sample, reversed, row 1 zero."""
