@@ -52,3 +52,24 @@ def test_create_rejects_bad_descriptor(lib):
     d.pml_faces = 0x3F  # CPML on every face
     d.nz = 60  # too small for two PML strips
     assert lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan)) == -1
+
+
+def test_create_rejects_bad_checkpoint_requests(lib):
+    """A checkpointed adjoint needs npw = 2 and an acoustic medium (checked
+    before any device call)."""
+    import ctypes
+
+    d = _lib.PlanDesc()
+    d.physics, d.ndim, d.order = 0, 2, 4
+    d.nz, d.ny, d.nx, d.npml, d.nbound, d.nt, d.nshots, d.npw = 200, 1, 200, 41, 3, 10, 1, 1
+    d.dt, d.dz, d.dx, d.dy = 1e-3, 5.0, 5.0, 1.0
+    d.pml_faces = 0x3F
+    plan = ctypes.c_void_p()
+    d.checkpoints = 4  # npw = 1: no adjoint to checkpoint
+    assert lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan)) == -1
+    assert b"checkpoints" in lib.gpi_last_error(None)
+    d.npw, d.physics = 2, 1  # elastic: no gradient
+    assert lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan)) == -4
+    assert b"acoustic" in lib.gpi_last_error(None)
+    d.checkpoints = -1
+    assert lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan)) == -1
