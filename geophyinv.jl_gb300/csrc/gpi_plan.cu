@@ -463,8 +463,9 @@ int set_medium(Plan &p, const float *const *mod, int on_device) {
   return GPI_OK;
 }
 
-int set_pml(Plan &p, int q, const float *a, const float *b, const float *kI) {
+int set_pml(Plan &p, int q, int len, const float *a, const float *b, const float *kI) {
   if (q < 0 || q >= p.nder || !a || !b || !kI) return fail(&p, GPI_E_INVALID, "pml field index or null array");
+  if (len != 2 * p.d.npml) return fail(&p, GPI_E_INVALID, "pml arrays must hold 2*npml values");
   const size_t n = 2 * (size_t)p.d.npml;
   float *dst = p.pml + (size_t)q * 3 * n;
   GPI_CUDA(&p, cudaMemcpyAsync(dst, a, n * sizeof(float), cudaMemcpyHostToDevice, p.stream));
@@ -1230,8 +1231,8 @@ int gpi_plan_bytes(const gpi_plan *plan, size_t *bytes) {
 int gpi_set_medium(gpi_plan *plan, const float *const *mod, int on_device) {
   return plan ? gpi::set_medium(plan->p, mod, on_device) : GPI_E_INVALID;
 }
-int gpi_set_pml(gpi_plan *plan, int q, const float *a, const float *b, const float *kI) {
-  return plan ? gpi::set_pml(plan->p, q, a, b, kI) : GPI_E_INVALID;
+int gpi_set_pml(gpi_plan *plan, int q, int len, const float *a, const float *b, const float *kI) {
+  return plan ? gpi::set_pml(plan->p, q, len, a, b, kI) : GPI_E_INVALID;
 }
 int gpi_set_sources(gpi_plan *plan, int ipw, int shot, int field, int ns, const int64_t *colptr, const int64_t *rowval,
                     const float *nzval, const float *wavelets) {

@@ -19,8 +19,12 @@
 // start at zero, and two calls whose work overlaps on the GPU (different
 // streams, or different host threads) race on it.  The first call on a
 // device looks up the device address of the array (cudaGetSymbolAddress)
-// with that device current; make that first call before any stream
-// capture begins.
+// with that device current and keeps it for the life of the process; make
+// that first call before any stream capture begins, and do not reset the
+// device (cudaDeviceReset) while the library is loaded.  Every call
+// synchronises `stream` twice -- after the table uploads, because the host
+// staging tables are static and reused by the next call, and at the end, to
+// read the kernels' error flag -- so it returns when the run has finished.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -54,7 +58,15 @@ static int4 h_tiles[kMaxTiles];
 static int h_xcut[kMaxCuts];
 static Plan g_plan;  // descriptor filled per call; its pointers point into the scratch
 
+static int h_err;  // the kernels' error flag, read back at the end of a call
+
 static int nfail(int code, const char *msg) { return fail(nullptr, code, msg); }
+
+#define NA_CUDA(call)                                                   \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) return nfail(GPI_E_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
 
 // device address of the scratch on the current device (looked up once)
 static int scratch_base(float **out) {
@@ -101,6 +113,8 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
   if (src_field != GPI_P && src_field != GPI_VX && src_field != GPI_VZ) return nfail(GPI_E_INVALID, "source field");
   if (ns < 1 || !src_colptr || !src_rowval || !src_nzval) return nfail(GPI_E_INVALID, "source matrix");
   if (nrf < 0 || nrf > kMaxRecFields) return nfail(GPI_E_INVALID, "at most 3 receiver fields");
+  if (nrf > 0 && (!rfields || !nr || !rec_colptr || !rec_rowval || !rec_nzval || !records))
+    return nfail(GPI_E_INVALID, "null receiver array");
   float *base = nullptr;
   int rc = scratch_base(&base);
   if (rc) return rc;
@@ -267,25 +281,25 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     P.d_tiles = (int4 *)carve((int64_t)(sizeof(int4) * ntile + 3) / 4);
     if (!room) return nfail(GPI_E_INVALID, "problem exceeds the 64 MiB no-alloc scratch");
     cudaStream_t s = P.stream;
-    cudaMemcpyAsync(P.d_cells, h_cells, sizeof(InjCell) * m, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.d_pair_j, h_pj, sizeof(int32_t) * np, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.d_pair_w, h_pw, sizeof(float) * np, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.d_group_ptr, h_gptr, sizeof(h_gptr), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.d_wav, h_wavptr, sizeof(h_wavptr), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.d_tiles, h_tiles, sizeof(int4) * ntile, cudaMemcpyHostToDevice, s);
+    NA_CUDA(cudaMemcpyAsync(P.d_cells, h_cells, sizeof(InjCell) * m, cudaMemcpyHostToDevice, s));
+    NA_CUDA(cudaMemcpyAsync(P.d_pair_j, h_pj, sizeof(int32_t) * np, cudaMemcpyHostToDevice, s));
+    NA_CUDA(cudaMemcpyAsync(P.d_pair_w, h_pw, sizeof(float) * np, cudaMemcpyHostToDevice, s));
+    NA_CUDA(cudaMemcpyAsync(P.d_group_ptr, h_gptr, sizeof(h_gptr), cudaMemcpyHostToDevice, s));
+    NA_CUDA(cudaMemcpyAsync(P.d_wav, h_wavptr, sizeof(h_wavptr), cudaMemcpyHostToDevice, s));
+    NA_CUDA(cudaMemcpyAsync(P.d_tiles, h_tiles, sizeof(int4) * ntile, cudaMemcpyHostToDevice, s));
   }
   if (!room) return nfail(GPI_E_INVALID, "problem exceeds the 64 MiB no-alloc scratch");
   cudaStream_t s = P.stream;
-  cudaMemcpyAsync(P.d_rtask, h_tasks, sizeof(RecTask) * ntask, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(P.d_roff, h_roff, sizeof(int64_t) * nent, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(P.d_rw, h_rw, sizeof(float) * nent, cudaMemcpyHostToDevice, s);
+  NA_CUDA(cudaMemcpyAsync(P.d_rtask, h_tasks, sizeof(RecTask) * ntask, cudaMemcpyHostToDevice, s));
+  NA_CUDA(cudaMemcpyAsync(P.d_roff, h_roff, sizeof(int64_t) * nent, cudaMemcpyHostToDevice, s));
+  NA_CUDA(cudaMemcpyAsync(P.d_rw, h_rw, sizeof(float) * nent, cudaMemcpyHostToDevice, s));
   // the wavefields, CPML memory and records start at zero
   for (int b = 0; b < 2; b++) {
-    for (int f : {GPI_P, GPI_VX, GPI_VZ}) cudaMemsetAsync(P.state[b][0][f], 0, P.fstride * sizeof(float), s);
-    for (int q = 0; q < 4; q++) cudaMemsetAsync(P.psi[b][0][q], 0, P.psi_stride[q] * sizeof(float), s);
+    for (int f : {GPI_P, GPI_VX, GPI_VZ}) NA_CUDA(cudaMemsetAsync(P.state[b][0][f], 0, P.fstride * sizeof(float), s));
+    for (int q = 0; q < 4; q++) NA_CUDA(cudaMemsetAsync(P.psi[b][0][q], 0, P.psi_stride[q] * sizeof(float), s));
   }
-  if (pool) cudaMemsetAsync(P.rec_pool, 0, pool * sizeof(float), s);
-  cudaMemsetAsync(P.d_err, 0, sizeof(int), s);
+  if (pool) NA_CUDA(cudaMemsetAsync(P.rec_pool, 0, pool * sizeof(float), s));
+  NA_CUDA(cudaMemsetAsync(P.d_err, 0, sizeof(int), s));
   // medium -> storage layout (device to device), then update coefficients
   for (int i = 0; i < 2; i++) {
     cudaMemcpy3DParms mp = {};
@@ -294,7 +308,7 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     mp.dstPos = make_cudaPos((size_t)ZOFF * sizeof(float), 0, XOFF);
     mp.extent = make_cudaExtent((size_t)d.nz * sizeof(float), 1, d.nx);
     mp.kind = cudaMemcpyDeviceToDevice;
-    cudaMemcpy3DAsync(&mp, s);
+    NA_CUDA(cudaMemcpy3DAsync(&mp, s));
   }
   // the static host staging is reused by the next call: wait for the uploads
   cudaError_t e = cudaStreamSynchronize(s);
@@ -311,6 +325,11 @@ extern "C" int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const f
     off += (int64_t)nr[k] * d.nt;
   }
   if (rc) return nfail(rc, P.err.c_str());
+  // a bounded pipeline wait that gave up sets the flag and leaves the
+  // records incomplete: report it instead of returning success
+  NA_CUDA(cudaMemcpyAsync(&h_err, P.d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NA_CUDA(cudaStreamSynchronize(s));
+  if (h_err) return nfail(GPI_E_CUDA, "a step kernel's pipeline wait timed out (records incomplete)");
   e = cudaGetLastError();
   if (e != cudaSuccess) return nfail(GPI_E_CUDA, cudaGetErrorString(e));
   return GPI_OK;

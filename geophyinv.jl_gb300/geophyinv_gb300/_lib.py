@@ -74,7 +74,7 @@ def _load():
     L.gpi_set_stream.argtypes = [vp, vp]
     L.gpi_plan_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
     L.gpi_set_medium.argtypes = [vp, vp, i32]
-    L.gpi_set_pml.argtypes = [vp, i32, fp, fp, fp]
+    L.gpi_set_pml.argtypes = [vp, i32, i32, fp, fp, fp]
     L.gpi_set_sources.argtypes = [vp, i32, i32, i32, i32, i64p, i64p, fp, fp]
     L.gpi_clear_sources.argtypes = [vp, i32, i32]
     L.gpi_set_receivers.argtypes = [vp, i32, i32, i32, i64p, i64p, fp]

@@ -22,6 +22,7 @@ import numpy as np
 
 from . import _lib
 from . import setup as S
+from . import shots as _shots
 from .setup import Grid
 
 ALL_FACES = ["zmin", "zmax", "ymin", "ymax", "xmax", "xmin"]
@@ -127,7 +128,7 @@ class SeisForwExpt:
 
     def __init__(self, attrib, *, medium, ageom, srcwav, tgrid, rfields=("vz",), pml_faces=ALL_FACES,
                  rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False,
-                 npml=None, checkpoints=0, tsnaps=None, snaps_field=None):
+                 npml=None, checkpoints=0, tsnaps=None, snaps_field=None, shard=False):
         L = _lib.load()
         self.L = L
         self.attrib = attrib
@@ -154,6 +155,24 @@ class SeisForwExpt:
         for s in srcwav:
             for f in s.fields:
                 assert f in fields, "source field %s not in %s" % (f, fields)
+        # shard=True under an initialised torch.distributed group: this rank
+        # holds only its contiguous chunk of the supersources (sschunks,
+        # src/fdtd/fdtd.jl:246-255); gradients and misfits are summed over
+        # the ranks once per gradient! / lossvalue (sum_grads!,
+        # src/fdtd/gradient.jl:2-12).  Lists indexed by supersource that the
+        # caller passes later (srcwav, dobs) may cover all of them.
+        self.nss_global = len(ageom)
+        self.shot_ids = list(range(len(ageom)))
+        self.shard = False
+        if shard:
+            rank, world = _shots.rank_world()
+            if world > 1:
+                self.shot_ids = list(_shots.my_shots(len(ageom), rank, world))
+                if not self.shot_ids:
+                    raise ValueError("rank %d of %d holds no supersource (%d in all)" % (rank, world, len(ageom)))
+                ageom = [ageom[i] for i in self.shot_ids]
+                srcwav = [srcwav[i] for i in self.shot_ids]
+                self.shard = True
         self.ageom = ageom
         self.nss = len(ageom)
         # adjoint geometry/wavelets of the second wavefield (fdtd.jl:90-99)
@@ -285,9 +304,9 @@ class SeisForwExpt:
         _, vb = S.ref_bounds(self.exvp)
         velavg = np.float32((vb[0] + vb[1]) / np.float32(2.0))
         self.pml = S.cpml_all(self.attrib.physics, self.ndim, self.order, self.medium.grid, self.pml_mask,
-                              np.float32(self.dt), velavg, np.float32(self.freqpeak))
+                              np.float32(self.dt), velavg, np.float32(self.freqpeak), self.npml)
         for q, (a, b, k) in enumerate(self.pml):
-            self._check(self.L.gpi_set_pml(self.plan, q, _ptr(a), _ptr(b), _ptr(k)))
+            self._check(self.L.gpi_set_pml(self.plan, q, len(a), _ptr(a), _ptr(b), _ptr(k)))
 
     def check_stability(self, verbose=False):
         """check_stability (src/fdtd/stability.jl:8-60): warnings only.
@@ -444,7 +463,7 @@ def _update_srcwav(pa, srcwav, src_types=None):
         src_types = [1] * len(srcwav)
     assert len(srcwav) == len(pa.srcwav) or len(srcwav) == 1
     for ipw, sw in enumerate(srcwav):
-        pa.srcwav[ipw] = [s.copy() for s in sw]
+        pa.srcwav[ipw] = [s.copy() for s in _local(pa, sw)]
     peaks = []
     fmaxs = []
     for ipw in range(pa.attrib.npw):
@@ -476,6 +495,14 @@ def _update_srcwav(pa, srcwav, src_types=None):
                                                    _ptr(wf)))
             if fpeaks and ipw == 0:
                 peaks.append(np.mean(fpeaks))
+    if pa.shard:
+        # the peak frequency (it sets the CPML alpha) and the highest
+        # frequency come from the sources of every rank, as on one host
+        n = _shots.reduce_scalar(len(peaks))
+        tot = _shots.reduce_scalar(float(np.sum(np.asarray(peaks, np.float64))))
+        peaks = [tot / n] if n else []
+        fm = -_shots.reduce_scalar(-(min(fmaxs) if fmaxs else np.inf), op="max")
+        fmaxs = [fm] if np.isfinite(fm) else []
     if fmaxs:
         pa.freqmax = float(min(fmaxs))  # fill_wavelets! (src/fdtd/source.jl:46-53)
     if peaks:
@@ -525,11 +552,22 @@ def lossvalue(m, loss, dobs, pa, mparams=("invK", "rho")):
     update(pa, pa.srcwav, [1, 0])
     update(pa)
     pa.attrib.mode = mode_save
-    return _loss(loss, dobs, pa.data[0])
+    return _loss(loss, dobs, pa)
 
 
-def _loss(loss, dobs, dcal):
-    return sum(loss.value(o.d[f], c.d[f]) for o, c in zip(dobs, dcal) for f in o.fields)
+def _local(pa, lst):
+    """The entries of this rank's supersources from a list over all of them
+    (unchanged when the experiment is not sharded or `lst` is local)."""
+    if pa.shard and len(lst) == pa.nss_global:
+        return [lst[i] for i in pa.shot_ids]
+    return lst
+
+
+def _loss(loss, dobs, pa):
+    """Misfit of the last forward records against dobs, summed over the
+    ranks of a sharded experiment."""
+    J = sum(loss.value(o.d[f], c.d[f]) for o, c in zip(_local(pa, dobs), pa.data[0]) for f in o.fields)
+    return _shots.reduce_scalar(J) if pa.shard else J
 
 
 def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
@@ -540,7 +578,7 @@ def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
     gv = _adjoint(pa, m, loss, dobs, mparams)
     if g is not None:
         g[:] = gv
-    return _loss(loss, dobs, pa.data[0])
+    return _loss(loss, dobs, pa)
 
 
 def _forward_save(pa, m, mparams):
@@ -561,7 +599,7 @@ def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
     `scale`)."""
     mparams = list(mparams)
     adj = []
-    for o, c in zip(dobs, pa.data[0]):
+    for o, c in zip(_local(pa, dobs), pa.data[0]):
         s = Srcs(o.n, pa.tgrid, pa.rfields)
         for f in pa.rfields:
             s.d[f] = loss.deriv(o.d[f], c.d[f])[::-1].copy()  # reverse!(srcwav[2])
@@ -587,4 +625,6 @@ def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
         out.append(gm.astype(np.float32).ravel(order="F"))
     pa.gradients = raw
     gv = np.concatenate(out)
+    if pa.shard:
+        _shots.reduce_gradient(gv)
     return gv if scale == 1.0 else (gv * np.float32(scale)).astype(np.float32)

@@ -39,7 +39,7 @@ def rrule(f, m, loss, dobs, pa, mparams=("invK", "rho")):
     mparams = tuple(mparams)
     m = np.asarray(m, np.float32)
     _forward_save(pa, m, mparams)
-    J = _loss(loss, dobs, pa.data[0])
+    J = _loss(loss, dobs, pa)
     done = []
 
     def pullback(dJ):

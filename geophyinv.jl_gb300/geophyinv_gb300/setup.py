@@ -156,10 +156,16 @@ def cpml_profile(x, g, flags, dt32, velavg32, fpeak32, npml):
     return a[sel].astype(np.float32), b[sel].astype(np.float32), (1.0 / k[sel]).astype(np.float32)
 
 
-def cpml_all(physics, ndim, order, grid, mask, dt32, velavg32, fpeak32):
-    """update_pml! for every derivative field (src/fdtd/cpml.jl:125-155)."""
+def cpml_all(physics, ndim, order, grid, mask, dt32, velavg32, fpeak32, npml):
+    """update_pml! for every derivative field (src/fdtd/cpml.jl:125-155).
+    `npml` is the plan's PML width: it sets the padding of the extended
+    grid, the damping thickness (npml - 1) * step and the strips kept (the
+    reference uses its constant _fd_npml = 40 + order - 1 for all three,
+    src/fdtd/cpml.jl:29,88-99)."""
     h = order - 1
-    npml = 40 + h
+    npml = int(npml)
+    if npml < 1:
+        raise ValueError("npml must be positive")
     ex = padgrid(grid, npml, mask)
     names = axis_names(ndim)
     out = []

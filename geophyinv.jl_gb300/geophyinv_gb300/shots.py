@@ -28,6 +28,29 @@ def my_shots(nss, rank, world):
     return range(*chunks[rank]) if rank < len(chunks) else range(0)
 
 
+def rank_world(group=None):
+    """(rank, world size) of an initialised torch.distributed group, else
+    (0, 1)."""
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()):
+        return 0, 1
+    return dist.get_rank(group), dist.get_world_size(group)
+
+
+def reduce_scalar(x, group=None, op="sum"):
+    """Sum (or max) of a per-rank float (a misfit) over the ranks, in
+    float64."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()):
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM if op == "sum" else dist.ReduceOp.MAX, group=group)
+    return float(t.item())
+
+
 def reduce_gradient(g, group=None):
     """Sum a per-rank gradient (numpy array or torch tensor) over the ranks of
     `group` in place and return it; a no-op without an initialised process

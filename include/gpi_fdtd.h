@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define GPI_ABI_VERSION 1
+#define GPI_ABI_VERSION 2
 
 enum gpi_status {
   GPI_OK = 0,
@@ -97,8 +97,9 @@ int gpi_set_medium(gpi_plan *plan, const float *const *mod, int on_device);
 
 /* update_pml! result (src/fdtd/cpml.jl:8-155): for derivative field q
  * (canonical order of the physics, see docs) the arrays a, b, kI, each of
- * length 2*npml. */
-int gpi_set_pml(gpi_plan *plan, int q, const float *a, const float *b, const float *kI);
+ * length len, which must equal 2*npml of the plan (the first npml values
+ * serve the min face, the last npml the max face, cpml.jl:88-99). */
+int gpi_set_pml(gpi_plan *plan, int q, int len, const float *a, const float *b, const float *kI);
 
 /* Source spray matrix and wavelets of one supersource (fill_wavelets!,
  * src/fdtd/source.jl:24-58, and ssprayw, src/fdtd/ageom.jl:33-45).
@@ -171,8 +172,9 @@ int gpi_checkpoint_schedule(int nt, int slots, int64_t *advances, int64_t *turns
  * GPI_NOALLOC_SCRATCH_BYTES per GPU (held until the process exits); larger
  * problems are rejected with GPI_E_INVALID.  Calls share that array: calls
  * that overlap on the GPU race.  The first call on a device looks up the
- * array's address with that device current; make it before any stream
- * capture begins.
+ * array's address with that device current and keeps it until the process
+ * exits; make it before any stream capture begins, and do not reset the
+ * device while the library is loaded.
  *   desc      physics GPI_ACOUSTIC, ndim 2, order 4, nshots 1, npw 1
  *   invK, rho device, extended grid, column-major (nz*nx each)
  *   pml       device, 4 x 3 x 2*npml floats: a, b, kI of dpdx, dpdz, dvxdx, dvzdz
@@ -180,7 +182,10 @@ int gpi_checkpoint_schedule(int nt, int slots, int64_t *advances, int64_t *turns
  *             (GPI_P, GPI_VX or GPI_VZ); wavelets: device, nt x ns
  *   rfields   nrf (<= 3) receiver fields among p, vx, vz, each with nr[k]
  *             (<= 4096) receivers as host CSC; records[k]: device, nt x nr[k]
- * Asynchronous on `stream` (cudaStream_t) after the table uploads. */
+ * Runs on `stream` (cudaStream_t) and synchronises it before returning
+ * (once after the table uploads, once to read the kernels' error flag), so
+ * the host blocks until the records are written.  GPI_E_CUDA if a CUDA
+ * call failed or a kernel's bounded pipeline wait gave up. */
 int gpi_forward_acoustic2d_noalloc(const gpi_plan_desc *desc, const float *invK, const float *rho, const float *pml,
                                    int src_field, int ns, const int64_t *src_colptr, const int64_t *src_rowval,
                                    const float *src_nzval, const float *wavelets, int nrf, const int *rfields,

@@ -113,7 +113,7 @@ class Prepared:
             peaks.append(np.mean(fp))
         self.fpeak = np.float32(np.mean(peaks))
         self.pml = S.pml_all(self.physics, self.ndim, self.order, self.grid, self.faces,
-                             np.float32(self.dt), self.velavg, self.fpeak)
+                             np.float32(self.dt), self.velavg, self.fpeak, self.npml)
         self.ref_compat = ref_compat
         self.shape = [g[2] for g in self.exgrid]
 

@@ -152,11 +152,14 @@ def pml_profile(exgrid_f, mgrid_start, mgrid_step, mgrid_n, flags, dt32, velavg3
     return (a[sel].astype(np.float32), b[sel].astype(np.float32), (1.0 / k[sel]).astype(np.float32))
 
 
-def pml_all(physics, ndim, order, mgrid, faces, dt32, velavg32, fpeak32):
+def pml_all(physics, ndim, order, mgrid, faces, dt32, velavg32, fpeak32, npml=None):
     """update_pml! over all derivative fields (src/fdtd/cpml.jl:125-155).
-    mgrid: physical (start, step, n) per axis (z, [y,] x)."""
+    mgrid: physical (start, step, n) per axis (z, [y,] x).  npml: the PML
+    width that replaces the reference's constant _fd_npml in the padding,
+    the thickness (npml - 1) * step and the kept strips (cpml.jl:29,88-99);
+    default _fd_npml."""
     h = order - 1
-    npml = npml_of(order)
+    npml = npml_of(order) if npml is None else int(npml)
     ex = padmgrid(mgrid, npml, faces)
     out = []
     names = "zyx" if ndim == 3 else "zx"

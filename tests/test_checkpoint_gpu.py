@@ -109,16 +109,14 @@ def test_acoustic3d_checkpointed_gradient_matches_oracle(engine, src_field):
 
 
 @pytest.mark.gpu
-def test_acoustic3d_checkpointed_invK_gradient_matches_finite_differences(engine):
+@pytest.mark.parametrize("npml", [43, 23, 10])
+def test_acoustic3d_checkpointed_invK_gradient_matches_finite_differences(engine, npml):
     """Central differences of lossvalue on blocks of the inner grid (the
     reference's gradient-accuracy test, test/fwi/gradient_accuracy.jl, in
-    3-D, which the reference cannot run).  With the reference's 43-cell PML
-    the two agree to about 1e-4; with a thin PML they do not (10 cells: 3 %,
-    23 cells: 1 %): the adjoint wavefield runs through the same CPML as the
-    forward one, which is the adjoint of the discrete CPML only where the
-    PML does not reflect."""
+    3-D, which the reference cannot run), with the reference's 43-cell PML
+    and with thin ones."""
     nz, ny, nx, nt = 32, 28, 34, 220
-    wl = configs.acoustic3d(nz=nz, ny=ny, nx=nx, nt=nt, npml=43, nrec_side=5, rfields=("vz",), src_field="p")
+    wl = configs.acoustic3d(nz=nz, ny=ny, nx=nx, nt=nt, npml=npml, nrec_side=5, rfields=("vz",), src_field="p")
     s, r = wl.shots[0]
     r = r.copy()
     r[:, 0] = 40.0  # receivers 4 cells below the surface
@@ -139,4 +137,5 @@ def test_acoustic3d_checkpointed_invK_gradient_matches_finite_differences(engine
         e[:n] = blk.ravel(order="F")
         fd = (lossvalue(m0 + h * e, L2DistLoss(), dobs, pa) - lossvalue(m0 - h * e, L2DistLoss(), dobs, pa)) / (2 * h)
         adj = float(g @ e)
+        print("npml %d block %s: fd %.6e adjoint %.6e rel %.2e" % (npml, (z0, y0, x0), fd, adj, abs(fd - adj) / abs(adj)))
         assert abs(fd - adj) <= 1e-2 * abs(adj), ((z0, y0, x0), fd, adj)

@@ -33,7 +33,7 @@ def test_cpml_profiles(physics, ndim):
                                                                                             P.Grid(0, 5, 41)]
     mask = 63 & ~1
     dt, va, fp = np.float32(0.0005), np.float32(2745.5), np.float32(15.0)
-    a = P.cpml_all(physics, ndim, 4, grid, mask, dt, va, fp)
+    a = P.cpml_all(physics, ndim, 4, grid, mask, dt, va, fp, 43)
     b = S.pml_all(physics, ndim, 4, [(g.start, g.step, g.n) for g in grid], mask, dt, va, fp)
     assert len(a) == len(b) == len(P.DERIV[(physics, ndim)])
     for x, y in zip(a, b):

@@ -20,13 +20,9 @@ def _dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float32).ravel(order="F"))).cuda()
 
 
-@pytest.mark.gpu
-def test_noalloc_forward_matches_plan_path(engine):
-    import torch
-
-    wl = configs.acoustic2d_layers(nz=101, nx=131, nt=400, nrec=31)
-    pa = wl.expt()
-    update(pa)
+def _noalloc(engine, torch, pa):
+    """One gpi_forward_acoustic2d_noalloc call on the inputs of plan `pa`;
+    returns {field: records nt x nr}."""
     invK = _dev(torch, pa.mod["invK"])
     rho = _dev(torch, pa.mod["rho"])
     pml = _dev(torch, np.concatenate([np.concatenate(x) for x in pa.pml]))
@@ -43,20 +39,58 @@ def test_noalloc_forward_matches_plan_path(engine):
     P = ctypes.c_void_p
     arrp = lambda xs: (P * len(xs))(*[x.ctypes.data for x in xs])  # noqa: E731
     stream = torch.cuda.current_stream().cuda_stream
+    outs = [torch.full((pa.nt * n,), np.nan, device="cuda") for n in nr]
+    rc = engine.gpi_forward_acoustic2d_noalloc(
+        ctypes.byref(pa.desc), P(invK.data_ptr()), P(rho.data_ptr()), P(pml.data_ptr()), fid[field], sw.n,
+        P(scp.ctypes.data), P(srv.ctypes.data), P(snz.ctypes.data), P(wav.data_ptr()), len(rf),
+        (ctypes.c_int * len(rf))(*[fid[f] for f in rf]), (ctypes.c_int * len(rf))(*nr), arrp(cps), arrp(rvs),
+        arrp(nzs), (P * len(rf))(*[o.data_ptr() for o in outs]), P(stream))
+    assert rc == 0, engine.gpi_last_error(None)
+    torch.cuda.synchronize()
+    return {f: o.cpu().numpy().reshape(n, pa.nt).T for f, o, n in zip(rf, outs, nr)}
+
+
+def _check(got, pa, what):
+    for f in pa.rfields:
+        ref = pa.data[0][0].d[f]
+        e = np.linalg.norm(got[f] - ref) / np.linalg.norm(ref)
+        assert e < TOL, (what, f, e)
+
+
+@pytest.mark.gpu
+def test_noalloc_forward_matches_plan_path(engine):
+    """Two calls in a row on the same inputs both give the plan's records."""
+    import torch
+
+    wl = configs.acoustic2d_layers(nz=101, nx=131, nt=400, nrec=31)
+    pa = wl.expt()
+    update(pa)
     for call in range(2):
-        outs = [torch.full((pa.nt * n,), np.nan, device="cuda") for n in nr]
-        rc = engine.gpi_forward_acoustic2d_noalloc(
-            ctypes.byref(pa.desc), P(invK.data_ptr()), P(rho.data_ptr()), P(pml.data_ptr()), fid[field], sw.n,
-            P(scp.ctypes.data), P(srv.ctypes.data), P(snz.ctypes.data), P(wav.data_ptr()), len(rf),
-            (ctypes.c_int * len(rf))(*[fid[f] for f in rf]), (ctypes.c_int * len(rf))(*nr), arrp(cps), arrp(rvs),
-            arrp(nzs), (P * len(rf))(*[o.data_ptr() for o in outs]), P(stream))
-        assert rc == 0, engine.gpi_last_error(None)
-        torch.cuda.synchronize()
-        for f, o, n in zip(rf, outs, nr):
-            got = o.cpu().numpy().reshape(n, pa.nt).T
-            ref = pa.data[0][0].d[f]
-            e = np.linalg.norm(got - ref) / np.linalg.norm(ref)
-            assert e < TOL, (call, f, e)
+        _check(_noalloc(engine, torch, pa), pa, call)
+
+
+@pytest.mark.gpu
+def test_noalloc_larger_then_smaller_call_leaves_nothing_behind(engine):
+    """A larger grid followed by a smaller one (the scratch layout shifts
+    between them) and a velocity source in the second call: each call
+    matches the plan path, and the second one also the CPU oracle."""
+    import torch
+
+    from oracle import oracle as O
+
+    big = configs.acoustic2d_layers(nz=161, nx=221, nt=300, nrec=41)
+    pb = big.expt()
+    update(pb)
+    _check(_noalloc(engine, torch, pb), pb, "big")
+    small = configs.acoustic2d_layers(nz=97, nx=123, nt=350, nrec=29, src_field="vz")
+    ps = small.expt()
+    update(ps)
+    got = _noalloc(engine, torch, ps)
+    _check(got, ps, "small after big")
+    ref = O.forward(small.as_dict())
+    for f in small.rfields:
+        e = np.linalg.norm(got[f] - ref[f][0]) / np.linalg.norm(ref[f][0])
+        assert e < TOL, ("oracle", f, e)
 
 
 @pytest.mark.gpu
