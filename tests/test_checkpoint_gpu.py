@@ -114,7 +114,9 @@ def test_acoustic3d_checkpointed_invK_gradient_matches_finite_differences(engine
     """Central differences of lossvalue on blocks of the inner grid (the
     reference's gradient-accuracy test, test/fwi/gradient_accuracy.jl, in
     3-D, which the reference cannot run), with the reference's 43-cell PML
-    and with thin ones."""
+    and with thin ones: measured on GB300, 1e-6 to 1e-4 on the blocks with
+    a large gradient at every width (the third block's gradient is 40 times
+    smaller, 5e-4 to 5e-3)."""
     nz, ny, nx, nt = 32, 28, 34, 220
     wl = configs.acoustic3d(nz=nz, ny=ny, nx=nx, nt=nt, npml=npml, nrec_side=5, rfields=("vz",), src_field="p")
     s, r = wl.shots[0]
