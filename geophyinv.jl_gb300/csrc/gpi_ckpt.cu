@@ -205,6 +205,7 @@ struct Grad3Args {
   const float *v2[3], *vs[3], *vs1[3];  // x, y, z: adjoint, V_s, V_{s+1}
   float *gK, *gR;
   float dtI;
+  int imaging;  // 0 the reference-style rho term, 1 the discrete model's
 };
 
 __global__ void __launch_bounds__(256) k_grad_a3(const Grad3Args a) {
@@ -222,7 +223,24 @@ __global__ void __launch_bounds__(256) k_grad_a3(const Grad3Args a) {
     };
     const int64_t o = S(r, y, c);
     a.gK[o] = a.gK[o] + a.p2[o] * (a.pold[o] - a.pnew[o]) * a.dtI;
-    if (r >= 4 && r <= a.nz - 3 && y >= 4 && y <= a.ny - 3 && c >= 4 && c <= a.nx - 3) {
+    if (a.imaging) {
+      // rho(r, y, c) sits in the coefficients of the velocity cells two and
+      // three cells further along each axis, where those are updated (vx:
+      // rows 4..nz-3, y 4..ny-3, columns 4..nx; vy: rows 4..nz-3, y 4..ny,
+      // columns 4..nx-3; vz: rows 4..nz, y 4..ny-3, columns 4..nx-3)
+      auto b = [&](int d, int rr, int yy, int cc, bool in) {
+        const int64_t q = S(rr, yy, cc);
+        return in ? a.v2[d][q] * (a.vs[d][q] - a.vs1[d][q]) * a.dtI : 0.f;
+      };
+      const bool rin = r >= 4 && r <= a.nz - 3, yin = y >= 4 && y <= a.ny - 3, cin = c >= 4 && c <= a.nx - 3;
+      const float avx = rin && yin ? (b(0, r, y, c + 2, c + 2 >= 4 && c + 2 <= a.nx) +
+                                      b(0, r, y, c + 3, c + 3 >= 4 && c + 3 <= a.nx)) * 0.5f : 0.f;
+      const float avy = rin && cin ? (b(1, r, y + 2, c, y + 2 >= 4 && y + 2 <= a.ny) +
+                                      b(1, r, y + 3, c, y + 3 >= 4 && y + 3 <= a.ny)) * 0.5f : 0.f;
+      const float avz = yin && cin ? (b(2, r + 2, y, c, r + 2 >= 4 && r + 2 <= a.nz) +
+                                      b(2, r + 3, y, c, r + 3 >= 4 && r + 3 <= a.nz)) * 0.5f : 0.f;
+      a.gR[o] = a.gR[o] - avx - avy - avz;
+    } else if (r >= 4 && r <= a.nz - 3 && y >= 4 && y <= a.ny - 3 && c >= 4 && c <= a.nx - 3) {
       auto b = [&](int d, int64_t q) { return a.v2[d][q] * (a.vs[d][q] - a.vs1[d][q]) * a.dtI; };
       const float bx1 = b(0, S(r, y, c - 3)), bx2 = b(0, S(r, y, c - 2));
       const float by1 = b(1, S(r, y - 3, c)), by2 = b(1, S(r, y - 2, c));
@@ -283,6 +301,7 @@ static int turn(Plan *p, int s) {
   g.gK = p->grad[0];
   g.gR = p->grad[1];
   g.dtI = (float)(1.0 / p->d.dt);
+  g.imaging = p->d.imaging;
   k_grad_a3<<<152 * 16, 256, 0, p->stream>>>(g);
   p->launches++;
   GPI_CUDA(p, cudaGetLastError());

@@ -161,6 +161,13 @@ struct Plan {
   int *d_it = nullptr;
   std::vector<InjCell> h_cells;  // host copy of the injection cells (tile classification)
 
+  // Born modelling (gpi_set_born): secondary-source ratios of p, vx, vz in
+  // the storage layout of one shot (zero outside the update domains), and
+  // the uploaded perturbations
+  float *born = nullptr;  // [5][fstride]: rp, rvx, rvz, dinvK, drho
+  bool have_born = false;
+  int rec_ipw = 0;  // wavefield the records are gathered from (1: Born runs)
+
   // snapshots (gpi_set_snapshots): field, steps, device copies
   // [ipw][k][shot][storage]
   int snap_field = -1;
@@ -260,6 +267,9 @@ int compute_coefficients(Plan *p);
 int boundary_io(Plan *p, int it, int dir);
 int boundary_io_dev(Plan *p, int off, int dir);  // step *d_it + off
 int snap_io(Plan *p, int tau, int dir);
+// Born modelling (k_born.cu)
+int born_coefficients(Plan *p);
+int born_run(Plan *p);
 
 }  // namespace gpi
 

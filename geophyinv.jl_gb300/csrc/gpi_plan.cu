@@ -182,6 +182,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   if (d.checkpoints > 0 && d.physics != GPI_ACOUSTIC)
     return fail(nullptr, GPI_E_UNSUPPORTED, "checkpointed gradients: acoustic media only");
   if (d.npml < 1 || d.nbound < 1) return fail(nullptr, GPI_E_INVALID, "npml/nbound");
+  if (d.imaging != 0 && d.imaging != 1) return fail(nullptr, GPI_E_INVALID, "imaging must be 0 or 1");
   if (!(d.dt > 0) || !(d.dz > 0) || !(d.dx > 0) || (d.ndim == 3 && !(d.dy > 0)))
     return fail(nullptr, GPI_E_INVALID, "dt and grid steps must be positive");
   const int h = d.order - 1;
@@ -415,6 +416,9 @@ void destroy(gpi_plan *pl) {
     void *sb = p.snap_buf;
     free_dev(p, sb);
     p.snap_buf = nullptr;
+    void *bb = p.born;
+    free_dev(p, bb);
+    p.born = nullptr;
   }
   free_dev(p, p.pool);
   if (p.own_stream) cudaStreamDestroy(p.own_stream);
@@ -460,6 +464,30 @@ int set_medium(Plan &p, const float *const *mod, int on_device) {
   if (rc) return rc;
   if (!on_device) GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
   p.src_dirty = true;  // injection scaling reads rho / dtK at run time, nothing to redo
+  return GPI_OK;
+}
+
+// update!(pa, medium, medium_pert) for Born plans: the perturbations, kept
+// in storage layout; the secondary-source ratios are formed from them and
+// the current medium at the start of each Born run (k_born.cu)
+int set_born(Plan &p, const float *const *dmod, int on_device) {
+  if (p.d.physics != GPI_ACOUSTIC || p.d.ndim != 2 || p.d.npw != 2)
+    return fail(&p, GPI_E_UNSUPPORTED, "Born modelling: 2-D acoustic plans with npw = 2");
+  if (!dmod || !dmod[0] || !dmod[1]) return fail(&p, GPI_E_INVALID, "dmod arrays");
+  if (!p.born) {
+    if (cudaMallocAsync((void **)&p.born, 5 * p.fstride * sizeof(float), p.stream) != cudaSuccess) {
+      cudaGetLastError();
+      p.born = nullptr;
+      return fail(&p, GPI_E_NOMEM, "Born perturbation buffers");
+    }
+    GPI_CUDA(&p, cudaMemsetAsync(p.born, 0, 5 * p.fstride * sizeof(float), p.stream));
+  }
+  for (int i = 0; i < 2; i++) {
+    int rc = to_storage(p, p.born + (3 + i) * p.fstride, dmod[i], p.d.nz, 1, p.d.nx, on_device);
+    if (rc) return rc;
+  }
+  if (!on_device) GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  p.have_born = true;
   return GPI_OK;
 }
 
@@ -900,7 +928,14 @@ static bool same_sources(const std::vector<std::vector<Plan::Src>> &a, const std
 void ckpt_prepare_forward(Plan *p);  // gpi_ckpt.cu
 
 int run(Plan &p, int mode) {
-  if (mode != GPI_FORWARD && mode != GPI_FORWARD_SAVE && mode != GPI_ADJOINT) return fail(&p, GPI_E_INVALID, "mode");
+  if (mode != GPI_FORWARD && mode != GPI_FORWARD_SAVE && mode != GPI_ADJOINT && mode != GPI_BORN)
+    return fail(&p, GPI_E_INVALID, "mode");
+  if (mode == GPI_BORN) {
+    if (!p.have_born) return fail(&p, GPI_E_STATE, "Born run before gpi_set_born");
+    for (auto &shot : p.src[1])
+      for (auto &s : shot)
+        if (s.ns) return fail(&p, GPI_E_STATE, "Born run: wavefield 2 takes no sources (clear them first)");
+  }
   if (mode != GPI_FORWARD && p.d.npw != 2) return fail(&p, GPI_E_INVALID, "forward_save/adjoint need npw = 2");
   if (mode == GPI_ADJOINT && !p.have_save) return fail(&p, GPI_E_STATE, "adjoint run needs a forward_save run first");
   if (mode == GPI_ADJOINT && !(p.d.physics == GPI_ACOUSTIC && (p.d.ndim == 2 || p.ck_slots > 0)))
@@ -932,7 +967,19 @@ int run(Plan &p, int mode) {
   }
   if (!rc && p.d.ndim == 2 && !p.d_tiles) rc = build_tiles(p);
   if (!rc && recompile) drop_graphs(p);
-  if (!rc && p.graph_kind == 2) {
+  if (!rc && mode == GPI_BORN) {
+    // plain launches
+    rc = zero_state(p);
+    p.launches = 0;
+    if (!rc && p.rec_pool)
+      rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
+    if (!rc) rc = born_coefficients(&p);
+    if (!rc) rc = born_run(&p);
+    if (!rc) {
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));
+    }
+  } else if (!rc && p.graph_kind == 2) {
     rc = run_body(p, mode, true);
   } else if (!rc && p.graph_kind == 1) {
     // the whole run as one CUDA graph: captured on first use per mode,
@@ -1230,6 +1277,9 @@ int gpi_plan_bytes(const gpi_plan *plan, size_t *bytes) {
 }
 int gpi_set_medium(gpi_plan *plan, const float *const *mod, int on_device) {
   return plan ? gpi::set_medium(plan->p, mod, on_device) : GPI_E_INVALID;
+}
+int gpi_set_born(gpi_plan *plan, const float *const *dmod, int on_device) {
+  return plan ? gpi::set_born(plan->p, dmod, on_device) : GPI_E_INVALID;
 }
 int gpi_set_pml(gpi_plan *plan, int q, int len, const float *a, const float *b, const float *kI) {
   return plan ? gpi::set_pml(plan->p, q, len, a, b, kI) : GPI_E_INVALID;

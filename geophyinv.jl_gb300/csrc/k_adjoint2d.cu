@@ -13,8 +13,12 @@
 //       bx = vx2_prev (vx1 - vx1_prev) dtI, bz likewise      (velocity grids)
 //       g_rho[iz+h, ix+h] -= (bx[iz+h, ix] + bx[iz+h, ix+1]) / 2
 //                          + (bz[iz, ix+h] + bz[iz+1, ix+h]) / 2,
-//       iz in 1..nz-2h, ix in 1..nx-2h (the averages sit one cell off the
-//       stencil centre, as in the reference)
+//       iz in 1..nz-2h, ix in 1..nx-2h (the averages sit four and five
+//       cells off the velocity cells whose coefficients hold rho(r, c), as in
+//       the reference); with Plan::d.imaging = 1 instead
+//       g_rho[r, c] -= (bx[r, c+2] + bx[r, c+3]) / 2 + (bz[r+2, c] + bz[r+3, c]) / 2
+//       over the updated velocity cells: the gradient of the discrete model
+//       (dt / avg(rho) at vx cell c averages rho at c-3 and c-2)
 // The imaging condition is one streaming pass over both wavefields' old and
 // new states (k_grad_a2); the velocity terms are recomputed at the two
 // neighbours each g_rho cell needs, in the reference's operation order.
@@ -34,6 +38,7 @@ struct GradArgs {
   int nb, npx, npz;   // strip width and PML offsets of the strips
   float *gK, *gR;
   float dtI;
+  int imaging;  // 0 the reference's rho term, 1 the discrete model's
 };
 
 // position of p cell (r, c) in the strip block of boundary_save! (x strips
@@ -69,8 +74,23 @@ __global__ void __launch_bounds__(256) k_grad_a2(const GradArgs a) {
     const int64_t sidx = strip_index(a, r, c);
     if (sidx >= 0) p1p = a.prev[shot * a.pstride + sidx];
     a.gK[o] = a.gK[o] + a.p2A[o] * (p1p - a.p1B[o]) * a.dtI;
-    // compute_gmodrho! + combine_gmodrho!
-    if (r >= 4 && r <= a.nz - 3 && c >= 4 && c <= a.nx - 3) {
+    if (a.imaging) {
+      // rho(r, c) sits in the coefficients of vx (r, c+2), (r, c+3) and vz
+      // (r+2, c), (r+3, c) where those are updated (vx rows 4..nz-3,
+      // columns 4..nx; vz rows 4..nz, columns 4..nx-3)
+      auto bx = [&](int cc) {
+        const int64_t q = S(r, cc);
+        return cc >= 4 && cc <= a.nx ? a.vx2A[q] * (a.vx1B[q] - a.vx1A[q]) * a.dtI : 0.f;
+      };
+      auto bz = [&](int rr) {
+        const int64_t q = S(rr, c);
+        return rr >= 4 && rr <= a.nz ? a.vz2A[q] * (a.vz1B[q] - a.vz1A[q]) * a.dtI : 0.f;
+      };
+      const float avx = r >= 4 && r <= a.nz - 3 ? (bx(c + 2) + bx(c + 3)) * 0.5f : 0.f;
+      const float avz = c >= 4 && c <= a.nx - 3 ? (bz(r + 2) + bz(r + 3)) * 0.5f : 0.f;
+      a.gR[o] = a.gR[o] - avx - avz;
+    } else if (r >= 4 && r <= a.nz - 3 && c >= 4 && c <= a.nx - 3) {
+      // compute_gmodrho! + combine_gmodrho!
       const int64_t x1 = S(r, c - 3), x2 = S(r, c - 2), z1 = S(r - 3, c), z2 = S(r - 2, c);
       const float bx1 = a.vx2A[x1] * (a.vx1B[x1] - a.vx1A[x1]) * a.dtI;
       const float bx2 = a.vx2A[x2] * (a.vx1B[x2] - a.vx1A[x2]) * a.dtI;
@@ -108,6 +128,7 @@ int grad_a2_launch(Plan *p, const float *p1A, const float *p1B, const float *vx1
   g.gK = p->grad[0];
   g.gR = p->grad[1];
   g.dtI = (float)(1.0 / p->d.dt);
+  g.imaging = p->d.imaging;
   k_grad_a2<<<152 * 16, 256, 0, p->stream>>>(g);
   p->launches++;
   GPI_CUDA(p, cudaGetLastError());
@@ -141,6 +162,7 @@ int step_adjoint_acoustic2d(Plan *p, int it) {
   g.gK = p->grad[0];
   g.gR = p->grad[1];
   g.dtI = (float)(1.0 / p->d.dt);
+  g.imaging = p->d.imaging;
   // wavefield 1 (time reversal, boundary already forced), then wavefield 2
   int rc = step_a2_wavefield(p, 0, 0);
   if (!rc) rc = step_a2_wavefield(p, 1, 0);

@@ -220,7 +220,9 @@ int aux_step(Plan *p, int it, int mode) {
   a.zero = 0;
   a.it_dev = nullptr;
   a.it_off = 0;
-  for (int f = 0; f < NFIELD; f++) a.field[f] = p->state[p->cur[0]][0][f];
+  // the records of a Born run are wavefield 2's
+  const int rw = p->rec_ipw;
+  for (int f = 0; f < NFIELD; f++) a.field[f] = p->state[p->cur[rw]][rw][f];
   a.fs = p->fstride;
   a.cells = p->d_cells;
   a.ncells = p->n_cells;

@@ -208,7 +208,59 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
       }
     }
   };
-  if (issuer) issue(xbase + RING - 1);
+  // interior and band tiles: each issuing lane keeps the source pointers of
+  // its share of a column (at most four copies: fields advance by NZP per
+  // column, z-strip CPML windows by zsw) and advances them per issue, so the
+  // steady-state producer work is a few instructions
+  constexpr bool PROD = MODE <= 1;
+  const float *fs0 = nullptr, *fs1 = nullptr, *fs2 = nullptr, *fs3 = nullptr;
+  int fd0 = 0, fd1 = 0, fd2 = 0, fd3 = 0, fst2 = NZP, fst3 = NZP;
+  uint32_t fn0 = 0, fn1 = 0, fn2 = 0, fn3 = 0;
+  if constexpr (PROD) {
+    const int64_t oT = so + S(z0 - 4, xbase), oV = S(z0, xbase);
+    if (wq == 0) {
+      fs0 = a.txxA + oT, fs1 = a.tzzA + oT, fs2 = a.txzA + oT;
+      fd0 = 0, fd1 = R8, fd2 = 2 * R8;
+      fn0 = fn1 = fn2 = R8 * 4;
+    } else if (wq == 1) {
+      fs0 = a.vxA + so + oV, fs1 = a.vzA + so + oV, fs2 = a.cx + oV;
+      fd0 = 3 * R8, fd1 = 3 * R8 + R4, fd2 = 3 * R8 + 2 * R4;
+      fn0 = fn1 = fn2 = R4 * 4;
+    } else if (wq == 2) {
+      fs0 = a.cz + oV, fs1 = a.dtM + oV;
+      fd0 = 3 * R8 + 3 * R4, fd1 = 3 * R8 + 4 * R4;
+      fn0 = R4 * 4, fn1 = TZ * 4;
+    } else {
+      fs0 = a.dtl + oV, fs1 = a.mu + oV;
+      fd0 = 3 * R8 + 4 * R4 + TZ, fd1 = 3 * R8 + 4 * R4 + 2 * TZ;
+      fn0 = fn1 = TZ * 4;
+    }
+    if (!FAST && zt && wq >= 2) {
+      // z-strip CPML windows: warp 2 derivatives 2 3, warp 3 derivatives 5 6
+      const int64_t oz = ZS(xbase, zoff);
+      const int i0 = wq == 2 ? 0 : 2;
+      fs2 = psA(wq == 2 ? 2 : 5) + oz, fs3 = psA(wq == 2 ? 3 : 6) + oz;
+      fd2 = SLOT + i0 * PZW, fd3 = SLOT + (i0 + 1) * PZW;
+      fn2 = fn3 = PZW * 4;
+      fst2 = fst3 = a.zsw;
+    }
+  }
+  // the next column of this warp's share into ring slot sl
+  auto issue_fast = [&](int sl) {
+    float *d = ring + sl * SL;
+    mbar_expect_tx(&bar[sl], fn0 + fn1 + fn2 + fn3);
+    bulk_g2s(d + fd0, fs0, fn0, &bar[sl]);
+    bulk_g2s(d + fd1, fs1, fn1, &bar[sl]);
+    if (fn2) bulk_g2s(d + fd2, fs2, fn2, &bar[sl]);
+    if (fn3) bulk_g2s(d + fd3, fs3, fn3, &bar[sl]);
+    fs0 += NZP, fs1 += NZP, fs2 += fst2, fs3 += fst3;
+  };
+  if constexpr (PROD) {
+    if (issuer)
+      for (int sl = 0; sl < RING && xbase + sl <= xlast; sl++) issue_fast(sl);
+  } else {
+    if (issuer) issue(xbase + RING - 1);
+  }
   auto wait_col = [&](int cc) {
     const int j = cc - xbase;
     if (!mbar_wait(&bar[j % RING], (j / RING) & 1)) s_err = 1;
@@ -310,6 +362,11 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
   if constexpr (FAST) {
     // interior tile: inside every update domain, no CPML, no face, no
     // source.
+    // global addresses of this thread's rows, advanced one column per
+    // iteration: velocities of column xbase+3+it, stresses of column xbase+it
+    float *pvx = a.vxB + so + S(q, xbase + 3), *pvz = a.vzB + so + S(q, xbase + 3);
+    float *ptxx = a.txxB + so + S(z0 + t, xbase), *ptzz = a.tzzB + so + S(z0 + t, xbase),
+          *ptxz = a.txzB + so + S(z0 + t, xbase);
     // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
     auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
       if (!vact) return;
@@ -325,9 +382,8 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
       svx[s0 * R4 + k] = vx;
       svz[s0 * R4 + k] = vz;
       if (cc < x1 && kq < TZ) {
-        const int64_t o = so + S(q, cc);
-        a.vxB[o] = vx;
-        a.vzB[o] = vz;
+        *pvx = vx;
+        *pvz = vz;
       }
     };
     // stresses of column c from velocity slots s0..s3 = columns c..c+3
@@ -345,20 +401,30 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
       const float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
       const float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
       const float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
-      const int64_t o = so + S(z0 + t, c);
-      a.txxB[o] = txx;
-      a.tzzB[o] = tzz;
-      a.txzB[o] = txz;
+      *ptxx = txx;
+      *ptzz = tzz;
+      *ptxz = txz;
     };
-    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
+    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) %
+    // RING.  The loop is unrolled by RING so that every slot index is a
+    // constant (base is a multiple of RING; the parity of a slot's mbarrier
+    // flips once per RING columns)
     const int ncol = x1 - xbase;
-    for (int it = 0; it < ncol; it++) {
-      const int c = xbase + it;
-      if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
-      vel_fast(c + 3, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
-      __syncthreads();
-      if (issuer) issue(c + RING - 1);
-      if (c >= x0) str_fast(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
+    for (int base = 0; base < ncol; base += RING) {
+      const uint32_t ph = (uint32_t)(base / RING) & 1u;
+#pragma unroll
+      for (int u = 0; u < RING; u++) {
+        const int it = base + u;
+        if (it >= ncol) break;
+        const int c = xbase + it;
+        if (!mbar_wait(&bar[(u + 3) % RING], ph ^ (uint32_t)((u + 3) / RING))) s_err = 1;
+        vel_fast(c + 3, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+        __syncthreads();
+        if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
+        if (c >= x0) str_fast(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+        pvx += NZP, pvz += NZP;
+        ptxx += NZP, ptzz += NZP, ptxz += NZP;
+      }
     }
   } else {
   // columns that need the full general code: x edges and mirrors, sources
@@ -478,17 +544,39 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
     if constexpr (MODE == 1 || MODE == 2) {
       // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
       const int ncol = x1 - xbase;
-      for (int it = 0; it < ncol; it++) {
-        const int c = xbase + it, cc = c + 3;
-        int ib0, ie0, ib1, ie1, bs = 0, es = 0;
-        cvx.range(a.cells, cc, ib0, ie0);
-        cvz.range(a.cells, cc, ib1, ie1);
-        if (c >= x0) cst.range(a.cells, c, bs, es);
-        if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
-        vel_band(cc, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, ib0, ie0, ib1, ie1);
-        __syncthreads();
-        if (issuer) issue(c + RING - 1);
-        if (c >= x0) str_band(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, bs, es);
+      if constexpr (MODE == 1) {
+        // unrolled by RING: constant slot indices (see the interior loop)
+        for (int base = 0; base < ncol; base += RING) {
+          const uint32_t ph = (uint32_t)(base / RING) & 1u;
+#pragma unroll
+          for (int u = 0; u < RING; u++) {
+            const int it = base + u;
+            if (it >= ncol) break;
+            const int c = xbase + it, cc = c + 3;
+            int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+            cvx.range(a.cells, cc, ib0, ie0);
+            cvz.range(a.cells, cc, ib1, ie1);
+            if (c >= x0) cst.range(a.cells, c, bs, es);
+            if (!mbar_wait(&bar[(u + 3) % RING], ph ^ (uint32_t)((u + 3) / RING))) s_err = 1;
+            vel_band(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, ib0, ie0, ib1, ie1);
+            __syncthreads();
+            if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
+            if (c >= x0) str_band(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, bs, es);
+          }
+        }
+      } else {
+        for (int it = 0; it < ncol; it++) {
+          const int c = xbase + it, cc = c + 3;
+          int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+          cvx.range(a.cells, cc, ib0, ie0);
+          cvz.range(a.cells, cc, ib1, ie1);
+          if (c >= x0) cst.range(a.cells, c, bs, es);
+          if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
+          vel_band(cc, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, ib0, ie0, ib1, ie1);
+          __syncthreads();
+          if (issuer) issue(c + RING - 1);
+          if (c >= x0) str_band(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, bs, es);
+        }
       }
     } else {
       // velocities of column cc: update_v! with CPML, mirrors, sources

@@ -14,7 +14,7 @@ GPI_OK = 0
 STATUS = {0: "GPI_OK", -1: "GPI_E_INVALID", -2: "GPI_E_NOMEM", -3: "GPI_E_CUDA", -4: "GPI_E_UNSUPPORTED",
           -5: "GPI_E_STATE"}
 ACOUSTIC, ELASTIC = 0, 1
-FORWARD, FORWARD_SAVE, ADJOINT = 0, 1, 2
+FORWARD, FORWARD_SAVE, ADJOINT, BORN = 0, 1, 2, 3
 FACE = {"zmin": 1, "zmax": 2, "ymin": 4, "ymax": 8, "xmin": 16, "xmax": 32}
 FIELD = {"p": 0, "vx": 1, "vy": 2, "vz": 3, "tauxx": 4, "tauyy": 5, "tauzz": 6, "tauxy": 7, "tauxz": 8, "tauyz": 9}
 
@@ -22,7 +22,7 @@ EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_str
            "gpi_set_medium", "gpi_set_pml", "gpi_set_sources", "gpi_clear_sources", "gpi_set_receivers",
            "gpi_run", "gpi_get_records", "gpi_get_gradient", "gpi_get_field", "gpi_last_launches",
            "gpi_set_graph", "gpi_query", "gpi_checkpoint_schedule", "gpi_set_snapshots", "gpi_get_snapshot",
-           "gpi_forward_acoustic2d_noalloc"]
+           "gpi_forward_acoustic2d_noalloc", "gpi_set_born"]
 
 
 class PlanDesc(ctypes.Structure):
@@ -31,7 +31,7 @@ class PlanDesc(ctypes.Structure):
                 ("npml", ctypes.c_int32), ("nbound", ctypes.c_int32), ("pml_faces", ctypes.c_int32),
                 ("rigid_faces", ctypes.c_int32), ("free_faces", ctypes.c_int32), ("nt", ctypes.c_int32),
                 ("nshots", ctypes.c_int32), ("npw", ctypes.c_int32), ("checkpoints", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 3),
+                ("imaging", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
                 ("dt", ctypes.c_double), ("dz", ctypes.c_double), ("dy", ctypes.c_double), ("dx", ctypes.c_double)]
 
 
@@ -74,6 +74,7 @@ def _load():
     L.gpi_set_stream.argtypes = [vp, vp]
     L.gpi_plan_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_size_t)]
     L.gpi_set_medium.argtypes = [vp, vp, i32]
+    L.gpi_set_born.argtypes = [vp, vp, i32]
     L.gpi_set_pml.argtypes = [vp, i32, i32, fp, fp, fp]
     L.gpi_set_sources.argtypes = [vp, i32, i32, i32, i32, i64p, i64p, fp, fp]
     L.gpi_clear_sources.argtypes = [vp, i32, i32]

@@ -41,6 +41,17 @@ class FdtdElastic(FdtdAcoustic):
     physics = "elastic"
 
 
+class FdtdAcousticBorn(FdtdAcoustic):
+    """FdtdAcoustic{Born}(mode, npw = 2) (src/physics_types.jl:25-49):
+    wavefield 1 the background, wavefield 2 the Born (single-scattering)
+    field of the perturbation set by update(pa, medium, medium_pert); its
+    records are pa.data[1]."""
+    born = True
+
+    def __init__(self, mode="forward", npw=2):
+        super().__init__(mode, 2)
+
+
 class AcousticMedium:
     """AcousticMedium (src/media/media.jl:40-51): grid per axis, vp, rho (Float32)."""
     params = ("vp", "rho")
@@ -128,7 +139,7 @@ class SeisForwExpt:
 
     def __init__(self, attrib, *, medium, ageom, srcwav, tgrid, rfields=("vz",), pml_faces=ALL_FACES,
                  rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False,
-                 npml=None, checkpoints=0, tsnaps=None, snaps_field=None, shard=False):
+                 npml=None, checkpoints=0, tsnaps=None, snaps_field=None, shard=False, ref_compat_grad=True):
         L = _lib.load()
         self.L = L
         self.attrib = attrib
@@ -207,6 +218,10 @@ class SeisForwExpt:
         # device slots of wavefield-1 states replace the boundary store
         d.checkpoints = int(checkpoints) if attrib.npw == 2 else 0
         self.checkpoints = d.checkpoints
+        # rho term of the imaging condition: the reference's
+        # (src/fdtd/gradient.jl:31-56) or, with ref_compat_grad=False, the
+        # gradient of the discrete model (agrees with finite differences)
+        d.imaging = 0 if ref_compat_grad else 1
         d.dt = self.dt
         self.desc = d
         plan = ctypes.c_void_p()
@@ -420,10 +435,12 @@ class SeisForwExpt:
 # ----------------------------------------------------------------------
 def update(pa, *args, _pml=True, **kw):
     """update!(pa) / update!(pa, medium) / update!(pa, srcwav, src_types) /
-    update!(pa, m, mparams)."""
+    update!(pa, m, mparams) / update!(pa, medium, medium_pert) (Born)."""
     if not args:
         return _update_run(pa)
     a0 = args[0]
+    if isinstance(a0, AcousticMedium) and len(args) > 1 and isinstance(args[1], AcousticMedium):
+        return _update_born(pa, a0, args[1])
     if isinstance(a0, AcousticMedium):
         return _update_medium(pa, a0)
     if isinstance(a0, np.ndarray) and a0.ndim == 1:
@@ -433,6 +450,8 @@ def update(pa, *args, _pml=True, **kw):
 
 def _update_run(pa):
     """update!(pa) (src/fdtd/propagate.jl:74-135)."""
+    if getattr(pa.attrib, "born", False) and pa.attrib.mode == "forward":
+        return _born_run(pa)
     mode = {"forward": _lib.FORWARD, "forward_save": _lib.FORWARD_SAVE, "adjoint": _lib.ADJOINT}[pa.attrib.mode]
     if pa.attrib.npw == 1:
         mode = _lib.FORWARD
@@ -451,6 +470,89 @@ def _update_medium(pa, medium):
     pa._set_exmedium(pa.medium)
     pa._upload_medium()
     return pa
+
+
+def _update_born(pa, medium, medium_pert):
+    """update!(pa, medium, medium_pert) (src/fdtd/medium.jl:103-126): the
+    background medium, then dmod = padded medium_pert - padded medium on the
+    extended grid (invK and rho)."""
+    _update_medium(pa, medium)
+    vp = S.padarray(medium_pert.vp, pa.npml, pa.pml_mask)
+    rho = S.padarray(medium_pert.rho, pa.npml, pa.pml_mask)
+    pert = {"invK": S.invK(vp, rho), "rho": rho}
+    set_born_perturbation(pa, [(pert[k] - pa.mod[k]).astype(np.float32) for k in ("invK", "rho")])
+    return pa
+
+
+def set_born_perturbation(pa, dmod):
+    """dmod = [dinvK, drho] on the extended grid (pac.δmod of the reference)."""
+    arrs = [np.asfortranarray(np.asarray(a, np.float32).reshape([len(g) for g in pa.exgrid], order="F")) for a in dmod]
+    pa._born_keep = arrs
+    ptrs = (ctypes.c_void_p * 2)(*[a.ctypes.data for a in arrs])
+    pa._check(pa.L.gpi_set_born(pa.plan, ptrs, 0))
+
+
+def _born_run(pa):
+    """Born run: the background with the plan's sources, the scattered
+    wavefield's records into pa.data[1]."""
+    pa._check(pa.L.gpi_clear_sources(pa.plan, 2, -1))
+    pa.run(_lib.BORN)
+    for iss in range(pa.nss):
+        for f in pa.rfields:
+            pa.data[1][iss].d[f] = pa.records(iss, f)
+    return pa
+
+
+class BornMap:
+    """LinearMap(pa) of a Born experiment (src/fdtd/func_grad.jl:53-120):
+    F x -> the Born records of every supersource for x = [dinvK; drho] on
+    the extended grid (column-major, flattened), and its transpose
+    F' y -> the imaging gradient with y as the adjoint sources.  The
+    transpose needs a plan created with checkpoints > 0 and
+    ref_compat_grad=False (the exact adjoint of the discrete scheme)."""
+
+    def __init__(self, pa):
+        self.pa = pa
+        self.nm = 2 * int(np.prod([len(g) for g in pa.exgrid]))
+        self.nd = sum(pa.nt * a.nr * len(pa.rfields) for a in pa.ageom)
+        self.shape = (self.nd, self.nm)
+
+    def _split(self, x):
+        n = [len(g) for g in self.pa.exgrid]
+        x = np.asarray(x, np.float32)
+        h = len(x) // 2
+        return [x[:h].reshape(n, order="F"), x[h:].reshape(n, order="F")]
+
+    def matvec(self, x):
+        pa = self.pa
+        set_born_perturbation(pa, self._split(x))
+        update(pa, pa.srcwav[0], [1, 0])
+        _born_run(pa)
+        return np.concatenate([pa.data[1][i].d[f].ravel(order="F") for i in range(pa.nss) for f in pa.rfields])
+
+    def rmatvec(self, y):
+        """F' y: the adjoint sources are y (time-reversed, as gradient!
+        does); the result is -(raw imaging accumulations), since the
+        imaging condition returns dJ/dm for adjoint sources -dJ/dd."""
+        pa = self.pa
+        mode_save = pa.attrib.mode
+        y = np.asarray(y, np.float32)
+        pa.attrib.mode = "forward_save"
+        update(pa, pa.srcwav[0], [1, 0])
+        update(pa)
+        adj, k = [], 0
+        for a in pa.ageom:
+            s = Srcs(a.nr, pa.tgrid, pa.rfields)
+            for f in pa.rfields:
+                n = pa.nt * a.nr
+                s.d[f] = y[k:k + n].reshape(pa.nt, a.nr, order="F")[::-1].copy()
+                k += n
+            adj.append(s)
+        update(pa, [pa.srcwav[0], adj], [1 if pa.checkpoints else -1, 1])
+        pa.attrib.mode = "adjoint"
+        update(pa)
+        pa.attrib.mode = mode_save
+        return -np.concatenate([pa.gradient_raw(0).ravel(order="F"), pa.gradient_raw(1).ravel(order="F")])
 
 
 def _update_srcwav(pa, srcwav, src_types=None):

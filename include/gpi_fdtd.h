@@ -39,7 +39,8 @@ enum gpi_status {
 };
 
 enum gpi_physics { GPI_ACOUSTIC = 0, GPI_ELASTIC = 1 };
-enum gpi_mode { GPI_FORWARD = 0, GPI_FORWARD_SAVE = 1, GPI_ADJOINT = 2 };
+/* GPI_BORN: linearised (Born) modelling, see gpi_set_born */
+enum gpi_mode { GPI_FORWARD = 0, GPI_FORWARD_SAVE = 1, GPI_ADJOINT = 2, GPI_BORN = 3 };
 /* faces, named as the reference's symbols :zmin, :zmax, :ymin, ... */
 enum gpi_face { GPI_ZMIN = 1, GPI_ZMAX = 2, GPI_YMIN = 4, GPI_YMAX = 8, GPI_XMIN = 16, GPI_XMAX = 32 };
 /* wavefields (the non-derivative Fields of src/fields.jl:27-42) */
@@ -73,7 +74,15 @@ typedef struct {
    * from them on a binomial schedule; 3-D acoustic gradients too.  No
    * counterpart in the reference.  0: the reference's boundary store. */
   int32_t checkpoints;
-  int32_t reserved[3];
+  /* rho term of the acoustic imaging condition: 0 the reference's
+   * (compute_gmodrho!/combine_gmodrho!, src/fdtd/gradient.jl:31-56: the
+   * velocity terms averaged 4-5 cells off the cells whose coefficients hold
+   * rho); 1 the gradient of the discrete model, rho at (r, c) taking half
+   * of the vx terms at columns c+2, c+3 and of the vz terms at rows r+2, r+3
+   * (and vy at y+2, y+3) where those cells are updated, which agrees with
+   * finite differences.  No counterpart in the reference. */
+  int32_t imaging;
+  int32_t reserved[2];
   double dt, dz, dy, dx; /* time step and grid steps (dy ignored in 2-D) */
 } gpi_plan_desc;
 
@@ -114,6 +123,22 @@ int gpi_clear_sources(gpi_plan *plan, int ipw, int shot);
 /* Receiver interpolation matrix (rinterpolatew, src/fdtd/ageom.jl:46-54). */
 int gpi_set_receivers(gpi_plan *plan, int shot, int field, int nr, const int64_t *colptr,
                       const int64_t *rowval, const float *nzval);
+
+/* Born modelling (FdtdAcoustic{Born}, update!(pa, medium, medium_pert),
+ * src/fdtd/medium.jl:103-126; the reference's secondary-source kernels,
+ * src/fdtd/born.jl:1-13, pass arguments its kernels do not take, so the
+ * engine implements the exact linearisation of its own scheme instead).
+ * dmod[0], dmod[1]: the perturbations of invK and rho on the extended grid
+ * (nz*nx floats each; on_device != 0 for device pointers).  A later
+ * gpi_run(plan, GPI_BORN) propagates wavefield 1 (the background, with the
+ * plan's sources) and wavefield 2, which has no sources of its own: after
+ * wavefield 1's velocity update each velocity cell of wavefield 2 gains
+ * rv (v1 - v1_prev), with rv = -(drho_a + drho_b) / (rho_a + rho_b) over
+ * the two density cells of the cell's update coefficient, and after the
+ * pressure update each p cell gains -(dinvK / invK) (p1 - p1_prev).
+ * gpi_get_records then returns wavefield 2's records (the Born data).
+ * 2-D acoustic plans with npw = 2 only. */
+int gpi_set_born(gpi_plan *plan, const float *const *dmod, int on_device);
 
 /* mod_x_proc! over every shot of the plan in the given mode
  * (src/fdtd/propagate.jl:74-261).  Asynchronous on the plan's stream. */

@@ -127,6 +127,10 @@ typedef struct gpo_ctx {
   size_t hstep;  /* REALs per step in the history: p, vx, [vy,] vz */
   size_t bstep;  /* REALs per time step in the store */
   size_t bsnap;  /* REALs of the final snapshots */
+  int imaging;   /* 0 the reference's imaging condition, 1 the
+                    FD-consistent rho term (gpo_set_imaging) */
+  arr born[4];   /* GPO_BORN secondary-source ratios: p, vx, vy, vz */
+  int have_born;
 } ctx;
 
 static int nk(const ctx *c, int kind, int n, int dimactive) {
@@ -707,6 +711,48 @@ static void compute_gradient(ctx *c, REAL *gK, REAL *gR) {
     arr vf = c->w[0][vids[q]], vfp = c->wp[0][vids[q]], vap = c->wp[1][vids[q]], bf = c->vbuf[q];
     for (size_t i = 0; i < alen(vf); i++) bf.a[i] = vap.a[i] * (vf.a[i] - vfp.a[i]) * dtI;
   }
+  if (c->imaging) {
+    /* FD-consistent rho term (no reference counterpart): rho at cell
+     * (R, [Y,] C) enters the update coefficient dt / avg(rho) of the
+     * velocity cells two and three cells further along each axis (vx
+     * (R, C+2), (R, C+3); vz (R+2, C), (R+3, C); vy (Y+2), (Y+3):
+     * store_invav averages rho at i-3 and i-2 for velocity cell i), each
+     * with weight 1/2 and only where that velocity cell is updated (the
+     * @inn domain of update_v!: rows 4..nz-3 for vx and vy, 4..nz for vz,
+     * and so on along each axis). */
+    arr bx = c->vbuf[0], bz = c->vbuf[1], by = c->vbuf[2];
+    const int nz = c->d.nz, nx = c->d.nx, ny = three ? c->d.ny : 1;
+    /* update domains: [lo, hi] per axis (z, y, x) of vx, vy, vz */
+    const int hz = nz - 3, hyy = ny - 3, hx = nx - 3;
+#define IN(a, lo, hi) ((a) >= (lo) && (a) <= (hi))
+    for (int C = 1; C <= nx; C++)
+      for (int Y = 1; Y <= ny; Y++)
+        for (int R = 1; R <= nz; R++) {
+          const int yin = !three || IN(Y, 4, hyy);
+          REAL avx = 0, avz = 0, avy = 0;
+          if (IN(R, 4, hz) && yin) {
+            REAL b2 = IN(C + 2, 4, nx) ? AT(bx, R, Y, C + 2) : (REAL)0;
+            REAL b3 = IN(C + 3, 4, nx) ? AT(bx, R, Y, C + 3) : (REAL)0;
+            avx = (b2 + b3) * (REAL)0.5;
+          }
+          if (IN(C, 4, hx) && yin) {
+            REAL b2 = IN(R + 2, 4, nz) ? AT(bz, R + 2, Y, C) : (REAL)0;
+            REAL b3 = IN(R + 3, 4, nz) ? AT(bz, R + 3, Y, C) : (REAL)0;
+            avz = (b2 + b3) * (REAL)0.5;
+          }
+          if (three && IN(R, 4, hz) && IN(C, 4, hx)) {
+            REAL b2 = IN(Y + 2, 4, ny) ? AT(by, R, Y + 2, C) : (REAL)0;
+            REAL b3 = IN(Y + 3, 4, ny) ? AT(by, R, Y + 3, C) : (REAL)0;
+            avy = (b2 + b3) * (REAL)0.5;
+          }
+          const size_t gi = ((size_t)(C - 1) * ny + (Y - 1)) * nz + (R - 1);
+          REAL gv = gR[gi] - avx;
+          if (three) gv = gv - avy;
+          gR[gi] = gv - avz;
+        }
+#undef IN
+    return;
+  }
   /* combine_gmodrho!: @inn(g) = @inn(g) - @av_xi(vxbuf) - @av_zi(vzbuf).
    * 3-D (no reference counterpart): the same with the y average between
    * them, g - avx - avy - avz, each average one cell off the stencil centre
@@ -894,6 +940,12 @@ static void save_tp(ctx *c, int ipw) {
     if (c->present[f]) acopy(c->wp[ipw][f], c->w[ipw][f]);
 }
 
+/* Born secondary source: dst += r * (now - prev) (GPO_BORN) */
+static void born_add(arr dst, arr r, arr now, arr prev) {
+  for (size_t i = 0; i < alen(dst); i++) dst.a[i] = dst.a[i] + r.a[i] * (now.a[i] - prev.a[i]);
+}
+
+
 /* mod_x_proc! for one supersource (src/fdtd/propagate.jl:138-261) */
 int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec, gpo_proj *rec,
                   int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho) {
@@ -912,6 +964,8 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
     c->hist[ishot] = (REAL *)calloc((size_t)(nt + 2) * c->hstep, sizeof(REAL));
   if (mode == GPO_ADJOINT_HIST && !c->hist[ishot]) return -3;
   if (mode == GPO_ADJOINT && (c->d.physics != GPO_ACOUSTIC || c->d.ndim != 2) && (grad_invK || grad_rho)) return -2;
+  const int born = mode == GPO_BORN;
+  if (born && !c->have_born) return -4;
   reset_w(c);
   if (mode == GPO_ADJOINT) {
     snap_io(c, ishot, 1, 1); /* boundary_force_snap_tau! */
@@ -919,11 +973,34 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
   }
   /* the history run propagates the adjoint wavefield alone */
   const int pw0 = mode == GPO_ADJOINT_HIST ? 1 : 0;
-  const int npw = adjoint ? 2 : 1;
+  const int npw = adjoint || born ? 2 : 1;
+  /* the records of a Born run are wavefield 2's */
+  arr *wr = born ? c->w[1] : c->w[0];
+  const int vids3[3] = {GPO_VX, GPO_VY, GPO_VZ};
   for (int it = 1; it <= nt; it++) {
     /* record! [:p] */
     for (int r = 0; r < nrec; r++)
-      if (rec[r].field == GPO_P) record(c, c->w[0], &rec[r], it - 1);
+      if (rec[r].field == GPO_P) record(c, wr, &rec[r], it - 1);
+    if (born) {
+      save_tp(c, 0);
+      for (int ipw = 0; ipw < 2; ipw++) update_dstress(c, ipw);
+      update_v(c, 0);
+      for (int s = 0; s < nsrc; s++)
+        if (is_velocity(src[s].field)) add_velocity_source(c, c->w[0], &src[s], it - 1);
+      /* velocity secondary sources, then wavefield 2's own update */
+      for (int q = 0; q < 3; q++)
+        if (c->present[vids3[q]])
+          born_add(c->w[1][vids3[q]], c->born[q + 1], c->w[0][vids3[q]], c->wp[0][vids3[q]]);
+      update_v(c, 1);
+      for (int r = 0; r < nrec; r++)
+        if (is_velocity(rec[r].field)) record(c, wr, &rec[r], it - 1);
+      for (int ipw = 0; ipw < 2; ipw++) update_dv(c, ipw);
+      for (int ipw = 0; ipw < 2; ipw++) update_stress(c, ipw);
+      for (int s = 0; s < nsrc; s++)
+        if (is_stress_src(src[s].field)) add_stress_source(c, c->w[0], &src[s], it - 1);
+      born_add(c->w[1][GPO_P], c->born[0], c->w[0][GPO_P], c->wp[0][GPO_P]);
+      continue;
+    }
     if (mode == GPO_ADJOINT) {
       save_tp(c, 0);
       save_tp(c, 1);
@@ -960,12 +1037,67 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
         memcpy(c->snaps[ishot] + (size_t)k * alen(f), f.a, alen(f) * sizeof(REAL));
       }
   }
-  if (mode == GPO_ADJOINT_HIST) return 0;
+  if (mode == GPO_ADJOINT_HIST || born) return 0;
   if (mode == GPO_FORWARD_SAVE) snap_io(c, ishot, 1, 0); /* boundary_save_snap_tau! */
   update_dstress(c, 0);
   update_v(c, 0);
   if (mode == GPO_FORWARD_SAVE) snap_io(c, ishot, 0, 0); /* boundary_save_snap_v! */
   if (mode == GPO_FORWARD_HIST) hist_io(c, ishot, nt + 1, 0, 0);
+  return 0;
+}
+
+/* Born secondary-source ratios (see GPO_BORN): rp on the p grid, rv on each
+ * velocity grid over its update domain (store_invav: velocity cell i along
+ * an axis averages rho at i-3 and i-2) */
+int SFX(gpo_set_born)(gpo_ctx *cc, const void *dinvK, const void *drho) {
+  ctx *c = (ctx *)cc;
+  if (c->d.physics != GPO_ACOUSTIC) return -1;
+  const REAL *dK = (const REAL *)dinvK, *dR = (const REAL *)drho;
+  const int three = c->d.ndim == 3, h = c->h, hy = c->hy;
+  const int ids[4] = {GPO_P, GPO_VX, GPO_VY, GPO_VZ};
+  for (int q = 0; q < 4; q++) {
+    if (!c->present[ids[q]]) continue;
+    if (!c->have_born) c->born[q] = field_arr(c, ids[q]);
+    azero(c->born[q]);
+  }
+  arr rho = c->mod[1], K = c->mod[0];
+  const int nz = c->d.nz, ny = three ? c->d.ny : 1, nx = c->d.nx;
+  for (int C = 1; C <= nx; C++)
+    for (int Y = 1; Y <= ny; Y++)
+      for (int R = 1; R <= nz; R++) {
+        const size_t i = ((size_t)(C - 1) * ny + (Y - 1)) * nz + (R - 1);
+        AT(c->born[0], R, Y, C) = -(dK[i] / K.a[i]);
+      }
+  /* velocity cells: (axis offset along the velocity's own axis) */
+  const int vq[3] = {1, 2, 3}; /* born index of vx, vy, vz */
+  for (int q = 0; q < 3; q++) {
+    if (q == 1 && !three) continue;
+    arr v = c->born[vq[q]];
+    const int ax = q == 0 ? 2 : q == 1 ? 1 : 0; /* x, y, z */
+    const int r1 = v.n1 - 2 * h, r2 = three ? v.n2 - 2 * hy : 1, r3 = v.n3 - 2 * h;
+    for (int ix = 1; ix <= r3; ix++)
+      for (int iy = 1; iy <= r2; iy++)
+        for (int iz = 1; iz <= r1; iz++) {
+          const int R = iz + h, Y = three ? iy + hy : 1, C = ix + h;
+          /* density cells of the coefficient (store_invav) */
+          int za = R, ya = Y, xa = C;
+          if (ax == 0) za = R - h;
+          if (ax == 1) ya = Y - h;
+          if (ax == 2) xa = C - h;
+          const int zb = za + (ax == 0), yb = ya + (ax == 1), xb = xa + (ax == 2);
+          const size_t ia = ((size_t)(xa - 1) * ny + (ya - 1)) * nz + (za - 1);
+          const size_t ib = ((size_t)(xb - 1) * ny + (yb - 1)) * nz + (zb - 1);
+          AT(v, R, Y, C) = -((dR[ia] + dR[ib]) / (rho.a[ia] + rho.a[ib]));
+        }
+  }
+  c->have_born = 1;
+  return 0;
+}
+
+int SFX(gpo_set_imaging)(gpo_ctx *cc, int mode) {
+  ctx *c = (ctx *)cc;
+  if (mode < 0 || mode > 1) return -1;
+  c->imaging = mode;
   return 0;
 }
 
@@ -1014,6 +1146,7 @@ void SFX(gpo_destroy)(gpo_ctx *cc) {
       free(c->mem[ipw][q].a);
     }
   }
+  for (int q = 0; q < 4; q++) free(c->born[q].a);
   free(c->vbuf[0].a);
   free(c->vbuf[1].a);
   free(c->vbuf[2].a);

@@ -29,7 +29,19 @@ extern "C" {
 #endif
 
 enum { GPO_ACOUSTIC = 0, GPO_ELASTIC = 1 };
-enum { GPO_FORWARD = 0, GPO_FORWARD_SAVE = 1, GPO_ADJOINT = 2, GPO_FORWARD_HIST = 3, GPO_ADJOINT_HIST = 4 };
+enum { GPO_FORWARD = 0, GPO_FORWARD_SAVE = 1, GPO_ADJOINT = 2, GPO_FORWARD_HIST = 3, GPO_ADJOINT_HIST = 4,
+       GPO_BORN = 5 };
+/* GPO_BORN (acoustic, after gpo_set_born): linearised (Born) modelling.
+ * Wavefield 1 is the background run; wavefield 2 runs the same scheme with
+ * no sources of its own, driven by the secondary sources of the
+ * perturbation: after wavefield 1's velocity update, each velocity cell of
+ * wavefield 2 gains rv * (v1 - v1_prev) (before its own update), and after
+ * the stress update each p cell gains rp * (p1 - p1_prev), with
+ * rv = -(drho_a + drho_b) / (rho_a + rho_b) over the two density cells of
+ * the cell's update coefficient and rp = -dinvK / invK.  The records are
+ * wavefield 2's.  This is the exact linearisation of the discrete scheme
+ * in the medium parameters (no reference counterpart: the reference's
+ * born.jl passes arguments its kernels do not take). */
 /* GPO_FORWARD_HIST / GPO_ADJOINT_HIST (acoustic, 2-D and 3-D): the same
  * gradient as forward_save -> adjoint, but wavefield 1 is not rebuilt by
  * time reversal: the forward run keeps its whole history (p and v after
@@ -93,6 +105,17 @@ int gpo_shot_f32(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src,
                  gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho);
 int gpo_shot_f64(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec,
                  gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho);
+/* Imaging condition of the rho gradient: 0 the reference's
+ * (src/fdtd/gradient.jl:31-56); 1 the gradient of the discrete model, over
+ * the velocity cells whose update coefficient holds rho (no reference
+ * counterpart; checked against finite differences). */
+int gpo_set_imaging_f32(gpo_ctx *c, int mode);
+/* Perturbations (dinvK, drho) of the medium on the extended grid for
+ * GPO_BORN runs (the medium perturbation minus the medium, as
+ * update!(pa, medium, medium_pert) forms it, src/fdtd/medium.jl:103-126). */
+int gpo_set_born_f32(gpo_ctx *c, const void *dinvK, const void *drho);
+int gpo_set_born_f64(gpo_ctx *c, const void *dinvK, const void *drho);
+int gpo_set_imaging_f64(gpo_ctx *c, int mode);
 /* snaps_save! (src/fdtd/fdtd.jl:586-591): keep wavefield 1's `field` at
  * the end of steps its[0..n) of later shots; read them per shot and k. */
 int gpo_set_snaps_f32(gpo_ctx *c, int field, int n, const int *its);

@@ -283,7 +283,7 @@ def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=Fal
     return res
 
 
-def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=False):
+def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=False, imaging=0):
     """gradient!(g, m, L2DistLoss(), dobs, pa) for 2-D acoustic
     (src/fdtd/func_grad.jl:11-49).  Returns (loss, {"invK": g, "rho": g},
     dcal) with g the chain-ruled gradient on the inner (non-PML) grid and the
@@ -291,9 +291,16 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
 
     history=True takes wavefield 1 from the stored forward history instead
     of rebuilding it by time reversal (GPO_FORWARD_HIST / GPO_ADJOINT_HIST):
-    the gradient of a checkpointed adjoint; 2-D and 3-D acoustic."""
+    the gradient of a checkpointed adjoint; 2-D and 3-D acoustic.
+
+    imaging selects the rho term of the imaging condition (gpo_set_imaging):
+    0 the reference's, 1 the finite-difference-consistent one."""
     prep = Prepared(ex, dtype, ref_compat)
     orc = Oracle(prep, nthreads)
+    if imaging:
+        fn = getattr(orc.L, "gpo_set_imaging_" + orc.sfx)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        assert fn(orc.ctx, int(imaging)) == 0
     shape = prep.shape
     gK = np.zeros(shape, dtype=dtype, order="F")
     gR = np.zeros(shape, dtype=dtype, order="F")
@@ -325,3 +332,26 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
     inner = tuple(inner)
     g = {"invK": (raw["invK"] * prep.mod[0])[inner], "rho": (raw["rho"] * prep.mod[1])[inner]}
     return loss, g, dcal, raw
+
+
+def born(ex, dinvK, drho, dtype=np.float32, nthreads=0):
+    """Born (linearised) records for the medium perturbation (dinvK, drho)
+    given on the extended grid (update!(pa, medium, medium_pert) forms it as
+    the padded perturbed medium minus the medium, src/fdtd/medium.jl:103-126):
+    records[field] of shape (nshots, nt, nr) of the scattered wavefield
+    (GPO_BORN, acoustic)."""
+    prep = Prepared(ex, dtype)
+    orc = Oracle(prep, nthreads)
+    a = np.ascontiguousarray(np.asarray(dinvK, dtype).reshape(-1, order="F"))
+    b = np.ascontiguousarray(np.asarray(drho, dtype).reshape(-1, order="F"))
+    fn = getattr(orc.L, "gpo_set_born_" + orc.sfx)
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    assert fn(orc.ctx, a.ctypes.data, b.ctypes.data) == 0
+    out = {f: [] for f in ex["rfields"]}
+    for i, shot in enumerate(ex["shots"]):
+        src, rec = _shot_inputs(prep, shot)
+        r = orc.shot(i, 5, src, rec)
+        for f in ex["rfields"]:
+            out[f].append(r[f])
+    orc.close()
+    return {f: np.stack(v) for f, v in out.items()}
