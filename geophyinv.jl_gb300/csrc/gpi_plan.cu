@@ -169,9 +169,10 @@ static int nsaved(const Plan &p, int *ids) {
   return 3;
 }
 
-int create(const gpi_plan_desc *desc, gpi_plan **out) {
-  if (!desc || !out) return fail(nullptr, GPI_E_INVALID, "null argument");
-  *out = nullptr;
+// with `bytes_only`, the device bytes of the plan's pool (no allocation)
+int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullptr) {
+  if (!desc || (!out && !bytes_only)) return fail(nullptr, GPI_E_INVALID, "null argument");
+  if (out) *out = nullptr;
   const gpi_plan_desc &d = *desc;
   if (d.physics != GPI_ACOUSTIC && d.physics != GPI_ELASTIC) return fail(nullptr, GPI_E_INVALID, "physics");
   if (d.ndim != 2 && d.ndim != 3) return fail(nullptr, GPI_E_INVALID, "ndim must be 2 or 3");
@@ -279,6 +280,11 @@ int create(const gpi_plan_desc *desc, gpi_plan **out) {
   }
   size_t total = 0;
   for (auto &a : allocs) total += (size_t)round_up(a.second, 64) * sizeof(float);
+  if (bytes_only) {
+    *bytes_only = total;
+    delete pl;
+    return GPI_OK;
+  }
   // one stream-ordered allocation (set-up stream, synchronised below)
   cudaStream_t cs = nullptr;
   if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
@@ -1262,6 +1268,10 @@ using namespace gpi;
 extern "C" {
 
 int gpi_plan_create(const gpi_plan_desc *desc, gpi_plan **out) { return gpi::create(desc, out); }
+int gpi_plan_estimate(const gpi_plan_desc *desc, size_t *bytes) {
+  if (!bytes) return gpi::fail(nullptr, GPI_E_INVALID, "null argument");
+  return gpi::create(desc, nullptr, bytes);
+}
 void gpi_plan_destroy(gpi_plan *plan) { gpi::destroy(plan); }
 const char *gpi_last_error(const gpi_plan *plan) { return plan ? plan->p.err.c_str() : g_create_err.c_str(); }
 int gpi_set_stream(gpi_plan *plan, void *stream) {

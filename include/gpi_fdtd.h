@@ -98,6 +98,12 @@ const char *gpi_last_error(const gpi_plan *plan);
 int gpi_set_stream(gpi_plan *plan, void *stream);
 /* Device bytes the plan holds. */
 int gpi_plan_bytes(const gpi_plan *plan, size_t *bytes);
+/* Device bytes gpi_plan_create would allocate for `desc` (wavefields, CPML
+ * memory, coefficients, boundary store or checkpoint slots), computed
+ * without allocating; the record buffers (nt x receivers per shot and
+ * field) come on top.  No counterpart in the reference; a server admits
+ * requests against its HBM budget with it. */
+int gpi_plan_estimate(const gpi_plan_desc *desc, size_t *bytes);
 
 /* update!(pac, medium) -> update_dmod! (src/fdtd/medium.jl:131-221):
  * mod[i] is the i-th MediumParameters array on the extended grid

@@ -283,7 +283,7 @@ def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=Fal
     return res
 
 
-def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=False, imaging=0):
+def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=False, imaging=0, mod=None):
     """gradient!(g, m, L2DistLoss(), dobs, pa) for 2-D acoustic
     (src/fdtd/func_grad.jl:11-49).  Returns (loss, {"invK": g, "rho": g},
     dcal) with g the chain-ruled gradient on the inner (non-PML) grid and the
@@ -294,8 +294,13 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
     the gradient of a checkpointed adjoint; 2-D and 3-D acoustic.
 
     imaging selects the rho term of the imaging condition (gpo_set_imaging):
-    0 the reference's, 1 the finite-difference-consistent one."""
+    0 the reference's, 1 the finite-difference-consistent one.
+
+    mod: extended-grid medium parameters that replace the ones padded from
+    ex (update!(pa, m, mparams) keeps the PML cells of the old medium)."""
     prep = Prepared(ex, dtype, ref_compat)
+    if mod is not None:
+        prep.mod = [np.asarray(m, np.float32) for m in mod]
     orc = Oracle(prep, nthreads)
     if imaging:
         fn = getattr(orc.L, "gpo_set_imaging_" + orc.sfx)

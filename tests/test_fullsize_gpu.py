@@ -3,9 +3,10 @@
   elastic 2-D batch   1000 x 3000 at 5 m (1086 x 3086 extended), 16 shots,
                       4000 steps, 601 vx / vz receivers, 16-step chunk graphs:
                       the whole batch on the GPU, shots 0 and 15 checked
-  acoustic 2-D FWI    500 x 1500 at 10 m (586 x 1586), 3000 steps; observed
-  gradient            data from the model with the anomaly, gradient! on the
-                      model without it for shots 15 and 16 of the 32
+  acoustic 2-D FWI    500 x 1500 at 10 m (586 x 1586), 3000 steps,
+  gradient            gradient! on the model without the anomaly for shots 15
+                      and 16 of the 32 (zero observed data, and observed data
+                      from the model with the anomaly)
   elastic 3-D         600^3 at 10 m with npml 23 (646^3 extended), the full
                       grid for 60 of its 2500 steps
 
@@ -62,40 +63,65 @@ def test_elastic2d_batch_full_size_matches_oracle(engine):
     pa.close()
 
 
-@pytest.mark.gpu
-def test_acoustic2d_fwi_gradient_full_size_matches_oracle(engine):
-    # two of the 32 shots above the anomaly (the outermost shots' records
-    # do not reach it within 3 s, so their residual would be rounding noise)
-    shots = [15, 16]
-    true = configs.acoustic2d_fwi()
-    assert len(true.shots) == 32 and true.nt == 3000
-    true.shots = [true.shots[i] for i in shots]
-    pt = true.expt()
-    update(pt)
-    dobs = [Recs(r.n, r.grid, r.fields, {f: r.d[f].copy() for f in r.fields}) for r in pt.data[0]]
-    pt.close()
+def _grad_case(engine_dobs, oracle_dobs, shots, label):
     wl = configs.acoustic2d_fwi(anomaly=False)
     wl.shots = [wl.shots[i] for i in shots]
     pa = wl.expt(mode="forward_save")
     pa.set_graph(2)
     m0 = get_modelvector(pa, ["invK", "rho"])
     g = np.zeros_like(m0)
-    J = gradient(g, m0, L2DistLoss(), dobs, pa)
-    od = {f: np.stack([d.d[f] for d in dobs]) for f in wl.rfields}
-    loss, _, dcal, raw = O.gradient(wl.as_dict(), od)
-    loss64, _, dcal64, raw64 = O.gradient(wl.as_dict(), od, dtype=np.float64)
-    case = "acoustic2d grad 586x1586 3000 st"
+    J = gradient(g, m0, L2DistLoss(), engine_dobs, pa)
+    loss, _, dcal, raw = O.gradient(wl.as_dict(), oracle_dobs)
+    _, _, dcal64, raw64 = O.gradient(wl.as_dict(), oracle_dobs, dtype=np.float64)
+    case = "acoustic2d grad 586x1586 3000 st " + label
     for i in range(len(shots)):
-        e = rel(pa.data[0][i].d["vz"], dcal["vz"][i])
-        _line(case + " shot %d" % shots[i], "rec vz", e, rel(pa.data[0][i].d["vz"], dcal64["vz"][i]))
-        assert e < TOL, ("records", i, e)
-    assert loss > 0 and np.linalg.norm(raw["rho"]) > 0
+        _line(case + " shot %d" % shots[i], "rec vz", rel(pa.data[0][i].d["vz"], dcal["vz"][i]),
+              rel(pa.data[0][i].d["vz"], dcal64["vz"][i]))
+    e = {}
     for k in ("invK", "rho"):
-        e = rel(pa.gradients[k], raw[k])
-        _line(case, "grad " + k, e, rel(pa.gradients[k], raw64[k]))
-        assert e < TOL, (k, e)
-    assert abs(J - loss) <= TOL * abs(loss), (J, loss)
+        e[k] = (rel(pa.gradients[k], raw[k]), rel(pa.gradients[k], raw64[k]), rel(raw[k], raw64[k]))
+        _line(case, "grad " + k, e[k][0], e[k][1])
+    recs = [rel(pa.data[0][i].d["vz"], dcal["vz"][i]) for i in range(len(shots))]
     pa.close()
+    return J, loss, e, recs
+
+
+@pytest.mark.gpu
+def test_acoustic2d_fwi_gradient_full_size_matches_oracle(engine):
+    """The FWI gradient at full size (586 x 1586, 3000 steps) for shots 15
+    and 16 of the 32, through the reference's time-reversal adjoint.
+
+    With zero observed data the adjoint sources are the whole records and
+    the gradient is well conditioned: engine and FP32 oracle agree within
+    1e-5.  With observed data from the model with the anomaly (the
+    benchmark's case) the residual is about 1e-5 of the records at these
+    offsets, so any FP32 run of the gradient carries rounding at the
+    percent level: the engine's distance from the FP64 gradient is then
+    required to stay within twice the FP32 oracle's own distance from it."""
+    shots = [15, 16]
+    nt, nr = 3000, 1500
+    zero_e = [Recs(nr, configs.acoustic2d_fwi().tgrid, ["vz"], {"vz": np.zeros((nt, nr), np.float32)})
+              for _ in shots]
+    zero_o = {"vz": np.zeros((len(shots), nt, nr), np.float32)}
+    J, loss, e, recs = _grad_case(zero_e, zero_o, shots, "zero dobs")
+    for r in recs:
+        assert r < TOL, r
+    for k in ("invK", "rho"):
+        assert e[k][0] < TOL, (k, e[k])
+    assert abs(J - loss) <= TOL * abs(loss), (J, loss)
+    # observed data from the model with the anomaly
+    true = configs.acoustic2d_fwi()
+    assert len(true.shots) == 32 and true.nt == nt
+    true.shots = [true.shots[i] for i in shots]
+    pt = true.expt()
+    update(pt)
+    dobs = [Recs(r.n, r.grid, r.fields, {f: r.d[f].copy() for f in r.fields}) for r in pt.data[0]]
+    pt.close()
+    od = {f: np.stack([d.d[f] for d in dobs]) for f in ["vz"]}
+    J, loss, e, recs = _grad_case(dobs, od, shots, "anomaly dobs")
+    for k in ("invK", "rho"):
+        print("FULL anomaly dobs grad %s: FP32 oracle vs FP64 oracle %.3e" % (k, e[k][2]))
+        assert e[k][1] <= 2 * e[k][2] + TOL, (k, e[k])
 
 
 @pytest.mark.gpu

@@ -37,3 +37,24 @@ def test_projection_and_its_transpose_are_adjoint():
     lhs = float(paw._to_full(x).astype(np.float64) @ y)
     rhs = float(x @ paw._to_inv(y))
     assert abs(lhs - rhs) <= 1e-5 * abs(rhs)
+
+
+def test_projections_match_the_oracle_restatement():
+    """The product's inversion-grid matrices and projections against the
+    oracle's restatement of SeisInvExpt (oracle/fwi_ref.py)."""
+    from oracle import fwi_ref as R
+
+    rng = np.random.default_rng(3)
+    mm = [np.linspace(0, 100, 21), np.linspace(0, 200, 31)]
+    mi = [np.linspace(10, 90, 5), np.linspace(20, 180, 7)]
+    P = R.inversion_matrices(mm, mi)
+    paw = fwi.SeisInvExpt.__new__(fwi.SeisInvExpt)
+    paw.mparams = ["invK", "rho"]
+    paw.mmgrid, paw.migrid = mm, mi
+    paw.P = [fwi.interp_matrix(a, b) for a, b in zip(mi, mm)]
+    for A, B in zip(paw.P, P):
+        np.testing.assert_array_equal(A, B)
+    x = rng.standard_normal(2 * 5 * 7).astype(np.float32)
+    y = rng.standard_normal(2 * 21 * 31).astype(np.float32)
+    np.testing.assert_allclose(paw._to_full(x), R.to_full(x, P, paw.mparams), rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(paw._to_inv(y), R.to_inversion(y, P, paw.mparams), rtol=1e-6, atol=1e-6)

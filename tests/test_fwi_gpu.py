@@ -38,3 +38,35 @@ def test_lbfgs_lowers_the_misfit(engine):
     res = fwi.update(paw, maxiter=4)
     assert np.isfinite(res.fun)
     assert paw.history[-1] < 0.8 * paw.history[0], paw.history
+
+
+@pytest.mark.gpu
+def test_inversion_grid_gradient_matches_oracle(engine):
+    """gradient!(g, m, pa::SeisInvExpt) (src/fwi/func_grad.jl:42-62) of the
+    engine against the oracle's restatement (oracle/fwi_ref.py: the model
+    through the inversion matrices, update!(pa, m) on the inner cells, the
+    oracle's gradient!, the transposed matrices) at a perturbed model."""
+    from oracle import fwi_ref as R
+    from oracle import oracle as O
+    from oracle import setup_ref as S
+
+    paw = _problem(nshots=2, nt=300)
+    pa = paw.paf
+    m0 = fwi.get_modelvector_inv(paw)
+    m = (m0 + 0.02 * np.random.default_rng(4).standard_normal(m0.size)).astype(np.float32)
+    g = np.zeros_like(m)
+    J, _ = fwi.gradient_inv(g, m, paw)
+    start = configs.acoustic2d_fwi(nz=50, nx=90, nt=300, nshots=2, nrec=45, anomaly=False)
+    ex = start.as_dict()
+    prep = O.Prepared(ex)
+    P = R.inversion_matrices(paw.mmgrid, paw.migrid)
+    ref = {k: S.bounds(prep.mod[i])[0] for i, k in enumerate(("invK", "rho"))}
+    mfull = R.to_full(m, P, paw.mparams)
+    mod = R.medium_from_modelvector(prep, mfull, paw.mparams, ref)
+    dobs = {"vz": np.stack([d.d["vz"] for d in paw.dobs])}
+    loss, go, _, _ = O.gradient(ex, dobs, mod=mod, history=True)  # the plan is checkpointed
+    gfull = np.concatenate([go["invK"].ravel(order="F"), go["rho"].ravel(order="F")])
+    want = R.to_inversion(gfull, P, paw.mparams)
+    e = np.linalg.norm(g - want) / np.linalg.norm(want)
+    assert e < 1e-5, e
+    assert abs(J - loss) <= 1e-5 * abs(loss), (J, loss)
