@@ -1,0 +1,417 @@
+// gpi_server.cu -- the serving loop behind the C ABI (gpi_server_*).
+//
+// Requests (forward runs or gradient! evaluations of 2-D / 3-D plans of any
+// size, step count and shot count) are queued in arrival order.  Each of
+// max_inflight worker threads owns a CUDA stream; a free worker admits the
+// request at the head of the queue as soon as the device bytes of the
+// requests already admitted plus its own stay within the HBM budget (a
+// request larger than the budget runs alone), builds its plan (stream-
+// ordered allocation, medium, CPML profiles, sources, receivers), runs it
+// with all of its shots batched into each launch and its forward runs
+// replayed as captured step chunks, copies the results to the host and
+// frees the plan.  Requests on different workers overlap on the GPU, and the
+// host set-up of one overlaps the device work of the others.  The device
+// arithmetic of a request does not depend on what else runs, so a result
+// is the same alone and in a mix.
+//
+// A gradient request is gradient!(g, m, L2DistLoss(), dobs, pa)
+// (src/fdtd/func_grad.jl:11-49): forward_save, adjoint sources
+// deriv(L2DistLoss(), dobs, dcal) = 2 (dobs - dcal) reversed in time, the
+// adjoint run (with the time-reversed wavefield-1 sources of
+// get_source(..., Val{-1}), src/fdtd/source.jl:8-19, when the plan uses the
+// boundary store), and the raw gradient accumulations summed over shots.
+//
+// No counterpart in the reference: its update!(pa) runs one experiment at a
+// time on each Distributed worker (src/fdtd/propagate.jl:100-106).
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/gpi_fdtd.h"
+
+namespace {
+
+struct Proj {
+  int shot = 0, field = 0, n = 0;
+  std::vector<int64_t> cp, rv;
+  std::vector<float> nz, data;
+  bool has_data = false;
+};
+
+enum { QUEUED = 0, RUNNING = 1, DONE = 2, FAILED = 3 };
+
+struct Job {
+  int64_t id = 0;
+  gpi_plan_desc desc{};
+  int gradient = 0, graph = 0;
+  std::vector<std::vector<float>> mod;
+  std::vector<float> pml;
+  std::vector<Proj> src, rec;
+  size_t bytes = 0;
+  int state = QUEUED;
+  int status = GPI_OK;
+  std::string message;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  std::vector<std::vector<float>> records;  // per rec entry: nt x n
+  std::vector<std::vector<float>> grad;     // invK (or invlambda), rho ...: extended grid
+  double loss = 0;
+};
+
+int nder_of(const gpi_plan_desc &d) {
+  if (d.physics == GPI_ACOUSTIC) return d.ndim == 2 ? 4 : 6;
+  return d.ndim == 2 ? 8 : 18;
+}
+int64_t grid_cells(const gpi_plan_desc &d) { return (int64_t)d.nz * (d.ndim == 3 ? d.ny : 1) * d.nx; }
+bool is_vel(int f) { return f == GPI_VX || f == GPI_VY || f == GPI_VZ; }
+
+}  // namespace
+
+struct gpi_server {
+  gpi_server_desc d{};
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Job *> queue;
+  std::map<int64_t, Job *> jobs;
+  size_t used = 0;
+  int inflight = 0;
+  bool stop = false;
+  int64_t next_id = 1;
+  std::vector<std::thread> workers;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  double now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+namespace {
+
+thread_local std::string g_msg;
+
+int sfail(int code, const std::string &m) {
+  g_msg = m;
+  return code;
+}
+
+// the whole life of one admitted request on a worker's stream
+int process(Job &j, cudaStream_t st) {
+  gpi_plan *plan = nullptr;
+  int rc = gpi_plan_create(&j.desc, &plan);
+  auto check = [&](int r) {
+    if (r && j.message.empty()) j.message = gpi_last_error(plan);
+    return r;
+  };
+  if (rc) {
+    j.message = gpi_last_error(nullptr);
+    return rc;
+  }
+  const gpi_plan_desc &d = j.desc;
+  const int nt = d.nt;
+  do {
+    if ((rc = check(gpi_set_stream(plan, st)))) break;
+    std::vector<const float *> mp;
+    for (auto &m : j.mod) mp.push_back(m.data());
+    if ((rc = check(gpi_set_medium(plan, mp.data(), 0)))) break;
+    const int nq = nder_of(d), P = 2 * d.npml;
+    for (int q = 0; q < nq && !rc; q++) {
+      const float *base = j.pml.data() + (size_t)q * 3 * P;
+      rc = check(gpi_set_pml(plan, q, P, base, base + P, base + 2 * P));
+    }
+    if (rc) break;
+    for (auto &r : j.rec)
+      if ((rc = check(gpi_set_receivers(plan, r.shot, r.field, r.n, r.cp.data(), r.rv.data(), r.nz.data())))) break;
+    if (rc) break;
+    for (auto &s : j.src)
+      if ((rc = check(gpi_set_sources(plan, 1, s.shot, s.field, s.n, s.cp.data(), s.rv.data(), s.nz.data(),
+                                       s.data.data()))))
+        break;
+    if (rc) break;
+    if (j.graph && (rc = check(gpi_set_graph(plan, j.graph)))) break;
+    if ((rc = check(gpi_run(plan, j.gradient ? GPI_FORWARD_SAVE : GPI_FORWARD)))) break;
+    j.records.assign(j.rec.size(), {});
+    for (size_t k = 0; k < j.rec.size() && !rc; k++) {
+      j.records[k].resize((size_t)nt * j.rec[k].n);
+      rc = check(gpi_get_records(plan, j.rec[k].shot, j.rec[k].field, j.records[k].data(), 0));
+    }
+    if (rc || !j.gradient) break;
+    // adjoint sources 2 (dobs - dcal), reversed in time; misfit sum (dobs - dcal)^2
+    double loss = 0;
+    for (size_t k = 0; k < j.rec.size() && !rc; k++) {
+      const Proj &r = j.rec[k];
+      const std::vector<float> &dc = j.records[k];
+      std::vector<float> adj((size_t)nt * r.n);
+      for (int i = 0; i < r.n; i++)
+        for (int t = 0; t < nt; t++) {
+          const size_t o = (size_t)i * nt + t;
+          const float ob = r.has_data ? r.data[o] : 0.f;
+          const double e = (double)ob - (double)dc[o];
+          loss += e * e;
+          adj[(size_t)i * nt + (nt - 1 - t)] = 2.0f * (ob - dc[o]);
+        }
+      rc = check(gpi_set_sources(plan, 2, r.shot, r.field, r.n, nullptr, nullptr, nullptr, adj.data()));
+    }
+    if (rc) break;
+    j.loss = loss;
+    if (d.checkpoints == 0) {
+      // the boundary-store adjoint runs wavefield 1 backwards with the
+      // time-reversed sources: -w shifted by one step, reversed, row 1 zero
+      for (auto &s : j.src) {
+        if (!is_vel(s.field)) {
+          rc = sfail(GPI_E_UNSUPPORTED, "time-reversed sources act on velocities only (source.jl:8-19)");
+          j.message = g_msg;
+          break;
+        }
+        std::vector<float> w((size_t)nt * s.n, 0.f);
+        for (int i = 0; i < s.n; i++)
+          for (int t = 1; t < nt; t++) w[(size_t)i * nt + t] = -s.data[(size_t)i * nt + (nt - t)];
+        if ((rc = check(gpi_set_sources(plan, 1, s.shot, s.field, s.n, s.cp.data(), s.rv.data(), s.nz.data(),
+                                         w.data()))))
+          break;
+      }
+      if (rc) break;
+    }
+    if ((rc = check(gpi_run(plan, GPI_ADJOINT)))) break;
+    const int64_t n = grid_cells(d);
+    j.grad.assign(2, std::vector<float>(n));
+    for (int q = 0; q < 2 && !rc; q++) rc = check(gpi_get_gradient(plan, q, j.grad[q].data(), 0));
+  } while (false);
+  if (!rc && cudaStreamSynchronize(st) != cudaSuccess) {
+    rc = GPI_E_CUDA;
+    j.message = cudaGetErrorString(cudaGetLastError());
+  }
+  gpi_plan_destroy(plan);
+  return rc;
+}
+
+void worker(gpi_server *s) {
+  cudaSetDevice(s->d.device);
+  cudaStream_t st = nullptr;
+  const bool have_stream = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+  for (;;) {
+    Job *j = nullptr;
+    {
+      std::unique_lock<std::mutex> lock(s->mu);
+      s->cv.wait(lock, [&] {
+        if (s->stop) return true;
+        if (s->queue.empty()) return false;
+        Job *h = s->queue.front();
+        return s->inflight == 0 || s->used + h->bytes <= s->d.hbm_budget;
+      });
+      if (s->stop) break;
+      j = s->queue.front();
+      s->queue.pop_front();
+      s->used += j->bytes;
+      s->inflight++;
+      j->state = RUNNING;
+      j->t_admit = s->now();
+    }
+    const int rc = have_stream ? process(*j, st) : GPI_E_CUDA;
+    if (!have_stream) j->message = "worker stream creation failed";
+    {
+      std::lock_guard<std::mutex> lock(s->mu);
+      j->status = rc;
+      j->state = rc ? FAILED : DONE;
+      j->t_done = s->now();
+      s->used -= j->bytes;
+      s->inflight--;
+    }
+    s->cv.notify_all();
+  }
+  if (have_stream) cudaStreamDestroy(st);
+}
+
+Job *find(gpi_server *s, int64_t id) {
+  auto it = s->jobs.find(id);
+  return it == s->jobs.end() ? nullptr : it->second;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gpi_server_create(const gpi_server_desc *desc, gpi_server **out) {
+  if (!desc || !out) return sfail(GPI_E_INVALID, "null argument");
+  *out = nullptr;
+  if (desc->max_inflight < 1 || desc->max_inflight > 64) return sfail(GPI_E_INVALID, "max_inflight: 1..64");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || desc->device < 0 || desc->device >= ndev) {
+    cudaGetLastError();
+    return sfail(GPI_E_CUDA, "no such CUDA device");
+  }
+  gpi_server *s = new gpi_server();
+  s->d = *desc;
+  for (int i = 0; i < desc->max_inflight; i++) s->workers.emplace_back(worker, s);
+  *out = s;
+  return GPI_OK;
+}
+
+void gpi_server_destroy(gpi_server *s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  // a worker finishes the request it is running before it leaves
+  for (auto &t : s->workers) t.join();
+  for (auto &kv : s->jobs) delete kv.second;
+  delete s;
+}
+
+static int copy_proj(const gpi_proj &p, int nt, bool with_data, bool data_optional, Proj *out) {
+  if (p.n < 1 || !p.colptr || !p.rowval || !p.nzval) return sfail(GPI_E_INVALID, "projection arrays");
+  if (p.colptr[0] != 0) return sfail(GPI_E_INVALID, "colptr[0] must be 0");
+  for (int j = 0; j < p.n; j++)
+    if (p.colptr[j + 1] < p.colptr[j]) return sfail(GPI_E_INVALID, "colptr not monotone");
+  const int64_t nnz = p.colptr[p.n];
+  out->shot = p.shot;
+  out->field = p.field;
+  out->n = p.n;
+  out->cp.assign(p.colptr, p.colptr + p.n + 1);
+  out->rv.assign(p.rowval, p.rowval + nnz);
+  out->nz.assign(p.nzval, p.nzval + nnz);
+  if (with_data) {
+    if (!p.data && !data_optional) return sfail(GPI_E_INVALID, "source wavelets missing");
+    if (p.data) {
+      out->data.assign(p.data, p.data + (size_t)nt * p.n);
+      out->has_data = true;
+    }
+  }
+  return GPI_OK;
+}
+
+int gpi_server_submit(gpi_server *s, const gpi_request *r, int64_t *id) {
+  if (!s || !r || !id) return sfail(GPI_E_INVALID, "null argument");
+  const gpi_plan_desc &d = r->plan;
+  if (r->gradient && d.npw != 2) return sfail(GPI_E_INVALID, "a gradient request needs npw = 2");
+  if (!r->gradient && d.npw != 1) return sfail(GPI_E_INVALID, "a forward request needs npw = 1");
+  if (r->nsrc < 1 || r->nrec < 1 || !r->src || !r->rec || !r->mod || !r->pml)
+    return sfail(GPI_E_INVALID, "sources, receivers, medium and PML profiles are required");
+  size_t bytes = 0;
+  if (int rc = gpi_plan_estimate(&d, &bytes)) return sfail(rc, gpi_last_error(nullptr));
+  Job *j = new Job();
+  j->desc = d;
+  j->gradient = r->gradient;
+  j->graph = r->graph;
+  const int nmod = d.physics == GPI_ACOUSTIC ? 2 : 3;
+  const int64_t cells = grid_cells(d);
+  for (int i = 0; i < nmod; i++) {
+    if (!r->mod[i]) {
+      delete j;
+      return sfail(GPI_E_INVALID, "medium array missing");
+    }
+    j->mod.emplace_back(r->mod[i], r->mod[i] + cells);
+  }
+  j->pml.assign(r->pml, r->pml + (size_t)nder_of(d) * 3 * 2 * d.npml);
+  size_t rec_floats = 0;
+  for (int k = 0; k < r->nsrc; k++) {
+    Proj p;
+    if (int rc = copy_proj(r->src[k], d.nt, true, false, &p)) {
+      delete j;
+      return rc;
+    }
+    j->src.push_back(std::move(p));
+  }
+  for (int k = 0; k < r->nrec; k++) {
+    Proj p;
+    if (int rc = copy_proj(r->rec[k], d.nt, r->gradient != 0, true, &p)) {
+      delete j;
+      return rc;
+    }
+    rec_floats += (size_t)d.nt * p.n;
+    j->rec.push_back(std::move(p));
+  }
+  // the plan's pool plus its record buffers (and the adjoint sources)
+  j->bytes = bytes + rec_floats * sizeof(float) * (r->gradient ? 3 : 2);
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    j->id = s->next_id++;
+    j->t_submit = s->now();
+    s->jobs[j->id] = j;
+    s->queue.push_back(j);
+    *id = j->id;
+  }
+  s->cv.notify_all();
+  return GPI_OK;
+}
+
+int gpi_server_poll(gpi_server *s, int64_t id, int *state) {
+  if (!s || !state) return sfail(GPI_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lock(s->mu);
+  Job *j = find(s, id);
+  if (!j) return sfail(GPI_E_INVALID, "unknown request");
+  *state = j->state;
+  return GPI_OK;
+}
+
+int gpi_server_wait(gpi_server *s, int64_t id) {
+  if (!s) return sfail(GPI_E_INVALID, "null argument");
+  std::unique_lock<std::mutex> lock(s->mu);
+  Job *j = find(s, id);
+  if (!j) return sfail(GPI_E_INVALID, "unknown request");
+  s->cv.wait(lock, [&] { return j->state == DONE || j->state == FAILED || s->stop; });
+  if (j->state == FAILED) return sfail(j->status, j->message);
+  return j->state == DONE ? GPI_OK : sfail(GPI_E_STATE, "server stopped");
+}
+
+int gpi_server_records(gpi_server *s, int64_t id, int shot, int field, float *out) {
+  if (!s || !out) return sfail(GPI_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lock(s->mu);
+  Job *j = find(s, id);
+  if (!j) return sfail(GPI_E_INVALID, "unknown request");
+  if (j->state != DONE) return sfail(GPI_E_STATE, "request not done");
+  for (size_t k = 0; k < j->rec.size(); k++)
+    if (j->rec[k].shot == shot && j->rec[k].field == field) {
+      std::copy(j->records[k].begin(), j->records[k].end(), out);
+      return GPI_OK;
+    }
+  return sfail(GPI_E_INVALID, "no such receiver entry");
+}
+
+int gpi_server_gradient(gpi_server *s, int64_t id, int param, float *out, double *loss) {
+  if (!s) return sfail(GPI_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lock(s->mu);
+  Job *j = find(s, id);
+  if (!j) return sfail(GPI_E_INVALID, "unknown request");
+  if (j->state != DONE) return sfail(GPI_E_STATE, "request not done");
+  if (!j->gradient) return sfail(GPI_E_INVALID, "not a gradient request");
+  if (param < 0 || param >= 2) return sfail(GPI_E_INVALID, "param");
+  if (out) std::copy(j->grad[param].begin(), j->grad[param].end(), out);
+  if (loss) *loss = j->loss;
+  return GPI_OK;
+}
+
+int gpi_server_times(gpi_server *s, int64_t id, double *t) {
+  if (!s || !t) return sfail(GPI_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lock(s->mu);
+  Job *j = find(s, id);
+  if (!j) return sfail(GPI_E_INVALID, "unknown request");
+  t[0] = j->t_submit;
+  t[1] = j->t_admit;
+  t[2] = j->t_done;
+  return GPI_OK;
+}
+
+const char *gpi_server_message(gpi_server *s, int64_t id) {
+  if (!s) return g_msg.c_str();
+  std::lock_guard<std::mutex> lock(s->mu);
+  Job *j = find(s, id);
+  return j ? j->message.c_str() : g_msg.c_str();
+}
+
+int gpi_server_release(gpi_server *s, int64_t id) {
+  if (!s) return sfail(GPI_E_INVALID, "null argument");
+  std::lock_guard<std::mutex> lock(s->mu);
+  Job *j = find(s, id);
+  if (!j) return sfail(GPI_E_INVALID, "unknown request");
+  if (j->state != DONE && j->state != FAILED) return sfail(GPI_E_STATE, "request still queued or running");
+  s->jobs.erase(id);
+  delete j;
+  return GPI_OK;
+}
+
+}  // extern "C"

@@ -22,7 +22,9 @@ EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_str
            "gpi_set_medium", "gpi_set_pml", "gpi_set_sources", "gpi_clear_sources", "gpi_set_receivers",
            "gpi_run", "gpi_get_records", "gpi_get_gradient", "gpi_get_field", "gpi_last_launches",
            "gpi_set_graph", "gpi_query", "gpi_checkpoint_schedule", "gpi_set_snapshots", "gpi_get_snapshot",
-           "gpi_forward_acoustic2d_noalloc", "gpi_set_born"]
+           "gpi_forward_acoustic2d_noalloc", "gpi_set_born", "gpi_plan_estimate", "gpi_server_create",
+           "gpi_server_destroy", "gpi_server_submit", "gpi_server_poll", "gpi_server_wait", "gpi_server_records",
+           "gpi_server_gradient", "gpi_server_times", "gpi_server_message", "gpi_server_release"]
 
 
 class PlanDesc(ctypes.Structure):
@@ -33,6 +35,23 @@ class PlanDesc(ctypes.Structure):
                 ("nshots", ctypes.c_int32), ("npw", ctypes.c_int32), ("checkpoints", ctypes.c_int32),
                 ("imaging", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
                 ("dt", ctypes.c_double), ("dz", ctypes.c_double), ("dy", ctypes.c_double), ("dx", ctypes.c_double)]
+
+
+class ServerDesc(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("max_inflight", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
+                ("hbm_budget", ctypes.c_size_t)]
+
+
+class Proj(ctypes.Structure):
+    _fields_ = [("shot", ctypes.c_int32), ("field", ctypes.c_int32), ("n", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("colptr", ctypes.c_void_p), ("rowval", ctypes.c_void_p), ("nzval", ctypes.c_void_p),
+                ("data", ctypes.c_void_p)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("plan", PlanDesc), ("gradient", ctypes.c_int32), ("nsrc", ctypes.c_int32), ("nrec", ctypes.c_int32),
+                ("graph", ctypes.c_int32), ("mod", ctypes.c_void_p), ("pml", ctypes.c_void_p),
+                ("src", ctypes.POINTER(Proj)), ("rec", ctypes.POINTER(Proj))]
 
 
 class EngineError(RuntimeError):
@@ -92,6 +111,19 @@ def _load():
                                           ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]
     L.gpi_forward_acoustic2d_noalloc.argtypes = [ctypes.POINTER(PlanDesc), fp, fp, fp, i32, i32, i64p, i64p, fp, fp,
                                                  i32, vp, vp, vp, vp, vp, vp, vp]
+    L.gpi_plan_estimate.argtypes = [ctypes.POINTER(PlanDesc), ctypes.POINTER(ctypes.c_size_t)]
+    L.gpi_server_create.argtypes = [ctypes.POINTER(ServerDesc), ctypes.POINTER(ctypes.c_void_p)]
+    L.gpi_server_destroy.argtypes = [vp]
+    L.gpi_server_destroy.restype = None
+    L.gpi_server_submit.argtypes = [vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)]
+    L.gpi_server_poll.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
+    L.gpi_server_wait.argtypes = [vp, ctypes.c_int64]
+    L.gpi_server_records.argtypes = [vp, ctypes.c_int64, i32, i32, fp]
+    L.gpi_server_gradient.argtypes = [vp, ctypes.c_int64, i32, fp, ctypes.POINTER(ctypes.c_double)]
+    L.gpi_server_times.argtypes = [vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
+    L.gpi_server_message.argtypes = [vp, ctypes.c_int64]
+    L.gpi_server_message.restype = ctypes.c_char_p
+    L.gpi_server_release.argtypes = [vp, ctypes.c_int64]
     _LIB = L
     return L
 

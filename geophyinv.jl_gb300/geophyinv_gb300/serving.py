@@ -1,26 +1,26 @@
 """Continuous-batching serving loop for forward and gradient shot requests.
 
 Requests of uneven grid sizes, step counts and shot counts arrive over time.
-The server admits a request as soon as an in-flight slot is free and its
-plan fits the HBM budget, prepares it on a host worker thread (model, CPML
-profiles, projections, a plan of its own with stream-ordered device
-allocations) while other requests run, then launches it on its own CUDA
-stream (all of its shots in one multi-shot launch per step; optionally the
-whole time loop as one CUDA graph, worth it for plans that run more than
-once) and keeps its wavefields, boundary store and records resident until it
-completes.  Requests on the GPU overlap, and the host work of one request
-overlaps the device work of the others.  A gradient request runs forward_save, builds its adjoint
-sources from the residuals and runs the adjoint (gradient!,
-src/fdtd/func_grad.jl:11-49).
+`serve` hands each one, when it arrives, to the engine's C server
+(gpi_server_*, csrc/gpi_server.cu): the client builds the request's arrays
+(padding, CPML profiles, projections: `RequestBuffers`) on a pool of host
+threads, the server admits requests in arrival order while its worker
+slots and HBM budget allow, runs each on its own CUDA stream (all of its
+shots in one multi-shot launch per step, forward runs replayed as captured
+16-step chunks) and returns records and gradients.  Requests on the GPU
+overlap, and the host work of one overlaps the device work of the others.
+A gradient request runs forward_save, builds its adjoint sources from the
+residuals and runs the adjoint (gradient!, src/fdtd/func_grad.jl:11-49).
 
 A request carries its payload (model, geometry, wavelets: `Request.payload`,
-built by the client before it is sent); the server's own work starts at
-admission.  The baselines (`serve_plain`) take the same stream one shot at a
-time (a single-shot plan per shot, plain launches, no overlap), or one
-request at a time with its shots batched.  Results do not depend on what else
-runs: every request's arithmetic is its own and deterministic.
+built by the client before it is sent).  The baselines (`serve_plain`) take
+the same stream one shot at a time (a single-shot plan per shot, plain
+launches, no overlap), or one request at a time with its shots batched.
+Results do not depend on what else runs: every request's arithmetic is its
+own and deterministic.
 """
 import copy
+import ctypes
 import time
 from dataclasses import dataclass, field
 
@@ -85,22 +85,6 @@ def make_stream(n, rate, seed=4, sides=(200, 2000), steps=(1000, 6000), shots=(1
                            int(rng.integers(steps[0], steps[1] + 1)), int(rng.integers(shots[0], shots[1] + 1)), t,
                            seed=int(rng.integers(0, 1 << 30))))
     return out
-
-
-def plan_bytes_estimate(req):
-    """Device bytes of a request's plan (state, CPML strips, coefficients,
-    records, boundary store), from the layout of the engine."""
-    nz, nx = req.nz + 86, req.nx + 86
-    nzp = (nz + 124 + 12 + 31) // 32 * 32
-    f = nzp * (nx + 15) * 4
-    ela = req.kind == "elastic_forward"
-    npw = 2 if req.kind == "acoustic_gradient" else 1
-    state = (5 if ela else 3) * 2 * npw * req.nshots * f
-    coef = ((5 if ela else 3) + 3) * f
-    psi = (8 if ela else 4) * 2 * npw * req.nshots * 88 * max(nzp, nx + 15) * 4
-    rec = req.nt * (req.nx // 4 + 8) * 2 * req.nshots * 4
-    store = (req.nt * 6 * (nz + nx) + 3 * nzp * (nx + 15)) * 4 * req.nshots if npw == 2 else 0
-    return state + coef + psi + rec + store + npw * 2 * req.nshots * f
 
 
 @dataclass
@@ -190,75 +174,194 @@ class _Job:
         self.pa = None
 
 
-def _prepare(req, graphs, stream):
-    job = _Job(req, graphs, stream)
-    job.launch()
-    return job
+class RequestBuffers:
+    """The arrays of one request as the C server takes them (gpi_request):
+    the host set-up of the reference's PFdtd constructor (padding, derived
+    parameters, peak frequency and CPML profiles, projection matrices), in
+    the same steps as SeisForwExpt, without creating a plan."""
+
+    def __init__(self, req, graphs=True):
+        from . import setup as S
+
+        wl = req.payload()
+        gradient = req.kind == "acoustic_gradient"
+        npml = wl.npml if wl.npml is not None else 43
+        mask = S.face_mask(wl.pml_faces)
+        exgrid = S.padgrid(wl.grid, npml, mask)
+        vp = S.padarray(wl.vp, npml, mask)
+        rho = S.padarray(wl.rho, npml, mask)
+        if wl.physics == "acoustic":
+            mod = [S.invK(vp, rho), rho]
+        else:
+            vs = S.padarray(wl.vs, npml, mask)
+            mod = [S.invlambda(vp, vs, rho), S.invmu(vs, rho), rho]
+        self.mod = [np.asfortranarray(m, np.float32) for m in mod]
+        d = _lib.PlanDesc()
+        d.physics = _lib.ACOUSTIC if wl.physics == "acoustic" else _lib.ELASTIC
+        d.ndim, d.order = 2, 4
+        d.nz, d.ny, d.nx = len(exgrid[0]), 1, len(exgrid[1])
+        d.dz, d.dy, d.dx = wl.grid[0].step, 1.0, wl.grid[1].step
+        d.npml, d.nbound = npml, 3
+        d.pml_faces = mask
+        d.rigid_faces = mask
+        d.free_faces = S.face_mask(wl.stressfree_faces)
+        d.nt, d.nshots = wl.nt, len(wl.shots)
+        d.npw = 2 if gradient else 1
+        d.dt = wl.tgrid.step
+        srcwav = wl.srcwav()
+        peaks = [np.mean([S.findfreq_peak(np.asarray(s.d[f], np.float32), d.dt) for f in s.fields]) for s in srcwav]
+        _, vb = S.ref_bounds(vp)
+        velavg = np.float32((vb[0] + vb[1]) / np.float32(2.0))
+        pml = S.cpml_all(wl.physics, 2, 4, wl.grid, mask, np.float32(d.dt), velavg, np.float32(np.mean(peaks)), npml)
+        self.pml = np.ascontiguousarray(np.concatenate([np.concatenate(x) for x in pml]), np.float32)
+        self.keep = []
+        src, rec = [], []
+        ageom = wl.ageom()
+        for iss, (a, sw) in enumerate(zip(ageom, srcwav)):
+            for f in sw.fields:
+                cp, rv, nz = S.projection(f, exgrid, a.points("s", 2), 4)
+                w = np.asfortranarray(sw.d[f], np.float32)
+                src.append((iss, f, len(cp) - 1, cp, rv, nz, w))
+            for f in wl.rfields:
+                cp, rv, nz = S.projection(f, exgrid, a.points("r", 2), 4)
+                rec.append((iss, f, len(cp) - 1, cp, rv, nz, None))
+        self.src_entries, self.rec_entries = src, rec
+
+        def projs(entries):
+            arr = (_lib.Proj * len(entries))()
+            for i, (iss, f, n, cp, rv, nz, data) in enumerate(entries):
+                self.keep += [cp, rv, nz] + ([data] if data is not None else [])
+                arr[i].shot, arr[i].field, arr[i].n = iss, _lib.FIELD[f], n
+                arr[i].colptr, arr[i].rowval, arr[i].nzval = cp.ctypes.data, rv.ctypes.data, nz.ctypes.data
+                arr[i].data = data.ctypes.data if data is not None else None
+            return arr
+
+        self.src_arr, self.rec_arr = projs(src), projs(rec)
+        self.mod_ptrs = (ctypes.c_void_p * len(self.mod))(*[m.ctypes.data for m in self.mod])
+        r = _lib.Request()
+        r.plan = d
+        r.gradient = int(gradient)
+        r.nsrc, r.nrec = len(src), len(rec)
+        # forward runs replay a captured 16-step chunk (a whole-run graph
+        # costs more to capture than one run saves)
+        r.graph = 2 if graphs else 0
+        r.mod = ctypes.cast(self.mod_ptrs, ctypes.c_void_p)
+        r.pml = self.pml.ctypes.data
+        r.src, r.rec = self.src_arr, self.rec_arr
+        self.request = r
+        self.desc = d
+        self.rfields = list(wl.rfields)
+        self.nt = wl.nt
+        self.nshots = len(wl.shots)
 
 
-def _streams(n):
-    import torch
+def request_bytes(req):
+    """Device bytes the server charges a request against its HBM budget (the
+    plan's pool by gpi_plan_estimate plus its record buffers)."""
+    L = _lib.load()
+    rb = RequestBuffers(req)
+    b = ctypes.c_size_t()
+    _lib.check(L.gpi_plan_estimate(ctypes.byref(rb.desc), ctypes.byref(b)))
+    recs = sum(rb.nt * e[2] for e in rb.rec_entries)
+    return b.value + recs * 4 * (3 if req.kind == "acoustic_gradient" else 2)
 
-    return [torch.cuda.Stream() for _ in range(n)]
+
+class Server:
+    """The C ABI server (gpi_server_*): requests in, results out."""
+
+    def __init__(self, max_inflight=8, hbm_budget=64 << 30, device=0):
+        self.L = _lib.load()
+        d = _lib.ServerDesc()
+        d.device, d.max_inflight, d.hbm_budget = device, max_inflight, hbm_budget
+        h = ctypes.c_void_p()
+        rc = self.L.gpi_server_create(ctypes.byref(d), ctypes.byref(h))
+        if rc:
+            raise _lib.EngineError("gpi_server_create: %s" % self.L.gpi_server_message(None, 0).decode())
+        self.h = h
+
+    def submit(self, rb):
+        i = ctypes.c_int64()
+        rc = self.L.gpi_server_submit(self.h, ctypes.byref(rb.request), ctypes.byref(i))
+        if rc:
+            raise _lib.EngineError("gpi_server_submit: %s" % self.L.gpi_server_message(self.h, 0).decode())
+        return i.value
+
+    def _check(self, rc, sid):
+        if rc:
+            raise _lib.EngineError("request %d: %s: %s" % (sid, _lib.STATUS.get(rc, rc),
+                                                          self.L.gpi_server_message(self.h, sid).decode()))
+
+    def result(self, sid, req, rb):
+        L = self.L
+        self._check(L.gpi_server_wait(self.h, sid), sid)
+        res = Result(req.rid, req.kind)
+        for iss in range(rb.nshots):
+            per = {}
+            for (s, f, n, *_rest) in rb.rec_entries:
+                if s == iss:
+                    out = np.zeros((rb.nt, n), np.float32, order="F")
+                    self._check(L.gpi_server_records(self.h, sid, iss, _lib.FIELD[f], out.ctypes.data), sid)
+                    per[f] = out
+            res.records.append(per)
+        if req.kind == "acoustic_gradient":
+            n = [rb.desc.nz, rb.desc.nx]
+            res.gradient = {}
+            loss = ctypes.c_double()
+            for q, k in enumerate(("invK", "rho")):
+                g = np.zeros(n, np.float32, order="F")
+                self._check(L.gpi_server_gradient(self.h, sid, q, g.ctypes.data, ctypes.byref(loss)), sid)
+                res.gradient[k] = g
+            res.loss = loss.value
+        t = (ctypes.c_double * 3)()
+        self._check(L.gpi_server_times(self.h, sid, t), sid)
+        res.t_admit, res.t_done = t[1], t[2]
+        L.gpi_server_release(self.h, sid)
+        return res
+
+    def close(self):
+        if self.h:
+            self.L.gpi_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=True, prep_threads=4):
-    """Continuous batching: admit arrived requests while slots and HBM budget
-    allow, prepare them on host threads, launch them when ready, poll the
-    in-flight ones, launch their next phase or collect their results.
-    Returns (results by id, stats)."""
+    """Continuous batching through the C server: each request is handed to
+    it when it arrives (its host set-up -- padding, CPML profiles,
+    projections -- on one of `prep_threads` client threads), the server
+    admits it while slots and the HBM budget allow, runs it on its own stream
+    overlapping the others, and returns its records (and gradient).
+    Returns (results by id, stats); admission and completion times are on
+    the stream's clock (seconds from its start)."""
     from concurrent.futures import ThreadPoolExecutor
 
-    import torch
-
-    streams = _streams(max_inflight)
-    free = list(range(max_inflight))
-    pending = sorted(requests, key=lambda r: r.arrival)
-    preparing = {}
-    inflight = {}
-    results = {}
-    used = 0
+    srv = Server(max_inflight=max_inflight, hbm_budget=hbm_budget)
     pool = ThreadPoolExecutor(max_workers=prep_threads)
+    pending = sorted(requests, key=lambda r: r.arrival)
+    # the stream's clock starts with the server's (gpi_server_times)
     t0 = time.perf_counter()
-    while pending or preparing or inflight:
-        now = time.perf_counter() - t0
-        # admission: arrival order, HBM budget, a free stream
-        while pending and free and (not realtime or pending[0].arrival <= now):
-            need = plan_bytes_estimate(pending[0])
-            if (inflight or preparing) and used + need > hbm_budget:
-                break
-            req = pending.pop(0)
-            slot = free.pop()
-            preparing[req.rid] = (pool.submit(_prepare, req, graphs, streams[slot].cuda_stream), slot, need,
-                                  time.perf_counter() - t0)
-            used += need
-        for rid in list(preparing):
-            fut, slot, need, t_admit = preparing[rid]
-            if fut.done():
-                job = fut.result()
-                job.res.t_admit = t_admit
-                inflight[rid] = (job, slot, need)
-                del preparing[rid]
-        done_any = False
-        for rid in list(inflight):
-            job, slot, need = inflight[rid]
-            if job.error is not None:
-                raise job.error
-            if job.busy is None and job.pa.done():
-                done_any = True
-                if job.finish_phase(pool):
-                    job.res.t_done = time.perf_counter() - t0
-                    results[rid] = job.res
-                    job.close()
-                    del inflight[rid]
-                    free.append(slot)
-                    used -= need
-        if not done_any:
-            time.sleep(0.0002)
+
+    def hand_in(req):
+        rb = RequestBuffers(req, graphs)
+        return rb, srv.submit(rb)
+
+    futs = []
+    for req in pending:
+        if realtime:
+            wait = req.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+        futs.append((req, pool.submit(hand_in, req)))
+    results = {}
+    for req, fut in futs:
+        rb, sid = fut.result()
+        results[req.rid] = srv.result(sid, req, rb)
     pool.shutdown()
-    if torch.cuda.is_available():
-        torch.cuda.synchronize()
-    return results, _stats(requests, results, time.perf_counter() - t0)
+    wall = time.perf_counter() - t0
+    srv.close()
+    return results, _stats(requests, results, wall)
 
 
 def _run_plain(job):

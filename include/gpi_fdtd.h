@@ -191,6 +191,74 @@ int gpi_query(gpi_plan *plan, int *done);
  * fills.  No counterpart in the reference. */
 int gpi_checkpoint_schedule(int nt, int slots, int64_t *advances, int64_t *turns, int *stored);
 
+/* ------------------------------------------------------------------------
+ * Serving (no counterpart in the reference, whose update!(pa) runs one
+ * experiment at a time on each Distributed worker,
+ * src/fdtd/propagate.jl:100-106).  A server admits queued requests in
+ * arrival order while the device bytes of the admitted ones stay within its
+ * HBM budget, runs up to max_inflight of them at once on their own streams
+ * (host set-up of one overlapping the device work of the others; each
+ * request's shots batched into every launch, forward runs replayed as
+ * captured step chunks) and keeps the results on the host until released.
+ * A request's results do not depend on what else runs.
+ * ------------------------------------------------------------------------ */
+typedef struct gpi_server gpi_server;
+
+typedef struct {
+  int32_t device;       /* CUDA device of every request */
+  int32_t max_inflight; /* requests on the device at once (1..64 worker threads) */
+  int32_t reserved[2];
+  size_t hbm_budget;    /* device bytes the admitted requests may hold together
+                           (a request larger than the budget runs alone) */
+} gpi_server_desc;
+
+/* One sparse projection of one shot and field (as gpi_set_sources /
+ * gpi_set_receivers take it) with its time series. */
+typedef struct {
+  int32_t shot, field, n, pad;
+  const int64_t *colptr, *rowval; /* CSC, 0-based */
+  const float *nzval;
+  const float *data; /* sources: wavelets nt x n (required); receivers of a
+                        gradient request: observed records nt x n (NULL:
+                        zero); receivers of a forward request: ignored */
+} gpi_proj;
+
+typedef struct {
+  gpi_plan_desc plan;      /* npw = 1 for a forward request, 2 for a gradient */
+  int32_t gradient;        /* 0: update!(pa); 1: gradient!(g, m, L2DistLoss(),
+                              dobs, pa) (src/fdtd/func_grad.jl:11-49) */
+  int32_t nsrc, nrec;      /* entries of src (wavefield-1 sources) and rec */
+  int32_t graph;           /* gpi_set_graph kind for the request's runs */
+  const float *const *mod; /* host medium parameters on the extended grid */
+  const float *pml;        /* host CPML profiles: per derivative field q
+                              (canonical order) a, b, kI of 2*npml each */
+  const gpi_proj *src, *rec;
+} gpi_request;
+
+int gpi_server_create(const gpi_server_desc *desc, gpi_server **out);
+/* Stops admitting, lets running requests finish, frees everything. */
+void gpi_server_destroy(gpi_server *server);
+/* Copies the request (the caller may free its arrays on return) and queues
+ * it; *id identifies it.  Returns at once. */
+int gpi_server_submit(gpi_server *server, const gpi_request *req, int64_t *id);
+/* *state: 0 queued, 1 running, 2 done, 3 failed. */
+int gpi_server_poll(gpi_server *server, int64_t id, int *state);
+/* Blocks until the request is done; returns its status. */
+int gpi_server_wait(gpi_server *server, int64_t id);
+/* Records (nt x n, column-major) of one receiver entry of a done request. */
+int gpi_server_records(gpi_server *server, int64_t id, int shot, int field, float *out);
+/* Raw gradient accumulations summed over shots (param as gpi_get_gradient,
+ * extended grid; out may be NULL) and the misfit of a gradient request. */
+int gpi_server_gradient(gpi_server *server, int64_t id, int param, float *out, double *loss);
+/* t[0..2]: submission, admission and completion times in seconds since the
+ * server was created. */
+int gpi_server_times(gpi_server *server, int64_t id, double *t);
+/* Message of a failed request (or, for an unknown id, of the last failing
+ * server call on this thread). */
+const char *gpi_server_message(gpi_server *server, int64_t id);
+/* Frees a done or failed request's results. */
+int gpi_server_release(gpi_server *server, int64_t id);
+
 /* Size of the device scratch array used by gpi_forward_acoustic2d_noalloc. */
 #define GPI_NOALLOC_SCRATCH_BYTES (64u << 20)
 

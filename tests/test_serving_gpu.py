@@ -15,7 +15,7 @@ def _same(a, b):
     if a.gradient is not None:
         for k in a.gradient:
             assert np.array_equal(a.gradient[k], b.gradient[k]), (a.rid, k)
-        assert a.loss == b.loss
+        assert abs(a.loss - b.loss) <= 1e-12 * abs(b.loss)  # summed in another order
 
 
 @pytest.mark.gpu
@@ -35,7 +35,7 @@ def test_results_alone_equal_results_in_the_mix(engine):
 @pytest.mark.gpu
 def test_admission_respects_the_hbm_budget(engine):
     reqs = serving.make_stream(4, rate=1000.0, seed=3, sides=(60, 100), steps=(50, 80), shots=(1, 2))
-    budget = max(serving.plan_bytes_estimate(r) for r in reqs)  # room for one request at a time
+    budget = max(serving.request_bytes(r) for r in reqs)  # room for one request at a time
     res, stats = serving.serve(reqs, hbm_budget=budget, max_inflight=4, realtime=False)
     order = sorted(res.values(), key=lambda r: r.t_admit)
     assert all(b.t_admit >= a.t_done for a, b in zip(order, order[1:]))

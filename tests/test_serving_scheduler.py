@@ -1,93 +1,77 @@
-"""The continuous-batching scheduler's host logic (no GPU): the device work
-of a request is replaced by a timer, so that admission by arrival, free
-slots and the HBM budget, the two phases of a gradient request and the
-statistics can be checked on the CPU."""
-import threading
-import time
+"""Host parts of the serving path (no GPU): the device bytes a request is
+charged against the HBM budget (gpi_plan_estimate, computed without
+allocating), the request arrays the client hands to the C server, and the
+server's refusal to start without a device.  Admission, overlap and the
+alone == mixed property run on the GPU (test_serving_gpu.py)."""
+import ctypes
+import os
 
+import numpy as np
 import pytest
 
-from geophyinv_gb300 import serving
+from geophyinv_gb300 import _build, _lib, serving
 
 
-class _FakeJob:
-    """A request whose phases take a fixed host time; records the set of
-    requests on the 'device' so that the test can check the budget."""
-    live = {}
-    peak_bytes = 0
-    peak_count = 0
-    lock = threading.Lock()
-    phase_s = 0.02
-
-    def __init__(self, req, graphs, stream):
-        self.req = req
-        self.res = serving.Result(req.rid, req.kind)
-        self.phase = 0
-        self.busy = None
-        self.error = None
-        self.pa = self
-        self.t_end = time.perf_counter() + self.phase_s
-        with self.lock:
-            _FakeJob.live[req.rid] = serving.plan_bytes_estimate(req)
-            _FakeJob.peak_bytes = max(_FakeJob.peak_bytes, sum(_FakeJob.live.values()))
-            _FakeJob.peak_count = max(_FakeJob.peak_count, len(_FakeJob.live))
-
-    def launch(self):
-        pass
-
-    def done(self):
-        return time.perf_counter() >= self.t_end
-
-    def finish_phase(self, pool=None):
-        if self.req.kind == "acoustic_gradient" and self.phase == 0:
-            self.phase = 1
-            self.t_end = time.perf_counter() + self.phase_s
-            return False
-        self.res.records = ["phase %d" % self.phase]
-        return True
-
-    def close(self):
-        with self.lock:
-            _FakeJob.live.pop(self.req.rid, None)
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    return _lib.load()
 
 
-class _FakeStream:
-    cuda_stream = 0
+def _desc(npw=1, checkpoints=0, nz=300, nx=400, nshots=2, nt=100):
+    d = _lib.PlanDesc()
+    d.physics, d.ndim, d.order = 0, 2, 4
+    d.nz, d.ny, d.nx, d.npml, d.nbound, d.nt, d.nshots, d.npw = nz, 1, nx, 43, 3, nt, nshots, npw
+    d.dt, d.dz, d.dx, d.dy = 5e-4, 5.0, 5.0, 1.0
+    d.pml_faces = d.rigid_faces = 0x33
+    d.checkpoints = checkpoints
+    return d
 
 
-@pytest.fixture
-def fake(monkeypatch):
-    _FakeJob.live = {}
-    _FakeJob.peak_bytes = 0
-    _FakeJob.peak_count = 0
-    monkeypatch.setattr(serving, "_prepare", lambda req, graphs, stream: _FakeJob(req, graphs, stream))
-    monkeypatch.setattr(serving, "_streams", lambda n: [_FakeStream() for _ in range(n)])
-    return _FakeJob
+def _estimate(lib, d):
+    b = ctypes.c_size_t()
+    assert lib.gpi_plan_estimate(ctypes.byref(d), ctypes.byref(b)) == 0, lib.gpi_last_error(None)
+    return b.value
 
 
-def test_every_request_completes_and_gradients_take_two_phases(fake):
-    reqs = serving.make_stream(20, rate=1000.0, seed=1, sides=(50, 100), steps=(10, 20), shots=(1, 3))
-    res, st = serving.serve(reqs, max_inflight=4, realtime=False)
-    assert sorted(res) == [r.rid for r in reqs]
-    for r in reqs:
-        assert res[r.rid].records == ["phase %d" % (1 if r.kind == "acoustic_gradient" else 0)]
-        assert res[r.rid].t_done >= res[r.rid].t_admit
-    assert st["requests"] == 20 and st["shots"] == sum(r.nshots for r in reqs)
-    assert 0 < st["p50_s"] <= st["p99_s"]
-    assert fake.peak_count <= 4
+def test_plan_estimate_covers_the_layout_and_grows_with_the_work(lib):
+    fwd = _estimate(lib, _desc())
+    # at least both buffers of p, vx, vz for every shot on the padded grid
+    assert fwd >= 2 * 3 * 2 * 300 * 400 * 4
+    assert _estimate(lib, _desc(nshots=4)) > fwd
+    grad = _estimate(lib, _desc(npw=2))
+    assert grad > 2 * fwd * 0.9  # two wavefields and the boundary store
+    c2, c4 = _estimate(lib, _desc(npw=2, checkpoints=2)), _estimate(lib, _desc(npw=2, checkpoints=4))
+    assert c4 > c2 and (c4 - c2) % 2 == 0
+    bad = _desc()
+    bad.order = 2
+    assert lib.gpi_plan_estimate(ctypes.byref(bad), ctypes.byref(ctypes.c_size_t())) == -4
 
 
-def test_admission_keeps_the_device_under_the_hbm_budget(fake):
-    reqs = serving.make_stream(12, rate=1000.0, seed=2, sides=(50, 100), steps=(10, 20), shots=(1, 3))
-    sizes = sorted(serving.plan_bytes_estimate(r) for r in reqs)
-    budget = sizes[-1] + sizes[-2] - 1  # never room for the two largest together
-    serving.serve(reqs, hbm_budget=budget, max_inflight=8, realtime=False)
-    assert fake.peak_bytes <= budget
-    assert fake.peak_count >= 2  # but smaller ones overlap
+def test_request_arrays_follow_the_workload(lib):
+    req = serving.make_stream(1, rate=10.0, seed=5, sides=(60, 90), steps=(40, 60), shots=(2, 3))[0]
+    rb = serving.RequestBuffers(req)
+    wl = req.payload()
+    d = rb.desc
+    assert (d.nz, d.nx) == (len(wl.grid[0]) + 86, len(wl.grid[1]) + 86)
+    assert d.nshots == len(wl.shots) and d.nt == wl.nt
+    assert d.npw == (2 if req.kind == "acoustic_gradient" else 1)
+    assert len(rb.pml) == (8 if wl.physics == "elastic" else 4) * 3 * 2 * 43
+    assert rb.request.nrec == len(wl.shots) * len(wl.rfields)
+    assert all(np.isfinite(m).all() for m in rb.mod)
+    assert serving.request_bytes(req) > _estimate(lib, rb.desc)
 
 
-def test_requests_are_admitted_after_they_arrive(fake):
-    reqs = serving.make_stream(6, rate=50.0, seed=3, sides=(50, 60), steps=(10, 12), shots=(1, 1))
-    res, _ = serving.serve(reqs, max_inflight=8, realtime=True)
-    for r in reqs:
-        assert res[r.rid].t_admit >= r.arrival - 1e-3
+def test_server_needs_a_device(lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    d = _lib.ServerDesc()
+    d.device, d.max_inflight, d.hbm_budget = 0, 2, 1 << 30
+    h = ctypes.c_void_p()
+    assert lib.gpi_server_create(ctypes.byref(d), ctypes.byref(h)) == -3
+    assert b"device" in lib.gpi_server_message(None, 0)
+    d.max_inflight = 0
+    assert lib.gpi_server_create(ctypes.byref(d), ctypes.byref(h)) == -1
