@@ -250,6 +250,109 @@ __global__ void __launch_bounds__(256) k_grad_a3(const Grad3Args a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// imaging condition, 3-D elastic (no counterpart in the reference, which
+// defines gradients for 2-D acoustic media only): the gradient of the
+// discrete scheme with respect to invlambda, invmu and rho.  Per step, with
+// X the forward state before step s, W after it (velocities: after the
+// velocity half step of s+1) and Y the adjoint state before adjoint step j:
+//   normal-stress cells: K = (dtM - dtl) I + dtl 1 1', a = K^-1 Y_n,
+//     b = K^-1 (X_n - W_n);  g_invlambda += (sum a)(sum b) dtl^2 / dt,
+//     g_invmu += (a . b) 2 dt / invmu^2
+//   shear cells: a quarter of Y_s (X_s - W_s) / dt to each of the four
+//     invmu cells of the cell's average (@av_xzi, @av_xyi, @av_yzi)
+//   velocity cells: the rho term of the acoustic discrete-model imaging
+//     condition (imaging = 1)
+// (K^-1 turns a stress into the strain that produced it, so no derivative
+// is recomputed.)  Checked against finite differences of the misfit.
+// ---------------------------------------------------------------------------
+struct GradE3Args {
+  int nz, ny, nx, NZP, NYP;
+  int64_t fs;
+  int nshots;
+  const float *Y[NFIELD], *X[NFIELD], *W[NFIELD];
+  const float *dtM, *dtl, *invmu;
+  float *gL, *gM, *gR;
+  float dt, dtI;
+};
+
+__global__ void __launch_bounds__(256) k_grad_e3(const GradE3Args a) {
+  const int64_t per = (int64_t)a.nz * a.ny * a.nx;
+  const int64_t total = per * a.nshots;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int shot = (int)(i / per);
+    int64_t k = i - shot * per;
+    const int r = (int)(k % a.nz) + 1;
+    k /= a.nz;
+    const int y = (int)(k % a.ny) + 1, c = (int)(k / a.ny) + 1;
+    const int64_t so = shot * a.fs;
+    auto L = [&](int rr, int yy, int cc) -> int64_t {
+      return ((int64_t)(cc - 1 + XOFF) * a.NYP + (yy - 1 + YOFF)) * a.NZP + (rr - 1 + ZOFF);
+    };
+    const int64_t lo = L(r, y, c), o = so + lo;
+    // normal stresses
+    const int nid[3] = {GPI_TAUXX, GPI_TAUYY, GPI_TAUZZ};
+    float q[3], dT[3], sq = 0.f, sT = 0.f;
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+      q[m] = a.Y[nid[m]][o];
+      dT[m] = a.X[nid[m]][o] - a.W[nid[m]][o];
+      sq = sq + q[m];
+      sT = sT + dT[m];
+    }
+    const float beta = a.dtl[lo], alpha = a.dtM[lo] - a.dtl[lo];
+    const float cq = beta / (alpha + 3.0f * beta);
+    float sa = 0.f, sb = 0.f, ab = 0.f;
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+      const float am = (q[m] - cq * sq) / alpha, bm = (dT[m] - cq * sT) / alpha;
+      sa = sa + am;
+      sb = sb + bm;
+      ab = ab + am * bm;
+    }
+    const float im = a.invmu[lo];
+    a.gL[o] = a.gL[o] + sa * sb * (beta * beta * a.dtI);
+    float gm = a.gM[o] + ab * (2.0f * a.dt / (im * im));
+    // shear stresses whose invmu average holds this cell, in the order
+    // tauxz, tauxy, tauyz and, within each, by column, y, row
+    auto sh = [&](int f, int rr, int yy, int cc) -> float {
+      const int64_t s = so + L(rr, yy, cc);
+      return a.Y[f][s] * (a.X[f][s] - a.W[f][s]) * a.dtI * 0.25f;
+    };
+    const int nz = a.nz, ny = a.ny, nx = a.nx;
+    // tauxz (nz-3, ny-6, nx-3): cell (iz, iy, ix) averages rows iz, iz+1,
+    // y iy+3, columns ix, ix+1
+    if (y - 3 >= 1 && y - 3 <= ny - 6)
+      for (int cc = c - 1; cc <= c; cc++)
+        for (int rr = r - 1; rr <= r; rr++)
+          if (cc >= 1 && cc <= nx - 3 && rr >= 1 && rr <= nz - 3) gm = gm + sh(GPI_TAUXZ, rr, y - 3, cc);
+    // tauxy (nz-6, ny-3, nx-3): row iz+3, y iy, iy+1, columns ix, ix+1
+    if (r - 3 >= 1 && r - 3 <= nz - 6)
+      for (int cc = c - 1; cc <= c; cc++)
+        for (int yy = y - 1; yy <= y; yy++)
+          if (cc >= 1 && cc <= nx - 3 && yy >= 1 && yy <= ny - 3) gm = gm + sh(GPI_TAUXY, r - 3, yy, cc);
+    // tauyz (nz-3, ny-3, nx-6): rows iz, iz+1, y iy, iy+1, column ix+3
+    if (c - 3 >= 1 && c - 3 <= nx - 6)
+      for (int yy = y - 1; yy <= y; yy++)
+        for (int rr = r - 1; rr <= r; rr++)
+          if (yy >= 1 && yy <= ny - 3 && rr >= 1 && rr <= nz - 3) gm = gm + sh(GPI_TAUYZ, rr, yy, c - 3);
+    a.gM[o] = gm;
+    // rho: velocity cells two and three cells further along each axis
+    auto b = [&](int f, int rr, int yy, int cc, bool in) -> float {
+      const int64_t s = so + L(rr, yy, cc);
+      return in ? a.Y[f][s] * (a.X[f][s] - a.W[f][s]) * a.dtI : 0.f;  // V_s - V_{s+1}
+    };
+    const bool rin = r >= 4 && r <= nz - 3, yin = y >= 4 && y <= ny - 3, cin = c >= 4 && c <= nx - 3;
+    const float avx = rin && yin ? (b(GPI_VX, r, y, c + 2, c + 2 >= 4 && c + 2 <= nx) +
+                                    b(GPI_VX, r, y, c + 3, c + 3 >= 4 && c + 3 <= nx)) * 0.5f : 0.f;
+    const float avy = rin && cin ? (b(GPI_VY, r, y + 2, c, y + 2 >= 4 && y + 2 <= ny) +
+                                    b(GPI_VY, r, y + 3, c, y + 3 >= 4 && y + 3 <= ny)) * 0.5f : 0.f;
+    const float avz = yin && cin ? (b(GPI_VZ, r + 2, y, c, r + 2 >= 4 && r + 2 <= nz) +
+                                    b(GPI_VZ, r + 3, y, c, r + 3 >= 4 && r + 3 <= nz)) * 0.5f : 0.f;
+    a.gR[o] = a.gR[o] - avx - avy - avz;
+  }
+}
+
 // k_grad_a2 with wavefield 1 given explicitly (k_adjoint2d.cu)
 int grad_a2_launch(Plan *p, const float *p1A, const float *p1B, const float *vx1A, const float *vx1B,
                    const float *vz1A, const float *vz1B);
@@ -274,13 +377,43 @@ static int turn(Plan *p, int s) {
   float *const *W = p->state[0][0], *const *X = p->state[1][0];  // X: scratch copies
   const size_t bytes = p->fstride * p->d.nshots * sizeof(float);
   const int vf[3] = {GPI_VX, GPI_VY, GPI_VZ};
+  const bool ela = p->d.physics == GPI_ELASTIC;
   if ((rc = aux_step2(p, s, j))) return rc;
-  GPI_CUDA(p, cudaMemcpyAsync(X[GPI_P], W[GPI_P], bytes, cudaMemcpyDeviceToDevice, p->stream));  // P_{s-1}
+  for (int f = 0; f < NFIELD; f++)  // the stresses (or p) of state s-1
+    if (p->present[f] && f != GPI_VX && f != GPI_VY && f != GPI_VZ)
+      GPI_CUDA(p, cudaMemcpyAsync(X[f], W[f], bytes, cudaMemcpyDeviceToDevice, p->stream));
   if ((rc = step3_wavefield(p, 0, 0))) return rc;
   for (int d = 0; d < 3; d++)
     GPI_CUDA(p, cudaMemcpyAsync(X[vf[d]], W[vf[d]], bytes, cudaMemcpyDeviceToDevice, p->stream));  // V_s
   if (s < nt && (rc = aux_step2(p, s + 1, j))) return rc;
   if ((rc = step3_wavefield(p, 0, vflags & 3))) return rc;  // V_{s+1} in place
+  if (ela) {
+    GradE3Args e;
+    e.nz = p->d.nz;
+    e.ny = p->d.ny;
+    e.nx = p->d.nx;
+    e.NZP = p->NZP;
+    e.NYP = p->NYP;
+    e.fs = p->fstride;
+    e.nshots = p->d.nshots;
+    for (int f = 0; f < NFIELD; f++) {
+      e.Y[f] = p->state[0][1][f];
+      e.X[f] = X[f];
+      e.W[f] = W[f];
+    }
+    e.dtM = p->coef[6];
+    e.dtl = p->coef[7];
+    e.invmu = p->mod[1];
+    e.gL = p->grad[0];
+    e.gM = p->grad[1];
+    e.gR = p->grad[2];
+    e.dt = (float)p->d.dt;
+    e.dtI = (float)(1.0 / p->d.dt);
+    k_grad_e3<<<152 * 16, 256, 0, p->stream>>>(e);
+    p->launches++;
+    GPI_CUDA(p, cudaGetLastError());
+    return step3_wavefield(p, 1, 0);  // adjoint step j
+  }
   Grad3Args g;
   g.nz = p->d.nz;
   g.ny = p->d.ny;
@@ -322,7 +455,7 @@ int ckpt_adjoint(Plan *p) {
   if (!p->grad[0] || !p->grad[1]) return fail(p, GPI_E_STATE, "adjoint run without gradient buffers");
   const Sched S = schedule(p->d.nt, p->ck_slots);
   int rc = zero_wavefield(p, 1);
-  for (int i = 0; i < 2 && !rc; i++)
+  for (int i = 0; i < p->nmod && !rc; i++)
     rc = cudaMemsetAsync(p->grad[i], 0, p->fstride * p->d.nshots * sizeof(float), p->stream) ? GPI_E_CUDA : 0;
   int held = -2;  // the state the working buffer of wavefield 1 holds (-2: none)
   for (size_t i = 0; i < S.ops.size() && !rc; i++) {

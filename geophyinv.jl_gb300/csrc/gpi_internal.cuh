@@ -91,7 +91,7 @@ struct Plan {
   float *mod[3] = {};  // medium parameters, storage layout
   int nmod = 0;
   float *pml = nullptr;  // [nder][3][2*npml]
-  float *grad[2] = {};   // per-shot gradients [shot][storage] (adjoint)
+  float *grad[3] = {};   // per-shot gradients [shot][storage] (adjoint), one per medium parameter
   float *bstore = nullptr;  // boundary store (forward_save -> adjoint)
   float *bprev = nullptr;   // adjoint: the strip values the forcing replaced, this step
   int64_t bstep = 0;         // floats per step per shot

@@ -180,8 +180,9 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
   if (d.nt < 1 || d.nshots < 1 || (d.npw != 1 && d.npw != 2)) return fail(nullptr, GPI_E_INVALID, "nt/nshots/npw");
   if (d.checkpoints < 0 || (d.checkpoints > 0 && d.npw != 2))
     return fail(nullptr, GPI_E_INVALID, "checkpoints: > 0 only with npw = 2");
-  if (d.checkpoints > 0 && d.physics != GPI_ACOUSTIC)
-    return fail(nullptr, GPI_E_UNSUPPORTED, "checkpointed gradients: acoustic media only");
+  if (d.checkpoints > 0 && d.physics != GPI_ACOUSTIC && (d.ndim != 3 || (d.free_faces & GPI_ZMIN)))
+    return fail(nullptr, GPI_E_UNSUPPORTED,
+                "checkpointed gradients: acoustic media, or 3-D elastic media without a free surface");
   if (d.npml < 1 || d.nbound < 1) return fail(nullptr, GPI_E_INVALID, "npml/nbound");
   if (d.imaging != 0 && d.imaging != 1) return fail(nullptr, GPI_E_INVALID, "imaging must be 0 or 1");
   if (!(d.dt > 0) || !(d.dz > 0) || !(d.dx > 0) || (d.ndim == 3 && !(d.dy > 0)))
@@ -252,7 +253,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
   allocs.push_back({(float **)&p.d_it, 64});
   if (d.npw == 2 && d.checkpoints > 0) {
     // checkpointed adjoint: state slots instead of the boundary store
-    for (int i = 0; i < p.nmod && i < 2; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
+    for (int i = 0; i < p.nmod; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
     p.ck_slots = d.checkpoints;
     p.ck_floats = ckpt_slot_floats(p);
     allocs.push_back({&p.ck_pool, p.ck_floats * p.ck_slots});
@@ -944,11 +945,12 @@ int run(Plan &p, int mode) {
   }
   if (mode != GPI_FORWARD && p.d.npw != 2) return fail(&p, GPI_E_INVALID, "forward_save/adjoint need npw = 2");
   if (mode == GPI_ADJOINT && !p.have_save) return fail(&p, GPI_E_STATE, "adjoint run needs a forward_save run first");
-  if (mode == GPI_ADJOINT && !(p.d.physics == GPI_ACOUSTIC && (p.d.ndim == 2 || p.ck_slots > 0)))
+  if (mode == GPI_ADJOINT && !((p.d.physics == GPI_ACOUSTIC && p.d.ndim == 2) || p.ck_slots > 0))
     return fail(&p, GPI_E_UNSUPPORTED,
-                "gradients: acoustic media only, 3-D with a checkpointed plan (the reference: 2-D acoustic)");
-  if (mode == GPI_FORWARD_SAVE && p.d.ndim == 3 && p.d.physics == GPI_ELASTIC)
-    return fail(&p, GPI_E_UNSUPPORTED, "the reference defines no boundary store for 3-D elastic media");
+                "gradients: 2-D acoustic media, or any checkpointed plan (the reference: 2-D acoustic)");
+  if (mode == GPI_FORWARD_SAVE && p.d.physics == GPI_ELASTIC && p.ck_slots == 0)
+    return fail(&p, GPI_E_UNSUPPORTED,
+                "elastic gradients need a checkpointed plan (the reference defines no elastic gradient)");
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev != p.device) GPI_CUDA(&p, cudaSetDevice(p.device));
@@ -1129,7 +1131,7 @@ static int run_body(Plan &p, int mode, bool chunked) {
   if (!rc && p.rec_pool && mode != GPI_ADJOINT)
     rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
   if (!rc && mode == GPI_ADJOINT) {
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < 3; i++)
       if (p.grad[i]) rc = cudaMemsetAsync(p.grad[i], 0, p.fstride * p.d.nshots * sizeof(float), p.stream) ? GPI_E_CUDA : rc;
     if (!rc) rc = snap_io(&p, 1, 1);
     if (!rc) rc = snap_io(&p, 0, 1);
@@ -1244,7 +1246,8 @@ int get_field(Plan &p, int ipw, int shot, int field, float *out, int on_device) 
 int reduce_gradient(Plan *p, int param, float *dst);  // k_common.cu
 
 int get_gradient(Plan &p, int param, float *out, int on_device) {
-  if (p.d.npw != 2 || param < 0 || param > 1 || !p.grad[param]) return fail(&p, GPI_E_INVALID, "no gradient for this parameter");
+  if (p.d.npw != 2 || param < 0 || param >= p.nmod || !p.grad[param])
+    return fail(&p, GPI_E_INVALID, "no gradient for this parameter");
   // sum over shots into shot 0's slot of a scratch area: reuse bstore's
   // snapshot region is not allowed (it is state), so reduce in place into a
   // temporary owned by the plan

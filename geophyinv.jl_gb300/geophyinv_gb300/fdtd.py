@@ -717,7 +717,7 @@ def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
     inn = _inner(pa)
     chunks = np.split(np.asarray(m, np.float32), len(mparams))
     out = []
-    pidx = {"invK": 0, "rho": 1}
+    pidx = {"invK": 0, "rho": 1} if pa.attrib.physics == "acoustic" else {"invlambda": 0, "invmu": 1, "rho": 2}
     raw = {}
     for k, x in zip(mparams, chunks):
         gr = pa.gradient_raw(pidx[k])

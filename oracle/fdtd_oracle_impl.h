@@ -698,7 +698,57 @@ static void snap_io(ctx *c, int ishot, int tau, int dir) {
 /* ------------------------------------------------------------------ */
 /* gradient (src/fdtd/gradient.jl:17-64), acoustic 2-D                 */
 /* ------------------------------------------------------------------ */
-static void compute_gradient(ctx *c, REAL *gK, REAL *gR) {
+static void compute_gradient_elastic(ctx *c, REAL *gL, REAL *gM, REAL *gR);
+
+static void rho_gather(ctx *c, REAL *gR) {
+  const int three = c->d.ndim == 3;
+  /* FD-consistent rho term (no reference counterpart): rho at cell
+   * (R, [Y,] C) enters the update coefficient dt / avg(rho) of the
+   * velocity cells two and three cells further along each axis (vx
+   * (R, C+2), (R, C+3); vz (R+2, C), (R+3, C); vy (Y+2), (Y+3):
+   * store_invav averages rho at i-3 and i-2 for velocity cell i), each
+   * with weight 1/2 and only where that velocity cell is updated (the
+   * @inn domain of update_v!: rows 4..nz-3 for vx and vy, 4..nz for vz,
+   * and so on along each axis). */
+  arr bx = c->vbuf[0], bz = c->vbuf[1], by = c->vbuf[2];
+  const int nz = c->d.nz, nx = c->d.nx, ny = three ? c->d.ny : 1;
+  /* update domains: [lo, hi] per axis (z, y, x) of vx, vy, vz */
+  const int hz = nz - 3, hyy = ny - 3, hx = nx - 3;
+#define IN(a, lo, hi) ((a) >= (lo) && (a) <= (hi))
+  for (int C = 1; C <= nx; C++)
+    for (int Y = 1; Y <= ny; Y++)
+      for (int R = 1; R <= nz; R++) {
+        const int yin = !three || IN(Y, 4, hyy);
+        REAL avx = 0, avz = 0, avy = 0;
+        if (IN(R, 4, hz) && yin) {
+          REAL b2 = IN(C + 2, 4, nx) ? AT(bx, R, Y, C + 2) : (REAL)0;
+          REAL b3 = IN(C + 3, 4, nx) ? AT(bx, R, Y, C + 3) : (REAL)0;
+          avx = (b2 + b3) * (REAL)0.5;
+        }
+        if (IN(C, 4, hx) && yin) {
+          REAL b2 = IN(R + 2, 4, nz) ? AT(bz, R + 2, Y, C) : (REAL)0;
+          REAL b3 = IN(R + 3, 4, nz) ? AT(bz, R + 3, Y, C) : (REAL)0;
+          avz = (b2 + b3) * (REAL)0.5;
+        }
+        if (three && IN(R, 4, hz) && IN(C, 4, hx)) {
+          REAL b2 = IN(Y + 2, 4, ny) ? AT(by, R, Y + 2, C) : (REAL)0;
+          REAL b3 = IN(Y + 3, 4, ny) ? AT(by, R, Y + 3, C) : (REAL)0;
+          avy = (b2 + b3) * (REAL)0.5;
+        }
+        const size_t gi = ((size_t)(C - 1) * ny + (Y - 1)) * nz + (R - 1);
+        REAL gv = gR[gi] - avx;
+        if (three) gv = gv - avy;
+        gR[gi] = gv - avz;
+      }
+#undef IN
+}
+
+
+static void compute_gradient(ctx *c, REAL *gK, REAL *gR, REAL *g3) {
+  if (c->d.physics == GPO_ELASTIC) {
+    compute_gradient_elastic(c, gK, gR, g3);
+    return;
+  }
   const int h = c->h;
   const REAL dtI = c->dtI;
   arr p1 = c->w[0][GPO_P], p1p = c->wp[0][GPO_P], p2p = c->wp[1][GPO_P];
@@ -712,45 +762,7 @@ static void compute_gradient(ctx *c, REAL *gK, REAL *gR) {
     for (size_t i = 0; i < alen(vf); i++) bf.a[i] = vap.a[i] * (vf.a[i] - vfp.a[i]) * dtI;
   }
   if (c->imaging) {
-    /* FD-consistent rho term (no reference counterpart): rho at cell
-     * (R, [Y,] C) enters the update coefficient dt / avg(rho) of the
-     * velocity cells two and three cells further along each axis (vx
-     * (R, C+2), (R, C+3); vz (R+2, C), (R+3, C); vy (Y+2), (Y+3):
-     * store_invav averages rho at i-3 and i-2 for velocity cell i), each
-     * with weight 1/2 and only where that velocity cell is updated (the
-     * @inn domain of update_v!: rows 4..nz-3 for vx and vy, 4..nz for vz,
-     * and so on along each axis). */
-    arr bx = c->vbuf[0], bz = c->vbuf[1], by = c->vbuf[2];
-    const int nz = c->d.nz, nx = c->d.nx, ny = three ? c->d.ny : 1;
-    /* update domains: [lo, hi] per axis (z, y, x) of vx, vy, vz */
-    const int hz = nz - 3, hyy = ny - 3, hx = nx - 3;
-#define IN(a, lo, hi) ((a) >= (lo) && (a) <= (hi))
-    for (int C = 1; C <= nx; C++)
-      for (int Y = 1; Y <= ny; Y++)
-        for (int R = 1; R <= nz; R++) {
-          const int yin = !three || IN(Y, 4, hyy);
-          REAL avx = 0, avz = 0, avy = 0;
-          if (IN(R, 4, hz) && yin) {
-            REAL b2 = IN(C + 2, 4, nx) ? AT(bx, R, Y, C + 2) : (REAL)0;
-            REAL b3 = IN(C + 3, 4, nx) ? AT(bx, R, Y, C + 3) : (REAL)0;
-            avx = (b2 + b3) * (REAL)0.5;
-          }
-          if (IN(C, 4, hx) && yin) {
-            REAL b2 = IN(R + 2, 4, nz) ? AT(bz, R + 2, Y, C) : (REAL)0;
-            REAL b3 = IN(R + 3, 4, nz) ? AT(bz, R + 3, Y, C) : (REAL)0;
-            avz = (b2 + b3) * (REAL)0.5;
-          }
-          if (three && IN(R, 4, hz) && IN(C, 4, hx)) {
-            REAL b2 = IN(Y + 2, 4, ny) ? AT(by, R, Y + 2, C) : (REAL)0;
-            REAL b3 = IN(Y + 3, 4, ny) ? AT(by, R, Y + 3, C) : (REAL)0;
-            avy = (b2 + b3) * (REAL)0.5;
-          }
-          const size_t gi = ((size_t)(C - 1) * ny + (Y - 1)) * nz + (R - 1);
-          REAL gv = gR[gi] - avx;
-          if (three) gv = gv - avy;
-          gR[gi] = gv - avz;
-        }
-#undef IN
+    rho_gather(c, gR);
     return;
   }
   /* combine_gmodrho!: @inn(g) = @inn(g) - @av_xi(vxbuf) - @av_zi(vzbuf).
@@ -775,17 +787,85 @@ static void compute_gradient(ctx *c, REAL *gK, REAL *gR) {
       }
 }
 
+/* imaging condition of the discrete elastic scheme (gpo.h, GPO_ADJOINT_HIST) */
+static void compute_gradient_elastic(ctx *c, REAL *gL, REAL *gM, REAL *gR) {
+  const int three = c->d.ndim == 3, h = c->h;
+  const REAL dt = c->dt, dtI = c->dtI;
+  arr M = c->dmod[c->ndmod - 2], L = c->dmod[c->ndmod - 1], imu = c->mod[1];
+  const int nid3[3] = {GPO_TAUXX, GPO_TAUYY, GPO_TAUZZ}, nid2[2] = {GPO_TAUXX, GPO_TAUZZ};
+  const int *nid = three ? nid3 : nid2;
+  const int d = three ? 3 : 2;
+  const size_t n = alen(c->w[0][GPO_TAUXX]);
+  for (size_t i = 0; i < n; i++) {
+    REAL q[3], dT[3], a[3], b[3], sq = 0, sT = 0;
+    for (int k = 0; k < d; k++) {
+      q[k] = c->wp[1][nid[k]].a[i];
+      dT[k] = c->wp[0][nid[k]].a[i] - c->w[0][nid[k]].a[i];
+      sq = sq + q[k];
+      sT = sT + dT[k];
+    }
+    const REAL beta = L.a[i], alpha = M.a[i] - L.a[i];
+    const REAL cq = beta / (alpha + (REAL)d * beta);
+    REAL sa = 0, sb = 0, ab = 0;
+    for (int k = 0; k < d; k++) {
+      a[k] = (q[k] - cq * sq) / alpha;
+      b[k] = (dT[k] - cq * sT) / alpha;
+      sa = sa + a[k];
+      sb = sb + b[k];
+      ab = ab + a[k] * b[k];
+    }
+    gL[i] = gL[i] + sa * sb * (beta * beta * dtI);
+    gM[i] = gM[i] + ab * ((REAL)2 * dt / (imu.a[i] * imu.a[i]));
+  }
+  /* shear cells: a quarter of q_s dT_s / dt to each invmu cell of the
+   * cell's average (store_invav4) */
+  arr g;
+  g.a = gM;
+  g.n1 = c->d.nz;
+  g.n2 = three ? c->d.ny : 1;
+  g.n3 = c->d.nx;
+  const int sid[3] = {GPO_TAUXZ, GPO_TAUXY, GPO_TAUYZ};
+  for (int k = 0; k < (three ? 3 : 1); k++) {
+    arr qa = c->wp[1][sid[k]], t0 = c->wp[0][sid[k]], t1 = c->w[0][sid[k]];
+    for (int ix = 1; ix <= qa.n3; ix++)
+      for (int iy = 1; iy <= qa.n2; iy++)
+        for (int iz = 1; iz <= qa.n1; iz++) {
+          const REAL v = AT(qa, iz, iy, ix) * (AT(t0, iz, iy, ix) - AT(t1, iz, iy, ix)) * dtI * (REAL)0.25;
+          /* the four cells (z, y, x) of the average and the two axes it spans */
+          int z = iz, y = iy, x = ix, a1 = 0, a2 = 2; /* z and x */
+          if (three && k == 0) y = iy + h;                 /* @av_xzi */
+          if (three && k == 1) z = iz + h, a1 = 1, a2 = 2; /* @av_xyi: y and x */
+          if (three && k == 2) x = ix + h, a1 = 0, a2 = 1; /* @av_yzi: z and y */
+          for (int u = 0; u < 2; u++)
+            for (int w = 0; w < 2; w++) {
+              int zz = z, yy = y, xx = x;
+              if (a1 == 0) zz += u; else yy += u;
+              if (a2 == 2) xx += w; else yy += w;
+              AT(g, zz, yy, xx) = AT(g, zz, yy, xx) + v;
+            }
+        }
+  }
+  /* rho: the velocity terms of the discrete model (gpo_set_imaging 1) */
+  const int vids[3] = {GPO_VX, GPO_VZ, GPO_VY};
+  for (int q = 0; q < 2 + three; q++) {
+    arr vf = c->w[0][vids[q]], vfp = c->wp[0][vids[q]], vap = c->wp[1][vids[q]], bf = c->vbuf[q];
+    for (size_t i = 0; i < alen(vf); i++) bf.a[i] = vap.a[i] * (vf.a[i] - vfp.a[i]) * dtI;
+  }
+  rho_gather(c, gR);
+}
+
 static void save_tp(ctx *c, int ipw);
 
-/* forward history (GPO_FORWARD_HIST): slot s holds p after step s and the
- * velocities after step s (s = nt + 1: after the extra half step) */
+/* forward history (GPO_FORWARD_HIST): slot s holds the stresses (p) after
+ * step s and the velocities after step s (s = nt + 1: after the extra half
+ * step) */
+static int is_stress_field(int f) { return f == GPO_P || f >= GPO_TAUXX; }
 static void hist_io(ctx *c, int ishot, int s, int dir, int with_p) {
   REAL *b = c->hist[ishot] + (size_t)s * c->hstep;
-  const int ids[4] = {GPO_P, GPO_VX, GPO_VY, GPO_VZ};
-  for (int q = 0; q < 4; q++) {
-    if (!c->present[ids[q]]) continue;
-    arr f = c->w[0][ids[q]];
-    if (q > 0 || with_p) {
+  for (int q = 0; q < GPO_NFIELD; q++) {
+    if (!c->present[q]) continue;
+    arr f = c->w[0][q];
+    if (!is_stress_field(q) || with_p) {
       if (dir == 0)
         memcpy(b, f.a, alen(f) * sizeof(REAL));
       else
@@ -797,15 +877,21 @@ static void hist_io(ctx *c, int ishot, int s, int dir, int with_p) {
 /* wavefield 1 of adjoint step it from the history: tp = (-p_s, v_{s+1}),
  * t = (-p_{s-1}, v_s) with s = nt - it + 1, as the time-reversed run holds
  * them (p reversed in sign, velocities not) */
+static void negate_stresses(ctx *c) {
+  for (int q = 0; q < GPO_NFIELD; q++)
+    if (c->present[q] && is_stress_field(q)) {
+      arr f = c->w[0][q];
+      for (size_t i = 0; i < alen(f); i++) f.a[i] = -f.a[i];
+    }
+}
 static void hist_states(ctx *c, int ishot, int it) {
   const int s = c->d.nt - it + 1;
-  arr p = c->w[0][GPO_P];
   hist_io(c, ishot, s, 1, 1);
-  for (size_t i = 0; i < alen(p); i++) p.a[i] = -p.a[i];
+  negate_stresses(c);
   hist_io(c, ishot, s + 1, 1, 0);
   save_tp(c, 0);
   hist_io(c, ishot, s - 1, 1, 1);
-  for (size_t i = 0; i < alen(p); i++) p.a[i] = -p.a[i];
+  negate_stresses(c);
   hist_io(c, ishot, s, 1, 0);
 }
 
@@ -892,9 +978,8 @@ gpo_ctx *SFX(gpo_create)(const gpo_desc *d, const void *const *mod, const void *
   c->vbuf[1] = field_arr(c, GPO_VZ);
   if (d->ndim == 3) c->vbuf[2] = field_arr(c, GPO_VY);
   c->hstep = 0;
-  if (c->present[GPO_P])
-    for (int f = 0; f < 4; f++)
-      if (c->present[f]) c->hstep += alen(c->w[0][f]);
+  for (int f = 0; f < GPO_NFIELD; f++)
+    if (c->present[f]) c->hstep += alen(c->w[0][f]);
   c->pvlen = maxlen;
   c->pv = (REAL *)calloc(maxlen, sizeof(REAL));
   c->pvflag = (unsigned char *)calloc(maxlen, 1);
@@ -948,7 +1033,7 @@ static void born_add(arr dst, arr r, arr now, arr prev) {
 
 /* mod_x_proc! for one supersource (src/fdtd/propagate.jl:138-261) */
 int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec, gpo_proj *rec,
-                  int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho) {
+                  int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho, void *grad_3) {
   ctx *c = (ctx *)cc;
   if (ishot < 0 || ishot >= c->nshots) return -1;
 #ifdef _OPENMP
@@ -959,7 +1044,7 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
   const int adjoint = mode == GPO_ADJOINT || mode == GPO_ADJOINT_HIST;
   if ((mode == GPO_FORWARD_SAVE || mode == GPO_ADJOINT) && !c->bstore[ishot])
     c->bstore[ishot] = (REAL *)calloc((size_t)nt * c->bstep + c->bsnap, sizeof(REAL));
-  if (hist && (c->d.physics != GPO_ACOUSTIC || !c->hstep)) return -2;
+  if (hist && c->d.physics != GPO_ACOUSTIC && (c->d.free_faces & GPO_ZMIN)) return -2;
   if (mode == GPO_FORWARD_HIST && !c->hist[ishot])
     c->hist[ishot] = (REAL *)calloc((size_t)(nt + 2) * c->hstep, sizeof(REAL));
   if (mode == GPO_ADJOINT_HIST && !c->hist[ishot]) return -3;
@@ -1028,7 +1113,7 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
       if (is_stress_src(src[s].field)) add_stress_source(c, c->w[0], &src[s], it - 1);
     if (mode == GPO_FORWARD_SAVE) boundary_save(c, ishot, it);
     if (mode == GPO_FORWARD_HIST) hist_io(c, ishot, it, 0, 1);
-    if (adjoint && (grad_invK || grad_rho)) compute_gradient(c, (REAL *)grad_invK, (REAL *)grad_rho);
+    if (adjoint && (grad_invK || grad_rho)) compute_gradient(c, (REAL *)grad_invK, (REAL *)grad_rho, (REAL *)grad_3);
     /* snaps_save! for wavefield 1 at the end of step it (propagate.jl:238-245) */
     for (int k = 0; k < c->nsnap; k++)
       if (c->snap_its[k] == it) {

@@ -102,9 +102,23 @@ gpo_ctx *gpo_create_f64(const gpo_desc *d, const void *const *mod, const void *c
  * with GPO_ADJOINT_HIST): two extended-grid arrays {invK, rho} that the
  * shot's gradient is ADDED to. */
 int gpo_shot_f32(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec,
-                 gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho);
+                 gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho, void *grad_3);
 int gpo_shot_f64(gpo_ctx *c, int ishot, int mode, int nsrc, const gpo_proj *src, int nrec,
-                 gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho);
+                 gpo_proj *rec, int nadj, const gpo_proj *adj, void *grad_invK, void *grad_rho, void *grad_3);
+/* Elastic media (GPO_ADJOINT_HIST only, no free surface): the three arrays
+ * are the gradients with respect to {invlambda, invmu, rho}, from the
+ * imaging condition of the discrete elastic scheme (no reference
+ * counterpart: the reference defines gradients for 2-D acoustic media
+ * only, src/fdtd/gradient.jl:17-64):
+ *   normal-stress cells, with K = (dtM - dtl) I + dtl 1 1' the cell's
+ *   stiffness, q the adjoint normal stresses before the adjoint step and
+ *   dT the forward normal-stress decrease of the forward step,
+ *   a = K^-1 q, b = K^-1 dT:
+ *     g_invlambda += (sum a)(sum b) dtl^2 / dt
+ *     g_invmu     += (a . b) 2 dt / invmu^2
+ *   shear cells: each of the four invmu cells of the cell's average gains
+ *     q_s dT_s / (4 dt)
+ *   velocity cells: the rho term of gpo_set_imaging mode 1. */
 /* Imaging condition of the rho gradient: 0 the reference's
  * (src/fdtd/gradient.jl:31-56); 1 the gradient of the discrete model, over
  * the velocity cells whose update coefficient holds rho (no reference

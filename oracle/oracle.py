@@ -51,7 +51,8 @@ def lib():
             getattr(_LIB, "gpo_create_" + sfx).argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
             getattr(_LIB, "gpo_shot_" + sfx).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
-                                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+                                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                        ctypes.c_void_p]
             getattr(_LIB, "gpo_get_field_" + sfx).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
             getattr(_LIB, "gpo_destroy_" + sfx).argtypes = [ctypes.c_void_p]
         _LIB.gpo_get_dmod_f32.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
@@ -197,12 +198,13 @@ class Oracle:
         sp = self._projs(srcs, nt)
         rp = self._projs(recs, nt)
         ap = self._projs(adjs, nt)
-        gK = gR = None
+        gs = [None, None, None]
         if grads is not None:
-            gK, gR = grads
+            for i, g in enumerate(grads):
+                gs[i] = g
         rc = getattr(self.L, "gpo_shot_" + self.sfx)(
             self.ctx, ishot, mode, len(srcs), sp, len(recs), rp, len(adjs), ap,
-            None if gK is None else gK.ctypes.data, None if gR is None else gR.ctypes.data)
+            *[None if g is None else g.ctypes.data for g in gs])
         self._keep = self._keep[: 0]
         if rc != 0:
             raise RuntimeError("oracle shot failed: %d" % rc)
@@ -301,14 +303,16 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
     prep = Prepared(ex, dtype, ref_compat)
     if mod is not None:
         prep.mod = [np.asarray(m, np.float32) for m in mod]
+    if prep.physics == "elastic" and not history:
+        raise ValueError("elastic gradients: history mode only (no boundary store in 3-D)")
     orc = Oracle(prep, nthreads)
     if imaging:
         fn = getattr(orc.L, "gpo_set_imaging_" + orc.sfx)
         fn.argtypes = [ctypes.c_void_p, ctypes.c_int]
         assert fn(orc.ctx, int(imaging)) == 0
     shape = prep.shape
-    gK = np.zeros(shape, dtype=dtype, order="F")
-    gR = np.zeros(shape, dtype=dtype, order="F")
+    names = ["invK", "rho"] if prep.physics == "acoustic" else ["invlambda", "invmu", "rho"]
+    gs = [np.zeros(shape, dtype=dtype, order="F") for _ in names]
     dcal = {f: [] for f in ex["rfields"]}
     # forward_save with src_types [1, 0]
     for i, shot in enumerate(ex["shots"]):
@@ -325,17 +329,17 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
         for f in ex["rfields"]:
             a = S.l2_deriv(dobs[f][i], dcal[f][i])[::-1].copy()
             adj.append((f, prep.proj(f, shot["rec"]), a))
-        orc.shot(i, 4 if history else 2, src, [], adj, (gK, gR))
+        orc.shot(i, 4 if history else 2, src, [], adj, gs)
     orc.close()
-    raw = {"invK": gK.copy(), "rho": gR.copy()}
+    raw = {k: g.copy() for k, g in zip(names, gs)}
     inner = []
-    names = "zyx" if prep.ndim == 3 else "zx"
-    for i, d in enumerate(names):
+    axes = "zyx" if prep.ndim == 3 else "zx"
+    for i, d in enumerate(axes):
         lo = prep.npml if prep.faces & S.FACE_BITS[d + "min"] else 0
         hi = prep.npml if prep.faces & S.FACE_BITS[d + "max"] else 0
         inner.append(slice(lo, shape[i] - hi))
     inner = tuple(inner)
-    g = {"invK": (raw["invK"] * prep.mod[0])[inner], "rho": (raw["rho"] * prep.mod[1])[inner]}
+    g = {k: (raw[k] * prep.mod[i])[inner] for i, k in enumerate(names)}
     return loss, g, dcal, raw
 
 
