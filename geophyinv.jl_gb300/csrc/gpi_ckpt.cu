@@ -353,6 +353,47 @@ __global__ void __launch_bounds__(256) k_grad_e3(const GradE3Args a) {
   }
 }
 
+// The source terms at the cells of explosive sources (stress kind): the
+// forward step added A = dtM pv to every normal stress there, so the stress
+// decrease is K e - A 1 and dtM also multiplies the source; with
+// sa = sum(K^-1 q) and corr = A / (dtM + 2 dtl):
+//   g_invlambda += sa (3 corr - A / dtM) dtl^2 / dt
+//   g_invmu     += sa (corr - A / dtM) 2 dt / invmu^2
+// added right after forward step s (while the cells' amounts are those of
+// step s), before the main kernel's terms.  One thread per shot walks its
+// cells in order (two source fields may share a cell).
+struct GradE3SrcArgs {
+  int64_t fs;
+  int nshots;
+  const InjCell *cells;
+  const int32_t *gptr;  // wavefield 1's groups
+  const float *amount;
+  const float *Y[3], *dtM, *dtl, *invmu;  // Y: adjoint txx, tyy, tzz
+  float *gL, *gM;
+  float dt, dtI;
+};
+
+__global__ void k_grad_e3_src(const GradE3SrcArgs a) {
+  const int shot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (shot >= a.nshots) return;
+  const int g = shot * NKIND + 3;
+  const int64_t so = shot * a.fs;
+  for (int k = a.gptr[g]; k < a.gptr[g + 1]; k++) {
+    const int64_t lo = a.cells[k].off, o = so + lo;
+    const float A = a.amount[k];
+    float sq = 0.f;
+    sq = sq + a.Y[0][o];
+    sq = sq + a.Y[1][o];
+    sq = sq + a.Y[2][o];
+    const float beta = a.dtl[lo], alpha = a.dtM[lo] - a.dtl[lo];
+    const float sa = sq / (alpha + 3.0f * beta);
+    const float corr = A / (alpha + 3.0f * beta), own = A / a.dtM[lo];
+    const float im = a.invmu[lo];
+    a.gL[o] = a.gL[o] + sa * (3.0f * corr - own) * (beta * beta * a.dtI);
+    a.gM[o] = a.gM[o] + sa * (corr - own) * (2.0f * a.dt / (im * im));
+  }
+}
+
 // k_grad_a2 with wavefield 1 given explicitly (k_adjoint2d.cu)
 int grad_a2_launch(Plan *p, const float *p1A, const float *p1B, const float *vx1A, const float *vx1B,
                    const float *vz1A, const float *vz1B);
@@ -383,6 +424,27 @@ static int turn(Plan *p, int s) {
     if (p->present[f] && f != GPI_VX && f != GPI_VY && f != GPI_VZ)
       GPI_CUDA(p, cudaMemcpyAsync(X[f], W[f], bytes, cudaMemcpyDeviceToDevice, p->stream));
   if ((rc = step3_wavefield(p, 0, 0))) return rc;
+  if (ela && p->n_cells > 0) {
+    GradE3SrcArgs sa;
+    sa.fs = p->fstride;
+    sa.nshots = p->d.nshots;
+    sa.cells = p->d_cells;
+    sa.gptr = p->d_group_ptr;
+    sa.amount = p->d_amount;
+    sa.Y[0] = p->state[0][1][GPI_TAUXX];
+    sa.Y[1] = p->state[0][1][GPI_TAUYY];
+    sa.Y[2] = p->state[0][1][GPI_TAUZZ];
+    sa.dtM = p->coef[6];
+    sa.dtl = p->coef[7];
+    sa.invmu = p->mod[1];
+    sa.gL = p->grad[0];
+    sa.gM = p->grad[1];
+    sa.dt = (float)p->d.dt;
+    sa.dtI = (float)(1.0 / p->d.dt);
+    k_grad_e3_src<<<(p->d.nshots + 63) / 64, 64, 0, p->stream>>>(sa);
+    p->launches++;
+    GPI_CUDA(p, cudaGetLastError());
+  }
   for (int d = 0; d < 3; d++)
     GPI_CUDA(p, cudaMemcpyAsync(X[vf[d]], W[vf[d]], bytes, cudaMemcpyDeviceToDevice, p->stream));  // V_s
   if (s < nt && (rc = aux_step2(p, s + 1, j))) return rc;

@@ -168,7 +168,52 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
       }
     }
   };
-  if (issuer) issue(xbase + RING - 1);
+  // interior and band tiles: each issuing lane keeps the source pointers of
+  // its share of a column (at most three copies: fields advance by NZP per
+  // column, z-strip CPML windows by zsw) and advances them per issue
+  constexpr bool PROD = MODE <= 1;
+  const float *fs0 = nullptr, *fs1 = nullptr, *fs2 = nullptr;
+  int fd0 = 0, fd1 = 0, fd2 = 0, fst2 = NZP;
+  uint32_t fn0 = 0, fn1 = 0, fn2 = 0;
+  if constexpr (PROD) {
+    const int64_t oV = S(z0, xbase);
+    if (wq == 0) {
+      fs0 = a.pA + so + S(z0 - 4, xbase), fd0 = 0, fn0 = R8 * 4;
+    } else if (wq == 1) {
+      fs0 = a.vxA + so + oV, fs1 = a.vzA + so + oV;
+      fd0 = R8, fd1 = R8 + R4, fn0 = fn1 = R4 * 4;
+    } else if (wq == 2) {
+      fs0 = a.cx + oV, fd0 = R8 + 2 * R4, fn0 = R4 * 4;
+    } else {
+      fs0 = a.cz + oV, fs1 = a.dtK + oV;
+      fd0 = R8 + 3 * R4, fd1 = R8 + 4 * R4, fn0 = R4 * 4, fn1 = TZ * 4;
+    }
+    if (!FAST && zt && wq >= 2) {
+      // z-strip CPML windows: warp 2 dpdz, warp 3 dvzdz
+      const float *pz = psA(wq == 2 ? 1 : 3) + ZS(xbase, zoff);
+      const int dz = SLOT + (wq - 2) * PZW;
+      if (wq == 2)
+        fs1 = pz, fd1 = dz, fn1 = PZW * 4;
+      else
+        fs2 = pz, fd2 = dz, fn2 = PZW * 4, fst2 = a.zsw;
+    }
+  }
+  const int fst1 = (!FAST && zt && wq == 2) ? a.zsw : NZP;
+  // the next column of this warp's share into ring slot sl
+  auto issue_fast = [&](int sl) {
+    float *d = ring + sl * SL;
+    mbar_expect_tx(&bar[sl], fn0 + fn1 + fn2);
+    bulk_g2s(d + fd0, fs0, fn0, &bar[sl]);
+    if (fn1) bulk_g2s(d + fd1, fs1, fn1, &bar[sl]);
+    if (fn2) bulk_g2s(d + fd2, fs2, fn2, &bar[sl]);
+    fs0 += NZP, fs1 += fst1, fs2 += fst2;
+  };
+  if constexpr (PROD) {
+    if (issuer)
+      for (int sl = 0; sl < RING && xbase + sl <= xlast; sl++) issue_fast(sl);
+  } else {
+    if (issuer) issue(xbase + RING - 1);
+  }
   auto wait_col = [&](int cc) {
     const int j = cc - xbase;
     if (!mbar_wait(&bar[j % RING], (j / RING) & 1)) s_err = 1;
@@ -226,49 +271,64 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
     return on ? D * __ldg(cf + 4 * npml + j) + psi : D;
   };
 
+  // the interior code: every row inside every update domain, no CPML, no
+  // face, no source (interior tiles, and the clean warps of band tiles);
+  // global offsets of this thread's rows, advanced one column per
+  // iteration: velocities of column xbase+3+it, pressure of column xbase+it
+  int64_t ov = so + S(q, xbase + 3), os = so + S(r, xbase);
+  // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
+  auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
+    if (!vact) return;
+    const int k = kq, kk = kq + 4;
+    const float *pc = ring + s0 * SL, *v0 = pc + R8;
+    const float vz = v0[R4 + k] + v0[3 * R4 + k] * (st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI);
+    svz[s0 * R4 + k] = vz;
+    if (kq < TZ) {
+      const float *p3 = ring + s3 * SL, *p2 = ring + s2 * SL, *p1 = ring + s1 * SL;
+      const float vx = v0[k] + v0[2 * R4 + k] * (st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI);
+      svx[s0 * R4 + k] = vx;
+      if (cc < x1) {
+        a.vxB[ov] = vx;
+        a.vzB[ov] = vz;
+      }
+    }
+  };
+  // pressure of column c from velocity slots s0..s3 = columns c..c+3
+  auto str_fast = [&](int c, int s0, int s1, int s2, int s3) {
+    if (t >= TZ) return;
+    const int k = t;
+    const float *pc = ring + s0 * SL;
+    const float *w = svz + s0 * R4;
+    const float Dx = st4(svx[s0 * R4 + k], svx[s1 * R4 + k], svx[s2 * R4 + k], svx[s3 * R4 + k]) * a.dxI;
+    const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
+    a.pB[os] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
+  };
+
   // Dispatch per warp and per column: a warp runs the straight-line code
   // unless one of its rows or the current column touches a CPML strip, a
   // rigid face, a domain edge or a source cell.
   if constexpr (FAST) {
     // interior tile: inside every update domain, no CPML, no face, no
     // source.
-    // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
-    auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
-      if (!vact) return;
-      const int k = kq, kk = kq + 4;
-      const float *pc = ring + s0 * SLOT, *v0 = pc + R8;
-      const float vz = v0[R4 + k] + v0[3 * R4 + k] * (st4(pc[kk - 3], pc[kk - 2], pc[kk - 1], pc[kk]) * a.dzI);
-      svz[s0 * R4 + k] = vz;
-      if (kq < TZ) {
-        const float *p3 = ring + s3 * SLOT, *p2 = ring + s2 * SLOT, *p1 = ring + s1 * SLOT;
-        const float vx = v0[k] + v0[2 * R4 + k] * (st4(p3[kk], p2[kk], p1[kk], pc[kk]) * a.dxI);
-        svx[s0 * R4 + k] = vx;
-        if (cc < x1) {
-          const int64_t o = so + S(q, cc);
-          a.vxB[o] = vx;
-          a.vzB[o] = vz;
-        }
-      }
-    };
-    // pressure of column c from velocity slots s0..s3 = columns c..c+3
-    auto str_fast = [&](int c, int s0, int s1, int s2, int s3) {
-      if (t >= TZ) return;
-      const int k = t;
-      const float *pc = ring + s0 * SLOT;
-      const float *w = svz + s0 * R4;
-      const float Dx = st4(svx[s0 * R4 + k], svx[s1 * R4 + k], svx[s2 * R4 + k], svx[s3 * R4 + k]) * a.dxI;
-      const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
-      a.pB[so + S(r, c)] = pc[k + 4] + (Dx + Dz) * pc[R8 + 4 * R4 + k];
-    };
-    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
+    // iteration it handles column c = xbase + it: slot(c + m) = (it + m) %
+    // RING; unrolled by RING so that every slot index is a constant (base is
+    // a multiple of RING; a slot's mbarrier parity flips once per RING
+    // columns)
     const int ncol = x1 - xbase;
-    for (int it = 0; it < ncol; it++) {
-      const int c = xbase + it;
-      if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
-      vel_fast(c + 3, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
-      __syncthreads();
-      if (issuer) issue(c + RING - 1);
-      if (c >= x0) str_fast(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING);
+    for (int base = 0; base < ncol; base += RING) {
+      const uint32_t ph = (uint32_t)(base / RING) & 1u;
+#pragma unroll
+      for (int u = 0; u < RING; u++) {
+        const int it = base + u;
+        if (it >= ncol) break;
+        const int c = xbase + it;
+        if (!mbar_wait(&bar[(u + 3) % RING], ph ^ (uint32_t)((u + 3) / RING))) s_err = 1;
+        vel_fast(c + 3, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+        __syncthreads();
+        if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
+        if (c >= x0) str_fast(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+        ov += NZP, os += NZP;
+      }
     }
   } else {
   // columns that need the full general code: x edges and mirrors, sources
@@ -291,6 +351,27 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
   const bool gok = lane + gdl >= 0 && lane + gdl < 32;
   const int glane = gok ? lane + gdl : lane;
   const bool gany = __any_sync(0xffffffffu, gsrc != 0);
+  // band tiles: a warp whose rows (velocity rows with the halo lanes, and
+  // pressure rows) meet no strip, face, domain end or source cell runs the
+  // interior code
+  bool cleanr = true;
+  if (vact) cleanr = (kq < TZ ? vxr : true) && vzr && jq1 < 0 && gsrc == 0;
+  if (t < TZ) cleanr = cleanr && srow && jr3 < 0;
+  bool srcw = false;
+  if (MODE == 1 && (t & 31) == 0) {
+    const int wr0 = z0 + (t & ~31), wr1 = wr0 + 31;
+    for (int kd = 0; kd < 3 && !srcw; kd++)
+      for (int i2 = s_rng[kd][0]; i2 < s_rng[kd][1]; i2++) {
+        const InjCell &cl = a.cells[i2];
+        if (cl.col > x1 + 2) break;
+        if (cl.row >= wr0 && cl.row <= wr1) {
+          srcw = true;
+          break;
+        }
+      }
+  }
+  srcw = __shfl_sync(0xffffffffu, srcw, 0);
+  const bool fastw = MODE == 1 && !a.vonly && __all_sync(0xffffffffu, cleanr) && !srcw;
   {
     // vz at row qq of column cc before its source (source of a mirror row)
     auto vz_any = [&](int qq, int cc) -> float {
@@ -360,7 +441,37 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
       if (bs < es) inject(a.cells, a.amount, bs, es, r, pn);  // add_stress_source!
       if (srow) a.pB[so + S(r, c)] = pn;
     };
-    if constexpr (MODE == 1 || MODE == 2) {
+    if constexpr (MODE == 1) {
+      // unrolled by RING: constant slot indices (see the interior loop)
+      const int ncol = x1 - xbase;
+      for (int base = 0; base < ncol; base += RING) {
+        const uint32_t ph = (uint32_t)(base / RING) & 1u;
+#pragma unroll
+        for (int u = 0; u < RING; u++) {
+          const int it = base + u;
+          if (it >= ncol) break;
+          const int c = xbase + it, cc = c + 3;
+          int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+          cvx.range(a.cells, cc, ib0, ie0);
+          cvz.range(a.cells, cc, ib1, ie1);
+          if (c >= x0) cst.range(a.cells, c, bs, es);
+          if (!mbar_wait(&bar[(u + 3) % RING], ph ^ (uint32_t)((u + 3) / RING))) s_err = 1;
+          if (fastw)
+            vel_fast(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+          else
+            vel_band(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, ib0, ie0, ib1, ie1);
+          __syncthreads();
+          if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
+          if (c >= x0) {
+            if (fastw)
+              str_fast(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+            else
+              str_band(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, bs, es);
+          }
+          ov += NZP, os += NZP;
+        }
+      }
+    } else if constexpr (MODE == 2) {
       // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
       const int ncol = x1 - xbase;
       for (int it = 0; it < ncol; it++) {

@@ -356,55 +356,56 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
   // ---- prologue: stresses of columns x0-3 .. x0-1 ----
   for (int cc = xbase; cc < x0 && cc <= xlast; cc++) wait_col(cc);
 
+  // the interior code: every row inside every update domain, no CPML, no
+  // face, no source (interior tiles, and the clean warps of band tiles)
+  // global addresses of this thread's rows, advanced one column per
+  // iteration: velocities of column xbase+3+it, stresses of column xbase+it
+  int64_t ov = so + S(q, xbase + 3), os = so + S(z0 + t, xbase);
+  // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
+  auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
+    if (!vact) return;
+    const int k = kq, kk = kq + 4;
+    const float *b3 = ring + s3 * SL, *b2 = ring + s2 * SL, *b1 = ring + s1 * SL, *b0 = ring + s0 * SL;
+    const float *v0 = b0 + 3 * R8, *z3 = b3 + 2 * R8, *zz = b0 + R8;
+    const float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
+    const float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
+    const float vx = v0[k] - v0[2 * R4 + k] * (Dx + Dz);
+    const float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
+    const float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
+    const float vz = v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2);
+    svx[s0 * R4 + k] = vx;
+    svz[s0 * R4 + k] = vz;
+    if (cc < x1 && kq < TZ) {
+      a.vxB[ov] = vx;
+      a.vzB[ov] = vz;
+    }
+  };
+  // stresses of column c from velocity slots s0..s3 = columns c..c+3
+  auto str_fast = [&](int c, int s0, int s1, int s2, int s3) {
+    if (t >= TZ) return;
+    const int k = t;
+    const float *u0 = svx + s0 * R4, *u1 = svx + s1 * R4, *u2 = svx + s2 * R4, *u3 = svx + s3 * R4;
+    const float *w0 = svz + s0 * R4, *w1 = svz + s1 * R4, *w2 = svz + s2 * R4, *w3 = svz + s3 * R4;
+    const float *bc = ring + s0 * SL, *cf = bc + 3 * R8 + 4 * R4;
+    const float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
+    const float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
+    const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
+    const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
+    const float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
+    const float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
+    const float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
+    const float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
+    a.txxB[os] = txx;
+    a.tzzB[os] = tzz;
+    a.txzB[os] = txz;
+  };
+
   // Dispatch per warp and per column: a warp runs the straight-line code
   // unless one of its rows or the current column touches a CPML strip, a
   // rigid or free face, a domain edge or a source cell.
   if constexpr (FAST) {
     // interior tile: inside every update domain, no CPML, no face, no
     // source.
-    // global addresses of this thread's rows, advanced one column per
-    // iteration: velocities of column xbase+3+it, stresses of column xbase+it
-    float *pvx = a.vxB + so + S(q, xbase + 3), *pvz = a.vzB + so + S(q, xbase + 3);
-    float *ptxx = a.txxB + so + S(z0 + t, xbase), *ptzz = a.tzzB + so + S(z0 + t, xbase),
-          *ptxz = a.txzB + so + S(z0 + t, xbase);
-    // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
-    auto vel_fast = [&](int cc, int s3, int s2, int s1, int s0) {
-      if (!vact) return;
-      const int k = kq, kk = kq + 4;
-      const float *b3 = ring + s3 * SLOT, *b2 = ring + s2 * SLOT, *b1 = ring + s1 * SLOT, *b0 = ring + s0 * SLOT;
-      const float *v0 = b0 + 3 * R8, *z3 = b3 + 2 * R8, *zz = b0 + R8;
-      const float Dx = st4(b3[kk], b2[kk], b1[kk], b0[kk]) * a.dxI;
-      const float Dz = st4(z3[kk - 3], z3[kk - 2], z3[kk - 1], z3[kk]) * a.dzI;
-      const float vx = v0[k] - v0[2 * R4 + k] * (Dx + Dz);
-      const float Dx2 = st4(z3[kk - 3], b2[2 * R8 + kk - 3], b1[2 * R8 + kk - 3], b0[2 * R8 + kk - 3]) * a.dxI;
-      const float Dz2 = st4(zz[kk - 3], zz[kk - 2], zz[kk - 1], zz[kk]) * a.dzI;
-      const float vz = v0[R4 + k] - v0[3 * R4 + k] * (Dx2 + Dz2);
-      svx[s0 * R4 + k] = vx;
-      svz[s0 * R4 + k] = vz;
-      if (cc < x1 && kq < TZ) {
-        *pvx = vx;
-        *pvz = vz;
-      }
-    };
-    // stresses of column c from velocity slots s0..s3 = columns c..c+3
-    auto str_fast = [&](int c, int s0, int s1, int s2, int s3) {
-      if (t >= TZ) return;
-      const int k = t;
-      const float *u0 = svx + s0 * R4, *u1 = svx + s1 * R4, *u2 = svx + s2 * R4, *u3 = svx + s3 * R4;
-      const float *w0 = svz + s0 * R4, *w1 = svz + s1 * R4, *w2 = svz + s2 * R4, *w3 = svz + s3 * R4;
-      const float *bc = ring + s0 * SLOT, *cf = bc + 3 * R8 + 4 * R4;
-      const float dvxdx = st4(u0[k], u1[k], u2[k], u3[k]) * a.dxI;
-      const float dvzdz = st4(w0[k], w0[k + 1], w0[k + 2], w0[k + 3]) * a.dzI;
-      const float M = cf[k], Lm = cf[TZ + k], mu = cf[2 * TZ + k];
-      const float txx = bc[k + 4] - (M * dvxdx) - (Lm * (dvzdz));
-      const float tzz = bc[R8 + k + 4] - (M * dvzdz) - (Lm * (dvxdx));
-      const float dvxdz = st4(u3[k], u3[k + 1], u3[k + 2], u3[k + 3]) * a.dzI;
-      const float dvzdx = st4(w0[k + 3], w1[k + 3], w2[k + 3], w3[k + 3]) * a.dxI;
-      const float txz = bc[2 * R8 + k + 4] - mu * (dvxdz + dvzdx);
-      *ptxx = txx;
-      *ptzz = tzz;
-      *ptxz = txz;
-    };
     // iteration it handles column c = xbase + it: slot(c + m) = (it + m) %
     // RING.  The loop is unrolled by RING so that every slot index is a
     // constant (base is a multiple of RING; the parity of a slot's mbarrier
@@ -422,8 +423,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
         __syncthreads();
         if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
         if (c >= x0) str_fast(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
-        pvx += NZP, pvz += NZP;
-        ptxx += NZP, ptzz += NZP, ptxz += NZP;
+        ov += NZP, os += NZP;
       }
     }
   } else {
@@ -451,6 +451,27 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
   const int glane = gok ? lane + gdl : lane;
   const bool gany = __any_sync(0xffffffffu, gsrc != 0);
   const bool fsblk = fsurf && z0 == 1;  // the free-surface row is lane 0 of warp 0
+  // band tiles: a warp whose rows (velocity rows with the halo lanes, and
+  // stress rows) meet no strip, face, domain end or source cell runs the
+  // interior code
+  bool cleanr = true;
+  if (vact) cleanr = vxr && vzr && jq3 < 0 && jq2 < 0 && gsrc == 0;
+  if (t < TZ) cleanr = cleanr && srow && xzrow && jr5 < 0 && jr6 < 0 && !fsrow;
+  bool srcw = false;
+  if (MODE == 1 && (t & 31) == 0) {
+    const int wr0 = z0 + (t & ~31), wr1 = wr0 + 31;
+    for (int kd = 0; kd < 3 && !srcw; kd++)
+      for (int i2 = s_rng[kd][0]; i2 < s_rng[kd][1]; i2++) {
+        const InjCell &cl = a.cells[i2];
+        if (cl.col > x1 + 2) break;
+        if (cl.row >= wr0 && cl.row <= wr1) {
+          srcw = true;
+          break;
+        }
+      }
+  }
+  srcw = __shfl_sync(0xffffffffu, srcw, 0);
+  const bool fastw = MODE == 1 && __all_sync(0xffffffffu, cleanr) && !srcw;
   {
     // Columns away from the x edges and from sources: every row in one
     // pass; rows outside an update domain keep their value, CPML terms where
@@ -558,10 +579,19 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
             cvz.range(a.cells, cc, ib1, ie1);
             if (c >= x0) cst.range(a.cells, c, bs, es);
             if (!mbar_wait(&bar[(u + 3) % RING], ph ^ (uint32_t)((u + 3) / RING))) s_err = 1;
-            vel_band(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, ib0, ie0, ib1, ie1);
+            if (fastw)
+              vel_fast(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+            else
+              vel_band(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, ib0, ie0, ib1, ie1);
             __syncthreads();
             if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
-            if (c >= x0) str_band(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, bs, es);
+            if (c >= x0) {
+              if (fastw)
+                str_fast(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
+              else
+                str_band(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, bs, es);
+            }
+            ov += NZP, os += NZP;
           }
         }
       } else {

@@ -131,6 +131,8 @@ typedef struct gpo_ctx {
                     FD-consistent rho term (gpo_set_imaging) */
   arr born[4];   /* GPO_BORN secondary-source ratios: p, vx, vy, vz */
   int have_born;
+  REAL *srcamt;  /* elastic history adjoint: stress-source amounts of the
+                    forward step being reversed, per normal-stress cell */
 } ctx;
 
 static int nk(const ctx *c, int kind, int n, int dimactive) {
@@ -698,7 +700,7 @@ static void snap_io(ctx *c, int ishot, int tau, int dir) {
 /* ------------------------------------------------------------------ */
 /* gradient (src/fdtd/gradient.jl:17-64), acoustic 2-D                 */
 /* ------------------------------------------------------------------ */
-static void compute_gradient_elastic(ctx *c, REAL *gL, REAL *gM, REAL *gR);
+static void compute_gradient_elastic(ctx *c, REAL *gL, REAL *gM, REAL *gR, const REAL *A);
 
 static void rho_gather(ctx *c, REAL *gR) {
   const int three = c->d.ndim == 3;
@@ -746,7 +748,7 @@ static void rho_gather(ctx *c, REAL *gR) {
 
 static void compute_gradient(ctx *c, REAL *gK, REAL *gR, REAL *g3) {
   if (c->d.physics == GPO_ELASTIC) {
-    compute_gradient_elastic(c, gK, gR, g3);
+    compute_gradient_elastic(c, gK, gR, g3, c->srcamt);
     return;
   }
   const int h = c->h;
@@ -787,8 +789,13 @@ static void compute_gradient(ctx *c, REAL *gK, REAL *gR, REAL *g3) {
       }
 }
 
-/* imaging condition of the discrete elastic scheme (gpo.h, GPO_ADJOINT_HIST) */
-static void compute_gradient_elastic(ctx *c, REAL *gL, REAL *gM, REAL *gR) {
+/* imaging condition of the discrete elastic scheme (gpo.h, GPO_ADJOINT_HIST).
+ * A: the amounts dtM pv the forward step added to every normal stress of a
+ * cell (explosive sources), or NULL.  There the stress decrease is K e - A 1
+ * instead of K e, and dtM multiplies the source too, so the normal terms
+ * gain (sum a)(d A / (dtM + (d-1) dtl) - A / dtM) dtl^2 / dt and
+ * (sum a)(A / (dtM + (d-1) dtl) - A / dtM) 2 dt / invmu^2, added first. */
+static void compute_gradient_elastic(ctx *c, REAL *gL, REAL *gM, REAL *gR, const REAL *A) {
   const int three = c->d.ndim == 3, h = c->h;
   const REAL dt = c->dt, dtI = c->dtI;
   arr M = c->dmod[c->ndmod - 2], L = c->dmod[c->ndmod - 1], imu = c->mod[1];
@@ -796,6 +803,16 @@ static void compute_gradient_elastic(ctx *c, REAL *gL, REAL *gM, REAL *gR) {
   const int *nid = three ? nid3 : nid2;
   const int d = three ? 3 : 2;
   const size_t n = alen(c->w[0][GPO_TAUXX]);
+  for (size_t i = 0; A && i < n; i++) {
+    if (A[i] == (REAL)0) continue;
+    REAL sq = 0;
+    for (int k = 0; k < d; k++) sq = sq + c->wp[1][nid[k]].a[i];
+    const REAL beta = L.a[i], alpha = M.a[i] - L.a[i];
+    const REAL sa = sq / (alpha + (REAL)d * beta); /* sum of K^-1 q */
+    const REAL corr = A[i] / (alpha + (REAL)d * beta), own = A[i] / M.a[i];
+    gL[i] = gL[i] + sa * ((REAL)d * corr - own) * (beta * beta * dtI);
+    gM[i] = gM[i] + sa * (corr - own) * ((REAL)2 * dt / (imu.a[i] * imu.a[i]));
+  }
   for (size_t i = 0; i < n; i++) {
     REAL q[3], dT[3], a[3], b[3], sq = 0, sT = 0;
     for (int k = 0; k < d; k++) {
@@ -1094,6 +1111,26 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
     if (mode == GPO_ADJOINT_HIST) {
       save_tp(c, 1);
       hist_states(c, ishot, it);
+      if (c->d.physics == GPO_ELASTIC) {
+        /* the amounts dtM pv the forward step s = nt - it + 1 added to the
+         * normal stresses (add_stress_source!, wavelet sample s - 1) */
+        const size_t n = alen(c->w[0][GPO_TAUXX]);
+        if (!c->srcamt) c->srcamt = (REAL *)calloc(n, sizeof(REAL));
+        memset(c->srcamt, 0, n * sizeof(REAL));
+        arr dM = c->dmod[c->ndmod - 2];
+        for (int s = 0; s < nsrc; s++) {
+          if (!is_stress_src(src[s].field)) continue;
+          spray(c, &src[s], nt - it);
+          for (int j = 0; j < src[s].n; j++)
+            for (int64_t k = src[s].colptr[j]; k < src[s].colptr[j + 1]; k++) {
+              const int64_t r = src[s].rowval[k];
+              if (c->pvflag[r] == 1) continue;
+              c->pvflag[r] = 1;
+              c->srcamt[r] = c->srcamt[r] + c->pv[r] * dM.a[r];
+            }
+          spray_clear(c, &src[s]);
+        }
+      }
     }
     for (int ipw = pw0; ipw < npw; ipw++) update_dstress(c, ipw);
     for (int ipw = pw0; ipw < npw; ipw++) update_v(c, ipw);
@@ -1232,6 +1269,7 @@ void SFX(gpo_destroy)(gpo_ctx *cc) {
     }
   }
   for (int q = 0; q < 4; q++) free(c->born[q].a);
+  free(c->srcamt);
   free(c->vbuf[0].a);
   free(c->vbuf[1].a);
   free(c->vbuf[2].a);

@@ -248,11 +248,15 @@ def _shot_inputs(prep, shot, src_types=1):
     return src, rec
 
 
-def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=False, snaps=None):
+def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=False, snaps=None, mod=None):
     """update!(pa) in :forward mode: records[field] of shape (nshots, nt, nr).
     snaps = (field, [steps]) also returns res["snaps"][shot][k], the field at
-    the end of step steps[k] (1-based; snaps_save!)."""
+    the end of step steps[k] (1-based; snaps_save!).  mod: extended-grid
+    medium parameters replacing the ones padded from ex (as after
+    update!(pa, m, mparams), which leaves the PML cells as they were)."""
     prep = Prepared(ex, dtype, ref_compat)
+    if mod is not None:
+        prep.mod = [np.asarray(m, np.float64 if dtype == np.float64 else np.float32) for m in mod]
     orc = Oracle(prep, nthreads)
     if snaps is not None:
         its = (ctypes.c_int * len(snaps[1]))(*snaps[1])
@@ -302,7 +306,7 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
     ex (update!(pa, m, mparams) keeps the PML cells of the old medium)."""
     prep = Prepared(ex, dtype, ref_compat)
     if mod is not None:
-        prep.mod = [np.asarray(m, np.float32) for m in mod]
+        prep.mod = [np.asarray(m, np.float64 if dtype == np.float64 else np.float32) for m in mod]
     if prep.physics == "elastic" and not history:
         raise ValueError("elastic gradients: history mode only (no boundary store in 3-D)")
     orc = Oracle(prep, nthreads)
@@ -322,9 +326,10 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
             dcal[f].append(r[f])
     dcal = {f: np.stack(v) for f, v in dcal.items()}
     loss = sum(S.l2_value(dobs[f], dcal[f]) for f in ex["rfields"])
-    # adjoint with src_types [-1, 1]
+    # adjoint with src_types [-1, 1] (history mode: the forward sources, for
+    # the source terms of the elastic imaging condition)
     for i, shot in enumerate(ex["shots"]):
-        src, _ = _shot_inputs(prep, shot, -1)
+        src, _ = _shot_inputs(prep, shot, 1 if history else -1)
         adj = []
         for f in ex["rfields"]:
             a = S.l2_deriv(dobs[f][i], dcal[f][i])[::-1].copy()

@@ -75,17 +75,19 @@ def _fd_setup():
 
 
 def _J(ex, dobs, scale):
-    """FP64 misfit with log-parameters scaled cell-wise by `scale`
-    (name -> factor array); invlambda, invmu, rho independent."""
-    vp0, vs0, rho0 = (ex[k].astype(np.float64) for k in ("vp", "vs", "rho"))
-    lam, mu = (vp0 ** 2 - 2 * vs0 ** 2) * rho0, vs0 ** 2 * rho0
-    lam = lam / scale.get("invlambda", 1.0)
-    mu = mu / scale.get("invmu", 1.0)
-    rho = rho0 * scale.get("rho", 1.0)
-    e = dict(ex)
-    e["rho"], e["vs"], e["vp"] = rho, np.sqrt(mu / rho), np.sqrt((lam + 2 * mu) / rho)
-    r = O.forward(e, dtype=np.float64)
-    return sum(S.l2_value(dobs[f], r[f]) for f in e["rfields"])
+    """FP64 misfit with the medium parameters of the inner (non-PML) cells
+    scaled by `scale` (name -> factor array on the physical grid), the PML
+    cells left as padded: the model vector's meaning (update!(pa, m,
+    mparams) changes the inner cells only)."""
+    prep = O.Prepared(ex)
+    npml = prep.npml
+    inner = tuple(slice(npml, n - npml) for n in prep.shape)
+    mod = [m.astype(np.float64) for m in prep.mod]
+    for i, k in enumerate(PARAMS):
+        if k in scale:
+            mod[i][inner] = mod[i][inner] * scale[k]
+    r = O.forward(ex, dtype=np.float64, mod=mod)
+    return sum(S.l2_value(dobs[f], r[f]) for f in ex["rfields"])
 
 
 @pytest.mark.gpu
