@@ -70,6 +70,14 @@ WORKLOADS = {
                              "bpc": None, "nshots": 1, "nt": 500, "slots": 8,
                              "kernel": "checkpointed gradient (k3 passes, recompute and turns, k_grad_a3), "
                                        "algorithmic 48 x (2 + recomputed/nt) + 184 B/cell"},
+    # 3-D elastic gradient (invlambda, invmu, rho) on the 3-D workload's grid,
+    # 500 of its 2500 steps, 8 state slots: forward_save (104 B) + recomputed
+    # steps (104 B) + turns: copies of the 9 fields (72 B), velocity half
+    # step (60 B), imaging condition (144 B), adjoint step (104 B)
+    "elastic3d_grad_ckpt": {"name": "elastic3d_gradient_checkpointed_600x600x600_10m_npml23_500steps_8slots",
+                            "bpc": None, "nshots": 1, "nt": 500, "slots": 8,
+                            "kernel": "checkpointed gradient (k3 elastic passes, recompute and turns, k_grad_e3), "
+                                      "algorithmic 104 x (2 + recomputed/nt) + 276 B/cell"},
 }
 
 
@@ -113,6 +121,9 @@ def workload(kind, nt=None, nshots=None, side=None):
     if kind == "acoustic3d_grad_ckpt":
         kw.setdefault("nt", WORKLOADS[kind]["nt"])
         return configs.acoustic3d(rfields=("vz",), src_field="p", **kw)
+    if kind == "elastic3d_grad_ckpt":
+        kw.setdefault("nt", WORKLOADS[kind]["nt"])
+        return configs.elastic3d(rfields=("vx", "vz"), **kw)
     if kind == "acoustic2d":
         wl = configs.acoustic2d_layers(**kw)
     elif kind == "elastic3d":
@@ -128,7 +139,7 @@ def config_json(kind, wl, n_gpus, shots_per_gpu=None):
     npml = wl.npml if wl.npml is not None else 43
     nsh = shots_per_gpu if shots_per_gpu is not None else len(wl.shots)
     state = {"elastic2d": 5, "acoustic2d": 3, "elastic3d": 9, "acoustic3d": 4, "acoustic2d_grad": 6,
-             "acoustic2d_grad_ckpt": 6, "acoustic3d_grad_ckpt": 8}[kind]
+             "acoustic2d_grad_ckpt": 6, "acoustic3d_grad_ckpt": 8, "elastic3d_grad_ckpt": 18}[kind]
     return {"workload": WORKLOADS[kind]["name"],
             "grid": [len(g) for g in wl.grid], "extended_grid": [len(g) + 2 * npml for g in wl.grid],
             "shots_per_gpu": nsh, "nt": wl.nt, "dt": wl.tgrid.step, "order": 4,
@@ -385,17 +396,18 @@ def gradient_arm(args, world, local, kind="acoustic2d_grad"):
     pa.set_graph(args.graph)
     cells = pa.nss * int(np.prod([len(g) for g in pa.exgrid]))
     units = cells * pa.nt
-    m0 = get_modelvector(pa, ["invK", "rho"])
+    params = ["invlambda", "invmu", "rho"] if wl.physics == "elastic" else ["invK", "rho"]
+    m0 = get_modelvector(pa, params)
     g = np.zeros_like(m0)
     for _ in range(args.warmup):
-        gradient(g, m0, L2DistLoss(), dobs, pa)
+        gradient(g, m0, L2DistLoss(), dobs, pa, params)
     torch.cuda.synchronize()
     clocks = Clocks(local)
     clocks.start()
     t0 = time.perf_counter()
     launches = 0
     for _ in range(args.steps):
-        gradient(g, m0, L2DistLoss(), dobs, pa)
+        gradient(g, m0, L2DistLoss(), dobs, pa, params)
         launches += pa.launches()
     torch.cuda.synchronize()
     ms = (time.perf_counter() - t0) * 1e3 / args.steps
@@ -409,7 +421,7 @@ def gradient_arm(args, world, local, kind="acoustic2d_grad"):
         _lib.load().gpi_checkpoint_schedule(pa.nt, slots, ctypes.byref(adv), ctypes.byref(turns), ctypes.byref(stored))
         sched = {"slots": slots, "recomputed_steps": adv.value, "turns": turns.value,
                  "slot_gb": round(pa.plan_bytes() / 1e9, 2) if hasattr(pa, "plan_bytes") else None}
-        base, turn = (36, 108) if kind.startswith("acoustic2d") else (48, 184)
+        base, turn = {"acoustic2d": (36, 108), "acoustic3d": (48, 184), "elastic3d": (104, 276)}[kind.split("_")[0]]
         bpc = base * (2 + adv.value / pa.nt) + turn
     achieved = bpc * cells / (ms * 1e-3 / pa.nt) / 1e9
     return {"metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
@@ -512,7 +524,7 @@ def main():
     if args.workload == "serving":
         print(json.dumps(serving_arm(args)))
         return
-    if args.workload in ("acoustic2d_grad", "acoustic2d_grad_ckpt", "acoustic3d_grad_ckpt"):
+    if args.workload in ("acoustic2d_grad", "acoustic2d_grad_ckpt", "acoustic3d_grad_ckpt", "elastic3d_grad_ckpt"):
         line, dist = gradient_arm(args, world, local, args.workload), None
     else:
         line, dist = engine_arm(args, rank, world, local)
