@@ -88,7 +88,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="elastic2d", choices=sorted(WORKLOADS) + ["serving"])
-    ap.add_argument("--requests", type=int, default=64, help="serving: requests in the stream")
+    ap.add_argument("--requests", type=int, default=24, help="serving: requests in the stream")
+    ap.add_argument("--dist", default="full", choices=["full", "small"],
+                    help="serving: request sizes of the 2000-request stream (sides 200-2000, 1000-6000 steps) "
+                         "or a small one (sides 200-800, 500-2000 steps)")
     ap.add_argument("--rate", type=float, default=32.0, help="serving: arrival rate, requests/s")
     ap.add_argument("--rates", default="", help="serving: also sweep these arrival rates (comma list)")
     ap.add_argument("--nt", type=int, default=None)
@@ -443,14 +446,16 @@ def serving_arm(args):
     20 % acoustic gradient; Poisson arrivals) through the continuous-batching
     loop, one shot at a time with plain launches (the baseline the serving
     target is quoted against) and one request at a time with its shots
-    batched.  The stream is a scaled version of the 2000-request one (sides
-    200-800 instead of 200-2000, 500-2000 steps instead of 1000-6000) so that
-    all arms finish in minutes.  Request payloads (models, geometry) are
-    built before the clock starts: they arrive with the request."""
+    batched.  The requests follow the size distribution of the 2000-request
+    stream (sides 200-2000, 1000-6000 steps, 1-8 shots; --dist small: sides
+    200-800, 500-2000 steps); fewer requests than 2000 so that the three arms
+    finish in minutes (the count is in the line).  Request payloads (models,
+    geometry) are built before the clock starts: they arrive with the
+    request."""
     from geophyinv_gb300 import serving
 
-    reqs = serving.make_stream(args.requests, rate=args.rate, seed=4, sides=(200, 800), steps=(500, 2000),
-                               shots=(1, 8))
+    sides, steps = SERVING_DIST[args.dist]
+    reqs = serving.make_stream(args.requests, rate=args.rate, seed=4, sides=sides, steps=steps, shots=(1, 8))
     for r in reqs:
         r.payload()
     warm = serving.make_stream(6, rate=1000.0, seed=5, sides=(100, 150), steps=(50, 60), shots=(1, 2))
@@ -466,7 +471,7 @@ def serving_arm(args):
             "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic request stream (seed 4)",
             "config": {"workload": "serving_stream_%d_requests_%g_per_s" % (len(reqs), args.rate),
-                       "sides": [200, 800], "steps": [500, 2000], "shots": [1, 8],
+                       "sides": list(sides), "steps": list(steps), "shots": [1, 8],
                        "mix": "50 % acoustic forward, 30 % elastic forward, 20 % acoustic gradient",
                        "max_inflight": 8},
             "serving": {k: round(v, 4) if isinstance(v, float) else v for k, v in st.items()},
@@ -474,16 +479,20 @@ def serving_arm(args):
             "plain_one_request_at_a_time": {k: round(v, 4) if isinstance(v, float) else v for k, v in pr.items()},
             "speedup_shots_per_s": round(st["shots_per_s"] / pl["shots_per_s"], 3),
             "speedup_vs_request_at_a_time": round(st["shots_per_s"] / pr["shots_per_s"], 3), "clocks": clk,
-            "sweep": [rate_point(float(r)) for r in args.rates.split(",") if r] or None}
+            "sweep": [rate_point(float(r), args.dist) for r in args.rates.split(",") if r] or None}
 
 
-def rate_point(rate):
+SERVING_DIST = {"full": ((200, 2000), (1000, 6000)), "small": ((200, 800), (500, 2000))}
+
+
+def rate_point(rate, dist):
     """Serving against one shot at a time at one arrival rate: 8 s of
     arrivals (16 to 48 requests), shots/s, p50 and p99 of both."""
     from geophyinv_gb300 import serving
 
     n = int(max(16, min(48, 8 * rate)))
-    reqs = serving.make_stream(n, rate=rate, seed=6, sides=(200, 800), steps=(500, 2000), shots=(1, 8))
+    sides, steps = SERVING_DIST[dist]
+    reqs = serving.make_stream(n, rate=rate, seed=6, sides=sides, steps=steps, shots=(1, 8))
     for r in reqs:
         r.payload()
     _, st = serving.serve(reqs, max_inflight=8)

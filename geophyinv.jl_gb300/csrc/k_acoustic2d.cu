@@ -272,8 +272,7 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
   };
 
   // the interior code: every row inside every update domain, no CPML, no
-  // face, no source (interior tiles, and the clean warps of band tiles);
-  // global offsets of this thread's rows, advanced one column per
+  // face, no source (interior tiles); global offsets of this thread's rows, advanced one column per
   // iteration: velocities of column xbase+3+it, pressure of column xbase+it
   int64_t ov = so + S(q, xbase + 3), os = so + S(r, xbase);
   // velocities of column cc from ring slots s3..s0 = columns cc-3..cc
@@ -351,27 +350,6 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
   const bool gok = lane + gdl >= 0 && lane + gdl < 32;
   const int glane = gok ? lane + gdl : lane;
   const bool gany = __any_sync(0xffffffffu, gsrc != 0);
-  // band tiles: a warp whose rows (velocity rows with the halo lanes, and
-  // pressure rows) meet no strip, face, domain end or source cell runs the
-  // interior code
-  bool cleanr = true;
-  if (vact) cleanr = (kq < TZ ? vxr : true) && vzr && jq1 < 0 && gsrc == 0;
-  if (t < TZ) cleanr = cleanr && srow && jr3 < 0;
-  bool srcw = false;
-  if (MODE == 1 && (t & 31) == 0) {
-    const int wr0 = z0 + (t & ~31), wr1 = wr0 + 31;
-    for (int kd = 0; kd < 3 && !srcw; kd++)
-      for (int i2 = s_rng[kd][0]; i2 < s_rng[kd][1]; i2++) {
-        const InjCell &cl = a.cells[i2];
-        if (cl.col > x1 + 2) break;
-        if (cl.row >= wr0 && cl.row <= wr1) {
-          srcw = true;
-          break;
-        }
-      }
-  }
-  srcw = __shfl_sync(0xffffffffu, srcw, 0);
-  const bool fastw = MODE == 1 && !a.vonly && __all_sync(0xffffffffu, cleanr) && !srcw;
   {
     // vz at row qq of column cc before its source (source of a mirror row)
     auto vz_any = [&](int qq, int cc) -> float {
@@ -456,19 +434,10 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
           cvz.range(a.cells, cc, ib1, ie1);
           if (c >= x0) cst.range(a.cells, c, bs, es);
           if (!mbar_wait(&bar[(u + 3) % RING], ph ^ (uint32_t)((u + 3) / RING))) s_err = 1;
-          if (fastw)
-            vel_fast(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
-          else
-            vel_band(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, ib0, ie0, ib1, ie1);
+          vel_band(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, ib0, ie0, ib1, ie1);
           __syncthreads();
           if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
-          if (c >= x0) {
-            if (fastw)
-              str_fast(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING);
-            else
-              str_band(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, bs, es);
-          }
-          ov += NZP, os += NZP;
+          if (c >= x0) str_band(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, bs, es);
         }
       }
     } else if constexpr (MODE == 2) {

@@ -63,6 +63,21 @@ def test_elastic3d_gradient_matches_oracle(engine, src_field):
     assert np.all(np.isfinite(g))
 
 
+@pytest.mark.gpu
+def test_elastic3d_gradient_mid_size_matches_oracle(engine):
+    """The same parity on a mid-size grid (100 x 68 x 76 extended), five
+    checkpoint slots."""
+    wl = configs.elastic3d(nz=80, ny=48, nx=56, nt=60, npml=10, nrec_side=5, rfields=("vx", "vz"))
+    dobs = {f: np.zeros((1, wl.nt, len(wl.shots[0][1])), np.float32) for f in wl.rfields}
+    loss_o, _, _, raw_o = O.gradient(wl.as_dict(), dobs, history=True)
+    J, raw, g, _ = _engine(wl, dobs, slots=5)
+    assert abs(J - loss_o) <= TOL * abs(loss_o)
+    for k in PARAMS:
+        assert np.linalg.norm(raw_o[k]) > 0, k
+        e = rel(raw[k], raw_o[k])
+        assert e < TOL, (k, e)
+
+
 def _fd_setup():
     wl = _workload("tauxx")
     ex = wl.as_dict()

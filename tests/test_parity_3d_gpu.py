@@ -55,3 +55,25 @@ def test_elastic3d_velocity_source_two_shots(engine):
     src, rec = wl.shots[0]
     wl.shots = [(src, rec), (src + np.array([[0.0, -40.0, 30.0]]), rec)]
     _check(wl, ("vx", "vy", "vz", "tauxx"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("surface", ["pml", "free"])
+def test_elastic3d_mid_size_two_shots(engine, surface):
+    """A mid-size grid (100 x 76 x 116 extended: several 32 x 8 tiles and
+    columns beyond the CPML reach on every axis), two shots in one launch,
+    every field at the end."""
+    wl = configs.elastic3d(nz=80, ny=56, nx=96, nt=100, npml=10, nrec_side=5, rfields=("vx", "vy", "vz"))
+    src, rec = wl.shots[0]
+    wl.shots = [(src, rec), (src + np.array([[60.0, -50.0, 40.0]]), rec)]
+    if surface == "free":
+        wl.pml_faces = ["zmax", "ymin", "ymax", "xmin", "xmax"]
+        wl.stressfree_faces = ["zmin"]
+    _check(wl, ("tauxx", "tauyy", "tauzz", "tauxy", "tauxz", "tauyz", "vx", "vy", "vz"))
+
+
+@pytest.mark.gpu
+def test_elastic3d_velocity_source_mid_size(engine):
+    """A vz body-force source on the mid-size grid."""
+    wl = configs.elastic3d(nz=80, ny=56, nx=96, nt=100, npml=10, nrec_side=5, rfields=("vz",), src_field="vz")
+    _check(wl, ("vx", "vy", "vz", "tauzz"))
