@@ -207,14 +207,14 @@ def peaks():
 # DRAM bytes per cell update of the step-kernel family, a CONSTANT taken
 # from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum of the
 # four tile-class launches of one step, divided by the cells they update):
-#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
-#       -k regex:k_e2 -s 64 -c 4 python bench.py --workload elastic2d --nshots 2
-#       --nt 40 --steps 1 --warmup 1 --graph 0 --no-cpu-baseline
-# (a 2-shot, 40-step case of the batch; traffic per cell grows with the shot
-# count only through the L2 reuse of the shared coefficient columns).  The
-# bench cannot measure it in the run; the value is re-taken when the kernel
-# changes.
-TRAFFIC_B_PER_CELL = {"elastic2d": (48.8, "ncu dram bytes of the k_e2 launches of one step, 16-shot batch")}
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+#       --clock-control none -k regex:k_e2 -s 16 -c 4 --csv python bench.py --nt 10
+#       --nshots 4 --steps 1 --warmup 3 --graph 0 --no-cpu-baseline
+# (the batch's grid with 4 shots: 13.4 M cells, 633 MB per step; traffic per
+# cell changes with the shot count only through the L2 reuse of the shared
+# coefficient columns).  The bench cannot measure it in the run; the value
+# is re-taken when the kernel changes.
+TRAFFIC_B_PER_CELL = {"elastic2d": (47.2, "ncu dram bytes of the four k_e2 launches of one step, batch grid with 4 shots")}
 
 
 def traffic_per_cell(kind):
