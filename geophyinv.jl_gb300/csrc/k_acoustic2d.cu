@@ -292,11 +292,16 @@ __global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
       }
     }
   };
-  // pressure of column c from velocity slots s0..s3 = columns c..c+3
+  // pressure of column c from velocity slots s0..s3 = columns c..c+3 (the
+  // velocity half step: the old pressure, or nothing with vonly bit 2)
   auto str_fast = [&](int c, int s0, int s1, int s2, int s3) {
     if (t >= TZ) return;
     const int k = t;
     const float *pc = ring + s0 * SL;
+    if (a.vonly) {
+      if (!(a.vonly & 4)) a.pB[os] = pc[k + 4];
+      return;
+    }
     const float *w = svz + s0 * R4;
     const float Dx = st4(svx[s0 * R4 + k], svx[s1 * R4 + k], svx[s2 * R4 + k], svx[s3 * R4 + k]) * a.dxI;
     const float Dz = st4(w[k], w[k + 1], w[k + 2], w[k + 3]) * a.dzI;
@@ -627,8 +632,15 @@ int step_a2_wavefield(Plan *p, int ipw, int vonly) {
   const int *n = p->n_tiles;
   const int ntot = n[0] + n[1] + n[2] + n[3];
   if (vonly) {
-    // the velocity-only half step runs every tile on the general code
-    launch(3, 0, ntot, p->stream);
+    // the velocity half step: interior tiles on the interior code (they
+    // hold no source), every other tile on the general code
+    const int nside = n[0] > 0 && ntot > n[0] ? 1 : 0;
+    cudaStream_t st[Plan::NSIDE] = {p->stream, p->stream, p->stream};
+    if (int rc = fork_side(p, nside, st)) return rc;
+    launch(3, n[0], ntot - n[0], st[0]);
+    launch(0, 0, n[0], p->stream);
+    GPI_CUDA(p, cudaGetLastError());
+    if (int rc = join_side(p, nside)) return rc;
   } else {
     // edge, x-band and band blocks (longer) go first, on their own streams,
     // so that interior blocks fill the SMs around them and their tails
