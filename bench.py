@@ -50,10 +50,12 @@ WORKLOADS = {
     "acoustic3d": {"name": "acoustic3d_600x600x600_10m_npml23_2500steps", "bpc": 48, "nshots": 1, "nt": 2500,
                    "kernel": "k3_vel_a + k3_str_a (two fused passes), algorithmic 48 B/cell"},
     # one bench step = one gradient!: forward_save (36 B) + adjoint step with
-    # the imaging condition (76 B fused) per cell and time step
+    # the imaging condition (76 B fused) per cell and time step; the engine's
+    # fused adjoint moves 84 B (per-velocity-cell rho sums in place of g_rho)
     "acoustic2d_grad": {"name": "acoustic2d_fwi_gradient_500x1500_10m_32shots_3000steps", "bpc": 112, "nshots": 32,
                         "nt": 3000,
-                        "kernel": "forward_save + adjoint (k_a2 x 3 + k_grad_a2), algorithmic 36 + 76 B/cell"},
+                        "kernel": "forward_save (k_a2<m,1>) + fused adjoint (k_a2<m,2>: both wavefields and the "
+                                  "imaging condition), algorithmic 36 + 76 B/cell"},
     # the same gradient through the checkpointed adjoint, a checkpoint every
     # 100 steps (30 state slots): forward_save (36 B) + the schedule's
     # recomputed steps (36 B each) + per step a turn: forward step (36 B),

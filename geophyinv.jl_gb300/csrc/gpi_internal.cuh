@@ -92,6 +92,11 @@ struct Plan {
   int nmod = 0;
   float *pml = nullptr;  // [nder][3][2*npml]
   float *grad[3] = {};   // per-shot gradients [shot][storage] (adjoint), one per medium parameter
+  // 2-D acoustic adjoint by time reversal: per velocity cell and shot, the
+  // sums over the steps of vx2_prev (vx1 - vx1_prev) / dt (img[0]) and of
+  // the vz products (img[1]); the rho gradient is formed from them at the
+  // end of the run
+  float *img[2] = {};
   float *bstore = nullptr;  // boundary store (forward_save -> adjoint)
   float *bprev = nullptr;   // adjoint: the strip values the forcing replaced, this step
   int64_t bstep = 0;         // floats per step per shot
@@ -139,6 +144,10 @@ struct Plan {
   // grouped by class: interior, band, x-band, edge (classify_tiles)
   int4 *d_tiles = nullptr;
   int n_tiles[4] = {0, 0, 0, 0};
+  // the most injection cells (columns x0 .. x1+2 of a tile, every kind) a
+  // tile of each class holds: wavefield 1, wavefield 2, both; sizes the
+  // shared-memory copy of the 2-D acoustic step kernel (0: none)
+  int inj_tile[3][4] = {};
   // 2-D z-strip CPML memory: column stride and the window of a column that
   // the general step kernel stages per ring slot
   int zsw = 0, pzw = 0;
@@ -233,6 +242,8 @@ int step_acoustic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_adjoint_acoustic2d(Plan *p, int it);
 int step_a2_wavefield(Plan *p, int ipw, int vonly);
+int step_a2_adjoint_fused(Plan *p);  // both wavefields + imaging condition
+int img_rho_finish(Plan *p);         // the rho gradient from img[0], img[1]
 int step3_wavefield(Plan *p, int ipw, int vonly);
 // checkpointed adjoint (gpi_ckpt.cu)
 int64_t ckpt_slot_floats(const Plan &p);

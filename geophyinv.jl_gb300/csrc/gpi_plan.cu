@@ -259,6 +259,8 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
     allocs.push_back({&p.ck_pool, p.ck_floats * p.ck_slots});
   } else if (d.npw == 2) {
     for (int i = 0; i < p.nmod && i < 2; i++) allocs.push_back({&p.grad[i], p.fstride * d.nshots});
+    if (d.physics == GPI_ACOUSTIC && d.ndim == 2)
+      for (int i = 0; i < 2; i++) allocs.push_back({&p.img[i], p.fstride * d.nshots});
     int ids[3];
     int ns = nsaved(p, ids);
     p.bstep = 0;
@@ -888,6 +890,28 @@ static int build_tiles(Plan &p) {
   std::vector<int32_t> zero(2 * p.d.nshots * NKIND + 1, 0);
   if (classify_tiles(p, p.xcut.data(), p.h_cells.data(), gp ? gp : zero.data(), t.data(), n, p.n_tiles) < 0)
     return fail(&p, GPI_E_INVALID, "tile list");
+  // injection cells per tile and class (the cells of a group are sorted by
+  // column)
+  const int32_t *g = gp ? gp : zero.data();
+  const InjCell *cells = p.h_cells.data();
+  for (auto &row : p.inj_tile)
+    for (int &v : row) v = 0;
+  for (int m = 0, at = 0; m < 4; m++)
+    for (int i = 0; i < p.n_tiles[m]; i++, at++) {
+      const int4 tl = t[at];
+      int cw[2] = {0, 0};
+      for (int ipw = 0; ipw < p.d.npw && ipw < 2; ipw++)
+        for (int kind = 0; kind < NKIND; kind++) {
+          const int gi = (ipw * p.d.nshots + tl.w) * NKIND + kind;
+          const InjCell *b = cells + g[gi], *e = cells + g[gi + 1];
+          const InjCell *lo = std::lower_bound(b, e, tl.y, [](const InjCell &c, int x) { return c.col < x; });
+          const InjCell *hi = std::lower_bound(lo, e, tl.z + 3, [](const InjCell &c, int x) { return c.col < x; });
+          cw[ipw] += (int)(hi - lo);
+        }
+      p.inj_tile[0][m] = std::max(p.inj_tile[0][m], cw[0]);
+      p.inj_tile[1][m] = std::max(p.inj_tile[1][m], cw[1]);
+      p.inj_tile[2][m] = std::max(p.inj_tile[2][m], cw[0] + cw[1]);
+    }
   if (p.d_tiles) cudaFreeAsync(p.d_tiles, p.stream);
   p.d_tiles = nullptr;
   GPI_CUDA(&p, dalloc(p, (void **)&p.d_tiles, n * sizeof(int4)));
@@ -1133,6 +1157,8 @@ static int run_body(Plan &p, int mode, bool chunked) {
   if (!rc && mode == GPI_ADJOINT) {
     for (int i = 0; i < 3; i++)
       if (p.grad[i]) rc = cudaMemsetAsync(p.grad[i], 0, p.fstride * p.d.nshots * sizeof(float), p.stream) ? GPI_E_CUDA : rc;
+    for (int i = 0; i < 2; i++)
+      if (p.img[i]) rc = cudaMemsetAsync(p.img[i], 0, p.fstride * p.d.nshots * sizeof(float), p.stream) ? GPI_E_CUDA : rc;
     if (!rc) rc = snap_io(&p, 1, 1);
     if (!rc) rc = snap_io(&p, 0, 1);
   }
@@ -1146,6 +1172,7 @@ static int run_body(Plan &p, int mode, bool chunked) {
   if (!rc && snaps) rc = snap_io(&p, 1, 0);
   if (!rc) rc = step(p, 1, p.d.nt + 1, mode, 1);  // the extra velocity half step (propagate.jl:254-255)
   if (!rc && snaps) rc = snap_io(&p, 0, 0);
+  if (!rc && mode == GPI_ADJOINT && p.img[0]) rc = img_rho_finish(&p);
   if (!rc) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));

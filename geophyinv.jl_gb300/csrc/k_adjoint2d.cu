@@ -7,7 +7,9 @@
 //       boundary_io before this call; the replaced strip values are kept in
 //       Plan::bprev, since the imaging condition uses the unforced field
 //   update of wavefield 1 (time reversal) and of wavefield 2 (adjoint, fed
-//       through the receiver interpolation) with the fused step kernel
+//       through the receiver interpolation) in one launch of the step
+//       kernel over both wavefields (k_a2<MODE, 2>, k_acoustic2d.cu), which
+//       also accumulates the imaging condition below
 //   compute_gradient! (src/fdtd/gradient.jl:27-56):
 //       g_invK += p2_prev (p1_prev - p1) dtI                 (every p cell)
 //       bx = vx2_prev (vx1 - vx1_prev) dtI, bz likewise      (velocity grids)
@@ -19,9 +21,14 @@
 //       g_rho[r, c] -= (bx[r, c+2] + bx[r, c+3]) / 2 + (bz[r+2, c] + bz[r+3, c]) / 2
 //       over the updated velocity cells: the gradient of the discrete model
 //       (dt / avg(rho) at vx cell c averages rho at c-3 and c-2)
-// The imaging condition is one streaming pass over both wavefields' old and
-// new states (k_grad_a2); the velocity terms are recomputed at the two
-// neighbours each g_rho cell needs, in the reference's operation order.
+// The time-reversal adjoint accumulates g_invK and, per velocity cell, the
+// sums of bx and bz over the steps inside the step kernel; k_img_rho forms
+// g_rho from those sums after the last step (the averages are linear, so
+// only the summation order differs from the reference's per-step form).
+// The checkpointed adjoint (gpi_ckpt.cu) runs the imaging condition as its
+// own streaming pass over both wavefields' old and new states (k_grad_a2),
+// with the velocity terms recomputed at the two neighbours each g_rho cell
+// needs, in the reference's operation order.
 #include "k_stencil.cuh"
 
 namespace gpi {
@@ -137,37 +144,47 @@ int grad_a2_launch(Plan *p, const float *p1A, const float *p1B, const float *vx1
 
 int step_adjoint_acoustic2d(Plan *p, int it) {
   (void)it;
-  if (!p->grad[0] || !p->grad[1] || !p->bprev) return fail(p, GPI_E_STATE, "adjoint step without gradient buffers");
-  const int A1 = p->cur[0], B1 = A1 ^ 1, A2 = p->cur[1];
-  GradArgs g;
-  g.nz = p->d.nz;
-  g.nx = p->d.nx;
-  g.NZP = p->NZP;
-  g.fs = p->fstride;
-  g.nshots = p->d.nshots;
-  g.p1A = p->state[A1][0][GPI_P];
-  g.p1B = p->state[B1][0][GPI_P];
-  g.p2A = p->state[A2][1][GPI_P];
-  g.vx1A = p->state[A1][0][GPI_VX];
-  g.vx1B = p->state[B1][0][GPI_VX];
-  g.vx2A = p->state[A2][1][GPI_VX];
-  g.vz1A = p->state[A1][0][GPI_VZ];
-  g.vz1B = p->state[B1][0][GPI_VZ];
-  g.vz2A = p->state[A2][1][GPI_VZ];
-  g.prev = p->bprev;
-  g.pstride = p->bstep;
-  g.nb = p->d.nbound;
-  g.npx = (p->d.pml_faces & GPI_XMIN) ? p->d.npml : 0;
-  g.npz = (p->d.pml_faces & GPI_ZMIN) ? p->d.npml : 0;
-  g.gK = p->grad[0];
-  g.gR = p->grad[1];
-  g.dtI = (float)(1.0 / p->d.dt);
-  g.imaging = p->d.imaging;
-  // wavefield 1 (time reversal, boundary already forced), then wavefield 2
-  int rc = step_a2_wavefield(p, 0, 0);
-  if (!rc) rc = step_a2_wavefield(p, 1, 0);
-  if (rc) return rc;
-  k_grad_a2<<<152 * 16, 256, 0, p->stream>>>(g);
+  if (!p->grad[0] || !p->grad[1] || !p->bprev || !p->img[0] || !p->img[1])
+    return fail(p, GPI_E_STATE, "adjoint step without gradient buffers");
+  // wavefield 1 (time reversal, boundary already forced), wavefield 2 and
+  // the imaging condition in one pass over the state
+  return step_a2_adjoint_fused(p);
+}
+
+// The rho gradient from the per-velocity-cell sums hx, hz of the adjoint
+// run (compute_gmodrho! + combine_gmodrho!, src/fdtd/gradient.jl:31-56, with
+// the sum over the steps taken before the neighbour averages):
+//   imaging 0: g_rho[r, c] = -(hx[r, c-3] + hx[r, c-2]) / 2 - (hz[r-3, c] + hz[r-2, c]) / 2,
+//              r in 4..nz-3, c in 4..nx-3
+//   imaging 1: g_rho[r, c] = -(hx[r, c+2] + hx[r, c+3]) / 2 - (hz[r+2, c] + hz[r+3, c]) / 2
+//              over the updated velocity cells (vx rows 4..nz-3, columns
+//              4..nx; vz rows 4..nz, columns 4..nx-3)
+__global__ void __launch_bounds__(256) k_img_rho(const float *hx, const float *hz, float *gR, int nz, int nx, int NZP,
+                                                 int64_t fs, int nshots, int imaging) {
+  const int64_t per = (int64_t)nz * nx;
+  const int64_t total = per * nshots;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int shot = (int)(i / per);
+    const int64_t k = i - shot * per;
+    const int r = (int)(k % nz) + 1, c = (int)(k / nz) + 1;
+    const int64_t so = shot * fs;
+    auto S = [&](int rr, int cc) -> int64_t { return so + (int64_t)(cc + XOFF - 1) * NZP + (rr + ZOFF - 1); };
+    const int64_t o = S(r, c);
+    if (imaging) {
+      auto bx = [&](int cc) { return cc >= 4 && cc <= nx ? hx[S(r, cc)] : 0.f; };
+      auto bz = [&](int rr) { return rr >= 4 && rr <= nz ? hz[S(rr, c)] : 0.f; };
+      const float avx = r >= 4 && r <= nz - 3 ? (bx(c + 2) + bx(c + 3)) * 0.5f : 0.f;
+      const float avz = c >= 4 && c <= nx - 3 ? (bz(r + 2) + bz(r + 3)) * 0.5f : 0.f;
+      gR[o] = gR[o] - avx - avz;
+    } else if (r >= 4 && r <= nz - 3 && c >= 4 && c <= nx - 3) {
+      gR[o] = gR[o] - (hx[S(r, c - 3)] + hx[S(r, c - 2)]) * 0.5f - (hz[S(r - 3, c)] + hz[S(r - 2, c)]) * 0.5f;
+    }
+  }
+}
+
+int img_rho_finish(Plan *p) {
+  k_img_rho<<<152 * 16, 256, 0, p->stream>>>(p->img[0], p->img[1], p->grad[1], p->d.nz, p->d.nx, p->NZP, p->fstride,
+                                              p->d.nshots, p->d.imaging);
   p->launches++;
   GPI_CUDA(p, cudaGetLastError());
   return GPI_OK;

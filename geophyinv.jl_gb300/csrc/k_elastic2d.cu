@@ -544,39 +544,23 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
     if constexpr (MODE == 1 || MODE == 2) {
       // iteration it handles column c = xbase + it: slot(c + m) = (it + m) % RING
       const int ncol = x1 - xbase;
-      if constexpr (MODE == 1) {
-        // unrolled by RING: constant slot indices (see the interior loop)
-        for (int base = 0; base < ncol; base += RING) {
-          const uint32_t ph = (uint32_t)(base / RING) & 1u;
-#pragma unroll
-          for (int u = 0; u < RING; u++) {
-            const int it = base + u;
-            if (it >= ncol) break;
-            const int c = xbase + it, cc = c + 3;
-            int ib0, ie0, ib1, ie1, bs = 0, es = 0;
-            cvx.range(a.cells, cc, ib0, ie0);
-            cvz.range(a.cells, cc, ib1, ie1);
-            if (c >= x0) cst.range(a.cells, c, bs, es);
-            if (!mbar_wait(&bar[(u + 3) % RING], ph ^ (uint32_t)((u + 3) / RING))) s_err = 1;
-            vel_band(cc, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, ib0, ie0, ib1, ie1);
-            __syncthreads();
-            if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((u + RING - 1) % RING);
-            if (c >= x0) str_band(c, u % RING, (u + 1) % RING, (u + 2) % RING, (u + 3) % RING, bs, es);
-          }
-        }
-      } else {
-        for (int it = 0; it < ncol; it++) {
-          const int c = xbase + it, cc = c + 3;
-          int ib0, ie0, ib1, ie1, bs = 0, es = 0;
-          cvx.range(a.cells, cc, ib0, ie0);
-          cvz.range(a.cells, cc, ib1, ie1);
-          if (c >= x0) cst.range(a.cells, c, bs, es);
-          if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
-          vel_band(cc, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, ib0, ie0, ib1, ie1);
-          __syncthreads();
+      // a rolled loop: the band code unrolled by the ring length overflows
+      // the instruction cache
+      for (int it = 0; it < ncol; it++) {
+        const int c = xbase + it, cc = c + 3;
+        int ib0, ie0, ib1, ie1, bs = 0, es = 0;
+        cvx.range(a.cells, cc, ib0, ie0);
+        cvz.range(a.cells, cc, ib1, ie1);
+        if (c >= x0) cst.range(a.cells, c, bs, es);
+        if (!mbar_wait(&bar[(it + 3) % RING], ((it + 3) / RING) & 1)) s_err = 1;
+        vel_band(cc, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, ib0, ie0, ib1, ie1);
+        __syncthreads();
+        if constexpr (MODE == 1) {
+          if (issuer && it >= 1 && c + RING - 1 <= xlast) issue_fast((it + RING - 1) % RING);
+        } else {
           if (issuer) issue(c + RING - 1);
-          if (c >= x0) str_band(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, bs, es);
         }
+        if (c >= x0) str_band(c, it % RING, (it + 1) % RING, (it + 2) % RING, (it + 3) % RING, bs, es);
       }
     } else {
       // velocities of column cc: update_v! with CPML, mirrors, sources

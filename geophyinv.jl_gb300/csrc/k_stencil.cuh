@@ -64,6 +64,36 @@ __device__ __forceinline__ void inject(const InjCell *cells, const float *amount
     if (cells[k].row == row) v = v + amount[k];
 }
 
+// Injection cells read through a view: column, row and amount of cell k at
+// col[k * st], row[k * st], amt[k] -- the cells in global memory (st =
+// sizeof(InjCell) / 4) or a block's copy in shared memory (st = 1).
+struct InjView {
+  const int *col, *row;
+  const float *amt;
+  int st;
+};
+struct InjVCursor {
+  int cur, end, ncol;
+  __device__ __forceinline__ void init(const InjView &v, int b, int e) {
+    cur = b;
+    end = e;
+    ncol = cur < end ? v.col[cur * v.st] : 0x7fffffff;
+  }
+  // the [b, e) range of cells in column `col`, advancing past it
+  __device__ __forceinline__ void range(const InjView &v, int col, int &b, int &e) {
+    b = cur;
+    if (ncol == col) {
+      while (cur < end && v.col[cur * v.st] == col) cur++;
+      ncol = cur < end ? v.col[cur * v.st] : 0x7fffffff;
+    }
+    e = cur;
+  }
+};
+__device__ __forceinline__ void inject(const InjView &v, int b, int e, int row, float &x) {
+  for (int k = b; k < e; k++)
+    if (v.row[k * v.st] == row) x = x + v.amt[k];
+}
+
 // ---------------------------------------------------------------------------
 // bulk asynchronous copies (TMA engine, 1-D form) completing on mbarriers
 // ---------------------------------------------------------------------------

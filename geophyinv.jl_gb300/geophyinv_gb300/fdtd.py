@@ -584,8 +584,10 @@ def _update_srcwav(pa, srcwav, src_types=None):
                     w = S.reverse_source(w)
                 if np.all(w == 0):
                     continue
-                fpeaks.append(S.findfreq_peak(w, pa.dt))
+                # frequency bounds come from the first wavefield only
+                # (source.jl:231-246); the adjoint sources need no spectrum
                 if ipw == 0:
+                    fpeaks.append(S.findfreq_peak(w, pa.dt))
                     fmaxs.append(S.findfreq(w, pa.dt, "max"))
                 wf = np.asfortranarray(w, np.float32)
                 if ipw == 0:
