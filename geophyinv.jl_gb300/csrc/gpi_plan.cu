@@ -29,7 +29,61 @@ int fail(Plan *p, int code, const std::string &msg) {
 
 // Stream-ordered device allocations and uploads on the plan's stream: no
 // device-wide synchronisation, so plans of other requests keep running.
-static cudaError_t dalloc(Plan &p, void **ptr, size_t bytes) { return cudaMallocAsync(ptr, bytes, p.stream); }
+// They come from one memory pool per device owned by the engine, which
+// keeps freed memory for the next plan: a pool that returns memory to the
+// system at a stream synchronisation (the default pool's behaviour) makes
+// that synchronisation wait for every stream of the device, so one request
+// finishing would stall all the others.  The pool is trimmed when the last
+// plan of its device is destroyed.
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pools[64] = {};
+static int g_live[64] = {};
+
+static cudaMemPool_t engine_pool(int dev) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (dev < 0 || dev >= 64) return nullptr;
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    g_pools[dev] = pool;
+  }
+  return g_pools[dev];
+}
+
+// a stream-ordered allocation from the engine's pool of the current device
+// (the device's default pool if the engine's could not be created)
+cudaError_t pool_alloc(void **ptr, size_t bytes, cudaStream_t st) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaMemPool_t pool = engine_pool(dev);
+  return pool ? cudaMallocFromPoolAsync(ptr, bytes, pool, st) : cudaMallocAsync(ptr, bytes, st);
+}
+
+static void plan_born(int dev) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (dev >= 0 && dev < 64) g_live[dev]++;
+}
+// the last plan of a device gives the pool's memory back (once its own
+// frees, ordered on its stream, have run)
+static void plan_gone(int dev, cudaStream_t st) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (dev < 0 || dev >= 64) return;
+  if (--g_live[dev] == 0 && g_pools[dev]) {
+    if (st) cudaStreamSynchronize(st);
+    cudaMemPoolTrimTo(g_pools[dev], 0);
+  }
+}
+
+static cudaError_t dalloc(Plan &p, void **ptr, size_t bytes) { return pool_alloc(ptr, bytes, p.stream); }
 static cudaError_t h2d(Plan &p, void *dst, const void *src, size_t bytes) {
   return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, p.stream);
 }
@@ -295,7 +349,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
     cudaGetLastError();
     return fail(nullptr, GPI_E_CUDA, "stream creation failed");
   }
-  cudaError_t e = cudaMallocAsync(&p.pool, total, cs);
+  cudaError_t e = pool_alloc(&p.pool, total, cs);
   if (e != cudaSuccess) {
     cudaStreamDestroy(cs);
     delete pl;
@@ -352,6 +406,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
       p.ev_fork = nullptr;
     }
   }
+  plan_born(p.device);
   *out = pl;
   return GPI_OK;
 }
@@ -430,6 +485,7 @@ void destroy(gpi_plan *pl) {
     p.born = nullptr;
   }
   free_dev(p, p.pool);
+  plan_gone(p.device, p.stream);
   if (p.own_stream) cudaStreamDestroy(p.own_stream);
   cudaSetDevice(dev);
   delete pl;
@@ -484,7 +540,7 @@ int set_born(Plan &p, const float *const *dmod, int on_device) {
     return fail(&p, GPI_E_UNSUPPORTED, "Born modelling: 2-D acoustic plans with npw = 2");
   if (!dmod || !dmod[0] || !dmod[1]) return fail(&p, GPI_E_INVALID, "dmod arrays");
   if (!p.born) {
-    if (cudaMallocAsync((void **)&p.born, 5 * p.fstride * sizeof(float), p.stream) != cudaSuccess) {
+    if (pool_alloc((void **)&p.born, 5 * p.fstride * sizeof(float), p.stream) != cudaSuccess) {
       cudaGetLastError();
       p.born = nullptr;
       return fail(&p, GPI_E_NOMEM, "Born perturbation buffers");
@@ -1204,7 +1260,7 @@ int get_records(Plan &p, int shot, int field, float *out, int on_device) {
   // pool layout [it][ir] -> Recs layout (it fastest)
   if (on_device) return transpose_records(&p, out, src, nt, nr);
   float *tmp = nullptr;
-  GPI_CUDA(&p, cudaMallocAsync(&tmp, (size_t)nt * nr * sizeof(float), p.stream));
+  GPI_CUDA(&p, pool_alloc((void **)&tmp, (size_t)nt * nr * sizeof(float), p.stream));
   int rc = transpose_records(&p, tmp, src, nt, nr);
   if (!rc) rc = cudaMemcpyAsync(out, tmp, (size_t)nt * nr * sizeof(float), cudaMemcpyDeviceToHost, p.stream)
                     ? fail(&p, GPI_E_CUDA, "records copy")
@@ -1228,7 +1284,7 @@ int set_snapshots(Plan &p, int field, int n, const int *its) {
   p.snap_its.assign(its, its + n);
   p.snap_field = field;
   const size_t bytes = (size_t)p.d.npw * n * p.fstride * p.d.nshots * sizeof(float);
-  if (cudaMallocAsync((void **)&p.snap_buf, bytes, p.stream) != cudaSuccess) {
+  if (pool_alloc((void **)&p.snap_buf, bytes, p.stream) != cudaSuccess) {
     cudaGetLastError();
     p.snap_buf = nullptr;
     p.snap_its.clear();
@@ -1279,7 +1335,7 @@ int get_gradient(Plan &p, int param, float *out, int on_device) {
   // snapshot region is not allowed (it is state), so reduce in place into a
   // temporary owned by the plan
   float *tmp = nullptr;
-  GPI_CUDA(&p, cudaMallocAsync(&tmp, p.fstride * sizeof(float), p.stream));
+  GPI_CUDA(&p, pool_alloc((void **)&tmp, p.fstride * sizeof(float), p.stream));
   int rc = reduce_gradient(&p, param, tmp);
   if (!rc) rc = from_storage(p, out, tmp, p.d.nz, p.d.ny, p.d.nx, on_device);
   cudaFreeAsync(tmp, p.stream);

@@ -124,7 +124,8 @@ class L2DistLoss:
     deriv 2 (output - target), called as loss(dobs, dcal)."""
 
     def value(self, output, target):
-        return float(np.sum((np.asarray(output, np.float64) - np.asarray(target, np.float64)) ** 2))
+        r = np.subtract(np.asarray(output), np.asarray(target), dtype=np.float64).ravel(order="K")
+        return float(np.dot(r, r))
 
     def deriv(self, output, target):
         return (np.float32(2) * (np.asarray(output, np.float32) - np.asarray(target, np.float32))).astype(np.float32)
@@ -706,7 +707,8 @@ def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
     for o, c in zip(_local(pa, dobs), pa.data[0]):
         s = Srcs(o.n, pa.tgrid, pa.rfields)
         for f in pa.rfields:
-            s.d[f] = loss.deriv(o.d[f], c.d[f])[::-1].copy()  # reverse!(srcwav[2])
+            # reverse!(srcwav[2]), laid out as the engine takes wavelets
+            s.d[f] = np.asfortranarray(loss.deriv(o.d[f], c.d[f])[::-1])
         adj.append(s)
     pa.srcwav[1] = adj
     # a checkpointed plan recomputes wavefield 1 forward in time, with the
