@@ -148,6 +148,7 @@ struct Plan {
   // tile of each class holds: wavefield 1, wavefield 2, both; sizes the
   // shared-memory copy of the 2-D acoustic step kernel (0: none)
   int inj_tile[3][4] = {};
+  std::vector<int4> h_tiles;  // host copy of the tile list (batches tag and concatenate them)
   // 2-D z-strip CPML memory: column stride and the window of a column that
   // the general step kernel stages per ring slot
   int zsw = 0, pzw = 0;
@@ -243,6 +244,21 @@ int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_adjoint_acoustic2d(Plan *p, int it);
 int step_a2_wavefield(Plan *p, int ipw, int vonly);
 int step_a2_adjoint_fused(Plan *p);  // both wavefields + imaging condition
+// batches of forward plans (gpi_batch.cu): argument tables and launches of
+// the step kernels over the tagged tiles of several plans
+size_t a2_args_bytes();
+void a2_batch_args(Plan *p, void *out, size_t smem[4]);
+int a2_batch_launch(Plan *p, int m, const void *args, const int4 *tiles, int n, int par, size_t smem, cudaStream_t st);
+size_t e2_args_bytes();
+void e2_batch_args(Plan *p, void *out, size_t smem[4]);
+int e2_batch_launch(Plan *p, int m, const void *args, const int4 *tiles, int n, int par, size_t smem, cudaStream_t st);
+size_t aux_args_bytes();
+int aux_batch_args(Plan *p, void *out);  // returns its block count
+int aux_batch_launch(Plan *p, const void *args, const int *first, int nplans, int nblocks, int par, int off,
+                     cudaStream_t st);
+int run_prepare_forward(Plan &p);
+cudaError_t pool_alloc(void **ptr, size_t bytes, cudaStream_t st);  // the engine's memory pool
+int run_finish_forward(Plan &p);
 int img_rho_finish(Plan *p);         // the rho gradient from img[0], img[1]
 int step3_wavefield(Plan *p, int ipw, int vonly);
 // checkpointed adjoint (gpi_ckpt.cu)

@@ -972,6 +972,7 @@ static int build_tiles(Plan &p) {
   p.d_tiles = nullptr;
   GPI_CUDA(&p, dalloc(p, (void **)&p.d_tiles, n * sizeof(int4)));
   GPI_CUDA(&p, h2d(p, p.d_tiles, t.data(), n * sizeof(int4)));
+  p.h_tiles = t;
   return GPI_OK;
 }
 
@@ -1103,12 +1104,44 @@ int run(Plan &p, int mode) {
   return rc;
 }
 
+// A forward run split for a batch (gpi_batch.cu), which issues the steps of
+// several plans together: what run() and run_body() do before the time loop
+// (tables compiled, state and records zeroed) ...
+int run_prepare_forward(Plan &p) {
+  int rc = GPI_OK;
+  const bool recompile = p.rec_dirty || p.src_dirty || !p.d_tiles;
+  if (p.rec_dirty) rc = compile_receivers(p);
+  if (!rc && p.src_dirty) {
+    rc = compile_sources(p);
+    if (!rc) rc = build_tiles(p);
+  }
+  if (!rc && !p.d_tiles) rc = build_tiles(p);
+  if (!rc && recompile) drop_graphs(p);
+  if (!rc) rc = zero_state(p);
+  p.launches = 0;
+  if (!rc && p.rec_pool)
+    rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
+  return rc;
+}
+
+// ... and after it: the velocity records of the last step and the extra
+// velocity half step (propagate.jl:254-255)
+int run_finish_forward(Plan &p) {
+  int rc = aux_step(&p, p.d.nt + 1, GPI_FORWARD);
+  if (!rc) rc = step(p, 1, p.d.nt + 1, GPI_FORWARD, 1);
+  if (!rc) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fail(&p, GPI_E_CUDA, cudaGetErrorString(e));
+  }
+  return rc;
+}
+
 int ensure_smem_attr(Plan *p, const void *fn, int slot, size_t bytes) {
   static std::mutex mu;
-  static size_t done[16][64] = {};
+  static size_t done[32][64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || slot < 0 || slot >= 16) return fail(p, GPI_E_UNSUPPORTED, "kernel slot or device index");
+  if (dev < 0 || dev >= 64 || slot < 0 || slot >= 32) return fail(p, GPI_E_UNSUPPORTED, "kernel slot or device index");
   std::lock_guard<std::mutex> lock(mu);
   if (done[slot][dev] >= bytes) return GPI_OK;
   GPI_CUDA(p, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));

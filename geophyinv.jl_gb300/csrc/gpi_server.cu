@@ -23,6 +23,7 @@
 //
 // No counterpart in the reference: its update!(pa) runs one experiment at a
 // time on each Distributed worker (src/fdtd/propagate.jl:100-106).
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -35,6 +36,10 @@
 #include "../../include/gpi_fdtd.h"
 
 namespace {
+
+// cells per step (extended grid x shots) up to which a 2-D forward request
+// joins a batch
+constexpr int64_t kBatchCells = 4 << 20;
 
 struct Proj {
   int shot = 0, field = 0, n = 0;
@@ -49,6 +54,7 @@ struct Job {
   int64_t id = 0;
   gpi_plan_desc desc{};
   int gradient = 0, graph = 0;
+  int kind = 0;  // 0 a worker thread's; 1 + physics: the batch of 2-D forward requests of that physics
   std::vector<std::vector<float>> mod;
   std::vector<float> pml;
   std::vector<Proj> src, rec;
@@ -82,6 +88,7 @@ struct gpi_server {
   bool stop = false;
   int64_t next_id = 1;
   std::vector<std::thread> workers;
+  int max_batch = 16;  // members of a batch (0: no batches)
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
   double now() const {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -97,9 +104,11 @@ int sfail(int code, const std::string &m) {
   return code;
 }
 
-// the whole life of one admitted request on a worker's stream
-int process(Job &j, cudaStream_t st) {
+// a request's plan with its medium, CPML profiles, receivers and sources,
+// its set-up work on stream st
+int prepare(Job &j, cudaStream_t st, gpi_plan **out) {
   gpi_plan *plan = nullptr;
+  *out = nullptr;
   int rc = gpi_plan_create(&j.desc, &plan);
   auto check = [&](int r) {
     if (r && j.message.empty()) j.message = gpi_last_error(plan);
@@ -110,7 +119,6 @@ int process(Job &j, cudaStream_t st) {
     return rc;
   }
   const gpi_plan_desc &d = j.desc;
-  const int nt = d.nt;
   do {
     if ((rc = check(gpi_set_stream(plan, st)))) break;
     std::vector<const float *> mp;
@@ -131,13 +139,42 @@ int process(Job &j, cudaStream_t st) {
         break;
     if (rc) break;
     if (j.graph && (rc = check(gpi_set_graph(plan, j.graph)))) break;
+  } while (false);
+  if (rc) {
+    gpi_plan_destroy(plan);
+    return rc;
+  }
+  *out = plan;
+  return GPI_OK;
+}
+
+// the records of a finished forward run
+int fetch_records(Job &j, gpi_plan *plan) {
+  int rc = GPI_OK;
+  j.records.assign(j.rec.size(), {});
+  for (size_t k = 0; k < j.rec.size() && !rc; k++) {
+    j.records[k].resize((size_t)j.desc.nt * j.rec[k].n);
+    rc = gpi_get_records(plan, j.rec[k].shot, j.rec[k].field, j.records[k].data(), 0);
+    if (rc && j.message.empty()) j.message = gpi_last_error(plan);
+  }
+  return rc;
+}
+
+// the whole life of one admitted request on a worker's stream
+int process(Job &j, cudaStream_t st) {
+  gpi_plan *plan = nullptr;
+  int rc = prepare(j, st, &plan);
+  if (rc) return rc;
+  auto check = [&](int r) {
+    if (r && j.message.empty()) j.message = gpi_last_error(plan);
+    return r;
+  };
+  const gpi_plan_desc &d = j.desc;
+  const int nt = d.nt;
+  do {
     if ((rc = check(gpi_run(plan, j.gradient ? GPI_FORWARD_SAVE : GPI_FORWARD)))) break;
-    j.records.assign(j.rec.size(), {});
-    for (size_t k = 0; k < j.rec.size() && !rc; k++) {
-      j.records[k].resize((size_t)nt * j.rec[k].n);
-      rc = check(gpi_get_records(plan, j.rec[k].shot, j.rec[k].field, j.records[k].data(), 0));
-    }
-    if (rc || !j.gradient) break;
+    if ((rc = fetch_records(j, plan))) break;
+    if (!j.gradient) break;
     // adjoint sources 2 (dobs - dcal), reversed in time; misfit sum (dobs - dcal)^2
     double loss = 0;
     for (size_t k = 0; k < j.rec.size() && !rc; k++) {
@@ -187,6 +224,13 @@ int process(Job &j, cudaStream_t st) {
   return rc;
 }
 
+// the first queued request of a kind (arrival order within each kind)
+Job *first_of(gpi_server *s, int kind) {
+  for (Job *j : s->queue)
+    if (j->kind == kind) return j;
+  return nullptr;
+}
+
 void worker(gpi_server *s) {
   cudaSetDevice(s->d.device);
   cudaStream_t st = nullptr;
@@ -197,13 +241,12 @@ void worker(gpi_server *s) {
       std::unique_lock<std::mutex> lock(s->mu);
       s->cv.wait(lock, [&] {
         if (s->stop) return true;
-        if (s->queue.empty()) return false;
-        Job *h = s->queue.front();
-        return s->inflight == 0 || s->used + h->bytes <= s->d.hbm_budget;
+        Job *h = first_of(s, 0);
+        return h && (s->inflight == 0 || s->used + h->bytes <= s->d.hbm_budget);
       });
       if (s->stop) break;
-      j = s->queue.front();
-      s->queue.pop_front();
+      j = first_of(s, 0);
+      s->queue.erase(std::find(s->queue.begin(), s->queue.end(), j));
       s->used += j->bytes;
       s->inflight++;
       j->state = RUNNING;
@@ -224,6 +267,111 @@ void worker(gpi_server *s) {
   if (have_stream) cudaStreamDestroy(st);
 }
 
+// The batch of 2-D forward requests of one physics: admitted requests join
+// it (their plans set up on a second stream while the batch runs), each
+// gpi_batch_advance issues a stretch of steps of every member, and the
+// records of the members that finished in the previous stretch are read
+// while the current one runs.  At most two stretches are in flight.
+void batch_worker(gpi_server *s, int physics) {
+  const int kind = 1 + physics;
+  constexpr int kStretch = 64;
+  cudaSetDevice(s->d.device);
+  cudaStream_t st = nullptr, prep = nullptr;
+  cudaEvent_t ev[2] = {};
+  gpi_batch *b = nullptr;
+  bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&prep, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming) == cudaSuccess &&
+            gpi_batch_create(s->d.device, st, &b) == GPI_OK;
+  std::map<gpi_plan *, Job *> members;
+  std::vector<std::pair<Job *, gpi_plan *>> finishing;  // finished in the previous stretch
+  int nev = 0;
+  auto complete = [&](Job *j, int rc) {
+    std::lock_guard<std::mutex> lock(s->mu);
+    j->status = rc;
+    j->state = rc ? FAILED : DONE;
+    j->t_done = s->now();
+    s->used -= j->bytes;
+    s->inflight--;
+  };
+  for (;;) {
+    std::vector<Job *> admit;
+    {
+      std::unique_lock<std::mutex> lock(s->mu);
+      if (members.empty() && finishing.empty())
+        s->cv.wait(lock, [&] { return s->stop || first_of(s, kind) != nullptr; });
+      if (s->stop && members.empty() && finishing.empty()) break;
+      for (;;) {
+        Job *h = first_of(s, kind);
+        if (!h || s->stop || (int)(members.size() + admit.size()) >= s->max_batch) break;
+        if (!(s->inflight == 0 || s->used + h->bytes <= s->d.hbm_budget)) break;
+        s->queue.erase(std::find(s->queue.begin(), s->queue.end(), h));
+        s->used += h->bytes;
+        s->inflight++;
+        h->state = RUNNING;
+        h->t_admit = s->now();
+        admit.push_back(h);
+      }
+    }
+    for (Job *j : admit) {
+      gpi_plan *plan = nullptr;
+      int rc = ok ? prepare(*j, prep, &plan) : GPI_E_CUDA;
+      if (!ok) j->message = "batch worker streams or batch creation failed";
+      if (!rc && (rc = gpi_batch_add(b, plan))) j->message = gpi_batch_error(b);
+      if (rc) {
+        if (plan) gpi_plan_destroy(plan);
+        complete(j, rc);
+        s->cv.notify_all();
+        continue;
+      }
+      members[plan] = j;
+    }
+    // at most two stretches in flight: wait for the one before the last
+    if (nev >= 2) cudaEventSynchronize(ev[nev & 1]);
+    int active = 0;
+    int rc = ok ? gpi_batch_advance(b, kStretch, &active) : GPI_E_CUDA;
+    if (ok) cudaEventRecord(ev[nev & 1], st);
+    nev++;
+    // records of the members that finished in the previous stretch
+    for (auto &f : finishing) {
+      const int r = rc ? rc : fetch_records(*f.first, f.second);
+      if (rc && f.first->message.empty()) f.first->message = gpi_batch_error(b);
+      gpi_plan_destroy(f.second);
+      complete(f.first, r);
+    }
+    if (!finishing.empty()) s->cv.notify_all();
+    finishing.clear();
+    gpi_plan *done[64];
+    int n = 0;
+    do {
+      if (gpi_batch_finished(b, done, 64, &n)) break;
+      for (int k = 0; k < n; k++) {
+        finishing.push_back({members[done[k]], done[k]});
+        members.erase(done[k]);
+      }
+    } while (n == 64);
+    if (rc) {
+      // a failed stretch fails every member
+      std::string msg = gpi_batch_error(b);
+      for (auto &m : members) {
+        m.second->message = msg;
+        complete(m.second, rc);
+      }
+      members.clear();
+      gpi_batch_destroy(b);
+      b = nullptr;
+      ok = gpi_batch_create(s->d.device, st, &b) == GPI_OK;
+      s->cv.notify_all();
+    }
+  }
+  if (b) gpi_batch_destroy(b);
+  if (ev[0]) cudaEventDestroy(ev[0]);
+  if (ev[1]) cudaEventDestroy(ev[1]);
+  if (prep) cudaStreamDestroy(prep);
+  if (st) cudaStreamDestroy(st);
+}
+
 Job *find(gpi_server *s, int64_t id) {
   auto it = s->jobs.find(id);
   return it == s->jobs.end() ? nullptr : it->second;
@@ -242,9 +390,13 @@ int gpi_server_create(const gpi_server_desc *desc, gpi_server **out) {
     cudaGetLastError();
     return sfail(GPI_E_CUDA, "no such CUDA device");
   }
+  if (desc->max_batch < -1 || desc->max_batch > 4096) return sfail(GPI_E_INVALID, "max_batch: -1..4096");
   gpi_server *s = new gpi_server();
   s->d = *desc;
+  s->max_batch = desc->max_batch == 0 ? 16 : desc->max_batch < 0 ? 0 : desc->max_batch;
   for (int i = 0; i < desc->max_inflight; i++) s->workers.emplace_back(worker, s);
+  if (s->max_batch > 0)
+    for (int ph : {GPI_ACOUSTIC, GPI_ELASTIC}) s->workers.emplace_back(batch_worker, s, ph);
   *out = s;
   return GPI_OK;
 }
@@ -297,6 +449,10 @@ int gpi_server_submit(gpi_server *s, const gpi_request *r, int64_t *id) {
   j->desc = d;
   j->gradient = r->gradient;
   j->graph = r->graph;
+  // small 2-D forward requests (launch-bound alone) join the batch of their
+  // physics; large ones fill the device on their own
+  const bool small = (int64_t)d.nz * d.nx * d.nshots <= kBatchCells;
+  j->kind = (!r->gradient && d.ndim == 2 && small && s->max_batch > 0) ? 1 + d.physics : 0;
   const int nmod = d.physics == GPI_ACOUSTIC ? 2 : 3;
   const int64_t cells = grid_cells(d);
   for (int i = 0; i < nmod; i++) {

@@ -137,9 +137,10 @@ __device__ __forceinline__ int64_t a2_strip_index(const A2Img &g, int nz, int nx
 // code for the edge and source columns).
 // NW = 1: one wavefield (a.w[0]); NW = 2: the adjoint step of both
 // wavefields with the imaging condition (a.g), one pass over the state.
+// The body takes the arguments by reference: the kernel's own parameters
+// (one plan) or a plan's arguments copied to shared memory (k_a2_batch).
 template <int MODE, int NW>
-__global__ void __launch_bounds__(A2_THREADS, NW == 2 ? (MODE == 0 ? 5 : MODE == 1 ? 4 : 3) : (MODE == 0 ? 6 : MODE == 1 ? 5 : 4))
-    k_a2(const A2Args a) {
+__device__ __forceinline__ void a2_body(const A2Args &a, const int4 tile) {
   using L = A2L<NW>;
   constexpr bool FAST = MODE == 0, XPSI = MODE >= 2, IMG = NW == 2;
   constexpr int TZ = L::TZ, R8 = L::R8, R4 = L::R4, SLOT = L::SLOT, RING = L::RING;
@@ -153,8 +154,7 @@ __global__ void __launch_bounds__(A2_THREADS, NW == 2 ? (MODE == 0 ? 5 : MODE ==
   __shared__ int s_beg[3 * NW], s_cnt[3 * NW];
   __shared__ int s_err;
   const int t = threadIdx.x;
-  const int4 tile = a.tiles[blockIdx.x];
-  const int zb = tile.x, shot = tile.w;
+  const int zb = tile.x, shot = tile.w & 0xffff;  // (the high half: a batch's plan slot)
   const int z0 = 1 + zb * TZ, x0 = tile.y, x1 = tile.z;
   const int xbase = x0 - 3, xlast = x1 + 2;
   const bool lastx = x1 == a.nx + 1, lastz = zb == a.nzb - 1;
@@ -790,6 +790,29 @@ __global__ void __launch_bounds__(A2_THREADS, NW == 2 ? (MODE == 0 ? 5 : MODE ==
   }
 }
 
+template <int MODE, int NW>
+__global__ void __launch_bounds__(A2_THREADS, NW == 2 ? (MODE == 0 ? 5 : MODE == 1 ? 4 : 3) : (MODE == 0 ? 6 : MODE == 1 ? 5 : 4))
+    k_a2(const A2Args a) {
+  a2_body<MODE, NW>(a, a.tiles[blockIdx.x]);
+}
+
+// One step of several plans in one launch (a batch, gpi_batch.cu): the
+// tiles of every plan of one class, each tagged with its plan's slot in the
+// high half of .w; the block copies its plan's arguments for this class and
+// buffer parity (args[(slot * 4 + MODE) * 2 + par]) to shared memory.
+template <int MODE>
+__global__ void __launch_bounds__(A2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 5 : 4)
+    k_a2_batch(const A2Args *__restrict__ args, const int4 *__restrict__ tiles, int par) {
+  __shared__ __align__(16) A2Args sa;
+  const int4 tile = tiles[blockIdx.x];
+  const int slot = tile.w >> 16;
+  const int *src = reinterpret_cast<const int *>(args + ((int64_t)slot * 4 + MODE) * 2 + par);
+  int *dst = reinterpret_cast<int *>(&sa);
+  for (int i = threadIdx.x; i < (int)(sizeof(A2Args) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  a2_body<MODE, 1>(sa, tile);
+}
+
 int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   if (mode == GPI_ADJOINT && !vonly) return step_adjoint_acoustic2d(p, it);
   (void)ipw_mask;
@@ -797,10 +820,10 @@ int step_acoustic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   return step_a2_wavefield(p, 0, vonly);
 }
 
-// one time step of wavefield ipw (nw = 1: 0 the modelled, 1 the adjoint
-// wavefield) or of both wavefields with the imaging condition (nw = 2)
-static int a2_launch(Plan *p, int nw, int ipw, int vonly) {
-  A2Args a;
+// the arguments of one time step of wavefield ipw (nw = 1: 0 the modelled,
+// 1 the adjoint wavefield; `flip` swaps its buffers) or of both wavefields
+// with the imaging condition (nw = 2)
+static void a2_fill(Plan *p, int nw, int ipw, int vonly, int flip, A2Args &a) {
   a.nz = p->d.nz;
   a.nx = p->d.nx;
   a.NZP = p->NZP;
@@ -814,7 +837,7 @@ static int a2_launch(Plan *p, int nw, int ipw, int vonly) {
   a.w[1] = A2W{};
   for (int w = 0; w < nw; w++) {
     const int pw = nw == 2 ? w : ipw;
-    const int A = p->cur[pw], B = A ^ 1;
+    const int A = p->cur[pw] ^ flip, B = A ^ 1;
     A2W &f = a.w[w];
     f.pA = p->state[A][pw][GPI_P];
     f.vxA = p->state[A][pw][GPI_VX];
@@ -840,6 +863,8 @@ static int a2_launch(Plan *p, int nw, int ipw, int vonly) {
   a.tiles = p->d_tiles;
   a.zsw = p->zsw;
   a.pzw = p->pzw;
+  a.psf = 0;
+  a.inj_cap = 0;
   a.g = A2Img{};
   if (nw == 2) {
     a.g.gK = p->grad[0];
@@ -852,18 +877,32 @@ static int a2_launch(Plan *p, int nw, int ipw, int vonly) {
     a.g.npz = (p->d.pml_faces & GPI_ZMIN) ? p->d.npml : 0;
     a.g.dtI = (float)(1.0 / p->d.dt);
   }
-  // shared memory per block: the ring with the CPML memory each mode stages
+}
+
+// per tile class: CPML floats per ring slot and wavefield, room for the
+// injection cells of the largest tile (tiles with more than 2048 read them
+// from global memory), shared memory per block
+static void a2_sizes(const Plan *p, int nw, int ipw, int vonly, int psf[4], int cap[4], size_t smem[4]) {
   const bool zf = p->d.pml_faces & (GPI_ZMIN | GPI_ZMAX);
-  const int psf[4] = {0, zf ? 2 * p->pzw : 0, a2_psi_floats(*p), a2_psi_floats(*p)};
-  // room for the injection cells of the largest tile of each class (tiles
-  // with more than 2048 read them from global memory)
-  int cap[4];
+  psf[0] = 0;
+  psf[1] = zf ? 2 * p->pzw : 0;
+  psf[2] = psf[3] = a2_psi_floats(*p);
   for (int m = 0; m < 4; m++) cap[m] = p->inj_tile[nw == 2 ? 2 : ipw][m];
   if (vonly) cap[3] = std::max(cap[3], std::max(cap[1], cap[2]));  // every non-interior tile runs class 3's code
-  for (int m = 0; m < 4; m++)
+  for (int m = 0; m < 4; m++) {
     if (cap[m] > 2048) cap[m] = 0;
+    smem[m] = nw == 1 ? A2L<1>::smem(psf[m], cap[m]) : A2L<2>::smem(psf[m], cap[m]);
+  }
+}
+
+// one time step of wavefield ipw (nw = 1) or of both wavefields with the
+// imaging condition (nw = 2)
+static int a2_launch(Plan *p, int nw, int ipw, int vonly) {
+  A2Args a;
+  a2_fill(p, nw, ipw, vonly, 0, a);
+  int psf[4], cap[4];
   size_t smem[4];
-  for (int m = 0; m < 4; m++) smem[m] = nw == 1 ? A2L<1>::smem(psf[m], cap[m]) : A2L<2>::smem(psf[m], cap[m]);
+  a2_sizes(p, nw, ipw, vonly, psf, cap, smem);
   void (*const fn1[4])(A2Args) = {k_a2<0, 1>, k_a2<1, 1>, k_a2<2, 1>, k_a2<3, 1>};
   void (*const fn2[4])(A2Args) = {k_a2<0, 2>, k_a2<1, 2>, k_a2<2, 2>, k_a2<3, 2>};
   void (*const *fn)(A2Args) = nw == 1 ? fn1 : fn2;
@@ -910,6 +949,36 @@ static int a2_launch(Plan *p, int nw, int ipw, int vonly) {
 }
 
 int step_a2_wavefield(Plan *p, int ipw, int vonly) { return a2_launch(p, 1, ipw, vonly); }
+
+// --- batches of one-wavefield plans (gpi_batch.cu) ---
+size_t a2_args_bytes() { return sizeof(A2Args); }
+
+// a forward plan's arguments per tile class and buffer parity ([class][parity],
+// parity 1 with the buffers swapped) and its shared memory per class
+void a2_batch_args(Plan *p, void *out, size_t smem[4]) {
+  int psf[4], cap[4];
+  a2_sizes(p, 1, 0, 0, psf, cap, smem);
+  A2Args *o = static_cast<A2Args *>(out);
+  for (int m = 0; m < 4; m++)
+    for (int par = 0; par < 2; par++) {
+      A2Args &a = o[m * 2 + par];
+      a2_fill(p, 1, 0, 0, par, a);
+      a.tiles = nullptr;
+      a.psf = psf[m];
+      a.inj_cap = cap[m];
+    }
+}
+
+// one launch of tile class m over n tagged tiles of the batch's plans
+int a2_batch_launch(Plan *p, int m, const void *args, const int4 *tiles, int n, int par, size_t smem, cudaStream_t st) {
+  void (*const fn[4])(const A2Args *, const int4 *, int) = {k_a2_batch<0>, k_a2_batch<1>, k_a2_batch<2>,
+                                                             k_a2_batch<3>};
+  if (int rc = ensure_smem_attr(p, (const void *)fn[m], 16 + m, smem)) return rc;
+  if (n <= 0) return GPI_OK;  // (n = 0: only the kernel's shared-memory attribute)
+  fn[m]<<<n, A2_THREADS, smem, st>>>(static_cast<const A2Args *>(args), tiles, par);
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
 
 // the adjoint step of both wavefields with the imaging condition in one pass
 int step_a2_adjoint_fused(Plan *p) { return a2_launch(p, 2, 0, 0); }

@@ -134,13 +134,9 @@ struct AuxArgs {
   float dt;
 };
 
-__global__ void k_aux(AuxArgs a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a.it_dev) {
-    const int itd = *a.it_dev + a.it_off;
-    a.it = itd;
-    a.it2 = itd;
-  }
+// thread i of one plan's aux work (records first, then injection cells);
+// it, it2: the steps
+__device__ __forceinline__ void aux_body(const AuxArgs &a, int i, int it, int it2) {
   if (i < a.ntask) {
     // record!: p is sampled before step it, velocities after step it-1
     const RecTask t = a.tasks[i];
@@ -148,9 +144,9 @@ __global__ void k_aux(AuxArgs a) {
     // the reference records p (before the step) and velocities (after the
     // velocity sources) only; other rfields keep their zero records
     if (!isv && t.field != GPI_P) return;
-    const int tidx = isv ? a.it - 2 : a.it - 1;
+    const int tidx = isv ? it - 2 : it - 1;
     if (tidx < 0 || tidx >= a.nt) return;
-    if (!isv && a.it > a.nt) return;
+    if (!isv && it > a.nt) return;
     const float *f = a.field[t.field] + t.shot * a.fs;
     float s = 0.f;
     for (int e = t.e0; e < t.e1; e++) s = s + a.rw[e] * f[a.roff[e]];
@@ -159,7 +155,7 @@ __global__ void k_aux(AuxArgs a) {
   }
   i -= a.ntask;
   if (i >= a.ncells) return;
-  const int itc = i < a.split ? a.it : a.it2;
+  const int itc = i < a.split ? it : it2;
   if (itc < 1 || itc > a.nt) {
     if (a.zero) a.amount[i] = 0.f;
     return;
@@ -174,6 +170,88 @@ __global__ void k_aux(AuxArgs a) {
   else
     amt = pv * a.kcoef[c.off];  // muladd_tauii!
   a.amount[i] = amt;
+}
+
+__global__ void k_aux(AuxArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a.it_dev) {
+    const int itd = *a.it_dev + a.it_off;
+    aux_body(a, i, itd, itd);
+  } else {
+    aux_body(a, i, a.it, a.it2);
+  }
+}
+
+// The aux work of several plans in one launch (a batch, gpi_batch.cu):
+// plan k owns blocks [first[k], first[k+1]) and reads its arguments for
+// this buffer parity (args[2 k + par]) and its step (*it_dev + off).
+__global__ void k_aux_batch(const AuxArgs *__restrict__ args, const int *__restrict__ first, int nplans, int par,
+                            int off) {
+  __shared__ __align__(16) AuxArgs sa;
+  __shared__ int s_k;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nplans - 1;  // the last plan whose first block is <= blockIdx.x
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (first[mid] <= (int)blockIdx.x)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_k = lo;
+  }
+  __syncthreads();
+  const int k = s_k;
+  const int *src = reinterpret_cast<const int *>(args + 2 * k + par);
+  int *dst = reinterpret_cast<int *>(&sa);
+  for (int j = threadIdx.x; j < (int)(sizeof(AuxArgs) / sizeof(int)); j += blockDim.x) dst[j] = src[j];
+  __syncthreads();
+  const int itd = *sa.it_dev + off;
+  aux_body(sa, ((int)blockIdx.x - first[k]) * blockDim.x + threadIdx.x, itd, itd);
+}
+
+size_t aux_args_bytes() { return sizeof(AuxArgs); }
+
+// a forward plan's aux arguments for both buffer parities (its step read
+// from its device counter) and its block count (0: no aux work)
+int aux_batch_args(Plan *p, void *out) {
+  AuxArgs *o = static_cast<AuxArgs *>(out);
+  const int n = p->n_rtask + p->n_cells;
+  for (int par = 0; par < 2; par++) {
+    AuxArgs &a = o[par];
+    a = AuxArgs{};
+    a.tasks = p->d_rtask;
+    a.ntask = p->n_rtask;
+    a.roff = p->d_roff;
+    a.rw = p->d_rw;
+    a.rec = p->rec_pool;
+    a.it = a.it2 = 1;
+    a.nt = p->d.nt;
+    a.split = p->n_cells;
+    a.zero = 0;
+    a.it_dev = p->d_it;
+    a.it_off = 0;
+    for (int f = 0; f < NFIELD; f++) a.field[f] = p->state[p->cur[0] ^ par][0][f];
+    a.fs = p->fstride;
+    a.cells = p->d_cells;
+    a.ncells = p->n_cells;
+    a.pj = p->d_pair_j;
+    a.pw = p->d_pair_w;
+    a.wav = p->d_wav;
+    a.amount = p->d_amount;
+    a.rho = p->mod[p->d.physics == GPI_ACOUSTIC ? 1 : 2];
+    a.kcoef = p->d.physics == GPI_ACOUSTIC ? p->coef[p->ncoef - 1] : p->coef[p->ncoef - 2];
+    a.dt = (float)p->d.dt;
+  }
+  return (n + 127) / 128;
+}
+
+int aux_batch_launch(Plan *p, const void *args, const int *first, int nplans, int nblocks, int par, int off,
+                     cudaStream_t st) {
+  if (nblocks <= 0) return GPI_OK;
+  k_aux_batch<<<nblocks, 128, 0, st>>>(static_cast<const AuxArgs *>(args), first, nplans, par, off);
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
 }
 
 // source amounts of wavefield 1 at step it1 and of the adjoint wavefield at

@@ -79,8 +79,10 @@ inline size_t e2_smem_general(int psf, int ring) {
 // column: z strips, z mirrors, the free surface, sources); MODE 2: the same
 // with x-strip columns; MODE 3: tiles with x-edge columns (the band code plus
 // the general code for the edge and source columns).
+// The body takes the arguments by reference: the kernel's own parameters
+// (one plan) or a plan's arguments copied to shared memory (k_e2_batch).
 template <int MODE>
-__global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MODE == 2 ? 4 : 3) k_e2(const E2Args a) {
+__device__ __forceinline__ void e2_body(const E2Args &a, const int4 tile) {
   constexpr bool FAST = MODE == 0, XPSI = MODE >= 2;
   constexpr int RING = e2_ring(MODE);
   constexpr int TZ = E2_TZ, R8 = E2_R8, R4 = E2_R4, SLOT = E2_SLOT;
@@ -93,8 +95,7 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
   __shared__ int s_rng[3][2];
   __shared__ int s_err;
   const int t = threadIdx.x;
-  const int4 tile = a.tiles[blockIdx.x];
-  const int zb = tile.x, shot = tile.w;
+  const int zb = tile.x, shot = tile.w & 0xffff;  // (the high half: a batch's plan slot)
   const int z0 = 1 + zb * TZ, x0 = tile.y, x1 = tile.z;
   const int xbase = x0 - 3, xlast = x1 + 2;  // input columns of this block
   const bool lastx = x1 == a.nx + 1, lastz = zb == a.nzb - 1;
@@ -704,11 +705,30 @@ __global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MO
   }
 }
 
-int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
-  (void)ipw_mask;
-  (void)it;
-  (void)mode;
-  E2Args a;
+template <int MODE>
+__global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MODE == 2 ? 4 : 3) k_e2(const E2Args a) {
+  e2_body<MODE>(a, a.tiles[blockIdx.x]);
+}
+
+// One step of several plans in one launch (a batch, gpi_batch.cu): the
+// tiles of every plan of one class, each tagged with its plan's slot in the
+// high half of .w; the block copies its plan's arguments for this class and
+// buffer parity (args[(slot * 4 + MODE) * 2 + par]) to shared memory.
+template <int MODE>
+__global__ void __launch_bounds__(E2_THREADS, MODE == 0 ? 6 : MODE == 1 ? 6 : MODE == 2 ? 4 : 3)
+    k_e2_batch(const E2Args *__restrict__ args, const int4 *__restrict__ tiles, int par) {
+  __shared__ __align__(16) E2Args sa;
+  const int4 tile = tiles[blockIdx.x];
+  const int slot = tile.w >> 16;
+  const int *src = reinterpret_cast<const int *>(args + ((int64_t)slot * 4 + MODE) * 2 + par);
+  int *dst = reinterpret_cast<int *>(&sa);
+  for (int i = threadIdx.x; i < (int)(sizeof(E2Args) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  e2_body<MODE>(sa, tile);
+}
+
+// the arguments of one time step (`flip` swaps the buffers)
+static void e2_fill(Plan *p, int vonly, int flip, E2Args &a) {
   a.nz = p->d.nz;
   a.nx = p->d.nx;
   a.NZP = p->NZP;
@@ -720,7 +740,7 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.dxI = (float)(1.0 / (p->d.dx * 24.0));
   a.dzI = (float)(1.0 / (p->d.dz * 24.0));
   a.nzb = p->nzb;
-  const int A = p->cur[0], B = A ^ 1;
+  const int A = p->cur[0] ^ flip, B = A ^ 1;
   a.txxA = p->state[A][0][GPI_TAUXX];
   a.tzzA = p->state[A][0][GPI_TAUZZ];
   a.txzA = p->state[A][0][GPI_TAUXZ];
@@ -750,11 +770,28 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   a.tiles = p->d_tiles;
   a.zsw = p->zsw;
   a.pzw = p->pzw;
-  // shared memory per block: the ring with the CPML memory each mode stages
+  a.psf = 0;
+}
+
+// per tile class: CPML floats per ring slot and shared memory per block
+static void e2_sizes(const Plan *p, int psf[4], size_t smem[4]) {
   const bool zf = p->d.pml_faces & (GPI_ZMIN | GPI_ZMAX);
-  const int psf[4] = {0, zf ? 4 * p->pzw : 0, e2_psi_floats(*p), e2_psi_floats(*p)};
-  size_t smem[4];
+  psf[0] = 0;
+  psf[1] = zf ? 4 * p->pzw : 0;
+  psf[2] = psf[3] = e2_psi_floats(*p);
   for (int m = 0; m < 4; m++) smem[m] = m == 0 ? E2_SMEM : e2_smem_general(psf[m], e2_ring(m));
+}
+
+int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
+  (void)ipw_mask;
+  (void)it;
+  (void)mode;
+  E2Args a;
+  e2_fill(p, vonly, 0, a);
+  // shared memory per block: the ring with the CPML memory each mode stages
+  int psf[4];
+  size_t smem[4];
+  e2_sizes(p, psf, smem);
   void (*const fn[4])(E2Args) = {k_e2<0>, k_e2<1>, k_e2<2>, k_e2<3>};
   for (int m = 0; m < 4; m++)
     if (int rc = ensure_smem_attr(p, (const void *)fn[m], 4 + m, smem[m])) return rc;
@@ -787,6 +824,35 @@ int step_elastic2d(Plan *p, int ipw_mask, int it, int mode, int vonly) {
   }
   GPI_CUDA(p, cudaGetLastError());
   p->cur[0] ^= 1;
+  return GPI_OK;
+}
+
+// --- batches of plans (gpi_batch.cu) ---
+size_t e2_args_bytes() { return sizeof(E2Args); }
+
+// a forward plan's arguments per tile class and buffer parity ([class][parity],
+// parity 1 with the buffers swapped) and its shared memory per class
+void e2_batch_args(Plan *p, void *out, size_t smem[4]) {
+  int psf[4];
+  e2_sizes(p, psf, smem);
+  E2Args *o = static_cast<E2Args *>(out);
+  for (int m = 0; m < 4; m++)
+    for (int par = 0; par < 2; par++) {
+      E2Args &a = o[m * 2 + par];
+      e2_fill(p, 0, par, a);
+      a.tiles = nullptr;
+      a.psf = psf[m];
+    }
+}
+
+// one launch of tile class m over n tagged tiles of the batch's plans
+int e2_batch_launch(Plan *p, int m, const void *args, const int4 *tiles, int n, int par, size_t smem, cudaStream_t st) {
+  void (*const fn[4])(const E2Args *, const int4 *, int) = {k_e2_batch<0>, k_e2_batch<1>, k_e2_batch<2>,
+                                                             k_e2_batch<3>};
+  if (int rc = ensure_smem_attr(p, (const void *)fn[m], 20 + m, smem)) return rc;
+  if (n <= 0) return GPI_OK;  // (n = 0: only the kernel's shared-memory attribute)
+  fn[m]<<<n, E2_THREADS, smem, st>>>(static_cast<const E2Args *>(args), tiles, par);
+  GPI_CUDA(p, cudaGetLastError());
   return GPI_OK;
 }
 

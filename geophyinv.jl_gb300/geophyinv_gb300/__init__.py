@@ -7,7 +7,7 @@ reference's Julia API (SeisForwExpt, update!, gradient!, lossvalue).
 """
 from .fdtd import (AGeomss, AcousticMedium, BornMap, ElasticMedium, FdtdAcoustic, FdtdAcousticBorn,  # noqa
                    FdtdElastic, Fields, L2DistLoss, Recs, SeisForwExpt, Srcs, get_modelvector, gradient,
-                   lossvalue, set_born_perturbation, update)
+                   lossvalue, set_born_perturbation, update, update_batch)
 from . import fwi  # noqa
 from .rrule import NoTangent, misfit, rrule  # noqa
 from .setup import Grid, findfreq_peak, ricker  # noqa
@@ -15,4 +15,4 @@ from .setup import Grid, findfreq_peak, ricker  # noqa
 __all__ = ["AGeomss", "AcousticMedium", "BornMap", "ElasticMedium", "FdtdAcoustic", "FdtdAcousticBorn",
            "FdtdElastic", "Fields", "Grid", "set_born_perturbation",
            "L2DistLoss", "NoTangent", "fwi", "Recs", "SeisForwExpt", "Srcs", "findfreq_peak", "get_modelvector",
-           "gradient", "lossvalue", "misfit", "ricker", "rrule", "update"]
+           "gradient", "lossvalue", "misfit", "ricker", "rrule", "update", "update_batch"]

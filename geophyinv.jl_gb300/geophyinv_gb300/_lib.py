@@ -24,7 +24,9 @@ EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_str
            "gpi_set_graph", "gpi_query", "gpi_checkpoint_schedule", "gpi_set_snapshots", "gpi_get_snapshot",
            "gpi_forward_acoustic2d_noalloc", "gpi_set_born", "gpi_plan_estimate", "gpi_server_create",
            "gpi_server_destroy", "gpi_server_submit", "gpi_server_poll", "gpi_server_wait", "gpi_server_records",
-           "gpi_server_gradient", "gpi_server_times", "gpi_server_message", "gpi_server_release"]
+           "gpi_server_gradient", "gpi_server_times", "gpi_server_message", "gpi_server_release",
+           "gpi_batch_create", "gpi_batch_add", "gpi_batch_advance", "gpi_batch_finished", "gpi_batch_launches",
+           "gpi_batch_error", "gpi_batch_destroy"]
 
 
 class PlanDesc(ctypes.Structure):
@@ -38,8 +40,8 @@ class PlanDesc(ctypes.Structure):
 
 
 class ServerDesc(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int32), ("max_inflight", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2),
-                ("hbm_budget", ctypes.c_size_t)]
+    _fields_ = [("device", ctypes.c_int32), ("max_inflight", ctypes.c_int32), ("max_batch", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("hbm_budget", ctypes.c_size_t)]
 
 
 class Proj(ctypes.Structure):
@@ -124,6 +126,15 @@ def _load():
     L.gpi_server_message.argtypes = [vp, ctypes.c_int64]
     L.gpi_server_message.restype = ctypes.c_char_p
     L.gpi_server_release.argtypes = [vp, ctypes.c_int64]
+    L.gpi_batch_create.argtypes = [i32, vp, ctypes.POINTER(ctypes.c_void_p)]
+    L.gpi_batch_add.argtypes = [vp, vp]
+    L.gpi_batch_advance.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int32)]
+    L.gpi_batch_finished.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p), i32, ctypes.POINTER(ctypes.c_int32)]
+    L.gpi_batch_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.gpi_batch_error.argtypes = [vp]
+    L.gpi_batch_error.restype = ctypes.c_char_p
+    L.gpi_batch_destroy.argtypes = [vp]
+    L.gpi_batch_destroy.restype = None
     _LIB = L
     return L
 

@@ -230,6 +230,7 @@ class SeisForwExpt:
         if rc != 0:
             raise _lib.EngineError("gpi_plan_create: %s: %s" % (_lib.STATUS.get(rc, rc), L.gpi_last_error(None).decode()))
         self.plan = plan
+        self.stream = stream
         if stream is not None:
             self._check(L.gpi_set_stream(plan, ctypes.c_void_p(stream)))
         self._upload_medium()
@@ -462,6 +463,46 @@ def _update_run(pa):
             for f in pa.rfields:
                 pa.data[0][iss].d[f] = pa.records(iss, f)
     return pa
+
+
+def update_batch(pas, max_steps=256, stream=None):
+    """update!(pa) for several forward experiments at once (2-D, one
+    physics, npw = 1): the engine advances them together, one launch per
+    tile class and time step over the tiles of all of them (gpi_batch_*);
+    experiments with fewer steps finish first.  Each experiment's records
+    equal those of its own update!(pa) bit for bit.  No counterpart in the
+    reference, which runs one experiment per worker at a time."""
+    if not pas:
+        return pas
+    L = _lib.load()
+    import torch
+
+    dev = torch.cuda.current_device()
+    b = ctypes.c_void_p()
+    rc = L.gpi_batch_create(dev, ctypes.c_void_p(stream) if stream else None, ctypes.byref(b))
+    if rc:
+        raise _lib.EngineError("batch: %s" % L.gpi_batch_error(None).decode())
+    try:
+        for pa in pas:
+            if pa.attrib.mode != "forward" or getattr(pa.attrib, "born", False):
+                raise ValueError("update_batch takes forward experiments")
+            rc = L.gpi_batch_add(b, pa.plan)
+            if rc:
+                raise _lib.EngineError("batch: %s" % L.gpi_batch_error(b).decode())
+        active = ctypes.c_int32(len(pas))
+        while active.value > 0:
+            rc = L.gpi_batch_advance(b, max_steps, ctypes.byref(active))
+            if rc:
+                raise _lib.EngineError("batch: %s" % L.gpi_batch_error(b).decode())
+        for pa in pas:
+            for iss in range(pa.nss):
+                for f in pa.rfields:
+                    pa.data[0][iss].d[f] = pa.records(iss, f)
+    finally:
+        L.gpi_batch_destroy(b)
+        for pa in pas:
+            pa._check(L.gpi_set_stream(pa.plan, ctypes.c_void_p(pa.stream) if pa.stream else None))
+    return pas
 
 
 def _update_medium(pa, medium):

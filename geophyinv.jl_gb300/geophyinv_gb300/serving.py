@@ -269,10 +269,10 @@ def request_bytes(req):
 class Server:
     """The C ABI server (gpi_server_*): requests in, results out."""
 
-    def __init__(self, max_inflight=8, hbm_budget=64 << 30, device=0):
+    def __init__(self, max_inflight=8, hbm_budget=64 << 30, device=0, max_batch=0):
         self.L = _lib.load()
         d = _lib.ServerDesc()
-        d.device, d.max_inflight, d.hbm_budget = device, max_inflight, hbm_budget
+        d.device, d.max_inflight, d.hbm_budget, d.max_batch = device, max_inflight, hbm_budget, max_batch
         h = ctypes.c_void_p()
         rc = self.L.gpi_server_create(ctypes.byref(d), ctypes.byref(h))
         if rc:
@@ -327,17 +327,19 @@ class Server:
         self.close()
 
 
-def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=True, prep_threads=4):
+def serve(requests, hbm_budget=64 << 30, max_inflight=8, graphs=True, realtime=True, prep_threads=4, max_batch=0):
     """Continuous batching through the C server: each request is handed to
     it when it arrives (its host set-up -- padding, CPML profiles,
     projections -- on one of `prep_threads` client threads), the server
-    admits it while slots and the HBM budget allow, runs it on its own stream
-    overlapping the others, and returns its records (and gradient).
+    admits it while slots and the HBM budget allow -- 2-D forward requests
+    into the batch of their physics, advanced by shared launches (max_batch
+    members, 0: the server's default, -1: no batches), the others on their
+    own streams overlapping -- and returns its records (and gradient).
     Returns (results by id, stats); admission and completion times are on
     the stream's clock (seconds from its start)."""
     from concurrent.futures import ThreadPoolExecutor
 
-    srv = Server(max_inflight=max_inflight, hbm_budget=hbm_budget)
+    srv = Server(max_inflight=max_inflight, hbm_budget=hbm_budget, max_batch=max_batch)
     pool = ThreadPoolExecutor(max_workers=prep_threads)
     pending = sorted(requests, key=lambda r: r.arrival)
     # the stream's clock starts with the server's (gpi_server_times)

@@ -195,19 +195,27 @@ int gpi_checkpoint_schedule(int nt, int slots, int64_t *advances, int64_t *turns
  * Serving (no counterpart in the reference, whose update!(pa) runs one
  * experiment at a time on each Distributed worker,
  * src/fdtd/propagate.jl:100-106).  A server admits queued requests in
- * arrival order while the device bytes of the admitted ones stay within its
- * HBM budget, runs up to max_inflight of them at once on their own streams
- * (host set-up of one overlapping the device work of the others; each
- * request's shots batched into every launch, forward runs replayed as
- * captured step chunks) and keeps the results on the host until released.
- * A request's results do not depend on what else runs.
+ * arrival order (within each kind below) while the device bytes of the
+ * admitted ones stay within its HBM budget.  Small 2-D forward requests (up
+ * to 4 Mi cells per step over their shots) join the batch of their physics
+ * (gpi_batch_*): one launch per tile class and time step advances every
+ * admitted one, and requests join and leave it as they arrive and finish.
+ * Larger forward, gradient and 3-D requests run up to max_inflight at
+ * once on their own streams (host set-up of one overlapping the device work
+ * of the others; each request's shots batched into every launch, forward
+ * runs replayed as captured step chunks).  Results stay on the host until
+ * released; a request's results do not depend on what else runs.
  * ------------------------------------------------------------------------ */
 typedef struct gpi_server gpi_server;
 
 typedef struct {
   int32_t device;       /* CUDA device of every request */
-  int32_t max_inflight; /* requests on the device at once (1..64 worker threads) */
-  int32_t reserved[2];
+  int32_t max_inflight; /* gradient and 3-D requests on the device at once
+                           (1..64 worker threads) */
+  int32_t max_batch;    /* 2-D forward requests advanced together by one batch
+                           (gpi_batch_*) per physics (0: 16; -1: none, they run
+                           on the worker threads like the others) */
+  int32_t reserved;
   size_t hbm_budget;    /* device bytes the admitted requests may hold together
                            (a request larger than the budget runs alone) */
 } gpi_server_desc;
@@ -258,6 +266,36 @@ int gpi_server_times(gpi_server *server, int64_t id, double *t);
 const char *gpi_server_message(gpi_server *server, int64_t id);
 /* Frees a done or failed request's results. */
 int gpi_server_release(gpi_server *server, int64_t id);
+
+/* ---- batches: several forward plans advanced by the same launches ----
+ * No counterpart in the reference (its update!(pa) runs one experiment at a
+ * time per Distributed worker, src/fdtd/propagate.jl:100-106); the serving
+ * loop uses it for 2-D forward requests.  Every time step of a batch issues
+ * the source / record work of every member and one launch per tile class of
+ * the step kernel over the tiles of all members (runs of 16 steps replayed as
+ * a captured graph); a member's results equal its own gpi_run(plan,
+ * GPI_FORWARD) bit for bit. */
+typedef struct gpi_batch gpi_batch;
+/* stream: cudaStream_t the batch runs on (NULL: its own). */
+int gpi_batch_create(int device, void *stream, gpi_batch **out);
+/* A prepared 2-D forward plan (npw = 1, no snapshots, not Born; the same
+ * physics as the batch's other members) starts its run at step 1; its set-up
+ * work on its own stream is ordered before its first step.  The plan then
+ * belongs to the batch until it is handed back by gpi_batch_finished. */
+int gpi_batch_add(gpi_batch *batch, gpi_plan *plan);
+/* Issues up to max_steps steps of every member, asynchronously on the
+ * batch's stream; a member that reaches its last step runs the rest of its
+ * run (the last velocity records, the extra velocity half step) and leaves
+ * the batch.  *active: the members left (may be NULL). */
+int gpi_batch_advance(gpi_batch *batch, int max_steps, int *active);
+/* The plans whose runs were issued to the end since the last call (up to
+ * cap, oldest first), handed back: later calls on such a plan (records,
+ * destroy) wait for its own work only. */
+int gpi_batch_finished(gpi_batch *batch, gpi_plan **plans, int cap, int *n);
+int gpi_batch_launches(gpi_batch *batch, int64_t *n);
+const char *gpi_batch_error(const gpi_batch *batch);
+/* Waits for the batch's work; members still in it keep their state. */
+void gpi_batch_destroy(gpi_batch *batch);
 
 /* Size of the device scratch array used by gpi_forward_acoustic2d_noalloc. */
 #define GPI_NOALLOC_SCRATCH_BYTES (64u << 20)
