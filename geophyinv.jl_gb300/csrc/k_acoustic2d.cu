@@ -87,9 +87,9 @@ constexpr int A2_R4 = A2_TZ + 4;  // velocity-input rows z0 .. z0+TZ+3
 template <int NW>
 struct A2L {
   // 4 columns in use by the stencils plus 4 in flight (deep prefetch for the
-  // latency-bound small grids); the fused adjoint keeps 2 in flight so that
-  // four blocks fit on an SM
-  static constexpr int RING = NW == 1 ? 8 : 6;
+  // latency-bound small grids); the fused adjoint keeps 2 in flight (5
+  // blocks of interior tiles on an SM) and 1 in its band tiles (5 blocks)
+  __host__ __device__ static constexpr int ring(int mode) { return NW == 1 ? 8 : mode == 1 ? 5 : 6; }
   static constexpr int TZ = A2_TZ, R8 = A2_R8, R4 = A2_R4;
   static constexpr int P0 = 0, VX0 = R8, VZ0 = R8 + R4, CX = R8 + 2 * R4, CZ = R8 + 3 * R4, DTK = R8 + 4 * R4;
   static constexpr int SLOT1 = DTK + TZ;
@@ -98,9 +98,11 @@ struct A2L {
   __host__ __device__ static constexpr int OP(int w) { return w ? P1 : P0; }
   __host__ __device__ static constexpr int OVX(int w) { return w ? VX1 : VX0; }
   __host__ __device__ static constexpr int OVZ(int w) { return w ? VZ1 : VZ0; }
-  // shared memory of a block with `psf` CPML floats per slot and wavefield
-  // and room for `cap` injection cells (column, row, amount)
-  static size_t smem(int psf, int cap) {
+  // shared memory of a block of tile class `mode` with `psf` CPML floats per
+  // slot and wavefield and room for `cap` injection cells (column, row,
+  // amount)
+  static size_t smem(int mode, int psf, int cap) {
+    const int RING = ring(mode);
     return 128 + sizeof(float) * (RING * (SLOT + NW * psf) + 2 * NW * RING * R4 + 3 * cap);
   }
 };
@@ -143,7 +145,7 @@ template <int MODE, int NW>
 __device__ __forceinline__ void a2_body(const A2Args &a, const int4 tile) {
   using L = A2L<NW>;
   constexpr bool FAST = MODE == 0, XPSI = MODE >= 2, IMG = NW == 2;
-  constexpr int TZ = L::TZ, R8 = L::R8, R4 = L::R4, SLOT = L::SLOT, RING = L::RING;
+  constexpr int TZ = L::TZ, R8 = L::R8, R4 = L::R4, SLOT = L::SLOT, RING = L::ring(MODE);
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
   float *ring = reinterpret_cast<float *>(smem + 128);  // [RING][SL], layout A2L
@@ -791,7 +793,7 @@ __device__ __forceinline__ void a2_body(const A2Args &a, const int4 tile) {
 }
 
 template <int MODE, int NW>
-__global__ void __launch_bounds__(A2_THREADS, NW == 2 ? (MODE == 0 ? 5 : MODE == 1 ? 4 : 3) : (MODE == 0 ? 6 : MODE == 1 ? 5 : 4))
+__global__ void __launch_bounds__(A2_THREADS, NW == 2 ? (MODE <= 1 ? 5 : 3) : (MODE == 0 ? 6 : MODE == 1 ? 5 : 4))
     k_a2(const A2Args a) {
   a2_body<MODE, NW>(a, a.tiles[blockIdx.x]);
 }
@@ -891,7 +893,7 @@ static void a2_sizes(const Plan *p, int nw, int ipw, int vonly, int psf[4], int 
   if (vonly) cap[3] = std::max(cap[3], std::max(cap[1], cap[2]));  // every non-interior tile runs class 3's code
   for (int m = 0; m < 4; m++) {
     if (cap[m] > 2048) cap[m] = 0;
-    smem[m] = nw == 1 ? A2L<1>::smem(psf[m], cap[m]) : A2L<2>::smem(psf[m], cap[m]);
+    smem[m] = nw == 1 ? A2L<1>::smem(m, psf[m], cap[m]) : A2L<2>::smem(m, psf[m], cap[m]);
   }
 }
 
