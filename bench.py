@@ -391,7 +391,8 @@ def gradient_arm(args, world, local, kind="acoustic2d_grad"):
         true = configs.acoustic2d_fwi(nshots=nsh, **kw)
         pt = true.expt(stream=stream.cuda_stream)
         update(pt)
-        dobs = [Recs(r.n, r.grid, r.fields, {f: r.d[f].copy() for f in r.fields}) for r in pt.data[0]]
+        # observed records in the Recs layout (nt x nr, column-major)
+        dobs = [Recs(r.n, r.grid, r.fields, {f: np.array(r.d[f], order="F") for f in r.fields}) for r in pt.data[0]]
         del pt
     else:
         dobs = [Recs(len(s[1]), wl.tgrid, list(wl.rfields),

@@ -123,8 +123,10 @@ struct Plan {
     int ns = 0;
     std::vector<int64_t> cp, rv;
     std::vector<float> nz, wav;
+    bool on_dev = false;  // the adjoint wavefield's wavelets are in adj_dev (gpi_set_adjoint_l2)
   };
   std::vector<std::vector<std::vector<Src>>> src;  // [ipw][shot][field]
+  std::vector<std::vector<float *>> adj_dev;       // [shot][field]: device wavelets of the adjoint sources
   bool src_dirty = true;
   InjCell *d_cells = nullptr;
   int n_cells = 0;
@@ -252,6 +254,9 @@ int a2_batch_launch(Plan *p, int m, const void *args, const int4 *tiles, int n, 
 size_t e2_args_bytes();
 void e2_batch_args(Plan *p, void *out, size_t smem[4]);
 int e2_batch_launch(Plan *p, int m, const void *args, const int4 *tiles, int n, int par, size_t smem, cudaStream_t st);
+int adjoint_l2_launch(Plan *p, float *adj, double *partial, double *out, const float *dobs, const float *rec, int nt,
+                      int nr);
+int adjoint_l2_blocks(int nt, int nr);
 size_t aux_args_bytes();
 int aux_batch_args(Plan *p, void *out);  // returns its block count
 int aux_batch_launch(Plan *p, const void *args, const int *first, int nplans, int nblocks, int par, int off,

@@ -386,6 +386,7 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
   p.rec_w.assign(d.nshots, std::vector<std::vector<float>>(NFIELD));
   p.rec_base.assign(d.nshots, std::vector<int64_t>(NFIELD, -1));
   p.src.assign(2, std::vector<std::vector<Plan::Src>>(d.nshots, std::vector<Plan::Src>(NFIELD)));
+  p.adj_dev.assign(d.nshots, std::vector<float *>(NFIELD, nullptr));
   {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
@@ -476,6 +477,9 @@ void destroy(gpi_plan *pl) {
   // stream-ordered frees on the plan's stream, then its own stream if any
   free_sources(p);
   free_receivers(p);
+  for (auto &row : p.adj_dev)
+    for (float *&d : row)
+      if (d) cudaFreeAsync(d, p.stream), d = nullptr;
   {
     void *sb = p.snap_buf;
     free_dev(p, sb);
@@ -588,6 +592,14 @@ static int check_csc(Plan &p, int field, int n, const int64_t *cp, const int64_t
   return GPI_OK;
 }
 
+// the device wavelets of an adjoint source set by set_adjoint_l2
+static void drop_adj(Plan &p, int shot, int field) {
+  if (p.adj_dev.empty()) return;
+  float *&d = p.adj_dev[shot][field];
+  if (d) cudaFreeAsync(d, p.stream);
+  d = nullptr;
+}
+
 int set_sources(Plan &p, int ipw, int shot, int field, int ns, const int64_t *cp, const int64_t *rv, const float *nz,
                 const float *wav) {
   if (ipw < 1 || ipw > p.d.npw) return fail(&p, GPI_E_INVALID, "ipw");
@@ -596,6 +608,7 @@ int set_sources(Plan &p, int ipw, int shot, int field, int ns, const int64_t *cp
   if (ns < 0 || (ns > 0 && !wav)) return fail(&p, GPI_E_INVALID, "wavelets");
   Plan::Src &s = p.src[ipw - 1][shot][field];
   s = Plan::Src();
+  if (ipw == 2) drop_adj(p, shot, field);
   if (ipw == 1) {
     if (!is_vel(field) && !is_stress_src(field)) return fail(&p, GPI_E_INVALID, "sources act on p, tauii or velocities");
     int rc = check_csc(p, field, ns, cp, rv);
@@ -616,11 +629,72 @@ int set_sources(Plan &p, int ipw, int shot, int field, int ns, const int64_t *cp
   return GPI_OK;
 }
 
+static int check_err(Plan &p);
+
+// The adjoint sources of gradient! with L2DistLoss for one shot and
+// receiver field, computed on the device from the records of the last run
+// (src/fdtd/func_grad.jl:11-49: deriv(L2DistLoss(), dobs, dcal) =
+// 2 (dobs - dcal), reverse!, injected through the receiver interpolation);
+// *misfit = sum (dobs - dcal)^2 (value(L2DistLoss(), dobs, dcal)).
+int set_adjoint_l2(Plan &p, int shot, int field, const float *dobs, int on_device, double *misfit) {
+  if (p.d.npw != 2) return fail(&p, GPI_E_INVALID, "adjoint sources need npw = 2");
+  if (shot < 0 || shot >= p.d.nshots || field < 0 || field >= NFIELD) return fail(&p, GPI_E_INVALID, "shot/field");
+  if (!is_vel(field)) return fail(&p, GPI_E_UNSUPPORTED, "adjoint sources act on velocity fields only");
+  const int nr = p.rec_n[shot][field];
+  if (nr <= 0 || p.rec_base[shot][field] < 0 || !p.rec_pool)
+    return fail(&p, GPI_E_STATE, "no records of this shot and field (run forward_save first)");
+  if (!dobs || !misfit) return fail(&p, GPI_E_INVALID, "null argument");
+  const int nt = p.d.nt;
+  const size_t n = (size_t)nt * nr;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != p.device) GPI_CUDA(&p, cudaSetDevice(p.device));
+  p.src[1][shot][field] = Plan::Src();
+  drop_adj(p, shot, field);
+  float *adj = nullptr, *tmp = nullptr;
+  double *part = nullptr;
+  const int nblk = adjoint_l2_blocks(nt, nr);
+  int rc = GPI_OK;
+  if (pool_alloc((void **)&adj, n * sizeof(float), p.stream) != cudaSuccess ||
+      pool_alloc((void **)&part, (nblk + 1) * sizeof(double), p.stream) != cudaSuccess)
+    rc = fail(&p, GPI_E_NOMEM, "adjoint source buffers");
+  const float *d = dobs;
+  if (!rc && !on_device) {
+    if (pool_alloc((void **)&tmp, n * sizeof(float), p.stream) != cudaSuccess ||
+        cudaMemcpyAsync(tmp, dobs, n * sizeof(float), cudaMemcpyHostToDevice, p.stream) != cudaSuccess)
+      rc = fail(&p, GPI_E_CUDA, "observed data upload");
+    d = tmp;
+  }
+  if (!rc) rc = adjoint_l2_launch(&p, adj, part, part + nblk, d, p.rec_pool + p.rec_base[shot][field], nt, nr);
+  double h = 0.0;
+  if (!rc && (cudaMemcpyAsync(&h, part + nblk, sizeof(double), cudaMemcpyDeviceToHost, p.stream) != cudaSuccess ||
+              cudaStreamSynchronize(p.stream) != cudaSuccess))
+    rc = fail(&p, GPI_E_CUDA, "misfit read");
+  if (tmp) cudaFreeAsync(tmp, p.stream);
+  if (part) cudaFreeAsync(part, p.stream);
+  if (rc) {
+    if (adj) cudaFreeAsync(adj, p.stream);
+    if (dev != p.device) cudaSetDevice(dev);
+    return rc;
+  }
+  Plan::Src &s = p.src[1][shot][field];
+  s.ns = nr;
+  s.on_dev = true;
+  p.adj_dev[shot][field] = adj;
+  p.src_dirty = true;
+  *misfit = h;
+  if (dev != p.device) cudaSetDevice(dev);
+  return check_err(p);
+}
+
 int clear_sources(Plan &p, int ipw, int shot) {
   if (ipw < 1 || ipw > p.d.npw) return fail(&p, GPI_E_INVALID, "ipw");
   for (int s = 0; s < p.d.nshots; s++)
     if (shot < 0 || shot == s)
-      for (int f = 0; f < NFIELD; f++) p.src[ipw - 1][s][f] = Plan::Src();
+      for (int f = 0; f < NFIELD; f++) {
+        p.src[ipw - 1][s][f] = Plan::Src();
+        if (ipw == 2) drop_adj(p, s, f);
+      }
   p.src_dirty = true;
   return GPI_OK;
 }
@@ -720,6 +794,7 @@ static int compile_sources(Plan &p) {
     for (int s = 0; s < p.d.nshots; s++)
       for (int f = 0; f < NFIELD; f++) {
         const Plan::Src &src = p.src[ipw][s][f];
+        const bool dev_wav = ipw == 1 && src.on_dev;  // already on the device (set_adjoint_l2)
         if (src.ns <= 0) continue;
         const int kind = kind_of(f);
         // the adjoint wavefield takes velocity sources only: add_stress_source!
@@ -741,9 +816,13 @@ static int compile_sources(Plan &p) {
           lin.clear();
         }
         float *dw = nullptr;
-        GPI_CUDA(&p, dalloc(p, (void **)&dw, src.wav.size() * sizeof(float)));
-        GPI_CUDA(&p, h2d(p, dw, src.wav.data(), src.wav.size() * sizeof(float)));
-        p.wav_bufs.push_back(dw);
+        if (dev_wav) {
+          dw = p.adj_dev[s][f];
+        } else {
+          GPI_CUDA(&p, dalloc(p, (void **)&dw, src.wav.size() * sizeof(float)));
+          GPI_CUDA(&p, h2d(p, dw, src.wav.data(), src.wav.size() * sizeof(float)));
+          p.wav_bufs.push_back(dw);
+        }
         const int widx = (int)wavptr.size();
         wavptr.push_back(dw);
         wavns.push_back(src.ns);
@@ -1418,6 +1497,9 @@ int gpi_set_sources(gpi_plan *plan, int ipw, int shot, int field, int ns, const 
   return plan ? gpi::set_sources(plan->p, ipw, shot, field, ns, colptr, rowval, nzval, wavelets) : GPI_E_INVALID;
 }
 int gpi_clear_sources(gpi_plan *plan, int ipw, int shot) { return plan ? gpi::clear_sources(plan->p, ipw, shot) : GPI_E_INVALID; }
+int gpi_set_adjoint_l2(gpi_plan *plan, int shot, int field, const float *dobs, int on_device, double *misfit) {
+  return plan ? gpi::set_adjoint_l2(plan->p, shot, field, dobs, on_device, misfit) : GPI_E_INVALID;
+}
 int gpi_set_receivers(gpi_plan *plan, int shot, int field, int nr, const int64_t *colptr, const int64_t *rowval,
                       const float *nzval) {
   return plan ? gpi::set_receivers(plan->p, shot, field, nr, colptr, rowval, nzval) : GPI_E_INVALID;

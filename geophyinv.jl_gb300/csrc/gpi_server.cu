@@ -175,21 +175,16 @@ int process(Job &j, cudaStream_t st) {
     if ((rc = check(gpi_run(plan, j.gradient ? GPI_FORWARD_SAVE : GPI_FORWARD)))) break;
     if ((rc = fetch_records(j, plan))) break;
     if (!j.gradient) break;
-    // adjoint sources 2 (dobs - dcal), reversed in time; misfit sum (dobs - dcal)^2
+    // adjoint sources 2 (dobs - dcal), reversed in time, and the misfit
+    // sum (dobs - dcal)^2, on the device from the records there
     double loss = 0;
+    std::vector<float> zeros;
     for (size_t k = 0; k < j.rec.size() && !rc; k++) {
       const Proj &r = j.rec[k];
-      const std::vector<float> &dc = j.records[k];
-      std::vector<float> adj((size_t)nt * r.n);
-      for (int i = 0; i < r.n; i++)
-        for (int t = 0; t < nt; t++) {
-          const size_t o = (size_t)i * nt + t;
-          const float ob = r.has_data ? r.data[o] : 0.f;
-          const double e = (double)ob - (double)dc[o];
-          loss += e * e;
-          adj[(size_t)i * nt + (nt - 1 - t)] = 2.0f * (ob - dc[o]);
-        }
-      rc = check(gpi_set_sources(plan, 2, r.shot, r.field, r.n, nullptr, nullptr, nullptr, adj.data()));
+      if (!r.has_data) zeros.assign((size_t)nt * r.n, 0.f);
+      double mis = 0;
+      rc = check(gpi_set_adjoint_l2(plan, r.shot, r.field, r.has_data ? r.data.data() : zeros.data(), 0, &mis));
+      loss += mis;
     }
     if (rc) break;
     j.loss = loss;

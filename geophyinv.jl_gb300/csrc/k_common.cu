@@ -564,4 +564,53 @@ int transpose_records(Plan *p, float *out, const float *in, int nt, int nr) {
   return GPI_OK;
 }
 
+// gradient!'s adjoint sources for L2DistLoss (src/fdtd/func_grad.jl:11-49)
+// from the records in the pool ([it][ir]) and observed data dobs (Recs
+// layout, [ir][it]): adj[ir][nt-1-it] = 2 (dobs - dcal) (deriv(loss, dobs,
+// dcal), reverse!) and per block the sum of (dobs - dcal)^2 in double, each
+// 32 x 32 tile transposed through shared memory and summed in a fixed order
+__global__ void k_adjoint_l2(float *adj, double *partial, const float *dobs, const float *rec, int nt, int nr) {
+  __shared__ float tile[32][33];
+  __shared__ double red[256];
+  const int it0 = blockIdx.x * 32, ir0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int it = it0 + k, ir = ir0 + threadIdx.x;
+    if (it < nt && ir < nr) tile[k][threadIdx.x] = rec[(int64_t)it * nr + ir];
+  }
+  __syncthreads();
+  double acc = 0.0;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int ir = ir0 + k, it = it0 + threadIdx.x;
+    if (it < nt && ir < nr) {
+      const float ob = dobs[(int64_t)ir * nt + it], dc = tile[threadIdx.x][k];
+      adj[(int64_t)ir * nt + (nt - 1 - it)] = 2.0f * (ob - dc);
+      const double e = (double)ob - (double)dc;
+      acc += e * e;
+    }
+  }
+  const int t = threadIdx.y * 32 + threadIdx.x;
+  red[t] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w) red[t] += red[t + w];
+    __syncthreads();
+  }
+  if (t == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+// the partial sums in order (one thread: a few thousand values)
+__global__ void k_sum_ordered(double *out, const double *partial, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s += partial[i];
+  *out = s;
+}
+int adjoint_l2_launch(Plan *p, float *adj, double *partial, double *out, const float *dobs, const float *rec, int nt,
+                      int nr) {
+  dim3 grid((nt + 31) / 32, (nr + 31) / 32);
+  k_adjoint_l2<<<grid, dim3(32, 8), 0, p->stream>>>(adj, partial, dobs, rec, nt, nr);
+  k_sum_ordered<<<1, 1, 0, p->stream>>>(out, partial, (int)(grid.x * grid.y));
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+int adjoint_l2_blocks(int nt, int nr) { return ((nt + 31) / 32) * ((nr + 31) / 32); }
+
 }  // namespace gpi

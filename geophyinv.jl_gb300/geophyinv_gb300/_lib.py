@@ -26,7 +26,7 @@ EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_str
            "gpi_server_destroy", "gpi_server_submit", "gpi_server_poll", "gpi_server_wait", "gpi_server_records",
            "gpi_server_gradient", "gpi_server_times", "gpi_server_message", "gpi_server_release",
            "gpi_batch_create", "gpi_batch_add", "gpi_batch_advance", "gpi_batch_finished", "gpi_batch_launches",
-           "gpi_batch_error", "gpi_batch_destroy"]
+           "gpi_batch_error", "gpi_batch_destroy", "gpi_set_adjoint_l2"]
 
 
 class PlanDesc(ctypes.Structure):
@@ -126,6 +126,7 @@ def _load():
     L.gpi_server_message.argtypes = [vp, ctypes.c_int64]
     L.gpi_server_message.restype = ctypes.c_char_p
     L.gpi_server_release.argtypes = [vp, ctypes.c_int64]
+    L.gpi_set_adjoint_l2.argtypes = [vp, i32, i32, fp, i32, ctypes.POINTER(ctypes.c_double)]
     L.gpi_batch_create.argtypes = [i32, vp, ctypes.POINTER(ctypes.c_void_p)]
     L.gpi_batch_add.argtypes = [vp, vp]
     L.gpi_batch_advance.argtypes = [vp, i32, ctypes.POINTER(ctypes.c_int32)]

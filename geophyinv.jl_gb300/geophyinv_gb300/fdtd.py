@@ -597,8 +597,9 @@ class BornMap:
         return -np.concatenate([pa.gradient_raw(0).ravel(order="F"), pa.gradient_raw(1).ravel(order="F")])
 
 
-def _update_srcwav(pa, srcwav, src_types=None):
-    """update!(pa, srcwav, src_types) (src/fdtd/source.jl:192-246)."""
+def _update_srcwav(pa, srcwav, src_types=None, ipws=None):
+    """update!(pa, srcwav, src_types) (src/fdtd/source.jl:192-246); `ipws`
+    limits the engine update to those wavefields (0-based)."""
     if isinstance(srcwav, Srcs):
         srcwav = [[srcwav]]
     elif srcwav and isinstance(srcwav[0], Srcs):
@@ -611,6 +612,8 @@ def _update_srcwav(pa, srcwav, src_types=None):
     peaks = []
     fmaxs = []
     for ipw in range(pa.attrib.npw):
+        if ipws is not None and ipw not in ipws:
+            continue
         st = src_types[ipw] if ipw < len(src_types) else 0
         pa._check(pa.L.gpi_clear_sources(pa.plan, ipw + 1, -1))
         for iss in range(pa.nss):
@@ -709,9 +712,32 @@ def _local(pa, lst):
     return lst
 
 
+def _on_device(loss, pa):
+    """L2DistLoss on a plan with an adjoint wavefield and velocity records:
+    misfit and adjoint sources are computed on the device."""
+    return type(loss) is L2DistLoss and pa.attrib.npw == 2 and all(f in ("vx", "vy", "vz") for f in pa.rfields)
+
+
+def _device_l2(pa, dobs):
+    """Adjoint sources 2 (dobs - dcal) reversed and the misfit sum
+    (dobs - dcal)^2 from the records of the last run, on the device
+    (gpi_set_adjoint_l2); the misfit summed over the ranks."""
+    pa._check(pa.L.gpi_clear_sources(pa.plan, 2, -1))
+    J = 0.0
+    for iss, o in enumerate(_local(pa, dobs)):
+        for f in pa.rfields:
+            d = np.asfortranarray(o.d[f], dtype=np.float32)
+            mis = ctypes.c_double()
+            pa._check(pa.L.gpi_set_adjoint_l2(pa.plan, iss, _lib.FIELD[f], _ptr(d), 0, ctypes.byref(mis)))
+            J += mis.value
+    return _shots.reduce_scalar(J) if pa.shard else J
+
+
 def _loss(loss, dobs, pa):
     """Misfit of the last forward records against dobs, summed over the
     ranks of a sharded experiment."""
+    if _on_device(loss, pa):
+        return _device_l2(pa, dobs)
     J = sum(loss.value(o.d[f], c.d[f]) for o, c in zip(_local(pa, dobs), pa.data[0]) for f in o.fields)
     return _shots.reduce_scalar(J) if pa.shard else J
 
@@ -719,12 +745,16 @@ def _loss(loss, dobs, pa):
 def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
     """gradient!(g, m, loss, dobs, pa, mparams) (src/fdtd/func_grad.jl:11-49):
     forward_save, adjoint sources deriv(loss, dobs, dcal) reversed in time,
-    adjoint run with src_types [-1, 1], chain rule g * exp(m) * ref."""
+    adjoint run with src_types [-1, 1], chain rule g * exp(m) * ref.  With
+    L2DistLoss the adjoint sources and the misfit are computed on the device
+    from the records there (gpi_set_adjoint_l2); pa.srcwav[2] then keeps its
+    previous host contents."""
     _forward_save(pa, m, mparams)
     gv = _adjoint(pa, m, loss, dobs, mparams)
     if g is not None:
         g[:] = gv
-    return _loss(loss, dobs, pa)
+    J = getattr(pa, "_device_misfit", None)
+    return J if J is not None else _loss(loss, dobs, pa)
 
 
 def _forward_save(pa, m, mparams):
@@ -744,17 +774,25 @@ def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
     last forward_save run, the adjoint run, the chain rule onto m (times
     `scale`)."""
     mparams = list(mparams)
-    adj = []
-    for o, c in zip(_local(pa, dobs), pa.data[0]):
-        s = Srcs(o.n, pa.tgrid, pa.rfields)
-        for f in pa.rfields:
-            # reverse!(srcwav[2]), laid out as the engine takes wavelets
-            s.d[f] = np.asfortranarray(loss.deriv(o.d[f], c.d[f])[::-1])
-        adj.append(s)
-    pa.srcwav[1] = adj
     # a checkpointed plan recomputes wavefield 1 forward in time, with the
     # sources of its forward_save run (no time-reversed copy is needed)
-    update(pa, pa.srcwav, [1 if pa.checkpoints else -1, 1])
+    st1 = 1 if pa.checkpoints else -1
+    pa._device_misfit = None
+    if _on_device(loss, pa):
+        # adjoint sources 2 (dobs - dcal) reversed, and the misfit, on the
+        # device from the records there
+        pa._device_misfit = _device_l2(pa, dobs)
+        _update_srcwav(pa, [pa.srcwav[0]], [st1], ipws=(0,))
+    else:
+        adj = []
+        for o, c in zip(_local(pa, dobs), pa.data[0]):
+            s = Srcs(o.n, pa.tgrid, pa.rfields)
+            for f in pa.rfields:
+                # reverse!(srcwav[2]), laid out as the engine takes wavelets
+                s.d[f] = np.asfortranarray(loss.deriv(o.d[f], c.d[f])[::-1])
+            adj.append(s)
+        pa.srcwav[1] = adj
+        update(pa, pa.srcwav, [st1, 1])
     mode_save = pa.attrib.mode
     pa.attrib.mode = "adjoint"
     update(pa)

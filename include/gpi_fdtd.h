@@ -124,6 +124,16 @@ int gpi_set_pml(gpi_plan *plan, int q, int len, const float *a, const float *b, 
  * then ignored and ns must equal the receiver count.  wavelets: nt x ns. */
 int gpi_set_sources(gpi_plan *plan, int ipw, int shot, int field, int ns, const int64_t *colptr,
                     const int64_t *rowval, const float *nzval, const float *wavelets);
+/* gradient!'s adjoint sources for L2DistLoss (src/fdtd/func_grad.jl:11-49)
+ * computed on the device from the records of the last forward_save run of
+ * one shot and (velocity) receiver field: the adjoint wavefield's sources of
+ * that field become deriv(L2DistLoss(), dobs, dcal) = 2 (dobs - dcal),
+ * reversed in time (reverse!(srcwav[2])), injected through the receiver
+ * interpolation (as gpi_set_sources(plan, 2, ...) with those wavelets);
+ * *misfit = sum (dobs - dcal)^2 in double (value(L2DistLoss(), dobs, dcal)).
+ * dobs: nt x nr (Recs layout), host or device (on_device).  Synchronises
+ * the plan's stream (the misfit is read back). */
+int gpi_set_adjoint_l2(gpi_plan *plan, int shot, int field, const float *dobs, int on_device, double *misfit);
 /* Remove every source of wavefield ipw of one shot (-1: all shots). */
 int gpi_clear_sources(gpi_plan *plan, int ipw, int shot);
 /* Receiver interpolation matrix (rinterpolatew, src/fdtd/ageom.jl:46-54). */

@@ -41,3 +41,38 @@ def test_acoustic2d_gradient_matches_oracle(engine, nz, nx, nt, nshots):
         e = rel(pa.gradients[k], raw_o[k])
         assert e < TOL, (k, e)
     assert np.all(np.isfinite(g)) and np.linalg.norm(g) > 0
+
+
+class _HostL2(L2DistLoss):
+    """L2DistLoss evaluated on the host (gradient! takes the device path for
+    L2DistLoss itself only)."""
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("checkpoints", [0, 6])
+def test_device_adjoint_sources_equal_host_ones(engine, checkpoints):
+    """gpi_set_adjoint_l2 (adjoint sources and misfit from the records on the
+    device) gives the gradient of the host path bit for bit and its misfit
+    within summation-order rounding, with observed data from another model."""
+    nz, nx, nt, nshots = 60, 110, 400, 2
+    true = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=nshots, nrec=nx // 2)
+    pt = true.expt()
+    from geophyinv_gb300 import update
+
+    update(pt)
+    dobs = [Recs(r.n, r.grid, r.fields, {f: r.d[f].copy() for f in r.fields}) for r in pt.data[0]]
+    pt.close()
+    start = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=nshots, nrec=nx // 2, anomaly=False)
+    out = {}
+    for name, loss in (("device", L2DistLoss()), ("host", _HostL2())):
+        pa = start.expt(mode="forward_save", checkpoints=checkpoints)
+        m = get_modelvector(pa, ["invK", "rho"])
+        g = np.zeros_like(m)
+        J = gradient(g, m, loss, dobs, pa)
+        out[name] = (J, g.copy(), {k: v.copy() for k, v in pa.gradients.items()})
+        pa.close()
+    (Jd, gd, rd), (Jh, gh, rh) = out["device"], out["host"]
+    assert Jd > 0 and abs(Jd - Jh) <= 1e-12 * Jh, (Jd, Jh)
+    assert np.array_equal(gd, gh)
+    for k in rd:
+        assert np.array_equal(rd[k], rh[k]), k
