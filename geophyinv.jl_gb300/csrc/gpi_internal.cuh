@@ -92,6 +92,10 @@ struct Plan {
   int nmod = 0;
   float *pml = nullptr;  // [nder][3][2*npml]
   float *grad[3] = {};   // per-shot gradients [shot][storage] (adjoint), one per medium parameter
+  // stencil orders other than 4 (k_generic.cu): the materialised derivative
+  // fields (storage layout, per shot) and 1 / (den * d) per axis (z, y, x)
+  float *der[MAXDER] = {};
+  float gdsI[3] = {0.f, 0.f, 0.f};
   // 2-D acoustic adjoint by time reversal: per velocity cell and shot, the
   // sums over the steps of vx2_prev (vx1 - vx1_prev) / dt (img[0]) and of
   // the vz products (img[1]); the rho gradient is formed from them at the
@@ -246,6 +250,7 @@ int step_elastic3d(Plan *p, int ipw_mask, int it, int mode, int vonly);
 int step_adjoint_acoustic2d(Plan *p, int it);
 int step_a2_wavefield(Plan *p, int ipw, int vonly);
 int step_a2_adjoint_fused(Plan *p);  // both wavefields + imaging condition
+int step_generic(Plan *p, int vonly);  // stencil orders 2, 6, 8 (k_generic.cu)
 // batches of forward plans (gpi_batch.cu): argument tables and launches of
 // the step kernels over the tagged tiles of several plans
 size_t a2_args_bytes();

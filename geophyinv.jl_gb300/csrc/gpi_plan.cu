@@ -230,7 +230,11 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
   const gpi_plan_desc &d = *desc;
   if (d.physics != GPI_ACOUSTIC && d.physics != GPI_ELASTIC) return fail(nullptr, GPI_E_INVALID, "physics");
   if (d.ndim != 2 && d.ndim != 3) return fail(nullptr, GPI_E_INVALID, "ndim must be 2 or 3");
-  if (d.order != 4) return fail(nullptr, GPI_E_UNSUPPORTED, "the engine implements order 4 only");
+  if (d.order != 2 && d.order != 4 && d.order != 6 && d.order != 8)
+    return fail(nullptr, GPI_E_INVALID, "order must be 2, 4, 6 or 8");
+  // orders other than 4 (k_generic.cu): forward modelling only
+  if (d.order != 4 && (d.npw != 1 || d.checkpoints > 0))
+    return fail(nullptr, GPI_E_UNSUPPORTED, "stencil orders 2, 6, 8: forward runs only (npw = 1)");
   if (d.nt < 1 || d.nshots < 1 || (d.npw != 1 && d.npw != 2)) return fail(nullptr, GPI_E_INVALID, "nt/nshots/npw");
   if (d.checkpoints < 0 || (d.checkpoints > 0 && d.npw != 2))
     return fail(nullptr, GPI_E_INVALID, "checkpoints: > 0 only with npw = 2");
@@ -301,6 +305,15 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
   p.nmod = d.physics == GPI_ACOUSTIC ? 2 : 3;
   p.ncoef = d.physics == GPI_ACOUSTIC ? d.ndim + 1 : (d.ndim == 2 ? 5 : 8);
   for (int i = 0; i < p.nmod; i++) allocs.push_back({&p.mod[i], p.fstride});
+  if (d.order != 4)
+    for (int q = 0; q < p.nder; q++) allocs.push_back({&p.der[q], p.fstride * d.nshots});
+  {
+    // get_fc (src/fdtd/fdtd.jl:313-332): 1 / (den * d) in FP64, stored as FP32
+    const double den = d.order == 4 ? 24.0 : d.order == 6 ? 1920.0 : d.order == 8 ? 107520.0 : 1.0;
+    p.gdsI[0] = (float)(1.0 / (d.dz * den));
+    p.gdsI[1] = d.ndim == 3 ? (float)(1.0 / (d.dy * den)) : 0.f;
+    p.gdsI[2] = (float)(1.0 / (d.dx * den));
+  }
   for (int i = 0; i < p.ncoef; i++) allocs.push_back({&p.coef[i], p.fstride});
   allocs.push_back({&p.pml, (int64_t)p.nder * 3 * 2 * d.npml});
   allocs.push_back({(float **)&p.d_err, 64});
@@ -1059,6 +1072,7 @@ static int build_tiles(Plan &p) {
 // run
 // ---------------------------------------------------------------------------
 static int step(Plan &p, int ipw_mask, int it, int mode, int vonly) {
+  if (p.d.order != 4) return step_generic(&p, vonly);
   if (p.d.physics == GPI_ACOUSTIC)
     return p.d.ndim == 2 ? step_acoustic2d(&p, ipw_mask, it, mode, vonly) : step_acoustic3d(&p, ipw_mask, it, mode, vonly);
   return p.d.ndim == 2 ? step_elastic2d(&p, ipw_mask, it, mode, vonly) : step_elastic3d(&p, ipw_mask, it, mode, vonly);

@@ -444,7 +444,8 @@ __device__ __forceinline__ void inject_cell(const InjCell &c, float amt, int kin
       fld.f[GPI_P][so + c.off] = fld.f[GPI_P][so + c.off] + amt;
     } else {
       fld.f[GPI_TAUXX][so + c.off] = fld.f[GPI_TAUXX][so + c.off] + amt;
-      fld.f[GPI_TAUYY][so + c.off] = fld.f[GPI_TAUYY][so + c.off] + amt;
+      if (fld.f[GPI_TAUYY])  // absent in 2-D (the generic-order steps share this kernel)
+        fld.f[GPI_TAUYY][so + c.off] = fld.f[GPI_TAUYY][so + c.off] + amt;
       fld.f[GPI_TAUZZ][so + c.off] = fld.f[GPI_TAUZZ][so + c.off] + amt;
     }
   }
@@ -482,6 +483,27 @@ __global__ void k3_inject(const InjCell *cells, const int32_t *gptr, const float
   const int shot = lo / NKIND, kind = lo % NKIND;
   if ((kind < 3) != (velocity != 0)) return;
   inject_cell(cells[k], amount[k], kind, shot * fs, fld, physics);
+}
+
+// add_velocity_source! (velocity = 1) or add_stress_source! (0) of
+// wavefield ipw into its current buffer, from the amounts of this step
+int inject_sources(Plan *p, int ipw, int velocity) {
+  const int ng = p->d.nshots * NKIND;
+  const size_t g0 = (size_t)ipw * ng;
+  const int ncw = p->group_ptr.empty() ? 0 : p->group_ptr[g0 + ng] - p->group_ptr[g0];  // cells of this wavefield
+  if (ncw <= 0) return GPI_OK;
+  Fields3 fl;
+  for (int k = 0; k < NFIELD; k++) fl.f[k] = p->state[p->cur[ipw]][ipw][k];
+  const int32_t *gptr = p->d_group_ptr + g0;
+  if (p->inj_shared)
+    k3_inject_groups<<<(ng + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride,
+                                                              p->d.nshots, velocity, p->d.physics);
+  else
+    k3_inject<<<(ncw + 127) / 128, 128, 0, p->stream>>>(p->d_cells, gptr, p->d_amount, fl, p->fstride, p->d.nshots,
+                                                        velocity, p->d.physics);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
 }
 
 // one step of wavefield ipw (vonly: bit 0 velocity half step only, bit 1

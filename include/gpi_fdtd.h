@@ -58,7 +58,8 @@ typedef struct gpi_plan gpi_plan;
 typedef struct {
   int32_t physics;     /* gpi_physics */
   int32_t ndim;        /* 2 or 3 */
-  int32_t order;       /* stencil order (_fd_order); the engine implements 4 */
+  int32_t order;       /* stencil order (_fd_order): 2, 4, 6 or 8; other orders than 4
+                          run forward only (npw 1, no checkpoints) */
   int32_t nz, ny, nx;  /* extended grid sizes (ny = 1 for 2-D) */
   int32_t npml;        /* PML width, _fd_npml = 40 + order - 1 */
   int32_t nbound;      /* boundary strip width, _fd_nbound = 3 */

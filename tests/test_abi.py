@@ -45,10 +45,15 @@ def test_create_rejects_bad_descriptor(lib):
     d.nz, d.ny, d.nx, d.npml, d.nbound, d.nt, d.nshots, d.npw = 200, 1, 200, 41, 3, 10, 1, 1
     d.dt, d.dz, d.dx, d.dy = 1e-3, 5.0, 5.0, 1.0
     plan = ctypes.c_void_p()
+    d.order = 3
     rc = lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan))
-    assert rc == -4  # order 2 is not implemented by the engine
+    assert rc == -1  # orders 2, 4, 6, 8 only
     assert b"order" in lib.gpi_last_error(None)
-    d.order = 4
+    d.order, d.npw = 2, 2
+    rc = lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan))
+    assert rc == -4  # orders other than 4: forward runs only
+    assert b"order" in lib.gpi_last_error(None)
+    d.order, d.npw = 4, 1
     d.pml_faces = 0x3F  # CPML on every face
     d.nz = 60  # too small for two PML strips
     assert lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan)) == -1

@@ -19,9 +19,9 @@ def lib():
     return _lib.load()
 
 
-def _desc(npw=1, checkpoints=0, nz=300, nx=400, nshots=2, nt=100):
+def _desc(npw=1, checkpoints=0, nz=300, nx=400, nshots=2, nt=100, order=4):
     d = _lib.PlanDesc()
-    d.physics, d.ndim, d.order = 0, 2, 4
+    d.physics, d.ndim, d.order = 0, 2, order
     d.nz, d.ny, d.nx, d.npml, d.nbound, d.nt, d.nshots, d.npw = nz, 1, nx, 43, 3, nt, nshots, npw
     d.dt, d.dz, d.dx, d.dy = 5e-4, 5.0, 5.0, 1.0
     d.pml_faces = d.rigid_faces = 0x33
@@ -44,7 +44,10 @@ def test_plan_estimate_covers_the_layout_and_grows_with_the_work(lib):
     assert grad > 2 * fwd * 0.9  # two wavefields and the boundary store
     c2, c4 = _estimate(lib, _desc(npw=2, checkpoints=2)), _estimate(lib, _desc(npw=2, checkpoints=4))
     assert c4 > c2 and (c4 - c2) % 2 == 0
-    bad = _desc()
+    o2 = _estimate(lib, _desc(order=2))
+    o8 = _estimate(lib, _desc(order=8))
+    assert o8 > o2 > 0  # materialised derivative fields, a wider padding at order 8
+    bad = _desc(npw=2)
     bad.order = 2
     assert lib.gpi_plan_estimate(ctypes.byref(bad), ctypes.byref(ctypes.c_size_t())) == -4
 
