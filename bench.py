@@ -100,6 +100,8 @@ def parse():
     ap.add_argument("--nshots", type=int, default=None)
     ap.add_argument("--side", type=int, default=None, help="3-D workloads: a side^3 sub-grid (profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--order", type=int, default=4, choices=[2, 4, 6, 8],
+                    help="forward workloads: stencil order (orders other than 4 run the generic per-cell steps)")
     ap.add_argument("--graph", type=int, default=2, choices=[0, 1, 2],
                     help="forward workloads: CUDA graphs (0 plain, 1 whole run, 2 replayed 16-step chunks)")
     return ap.parse_args()
@@ -140,14 +142,14 @@ def workload(kind, nt=None, nshots=None, side=None):
     return wl
 
 
-def config_json(kind, wl, n_gpus, shots_per_gpu=None):
+def config_json(kind, wl, n_gpus, shots_per_gpu=None, order=4):
     npml = wl.npml if wl.npml is not None else 43
     nsh = shots_per_gpu if shots_per_gpu is not None else len(wl.shots)
     state = {"elastic2d": 5, "acoustic2d": 3, "elastic3d": 9, "acoustic3d": 4, "acoustic2d_grad": 6,
              "acoustic2d_grad_ckpt": 6, "acoustic3d_grad_ckpt": 8, "elastic3d_grad_ckpt": 18}[kind]
     return {"workload": WORKLOADS[kind]["name"],
             "grid": [len(g) for g in wl.grid], "extended_grid": [len(g) + 2 * npml for g in wl.grid],
-            "shots_per_gpu": nsh, "nt": wl.nt, "dt": wl.tgrid.step, "order": 4,
+            "shots_per_gpu": nsh, "nt": wl.nt, "dt": wl.tgrid.step, "order": order,
             "receivers_per_shot": len(wl.shots[0][1]), "rfields": wl.rfields,
             "parallelism": "shot replicas x%d" % n_gpus,
             "l2": "not flushed: per-step working set %.2f GB >> 129 MB L2" % (
@@ -223,7 +225,7 @@ def traffic_per_cell(kind):
     return TRAFFIC_B_PER_CELL.get(kind, (None, None))
 
 
-def cpu_sample(kind, nt_cap=None, target_s=12.0):
+def cpu_sample(kind, nt_cap=None, target_s=12.0, order=4):
     """The CPU oracle (all host threads) on one shot of the workload for a
     bounded number of time steps; returns (Gcell-updates/s, threads, sample).
     Gradient workloads time the whole gradient (forward_save and adjoint;
@@ -241,6 +243,7 @@ def cpu_sample(kind, nt_cap=None, target_s=12.0):
     def run(nt):
         wl = workload(kind, nt, 1, side)
         ex = wl.as_dict()
+        ex["order"] = order
         prep = O.Prepared(ex, np.float32)
         cells = int(np.prod(prep.shape))
         if grad:
@@ -288,7 +291,7 @@ def engine_arm(args, rank, world, local):
     # work per GPU stays fixed (weak scaling)
     nsh = (args.nshots or WORKLOADS[args.workload]["nshots"]) * world
     wl = workload(args.workload, args.nt, nsh, args.side)
-    pa = wl.expt(stream=stream.cuda_stream, shard=world > 1)
+    pa = wl.expt(stream=stream.cuda_stream, shard=world > 1, order=args.order)
     pa.set_graph(args.graph)
     medium = wl.medium()
     srcwav = wl.srcwav()
@@ -347,12 +350,15 @@ def engine_arm(args, rank, world, local):
     peak, peak_kind = peaks()
     W = WORKLOADS[args.workload]
     achieved = W["bpc"] * cells / (ms * 1e-3 / pa.nt) / 1e9  # per launch, all time charged to it
-    tpc, tpc_src = traffic_per_cell(args.workload)
+    tpc, tpc_src = traffic_per_cell(args.workload) if args.order == 4 else (None, None)
+    kernel = W["kernel"] if args.order == 4 else (
+        "generic order-%d steps (k_gvel, k_gstress_*: one thread per cell, derivatives in registers, two "
+        "passes), algorithmic %d B/cell (the fused one-pass minimum)" % (args.order, W["bpc"]))
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded gradient + smoothed perturbation model)",
-        "config": dict(config_json(args.workload, wl, world, pa.nss),
+        "config": dict(config_json(args.workload, wl, world, pa.nss, args.order),
                        cuda_graphs={0: "off", 1: "whole run", 2: "replayed 16-step chunks"}[args.graph]),
         "e2e": {"value": round(e2e, 3), "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
@@ -360,7 +366,7 @@ def engine_arm(args, rank, world, local):
                      "frac": round(achieved / peak, 4),
                      "traffic": None if tpc is None else round(tpc * cells),
                      "traffic_source": tpc_src,
-                     "kernel": W["kernel"],
+                     "kernel": kernel,
                      "peak_source": peak_kind + " hbm_gbs"},
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -513,14 +519,14 @@ def reference_arm(args):
     sample = ""
     threads = os.cpu_count() or 1
     for i in range(args.warmup + args.steps):
-        rate, threads, sample = cpu_sample(args.workload, nt_cap=60, target_s=6.0)
+        rate, threads, sample = cpu_sample(args.workload, nt_cap=60, target_s=6.0, order=args.order)
         if i >= args.warmup:
             rates.append(rate)
     v = float(np.mean(rates))
     return {"metric": METRIC, "value": round(v, 4), "unit": "Gcell/s", "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOADS[args.workload]["name"], "sample": sample},
+            "config": {"workload": WORKLOADS[args.workload]["name"], "order": args.order, "sample": sample},
             "cpu_baseline": {"value": round(v, 4), "unit": "Gcell/s", "cores": threads, "kind": "port",
                              "sample": sample + "; C restatement of the reference time loop (Julia is absent)"},
             "e2e": {"value": round(v, 4), "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -537,12 +543,14 @@ def main():
         print(json.dumps(serving_arm(args)))
         return
     if args.workload in ("acoustic2d_grad", "acoustic2d_grad_ckpt", "acoustic3d_grad_ckpt", "elastic3d_grad_ckpt"):
+        if args.order != 4:
+            raise SystemExit("gradients run at stencil order 4 only")
         line, dist = gradient_arm(args, world, local, args.workload), None
     else:
         line, dist = engine_arm(args, rank, world, local)
     if rank == 0:
         if not args.no_cpu_baseline:
-            rate, threads, sample = cpu_sample(args.workload)
+            rate, threads, sample = cpu_sample(args.workload, order=args.order)
             line["cpu_baseline"] = {"value": round(rate, 4), "unit": "Gcell/s", "cores": threads, "kind": "port",
                                     "sample": sample}
         print(json.dumps(line))

@@ -92,9 +92,7 @@ struct Plan {
   int nmod = 0;
   float *pml = nullptr;  // [nder][3][2*npml]
   float *grad[3] = {};   // per-shot gradients [shot][storage] (adjoint), one per medium parameter
-  // stencil orders other than 4 (k_generic.cu): the materialised derivative
-  // fields (storage layout, per shot) and 1 / (den * d) per axis (z, y, x)
-  float *der[MAXDER] = {};
+  // stencil orders other than 4 (k_generic.cu): 1 / (den * d) per axis (z, y, x)
   float gdsI[3] = {0.f, 0.f, 0.f};
   // 2-D acoustic adjoint by time reversal: per velocity cell and shot, the
   // sums over the steps of vx2_prev (vx1 - vx1_prev) / dt (img[0]) and of

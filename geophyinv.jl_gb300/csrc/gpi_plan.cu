@@ -235,6 +235,8 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
   // orders other than 4 (k_generic.cu): forward modelling only
   if (d.order != 4 && (d.npw != 1 || d.checkpoints > 0))
     return fail(nullptr, GPI_E_UNSUPPORTED, "stencil orders 2, 6, 8: forward runs only (npw = 1)");
+  if (d.order != 4 && d.nshots > 65535)
+    return fail(nullptr, GPI_E_UNSUPPORTED, "stencil orders 2, 6, 8: at most 65535 shots per plan");
   if (d.nt < 1 || d.nshots < 1 || (d.npw != 1 && d.npw != 2)) return fail(nullptr, GPI_E_INVALID, "nt/nshots/npw");
   if (d.checkpoints < 0 || (d.checkpoints > 0 && d.npw != 2))
     return fail(nullptr, GPI_E_INVALID, "checkpoints: > 0 only with npw = 2");
@@ -305,8 +307,6 @@ int create(const gpi_plan_desc *desc, gpi_plan **out, size_t *bytes_only = nullp
   p.nmod = d.physics == GPI_ACOUSTIC ? 2 : 3;
   p.ncoef = d.physics == GPI_ACOUSTIC ? d.ndim + 1 : (d.ndim == 2 ? 5 : 8);
   for (int i = 0; i < p.nmod; i++) allocs.push_back({&p.mod[i], p.fstride});
-  if (d.order != 4)
-    for (int q = 0; q < p.nder; q++) allocs.push_back({&p.der[q], p.fstride * d.nshots});
   {
     // get_fc (src/fdtd/fdtd.jl:313-332): 1 / (den * d) in FP64, stored as FP32
     const double den = d.order == 4 ? 24.0 : d.order == 6 ? 1920.0 : d.order == 8 ? 107520.0 : 1.0;

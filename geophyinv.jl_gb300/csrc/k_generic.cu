@@ -7,15 +7,21 @@
 // _fd_npml = 40 + h).  The fused order-4 kernels (k_acoustic2d.cu,
 // k_elastic2d.cu, k_3d.cu) carry the order-4 halos in their tiles; the
 // other orders run this path, which keeps the reference's structure: per
-// step the derivative fields of the stresses (or p) are materialised with
-// their CPML memory (update_dstress!), the velocities updated (compute_v!)
-// and the rigid faces mirrored (dirichlet*!, src/fdtd/dirichlet.jl:1-79),
-// the velocity sources added, then the velocity derivatives (update_dv!),
-// the stresses (compute_p! / compute_stress*!, free surface) and the stress
-// sources -- one thread per cell of each field, in place, on the plan's
-// padded storage (every field and derivative shares the index map, so a
-// cell (r, y, c) of any shape sits at the same offset).  Records and source
-// amounts come from the aux kernel as in the other paths.
+// step the velocities are updated (compute_v!) from the derivatives of the
+// stresses (or p) with their CPML memory (update_dstress!), the rigid faces
+// mirrored (dirichlet*!, src/fdtd/dirichlet.jl:1-79), the velocity sources
+// added, then the stresses (compute_p! / compute_stress*!) from the
+// velocity derivatives (update_dv!), the free surface and the stress
+// sources -- one thread per cell of each updated field, in place, on the
+// plan's padded storage (every field shares the index map, so a cell
+// (r, y, c) of any shape sits at the same offset).  The reference
+// materialises each derivative field; here the thread that consumes a
+// derivative cell computes it in registers: the derivative shapes equal
+// the update domains that read them (the @inn domain of a velocity, the
+// shape of a stress), so every derivative cell, and its CPML memory, is
+// still evaluated exactly once per step, with the same arithmetic.
+// Records and source amounts come from the aux kernel as in the other
+// paths.
 //
 // The derivative table restates the reference's (src/fdtd/advance_acou.jl:
 // 258-299, src/fdtd/advance_elastic.jl:10-153, src/fields.jl:92-671):
@@ -89,9 +95,7 @@ __device__ __forceinline__ float gstencil(const float *a, int64_t s) {
 // one derivative field: D = @d(src) * dsI over its shape, with the CPML
 // memory on the strips of its axis (memory{x,y,z}!, src/fdtd/cpml.jl:158-215)
 struct GDer {
-  GGeo g;
   const float *src;  // shot 0
-  float *out;        // shot 0
   int n1, n2, n3;    // derivative extents (z, y, x)
   int oz, oy, ox;    // source offset (inner: h on the other axes)
   int axis;
@@ -101,75 +105,72 @@ struct GDer {
   int64_t pss;
   const float *pa, *pb, *pk;  // profile of this derivative, 2 npml each
   int npml, lo, hi, zsw;
-  int nshots;
 };
 
+// derivative cell (iz, iy, ix) of shot `shot`, its CPML memory advanced
 template <int ORDER>
-__global__ void __launch_bounds__(256) k_gderiv(const GDer a) {
-  const GGeo &g = a.g;
-  const int64_t per = (int64_t)a.n1 * a.n2 * a.n3, total = per * a.nshots;
+__device__ __forceinline__ float gder_at(const GGeo &g, const GDer &a, int shot, int iz, int iy, int ix) {
   const int64_t st = a.axis == 0 ? 1 : a.axis == 1 ? (int64_t)g.NZP : (int64_t)g.NYP * g.NZP;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int shot = (int)(i / per);
-    const int64_t k = i - shot * per;
-    const int iz = (int)(k % a.n1) + 1;
-    const int iy = (int)((k / a.n1) % a.n2) + 1;
-    const int ix = (int)(k / ((int64_t)a.n1 * a.n2)) + 1;
-    const int64_t so = shot * g.fs;
-    float D = gstencil<ORDER>(a.src + so + g.S(iz + a.oz, iy + a.oy, ix + a.ox), st) * a.dsI;
-    if (a.psi) {
-      const int ia = a.axis == 0 ? iz : a.axis == 1 ? iy : ix, nd = a.axis == 0 ? a.n1 : a.axis == 1 ? a.n2 : a.n3;
-      const int j = pml_slot(ia, nd, a.npml, a.lo, a.hi);
-      if (j >= 0) {
-        int64_t pi;
-        if (g.ndim == 2)
-          pi = a.axis == 2 ? (int64_t)j * g.NZP + (iz + ZOFF - 1) : (int64_t)(ix + XOFF - 1) * a.zsw + j;
-        else if (a.axis == 2)
-          pi = ((int64_t)j * g.NYP + (iy + YOFF - 1)) * g.NZP + (iz + ZOFF - 1);
-        else if (a.axis == 1)
-          pi = ((int64_t)(ix + XOFF - 1) * (2 * a.npml) + j) * g.NZP + (iz + ZOFF - 1);
-        else
-          pi = ((int64_t)(ix + XOFF - 1) * g.NYP + (iy + YOFF - 1)) * (2 * a.npml) + j;
-        float *ps = a.psi + shot * a.pss + pi;
-        const float psi = a.pb[j] * *ps + a.pa[j] * D;
-        *ps = psi;
-        D = D * a.pk[j] + psi;
-      }
+  float D = gstencil<ORDER>(a.src + shot * g.fs + g.S(iz + a.oz, iy + a.oy, ix + a.ox), st) * a.dsI;
+  if (a.psi) {
+    const int ia = a.axis == 0 ? iz : a.axis == 1 ? iy : ix, nd = a.axis == 0 ? a.n1 : a.axis == 1 ? a.n2 : a.n3;
+    const int j = pml_slot(ia, nd, a.npml, a.lo, a.hi);
+    if (j >= 0) {
+      int64_t pi;
+      if (g.ndim == 2)
+        pi = a.axis == 2 ? (int64_t)j * g.NZP + (iz + ZOFF - 1) : (int64_t)(ix + XOFF - 1) * a.zsw + j;
+      else if (a.axis == 2)
+        pi = ((int64_t)j * g.NYP + (iy + YOFF - 1)) * g.NZP + (iz + ZOFF - 1);
+      else if (a.axis == 1)
+        pi = ((int64_t)(ix + XOFF - 1) * (2 * a.npml) + j) * g.NZP + (iz + ZOFF - 1);
+      else
+        pi = ((int64_t)(ix + XOFF - 1) * g.NYP + (iy + YOFF - 1)) * (2 * a.npml) + j;
+      float *ps = a.psi + shot * a.pss + pi;
+      const float psi = a.pb[j] * *ps + a.pa[j] * D;
+      *ps = psi;
+      D = D * a.pk[j] + psi;
     }
-    a.out[so + g.S(iz, iy, ix)] = D;
   }
+  return D;
 }
 
 // compute_v!: @inn(v) += c * D (acoustic, advance_acou.jl:273-284) or
 // -= c * (D1 + D2 [+ D3]) (elastic, advance_elastic.jl:69-110), the
-// coefficient stored at the velocity cell
+// coefficient stored at the velocity cell; the derivatives share the @inn
+// extents
 struct GVel {
   GGeo g;
   float *v;  // shot 0
   const float *cf;
-  const float *d1, *d2, *d3;  // derivatives at the @all index (d2, d3 null where absent)
-  int r1, r2, r3, hy;         // @inn extents and the y offset (0 in 2-D)
+  GDer d[3];  // nd of them
+  int nd, r1, r2, r3, hy;
   int elastic, nshots;
 };
-__global__ void __launch_bounds__(256) k_gvel(const GVel a) {
+// Launch shape of the per-cell kernels: GT threads along z, grid (the y-x
+// columns, z blocks, shots), so that a thread finds its cell without a
+// division.
+constexpr int GT = 128;
+template <int ORDER>
+__global__ void __launch_bounds__(GT) k_gvel(const GVel a) {
   const GGeo &g = a.g;
-  const int64_t per = (int64_t)a.r1 * a.r2 * a.r3, total = per * a.nshots;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int shot = (int)(i / per);
-    const int64_t k = i - shot * per;
-    const int iz = (int)(k % a.r1) + 1;
-    const int iy = (int)((k / a.r1) % a.r2) + 1;
-    const int ix = (int)(k / ((int64_t)a.r1 * a.r2)) + 1;
-    const int64_t so = shot * g.fs, od = so + g.S(iz, iy, ix);
+  const int iz = blockIdx.y * GT + threadIdx.x + 1;
+  if (iz > a.r1) return;
+  const int iy = (int)(blockIdx.x % (unsigned)a.r2) + 1, ix = (int)(blockIdx.x / (unsigned)a.r2) + 1;
+  const int shot = blockIdx.z;
+  {
     const int64_t ov = g.S(iz + g.h, iy + a.hy, ix + g.h);
     const float c = a.cf[ov];
-    float *v = a.v + so + ov;
+    float *v = a.v + shot * g.fs + ov;
+    const float D1 = gder_at<ORDER>(g, a.d[0], shot, iz, iy, ix);
     if (!a.elastic) {
-      *v = *v + c * a.d1[od];
-    } else if (!a.d3) {
-      *v = *v - c * (a.d1[od] + a.d2[od]);
+      *v = *v + c * D1;
+    } else if (a.nd == 2) {
+      const float D2 = gder_at<ORDER>(g, a.d[1], shot, iz, iy, ix);
+      *v = *v - c * (D1 + D2);
     } else {
-      *v = *v - c * (a.d1[od] + a.d2[od] + a.d3[od]);
+      const float D2 = gder_at<ORDER>(g, a.d[1], shot, iz, iy, ix);
+      const float D3 = gder_at<ORDER>(g, a.d[2], shot, iz, iy, ix);
+      *v = *v - c * (D1 + D2 + D3);
     }
   }
 }
@@ -210,68 +211,80 @@ __global__ void k_gdirichlet(float *vz, float *vy, float *vx, GGeo g, int nshots
 // compute_p! (advance_acou.jl:303-313) over every p cell
 struct GStr {
   GGeo g;
-  float *f[NFIELD];            // shot 0
-  const float *cf[8];          // coefficients
-  const float *d[18];          // derivatives
+  float *f[NFIELD];    // shot 0
+  const float *cf[8];  // coefficients
+  GDer d[9];           // the velocity derivatives, in the canonical order
   int elastic, nshots, free_zmin;
 };
-__global__ void __launch_bounds__(256) k_gstress_a(const GStr a) {
+template <int ORDER>
+__global__ void __launch_bounds__(GT) k_gstress_a(const GStr a) {
   const GGeo &g = a.g;
-  const int n2 = g.ndim == 3 ? g.ny : 1;
-  const int64_t per = (int64_t)g.nz * n2 * g.nx, total = per * a.nshots;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int shot = (int)(i / per);
-    const int64_t k = i - shot * per;
-    const int r = (int)(k % g.nz) + 1, y = (int)((k / g.nz) % n2) + 1, c = (int)(k / ((int64_t)g.nz * n2)) + 1;
+  const unsigned n2 = g.ndim == 3 ? g.ny : 1;
+  const int r = blockIdx.y * GT + threadIdx.x + 1;
+  if (r > g.nz) return;
+  const int y = (int)(blockIdx.x % n2) + 1, c = (int)(blockIdx.x / n2) + 1;
+  const int shot = blockIdx.z;
+  {
     const int64_t o = g.S(r, y, c), so = shot * g.fs;
     float *p = a.f[GPI_P] + so + o;
-    if (g.ndim == 3)  // (dvxdx + dvzdz + dvydy) * dtK
-      *p = *p + (a.d[3][so + o] + a.d[5][so + o] + a.d[4][so + o]) * a.cf[3][o];
-    else
-      *p = *p + (a.d[2][so + o] + a.d[3][so + o]) * a.cf[2][o];
+    if (g.ndim == 3) {  // (dvxdx + dvzdz + dvydy) * dtK
+      const float dx = gder_at<ORDER>(g, a.d[0], shot, r, y, c), dy = gder_at<ORDER>(g, a.d[1], shot, r, y, c),
+                  dz = gder_at<ORDER>(g, a.d[2], shot, r, y, c);
+      *p = *p + (dx + dz + dy) * a.cf[3][o];
+    } else {
+      const float dx = gder_at<ORDER>(g, a.d[0], shot, r, 1, c), dz = gder_at<ORDER>(g, a.d[1], shot, r, 1, c);
+      *p = *p + (dx + dz) * a.cf[2][o];
+    }
   }
 }
 
 // compute_stressii! / compute_stressij! (advance_elastic.jl:155-213): the
 // normal stresses over their (full) shape, each shear stress over its own
-__global__ void __launch_bounds__(256) k_gstress_e(const GStr a) {
+// (the shape of the two derivatives it reads)
+template <int ORDER>
+__global__ void __launch_bounds__(GT) k_gstress_e(const GStr a) {
   const GGeo &g = a.g;
   const int h = g.h, three = g.ndim == 3;
-  const int n2 = three ? g.ny : 1;
-  const int64_t per = (int64_t)g.nz * n2 * g.nx, total = per * a.nshots;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int shot = (int)(i / per);
-    const int64_t k = i - shot * per;
-    const int r = (int)(k % g.nz) + 1, y = (int)((k / g.nz) % n2) + 1, c = (int)(k / ((int64_t)g.nz * n2)) + 1;
+  const unsigned n2 = three ? g.ny : 1;
+  const int r = blockIdx.y * GT + threadIdx.x + 1;
+  if (r > g.nz) return;
+  const int y = (int)(blockIdx.x % n2) + 1, c = (int)(blockIdx.x / n2) + 1;
+  const int shot = blockIdx.z;
+  {
     const int64_t o = g.S(r, y, c), so = shot * g.fs, x = so + o;
     if (!three) {
       const float M = a.cf[3][o], L = a.cf[4][o];
-      const float dvxdx = a.d[4][x], dvzdz = a.d[5][x];
+      const float dvxdx = gder_at<ORDER>(g, a.d[0], shot, r, 1, c), dvzdz = gder_at<ORDER>(g, a.d[1], shot, r, 1, c);
       float *txx = a.f[GPI_TAUXX] + x, *tzz = a.f[GPI_TAUZZ] + x;
       *txx = *txx - (M * dvxdx) - (L * (dvzdz));
       *tzz = *tzz - (M * dvzdz) - (L * (dvxdx));
       if (r <= g.nz - h && c <= g.nx - h) {  // tauxz (n-h, n-h)
+        const float dvxdz = gder_at<ORDER>(g, a.d[2], shot, r, 1, c), dvzdx = gder_at<ORDER>(g, a.d[3], shot, r, 1, c);
         float *txz = a.f[GPI_TAUXZ] + x;
-        *txz = *txz - a.cf[2][o] * (a.d[6][x] + a.d[7][x]);
+        *txz = *txz - a.cf[2][o] * (dvxdz + dvzdx);
       }
     } else {
       const float M = a.cf[6][o], L = a.cf[7][o];
-      const float dvxdx = a.d[9][x], dvydy = a.d[10][x], dvzdz = a.d[11][x];
+      const float dvxdx = gder_at<ORDER>(g, a.d[0], shot, r, y, c), dvydy = gder_at<ORDER>(g, a.d[1], shot, r, y, c),
+                  dvzdz = gder_at<ORDER>(g, a.d[2], shot, r, y, c);
       float *txx = a.f[GPI_TAUXX] + x, *tyy = a.f[GPI_TAUYY] + x, *tzz = a.f[GPI_TAUZZ] + x;
       *txx = *txx - (M * dvxdx) - (L * (dvydy + dvzdz));
       *tyy = *tyy - (M * dvydy) - (L * (dvxdx + dvzdz));
       *tzz = *tzz - (M * dvzdz) - (L * (dvydy + dvxdx));
       if (r <= g.nz - h && y <= g.ny - 2 * h && c <= g.nx - h) {  // tauxz (n-h, n-2h, n-h)
+        const float d1 = gder_at<ORDER>(g, a.d[4], shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[7], shot, r, y, c);
         float *t = a.f[GPI_TAUXZ] + x;
-        *t = *t - a.cf[3][o] * (a.d[13][x] + a.d[16][x]);
+        *t = *t - a.cf[3][o] * (d1 + d2);
       }
       if (r <= g.nz - 2 * h && y <= g.ny - h && c <= g.nx - h) {  // tauxy (n-2h, n-h, n-h)
+        const float d1 = gder_at<ORDER>(g, a.d[3], shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[5], shot, r, y, c);
         float *t = a.f[GPI_TAUXY] + x;
-        *t = *t - a.cf[4][o] * (a.d[12][x] + a.d[14][x]);
+        *t = *t - a.cf[4][o] * (d1 + d2);
       }
       if (r <= g.nz - h && y <= g.ny - h && c <= g.nx - 2 * h) {  // tauyz (n-h, n-h, n-2h)
+        const float d1 = gder_at<ORDER>(g, a.d[6], shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[8], shot, r, y, c);
         float *t = a.f[GPI_TAUYZ] + x;
-        *t = *t - a.cf[5][o] * (a.d[15][x] + a.d[17][x]);
+        *t = *t - a.cf[5][o] * (d1 + d2);
       }
     }
   }
@@ -311,41 +324,31 @@ static int gstep_order(Plan *p, int vonly) {
   const int n[3] = {p->d.nz, p->d.ny, p->d.nx};
   const float dsI[3] = {p->gdsI[0], p->gdsI[1], p->gdsI[2]};
   const int fmin[3] = {GPI_ZMIN, GPI_YMIN, GPI_XMIN}, fmax[3] = {GPI_ZMAX, GPI_YMAX, GPI_XMAX};
-  const int grid = 152 * 16;
-  auto derivs = [&](int q0, int q1) -> int {
-    for (int q = q0; q < q1; q++) {
-      const GSpec &s = spec[q];
-      GDer a;
-      a.g = g;
-      a.src = f[s.src];
-      a.out = p->der[q];
-      a.n1 = gext(s.kz, n[0], h);
-      a.n2 = three ? gext(s.ky, n[1], h) : 1;
-      a.n3 = gext(s.kx, n[2], h);
-      a.oz = s.inner && s.axis != 0 ? h : 0;
-      a.oy = three && s.inner && s.axis != 1 ? h : 0;
-      a.ox = s.inner && s.axis != 2 ? h : 0;
-      a.axis = s.axis;
-      a.dsI = dsI[s.axis];
-      a.psi = p->psi[0][0][q];
-      a.pss = p->psi_stride[q];
-      const int P = 2 * p->d.npml;
-      a.pa = p->pml + (int64_t)q * 3 * P;
-      a.pb = a.pa + P;
-      a.pk = a.pb + P;
-      a.npml = p->d.npml;
-      a.lo = (p->d.pml_faces & fmin[s.axis]) != 0;
-      a.hi = (p->d.pml_faces & fmax[s.axis]) != 0;
-      a.zsw = p->zsw;
-      a.nshots = p->d.nshots;
-      k_gderiv<ORDER><<<grid, 256, 0, p->stream>>>(a);
-      p->launches++;
-    }
-    GPI_CUDA(p, cudaGetLastError());
-    return GPI_OK;
+  auto der = [&](int q) {
+    const GSpec &s = spec[q];
+    GDer a;
+    a.src = f[s.src];
+    a.n1 = gext(s.kz, n[0], h);
+    a.n2 = three ? gext(s.ky, n[1], h) : 1;
+    a.n3 = gext(s.kx, n[2], h);
+    a.oz = s.inner && s.axis != 0 ? h : 0;
+    a.oy = three && s.inner && s.axis != 1 ? h : 0;
+    a.ox = s.inner && s.axis != 2 ? h : 0;
+    a.axis = s.axis;
+    a.dsI = dsI[s.axis];
+    a.psi = p->psi[0][0][q];
+    a.pss = p->psi_stride[q];
+    const int P = 2 * p->d.npml;
+    a.pa = p->pml + (int64_t)q * 3 * P;
+    a.pb = a.pa + P;
+    a.pk = a.pb + P;
+    a.npml = p->d.npml;
+    a.lo = (p->d.pml_faces & fmin[s.axis]) != 0;
+    a.hi = (p->d.pml_faces & fmax[s.axis]) != 0;
+    a.zsw = p->zsw;
+    return a;
   };
   // update_dstress! + compute_v!
-  if (int rc = derivs(0, nstress)) return rc;
   const int vid[3] = {GPI_VX, GPI_VY, GPI_VZ};
   for (int q = 0; q < 3; q++) {
     if (q == 1 && !three) continue;
@@ -361,19 +364,20 @@ static int gstep_order(Plan *p, int vonly) {
     a.hy = three ? h : 0;
     a.elastic = !ac;
     a.nshots = p->d.nshots;
-    a.d2 = a.d3 = nullptr;
     if (ac) {
-      a.d1 = p->der[three ? q : (q == 0 ? 0 : 1)];
+      a.nd = 1;
+      a.d[0] = der(three ? q : (q == 0 ? 0 : 1));
     } else if (!three) {
-      a.d1 = p->der[q == 0 ? 0 : 1];
-      a.d2 = p->der[q == 0 ? 3 : 2];
+      a.nd = 2;
+      a.d[0] = der(q == 0 ? 0 : 1);
+      a.d[1] = der(q == 0 ? 3 : 2);
     } else {
       const int i3[3][3] = {{0, 4, 8}, {1, 3, 7}, {2, 5, 6}};
-      a.d1 = p->der[i3[q][0]];
-      a.d2 = p->der[i3[q][1]];
-      a.d3 = p->der[i3[q][2]];
+      a.nd = 3;
+      for (int k = 0; k < 3; k++) a.d[k] = der(i3[q][k]);
     }
-    k_gvel<<<grid, 256, 0, p->stream>>>(a);
+    const dim3 vg((unsigned)(a.r2 * a.r3), (a.r1 + GT - 1) / GT, p->d.nshots);
+    k_gvel<ORDER><<<vg, GT, 0, p->stream>>>(a);
     p->launches++;
   }
   // rigid faces in the order x, y, z; min, max (update_v!)
@@ -395,19 +399,19 @@ static int gstep_order(Plan *p, int vonly) {
     if (int rc = inject_sources(p, 0, 1)) return rc;
   if (vonly) return GPI_OK;
   // update_dv! + compute_stress
-  if (int rc = derivs(nstress, nder)) return rc;
   GStr a;
   a.g = g;
   for (int k = 0; k < NFIELD; k++) a.f[k] = f[k];
   for (int k = 0; k < 8; k++) a.cf[k] = p->coef[k];
-  for (int k = 0; k < 18; k++) a.d[k] = p->der[k];
+  for (int k = 0; k < nder - nstress; k++) a.d[k] = der(nstress + k);
   a.elastic = !ac;
   a.nshots = p->d.nshots;
   a.free_zmin = (p->d.free_faces & GPI_ZMIN) != 0;
+  const dim3 sg((unsigned)((three ? n[1] : 1) * n[2]), (n[0] + GT - 1) / GT, p->d.nshots);
   if (ac)
-    k_gstress_a<<<grid, 256, 0, p->stream>>>(a);
+    k_gstress_a<ORDER><<<sg, GT, 0, p->stream>>>(a);
   else
-    k_gstress_e<<<grid, 256, 0, p->stream>>>(a);
+    k_gstress_e<ORDER><<<sg, GT, 0, p->stream>>>(a);
   p->launches++;
   if (!ac && a.free_zmin) {
     const dim3 fb(32, 8), fg((n[2] + 31) / 32, three ? (n[1] + 7) / 8 : 1, nsz);

@@ -69,3 +69,19 @@ def test_acoustic3d_orders_match_oracle(engine, order):
 def test_elastic3d_orders_match_oracle(engine, order):
     wl = configs.elastic3d(nz=24, ny=20, nx=26, nt=200, dt=0.0005, npml=14, nrec_side=4, rfields=("vx", "vz"))
     _run(wl, order, ("tauxx", "tauyy", "tauzz", "tauxy", "tauxz", "tauyz", "vx", "vy", "vz"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("gkind", [1, 2])
+def test_generic_order_graph_replays_equal_plain_runs(engine, gkind):
+    wl = configs.elastic2d_batch(nz=80, nx=120, nt=100, nshots=2, nrec=15)
+    plain = wl.expt(order=6)
+    update(plain)
+    pa = wl.expt(order=6)
+    pa.set_graph(gkind)
+    for _ in range(2):  # capture, then replay
+        update(pa)
+        for i in range(len(wl.shots)):
+            for f in wl.rfields:
+                assert np.array_equal(pa.data[0][i].d[f], plain.data[0][i].d[f]), (i, f)
+    assert np.array_equal(pa.field("tauxz", iss=1), plain.field("tauxz", iss=1))

@@ -46,7 +46,7 @@ def test_plan_estimate_covers_the_layout_and_grows_with_the_work(lib):
     assert c4 > c2 and (c4 - c2) % 2 == 0
     o2 = _estimate(lib, _desc(order=2))
     o8 = _estimate(lib, _desc(order=8))
-    assert o8 > o2 > 0  # materialised derivative fields, a wider padding at order 8
+    assert o8 > o2 > 0  # a wider padding at order 8
     bad = _desc(npw=2)
     bad.order = 2
     assert lib.gpi_plan_estimate(ctypes.byref(bad), ctypes.byref(ctypes.c_size_t())) == -4
