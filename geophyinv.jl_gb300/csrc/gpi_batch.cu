@@ -293,8 +293,9 @@ int gpi_batch_add(gpi_batch *b, gpi_plan *plan) {
   if (!b || !plan) return bfail(b, GPI_E_INVALID, "null argument");
   Plan &p = plan->p;
   if (p.device != b->device) return bfail(b, GPI_E_INVALID, "plan on another device");
-  if (p.d.ndim != 2 || p.d.npw != 1 || p.ck_slots > 0 || p.snap_buf || p.have_born)
-    return bfail(b, GPI_E_UNSUPPORTED, "batches take 2-D forward plans (npw = 1) without snapshots");
+  if (p.d.ndim != 2 || p.d.npw != 1 || p.ck_slots > 0 || p.snap_buf || p.have_born || p.illum || p.d.order != 4)
+    return bfail(b, GPI_E_UNSUPPORTED,
+                 "batches take 2-D forward plans of stencil order 4 (npw = 1) without snapshots or illumination");
   if (b->physics >= 0 && p.d.physics != b->physics) return bfail(b, GPI_E_INVALID, "plans of one physics per batch");
   if (b->mem.size() >= 32767) return bfail(b, GPI_E_INVALID, "batch full");
   for (auto &m : b->mem)

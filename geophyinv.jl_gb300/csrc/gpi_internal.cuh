@@ -188,6 +188,10 @@ struct Plan {
   std::vector<int> snap_its;
   float *snap_buf = nullptr;
 
+  // source illumination (gpi_set_illum): per shot, sum over the steps of a
+  // run of p^2 of wavefield 1, FP64, storage layout [shot][storage]
+  double *illum = nullptr;
+
   // checkpointed adjoint (gpi_plan_desc.checkpoints > 0): full states of
   // wavefield 1 (fields and CPML memory) in ck_slots device slots instead of
   // the boundary store; the adjoint run recomputes forward states from them
@@ -249,6 +253,10 @@ int step_adjoint_acoustic2d(Plan *p, int it);
 int step_a2_wavefield(Plan *p, int ipw, int vonly);
 int step_a2_adjoint_fused(Plan *p);  // both wavefields + imaging condition
 int step_generic(Plan *p, int vonly);  // stencil orders 2, 6, 8 (k_generic.cu)
+// source illumination (k_common.cu): add p^2 of wavefield 1 to the per-shot
+// sums; the shot stack over the cells of the physical grid
+int illum_add(Plan *p);
+int illum_stack(Plan *p, double *dst);
 // batches of forward plans (gpi_batch.cu): argument tables and launches of
 // the step kernels over the tagged tiles of several plans
 size_t a2_args_bytes();

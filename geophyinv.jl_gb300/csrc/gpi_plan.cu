@@ -497,6 +497,9 @@ void destroy(gpi_plan *pl) {
     void *sb = p.snap_buf;
     free_dev(p, sb);
     p.snap_buf = nullptr;
+    void *il = p.illum;
+    free_dev(p, il);
+    p.illum = nullptr;
     void *bb = p.born;
     free_dev(p, bb);
     p.born = nullptr;
@@ -1282,6 +1285,7 @@ static int step_body(Plan &p, int mode, int it, bool dev, int off) {
   if (!rc && mode == GPI_FORWARD_SAVE)
     rc = p.ck_slots > 0 ? ckpt_forward_store(&p, it) : dev ? boundary_io_dev(&p, off, 0) : boundary_io(&p, it, 0);
   if (!rc && !dev && p.snap_buf) rc = save_snapshots(p, mode, it);
+  if (!rc && p.illum) rc = illum_add(&p);  // compute_illum! (propagate.jl:236)
   return rc;
 }
 
@@ -1333,6 +1337,9 @@ static int run_body(Plan &p, int mode, bool chunked) {
   }
   int rc = zero_state(p);
   p.launches = 0;
+  // initialize! (src/fdtd/types.jl:67-72): the illumination of this run
+  if (!rc && p.illum)
+    rc = cudaMemsetAsync(p.illum, 0, (size_t)p.fstride * p.d.nshots * sizeof(double), p.stream) ? GPI_E_CUDA : 0;
   // an adjoint run records nothing and keeps the records of the forward run
   if (!rc && p.rec_pool && mode != GPI_ADJOINT)
     rc = cudaMemsetAsync(p.rec_pool, 0, p.rec_pool_floats * sizeof(float), p.stream) ? GPI_E_CUDA : 0;
@@ -1437,6 +1444,52 @@ int get_snapshot(Plan &p, int ipw, int k, int shot, float *out, int on_device) {
   return GPI_OK;
 }
 
+// illum_flag (src/fdtd/fdtd.jl:59,177, types.jl:20): the per-shot sums of
+// p^2 over the steps of each run (a checkpointed adjoint run keeps those of
+// its forward_save run)
+int set_illum(Plan &p, int enable) {
+  if (enable && !p.present[GPI_P]) return fail(&p, GPI_E_UNSUPPORTED, "illumination sums p^2: acoustic media only");
+  if (!enable) {
+    if (p.illum) cudaFreeAsync(p.illum, p.stream);
+    p.illum = nullptr;
+    drop_graphs(p);
+    return GPI_OK;
+  }
+  if (p.illum) return GPI_OK;
+  const size_t bytes = (size_t)p.fstride * p.d.nshots * sizeof(double);
+  if (pool_alloc((void **)&p.illum, bytes, p.stream) != cudaSuccess) {
+    cudaGetLastError();
+    p.illum = nullptr;
+    return fail(&p, GPI_E_NOMEM, "illumination buffer of " + std::to_string(bytes) + " bytes");
+  }
+  GPI_CUDA(&p, cudaMemsetAsync(p.illum, 0, bytes, p.stream));
+  drop_graphs(p);
+  return GPI_OK;
+}
+
+int get_illum(Plan &p, double *out, int on_device) {
+  if (!p.illum) return fail(&p, GPI_E_STATE, "illumination not enabled");
+  if (!out) return fail(&p, GPI_E_INVALID, "null argument");
+  int64_t n = 1;
+  {
+    const int np = p.d.npml, f = p.d.pml_faces;
+    const int lo[3] = {GPI_ZMIN, GPI_YMIN, GPI_XMIN}, hi[3] = {GPI_ZMAX, GPI_YMAX, GPI_XMAX};
+    const int ext[3] = {p.d.nz, p.d.ndim == 3 ? p.d.ny : 1, p.d.nx};
+    for (int a = 0; a < 3; a++)
+      n *= (a == 1 && p.d.ndim == 2) ? 1 : ext[a] - ((f & lo[a]) ? np : 0) - ((f & hi[a]) ? np : 0);
+  }
+  if (on_device) return illum_stack(&p, out);
+  double *tmp = nullptr;
+  GPI_CUDA(&p, pool_alloc((void **)&tmp, (size_t)n * sizeof(double), p.stream));
+  int rc = illum_stack(&p, tmp);
+  if (!rc && cudaMemcpyAsync(out, tmp, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, p.stream))
+    rc = fail(&p, GPI_E_CUDA, "illumination copy");
+  cudaFreeAsync(tmp, p.stream);
+  if (rc) return rc;
+  GPI_CUDA(&p, cudaStreamSynchronize(p.stream));
+  return check_err(p);
+}
+
 int get_field(Plan &p, int ipw, int shot, int field, float *out, int on_device) {
   if (ipw < 1 || ipw > p.d.npw || shot < 0 || shot >= p.d.nshots || field < 0 || field >= NFIELD || !p.present[field])
     return fail(&p, GPI_E_INVALID, "ipw/shot/field");
@@ -1524,6 +1577,10 @@ int gpi_get_records(gpi_plan *plan, int shot, int field, float *out, int on_devi
 }
 int gpi_get_gradient(gpi_plan *plan, int param, float *out, int on_device) {
   return plan ? gpi::get_gradient(plan->p, param, out, on_device) : GPI_E_INVALID;
+}
+int gpi_set_illum(gpi_plan *plan, int enable) { return plan ? gpi::set_illum(plan->p, enable) : GPI_E_INVALID; }
+int gpi_get_illum(gpi_plan *plan, double *out, int on_device) {
+  return plan ? gpi::get_illum(plan->p, out, on_device) : GPI_E_INVALID;
 }
 int gpi_set_snapshots(gpi_plan *plan, int field, int n, const int *its) {
   return plan ? gpi::set_snapshots(plan->p, field, n, its) : GPI_E_INVALID;

@@ -444,10 +444,10 @@ int gpi_server_submit(gpi_server *s, const gpi_request *r, int64_t *id) {
   j->desc = d;
   j->gradient = r->gradient;
   j->graph = r->graph;
-  // small 2-D forward requests (launch-bound alone) join the batch of their
-  // physics; large ones fill the device on their own
+  // small 2-D forward requests of stencil order 4 (launch-bound alone) join
+  // the batch of their physics; large ones fill the device on their own
   const bool small = (int64_t)d.nz * d.nx * d.nshots <= kBatchCells;
-  j->kind = (!r->gradient && d.ndim == 2 && small && s->max_batch > 0) ? 1 + d.physics : 0;
+  j->kind = (!r->gradient && d.ndim == 2 && d.order == 4 && small && s->max_batch > 0) ? 1 + d.physics : 0;
   const int nmod = d.physics == GPI_ACOUSTIC ? 2 : 3;
   const int64_t cells = grid_cells(d);
   for (int i = 0; i < nmod; i++) {

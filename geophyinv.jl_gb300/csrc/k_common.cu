@@ -543,6 +543,56 @@ int reduce_gradient(Plan *p, int param, float *dst) {
   return GPI_OK;
 }
 
+// compute_illum! (src/fdtd/fdtd.jl:571-582): illum[i] += abs2(p[i]), the
+// square in FP32 and the sum in FP64, over the p cells of every shot
+__global__ void k_illum(double *illum, const float *p, Geo g, int64_t fs) {
+  const int r = blockIdx.y * 128 + threadIdx.x + 1;
+  if (r > g.nz) return;
+  const unsigned n2 = g.ndim == 3 ? g.ny : 1;
+  const int y = (int)(blockIdx.x % n2) + 1, c = (int)(blockIdx.x / n2) + 1;
+  const int64_t o = blockIdx.z * fs + g.off(r, y, c);
+  const float v = p[o];
+  illum[o] = illum[o] + (double)(v * v);
+}
+int illum_add(Plan *p) {
+  const Geo g = geo(*p);
+  const dim3 grid((unsigned)((p->d.ndim == 3 ? p->d.ny : 1) * p->d.nx), (p->d.nz + 127) / 128, p->d.nshots);
+  k_illum<<<grid, 128, 0, p->stream>>>(p->illum, p->state[p->cur[0]][0][GPI_P], g, p->fstride);
+  p->launches++;
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
+// stack_illums! (src/fdtd/fdtd.jl:556-566): the sum over shots, in shot
+// order from zero, of the cells of the physical grid (the padded faces
+// dropped), column-major with z fastest
+__global__ void k_illum_stack(double *dst, const double *illum, Geo g, int64_t fs, int nshots, int z0, int y0, int x0,
+                              int mz, int my, int mx) {
+  const int64_t n = (int64_t)mz * my * mx;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int iz = (int)(i % mz), iy = (int)((i / mz) % my), ix = (int)(i / ((int64_t)mz * my));
+    const int64_t o = g.off(z0 + iz, y0 + iy, x0 + ix);
+    double s = 0.0;
+    for (int k = 0; k < nshots; k++) s = s + illum[k * fs + o];
+    dst[i] = s;
+  }
+}
+int illum_stack(Plan *p, double *dst) {
+  const int np = p->d.npml;
+  const int f = p->d.pml_faces;
+  const int z0 = 1 + ((f & GPI_ZMIN) ? np : 0), mz = p->d.nz - ((f & GPI_ZMIN) ? np : 0) - ((f & GPI_ZMAX) ? np : 0);
+  const int x0 = 1 + ((f & GPI_XMIN) ? np : 0), mx = p->d.nx - ((f & GPI_XMIN) ? np : 0) - ((f & GPI_XMAX) ? np : 0);
+  int y0 = 1, my = 1;
+  if (p->d.ndim == 3) {
+    y0 = 1 + ((f & GPI_YMIN) ? np : 0);
+    my = p->d.ny - ((f & GPI_YMIN) ? np : 0) - ((f & GPI_YMAX) ? np : 0);
+  }
+  k_illum_stack<<<152 * 4, 256, 0, p->stream>>>(dst, p->illum, geo(*p), p->fstride, p->d.nshots, z0, y0, x0, mz, my,
+                                                mx);
+  GPI_CUDA(p, cudaGetLastError());
+  return GPI_OK;
+}
+
 // records: pool [it][ir] -> Recs layout [ir][it]
 __global__ void k_transpose(float *out, const float *in, int nt, int nr) {
   __shared__ float tile[32][33];

@@ -26,7 +26,7 @@ EXPORTS = ["gpi_plan_create", "gpi_plan_destroy", "gpi_last_error", "gpi_set_str
            "gpi_server_destroy", "gpi_server_submit", "gpi_server_poll", "gpi_server_wait", "gpi_server_records",
            "gpi_server_gradient", "gpi_server_times", "gpi_server_message", "gpi_server_release",
            "gpi_batch_create", "gpi_batch_add", "gpi_batch_advance", "gpi_batch_finished", "gpi_batch_launches",
-           "gpi_batch_error", "gpi_batch_destroy", "gpi_set_adjoint_l2"]
+           "gpi_batch_error", "gpi_batch_destroy", "gpi_set_adjoint_l2", "gpi_set_illum", "gpi_get_illum"]
 
 
 class PlanDesc(ctypes.Structure):
@@ -109,6 +109,8 @@ def _load():
     L.gpi_query.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
     L.gpi_set_snapshots.argtypes = [vp, i32, i32, ctypes.POINTER(ctypes.c_int32)]
     L.gpi_get_snapshot.argtypes = [vp, i32, i32, i32, fp, i32]
+    L.gpi_set_illum.argtypes = [vp, i32]
+    L.gpi_get_illum.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32]
     L.gpi_checkpoint_schedule.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
                                           ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)]
     L.gpi_forward_acoustic2d_noalloc.argtypes = [ctypes.POINTER(PlanDesc), fp, fp, fp, i32, i32, i64p, i64p, fp, fp,

@@ -140,10 +140,19 @@ class SeisForwExpt:
 
     def __init__(self, attrib, *, medium, ageom, srcwav, tgrid, rfields=("vz",), pml_faces=ALL_FACES,
                  rigid_faces=None, stressfree_faces=(), order=4, ref_compat_proj=True, stream=None, verbose=False,
-                 npml=None, checkpoints=0, tsnaps=None, snaps_field=None, shard=False, ref_compat_grad=True):
+                 npml=None, checkpoints=0, tsnaps=None, snaps_field=None, shard=False, ref_compat_grad=True,
+                 illum_flag=False, jobname="forward_propagation", backprop_flag=None, nworker=None):
         L = _lib.load()
         self.L = L
         self.attrib = attrib
+        # PFdtd keywords kept for their meaning only: the run mode (attrib)
+        # selects the boundary store, one process drives one device
+        self.jobname = jobname
+        self.backprop_flag = backprop_flag
+        self.nworker = nworker
+        self.illum_flag = bool(illum_flag)
+        if self.illum_flag and attrib.physics != "acoustic":
+            raise ValueError("illum_flag: the illumination sums p^2 (acoustic media only)")
         self.order = order
         self.h = order - 1
         # the reference pads by 40 + h cells (_fd_npml, GeoPhyInv.jl:90); a smaller CPML
@@ -254,6 +263,8 @@ class SeisForwExpt:
             self.itsnaps = [int(np.argmin(np.abs(t - x))) + 1 for x in ts]
             its = (ctypes.c_int32 * len(self.itsnaps))(*self.itsnaps)
             self._check(L.gpi_set_snapshots(self.plan, _lib.FIELD[snaps_field], len(self.itsnaps), its))
+        if self.illum_flag:
+            self._check(L.gpi_set_illum(self.plan, 1))
 
     # ------------------------------------------------------------------
     def _check(self, rc):
@@ -368,7 +379,21 @@ class SeisForwExpt:
             return self.data[0]
         if key == "srcwav":
             return self.srcwav
+        if key == "illum":
+            return self.illum_stack
         raise KeyError(key)
+
+    @property
+    def illum_stack(self):
+        """pac.illum_stack (src/fdtd/fdtd.jl:177, stack_illums! :556-566):
+        the sum over the supersources of sum_t p^2 of the last run, FP64 on
+        the physical grid (illum_flag=True; the reference declares it but its
+        calls are commented out, so there it stays zero)."""
+        if not self.illum_flag:
+            raise ValueError("illum_flag=False")
+        out = np.zeros([len(g) for g in self.medium.grid], np.float64, order="F")
+        self._check(self.L.gpi_get_illum(self.plan, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 0))
+        return _shots.reduce_gradient(out) if self.shard else out
 
     # ------------------------------------------------------------------
     def run(self, mode):

@@ -180,6 +180,19 @@ int gpi_set_snapshots(gpi_plan *plan, int field, int n, const int *its);
 /* Snapshot k (order of `its`) of wavefield ipw (1 or 2) for one shot, in
  * the field's reference shape (pa[:snaps, iss]). */
 int gpi_get_snapshot(gpi_plan *plan, int ipw, int k, int shot, float *out, int on_device);
+/* Source illumination (illum_flag of PFdtd, src/fdtd/fdtd.jl:59,73,177;
+ * compute_illum!, src/fdtd/fdtd.jl:571-582, at the end of every step of the
+ * loop, src/fdtd/propagate.jl:236; stack_illums!, src/fdtd/fdtd.jl:556-566).
+ * enable != 0: every later run sums, per shot and cell, p^2 of wavefield 1
+ * over its steps (the square in FP32, the sum in FP64); acoustic media only
+ * (GPI_E_UNSUPPORTED otherwise).  A checkpointed adjoint run keeps the sums
+ * of its forward_save run.  The reference declares the flag and both
+ * functions but leaves their calls commented out (its illum_stack stays 0). */
+int gpi_set_illum(gpi_plan *plan, int enable);
+/* The illumination of the last run summed over shots (shot order, from 0)
+ * on the physical grid (the padded PML cells dropped): FP64, column-major,
+ * z fastest, nz_phys x [ny_phys x] nx_phys values. */
+int gpi_get_illum(gpi_plan *plan, double *out, int on_device);
 /* Number of engine kernel launches issued by the last gpi_run. */
 int gpi_last_launches(const gpi_plan *plan, int64_t *launches);
 

@@ -124,6 +124,8 @@ typedef struct gpo_ctx {
   REAL **hist;   /* forward history per shot (GPO_FORWARD_HIST) */
   int snap_field, nsnap, snap_its[64]; /* snaps_save! (fdtd.jl:586-591) */
   REAL **snaps;  /* per shot: nsnap copies of wavefield 1's snap_field */
+  int illum_on;   /* illum_flag: compute_illum! (fdtd.jl:571-582) */
+  double **illum; /* per shot: sum over the steps of p^2 of wavefield 1 */
   size_t hstep;  /* REALs per step in the history: p, vx, [vy,] vz */
   size_t bstep;  /* REALs per time step in the store */
   size_t bsnap;  /* REALs of the final snapshots */
@@ -1018,6 +1020,7 @@ gpo_ctx *SFX(gpo_create)(const gpo_desc *d, const void *const *mod, const void *
   c->bstore = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
   c->hist = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
   c->snaps = (REAL **)calloc((size_t)nshots, sizeof(REAL *));
+  c->illum = (double **)calloc((size_t)nshots, sizeof(double *));
   c->snap_field = -1;
   return (gpo_ctx *)c;
 }
@@ -1069,6 +1072,11 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
   const int born = mode == GPO_BORN;
   if (born && !c->have_born) return -4;
   reset_w(c);
+  /* initialize! (types.jl:67-72): the illumination of this run */
+  if (c->illum_on) {
+    if (!c->illum[ishot]) c->illum[ishot] = (double *)malloc(alen(c->w[0][GPO_P]) * sizeof(double));
+    for (size_t i = 0; i < alen(c->w[0][GPO_P]); i++) c->illum[ishot][i] = 0.0;
+  }
   if (mode == GPO_ADJOINT) {
     snap_io(c, ishot, 1, 1); /* boundary_force_snap_tau! */
     snap_io(c, ishot, 0, 1); /* boundary_force_snap_v! */
@@ -1151,6 +1159,15 @@ int SFX(gpo_shot)(gpo_ctx *cc, int ishot, int mode, int nsrc, const gpo_proj *sr
     if (mode == GPO_FORWARD_SAVE) boundary_save(c, ishot, it);
     if (mode == GPO_FORWARD_HIST) hist_io(c, ishot, it, 0, 1);
     if (adjoint && (grad_invK || grad_rho)) compute_gradient(c, (REAL *)grad_invK, (REAL *)grad_rho, (REAL *)grad_3);
+    /* compute_illum! (propagate.jl:236, commented out in the reference):
+       illum[i] += abs2(p[i]), the square in the field's precision */
+    if (c->illum_on) {
+      const REAL *p = c->w[0][GPO_P].a;
+      for (size_t i = 0; i < alen(c->w[0][GPO_P]); i++) {
+        const REAL v = p[i] * p[i];
+        c->illum[ishot][i] += (double)v;
+      }
+    }
     /* snaps_save! for wavefield 1 at the end of step it (propagate.jl:238-245) */
     for (int k = 0; k < c->nsnap; k++)
       if (c->snap_its[k] == it) {
@@ -1232,6 +1249,21 @@ int SFX(gpo_set_snaps)(gpo_ctx *cc, int field, int n, const int *its) {
   return 0;
 }
 
+int SFX(gpo_set_illum)(gpo_ctx *cc, int on) {
+  ctx *c = (ctx *)cc;
+  if (on && !c->present[GPO_P]) return -1;
+  c->illum_on = on != 0;
+  return 0;
+}
+
+/* the illumination of shot ishot's last run over the p array (extended) */
+int SFX(gpo_get_illum)(gpo_ctx *cc, int ishot, double *out) {
+  ctx *c = (ctx *)cc;
+  if (ishot < 0 || ishot >= c->nshots || !c->illum[ishot]) return -1;
+  memcpy(out, c->illum[ishot], alen(c->w[0][GPO_P]) * sizeof(double));
+  return 0;
+}
+
 int SFX(gpo_get_snap)(gpo_ctx *cc, int ishot, int k, void *out) {
   ctx *c = (ctx *)cc;
   if (ishot < 0 || ishot >= c->nshots || k < 0 || k >= c->nsnap || !c->snaps[ishot]) return -1;
@@ -1277,6 +1309,8 @@ void SFX(gpo_destroy)(gpo_ctx *cc) {
   free(c->hist);
   for (int i = 0; i < c->nshots; i++) free(c->snaps[i]);
   free(c->snaps);
+  for (int i = 0; i < c->nshots; i++) free(c->illum[i]);
+  free(c->illum);
   free(c->pv);
   free(c->pvflag);
   for (int i = 0; i < c->nshots; i++) free(c->bstore[i]);

@@ -136,6 +136,13 @@ int gpo_set_snaps_f32(gpo_ctx *c, int field, int n, const int *its);
 int gpo_set_snaps_f64(gpo_ctx *c, int field, int n, const int *its);
 int gpo_get_snap_f32(gpo_ctx *c, int ishot, int k, void *out);
 int gpo_get_snap_f64(gpo_ctx *c, int ishot, int k, void *out);
+/* illum_flag (src/fdtd/fdtd.jl:571-582): per shot, sum over the steps of
+ * p^2 of wavefield 1 (the square in the oracle's precision, the sum in
+ * double) over the p array */
+int gpo_set_illum_f32(gpo_ctx *c, int on);
+int gpo_set_illum_f64(gpo_ctx *c, int on);
+int gpo_get_illum_f32(gpo_ctx *c, int ishot, double *out);
+int gpo_get_illum_f64(gpo_ctx *c, int ishot, double *out);
 /* Copy the current (last shot's final) state of a field of wavefield ipw (1 or 2). */
 int gpo_get_field_f32(gpo_ctx *c, int ipw, int field, void *out);
 int gpo_get_field_f64(gpo_ctx *c, int ipw, int field, void *out);

@@ -248,10 +248,14 @@ def _shot_inputs(prep, shot, src_types=1):
     return src, rec
 
 
-def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=False, snaps=None, mod=None):
+def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=False, snaps=None, mod=None,
+            illum=False):
     """update!(pa) in :forward mode: records[field] of shape (nshots, nt, nr).
     snaps = (field, [steps]) also returns res["snaps"][shot][k], the field at
-    the end of step steps[k] (1-based; snaps_save!).  mod: extended-grid
+    the end of step steps[k] (1-based; snaps_save!).  illum=True also returns
+    res["illum"], pac.illum_stack with illum_flag (compute_illum!, stack_illums!,
+    src/fdtd/fdtd.jl:556-582): the shot sum of sum_t p^2 on the physical
+    grid, FP64.  mod: extended-grid
     medium parameters replacing the ones padded from ex (as after
     update!(pa, m, mparams), which leaves the PML cells as they were)."""
     prep = Prepared(ex, dtype, ref_compat)
@@ -264,13 +268,28 @@ def forward(ex, dtype=np.float32, nthreads=0, ref_compat=True, return_oracle=Fal
         fn = getattr(orc.L, "gpo_set_snaps_" + sfx)
         fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         assert fn(orc.ctx, S.FIELD_ID[snaps[0]], len(snaps[1]), its) == 0
+    if illum:
+        fn = getattr(orc.L, "gpo_set_illum_" + orc.sfx)
+        fn.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        assert fn(orc.ctx, 1) == 0
     out = {f: [] for f in ex["rfields"]}
+    stack = None
     for i, shot in enumerate(ex["shots"]):
         src, rec = _shot_inputs(prep, shot)
         r = orc.shot(i, 0, src, rec)
         for f in ex["rfields"]:
             out[f].append(r[f])
+        if illum:
+            shape = orc.field("p").shape
+            a = np.zeros(int(np.prod(shape)), np.float64)
+            get = getattr(orc.L, "gpo_get_illum_" + orc.sfx)
+            get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+            assert get(orc.ctx, i, a.ctypes.data) == 0
+            gss = a.reshape(shape, order="F")[_inner(prep, shape)]
+            stack = (np.zeros_like(gss) if stack is None else stack) + gss  # illums += gss
     res = {f: np.stack(v) for f, v in out.items()}
+    if illum:
+        res["illum"] = stack
     if snaps is not None:
         shape = orc.field(snaps[0]).shape
         get = getattr(orc.L, "gpo_get_snap_" + orc.sfx)
@@ -337,15 +356,21 @@ def gradient(ex, dobs, dtype=np.float32, nthreads=0, ref_compat=True, history=Fa
         orc.shot(i, 4 if history else 2, src, [], adj, gs)
     orc.close()
     raw = {k: g.copy() for k, g in zip(names, gs)}
+    inner = _inner(prep, shape)
+    g = {k: (raw[k] * prep.mod[i])[inner] for i, k in enumerate(names)}
+    return loss, g, dcal, raw
+
+
+def _inner(prep, shape):
+    """Slices of the physical grid in an extended-grid array (the padding
+    sits on the PML faces only)."""
     inner = []
     axes = "zyx" if prep.ndim == 3 else "zx"
     for i, d in enumerate(axes):
         lo = prep.npml if prep.faces & S.FACE_BITS[d + "min"] else 0
         hi = prep.npml if prep.faces & S.FACE_BITS[d + "max"] else 0
         inner.append(slice(lo, shape[i] - hi))
-    inner = tuple(inner)
-    g = {k: (raw[k] * prep.mod[i])[inner] for i, k in enumerate(names)}
-    return loss, g, dcal, raw
+    return tuple(inner)
 
 
 def born(ex, dinvK, drho, dtype=np.float32, nthreads=0):
