@@ -10,9 +10,9 @@ from .fdtd import (AGeomss, AcousticMedium, BornMap, ElasticMedium, FdtdAcoustic
                    lossvalue, set_born_perturbation, update, update_batch)
 from . import fwi  # noqa
 from .rrule import NoTangent, misfit, rrule  # noqa
-from .setup import Grid, findfreq_peak, ricker  # noqa
+from .setup import Grid, findfreq_peak, ormsby, ricker  # noqa
 
 __all__ = ["AGeomss", "AcousticMedium", "BornMap", "ElasticMedium", "FdtdAcoustic", "FdtdAcousticBorn",
            "FdtdElastic", "Fields", "Grid", "set_born_perturbation",
            "L2DistLoss", "NoTangent", "fwi", "Recs", "SeisForwExpt", "Srcs", "findfreq_peak", "get_modelvector",
-           "gradient", "lossvalue", "misfit", "ricker", "rrule", "update", "update_batch"]
+           "gradient", "lossvalue", "misfit", "ormsby", "ricker", "rrule", "update", "update_batch"]

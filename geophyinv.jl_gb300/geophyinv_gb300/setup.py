@@ -238,6 +238,63 @@ def ricker(fqdom, tgrid, tpeak=None, maxamp=1.0):
     return (1.0 - 2.0 * pf * ts) * np.exp(-1.0 * pf * ts) * maxamp
 
 
+def taper(x, perc=0.0, bperc=None, eperc=None):
+    """taper! along the first axis (src/Utils/taper.jl:20-36): the first
+    round(nt perc / 100) samples times sin((i - 1) pi / (2 n - 1)), the last
+    ones times sin((nt - i) pi / (2 n - 1)) (1-based i; ties of the rounding
+    to even, as Julia's round)."""
+    x = np.array(x, np.float64, copy=True)
+    nt = x.shape[0]
+    bperc = perc if bperc is None else bperc
+    eperc = perc if eperc is None else eperc
+    nb, ne = int(round(nt * bperc * 0.01)), int(round(nt * eperc * 0.01))
+    ntb, nte = min(nb, nt), min(ne, nt)
+    kb, ke = math.pi / (2.0 * nb - 1), math.pi / (2.0 * ne - 1)
+    i = np.arange(1, nt + 1, dtype=np.float64)
+    shape = (nt,) + (1,) * (x.ndim - 1)
+    if ntb > 0:
+        w = np.where(i <= ntb, np.sin((i - 1) * kb), 1.0)
+        x *= w.reshape(shape)
+    if nte > 0:
+        w = np.where(i >= nt - nte + 1, np.sin((-i + nt) * ke), 1.0)
+        x *= w.reshape(shape)
+    return x
+
+
+def ormsby(fqdom, tgrid, fracbandwidth=1.2, f1=None, f4=None, f2=None, f3=None, tpeak=None, trim_tol=0.0,
+           tperc=0.0, maxamp_rand_flag=False, rng=None):
+    """Ormsby wavelet (src/srcwav/wavelets.jl:75-142): corner frequencies
+    f1 < f2 < f3 < f4 around fqdom (fracbandwidth 1.2 as for the Ricker),
+    w(t) = (A43 S4 - A34 S3) - (A21 S2 - A12 S1) with Sk = sinc(pi fk t)^2,
+    t = tgrid - tpeak, normalised to a maximum |w| of 1, then tapered by
+    tperc percent at both ends.  sinc is the normalised sinc (Julia's and
+    numpy's: sin(pi x) / (pi x)), so the reference's argument pi fk t puts
+    the pass band at pi [f1, f4]; kept as the reference computes it."""
+    f1 = fqdom - fracbandwidth * 0.5 * fqdom if f1 is None else f1
+    f4 = fqdom + fracbandwidth * 0.5 * fqdom if f4 is None else f4
+    f2 = 0.25 * f4 + 0.75 * f1 if f2 is None else f2
+    f3 = 0.25 * f1 + 0.75 * f4 if f3 is None else f3
+    if tpeak is None:
+        tpeak = tgrid.first + 1.5 / (0.25 * (f1 + f4))
+    pi = math.pi
+    A43 = (pi * f4) ** 2 / (pi * f4 - pi * f3)
+    A34 = (pi * f3) ** 2 / (pi * f4 - pi * f3)
+    A21 = (pi * f2) ** 2 / (pi * f2 - pi * f1)
+    A12 = (pi * f1) ** 2 / (pi * f2 - pi * f1)
+    t = tgrid.values() - tpeak
+    S4 = np.sinc(pi * f4 * t) ** 2
+    S3 = np.sinc(pi * f3 * t) ** 2
+    S2 = np.sinc(pi * f2 * t) ** 2
+    S1 = np.sinc(pi * f1 * t) ** 2
+    wav = (A43 * S4 - A34 * S3) - (A21 * S2 - A12 * S1)
+    wav = wav / np.max(np.abs(wav))
+    if maxamp_rand_flag:
+        wav = wav * (rng or np.random.default_rng()).uniform(-1.0, 1.0)
+    if trim_tol != 0.0:
+        wav = wav[np.abs(wav) >= trim_tol]
+    return taper(wav, tperc)
+
+
 def findfreq_peak(w, dt):
     """Peak frequency of |rfft|^2 over all columns (findfreq, src/Utils/freq.jl:28-57)."""
     w = np.asarray(w, np.float32)

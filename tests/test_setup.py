@@ -70,3 +70,43 @@ def test_wavelets():
     assert P.findfreq_peak(w, 0.0005) == S.findfreq_peak(w, 0.0005) == 15.0
     w2 = np.stack([w, 2 * w], 1)
     np.testing.assert_array_equal(P.reverse_source(w2), S.source_reverse(w2))
+
+
+def test_ormsby_wavelet():
+    """ormsby (src/srcwav/wavelets.jl:75-142), with Julia's normalised sinc:
+    unit peak at tpeak, symmetric about it, the pass band at pi [f1, f4],
+    and the taper! of src/Utils/taper.jl:20-36 zeroing the end samples."""
+    import math
+
+    from geophyinv_gb300.setup import Grid, findfreq_peak, ormsby, taper
+
+    tg = Grid(0.0, 0.001, 801)
+    f = 5.0
+    w = ormsby(f, tg)
+    f1, f4 = f - 0.6 * f, f + 0.6 * f
+    f2, f3 = 0.25 * f4 + 0.75 * f1, 0.25 * f1 + 0.75 * f4
+    tpeak = 1.5 / (0.25 * (f1 + f4))
+    ip = int(round(tpeak / 0.001))
+    assert abs(np.max(np.abs(w)) - 1.0) < 1e-15 and abs(w[ip] - 1.0) < 1e-12
+    assert np.allclose(w[ip - 100:ip], w[ip + 100:ip:-1], atol=1e-12)
+
+    # one sample against the formula written out with sin (Julia's sinc(x) = sin(pi x) / (pi x))
+    def S(fk, t):
+        x = math.pi * fk * t
+        return (math.sin(math.pi * x) / (math.pi * x)) ** 2
+
+    pi = math.pi
+    A43, A34 = (pi * f4) ** 2 / (pi * f4 - pi * f3), (pi * f3) ** 2 / (pi * f4 - pi * f3)
+    A21, A12 = (pi * f2) ** 2 / (pi * f2 - pi * f1), (pi * f1) ** 2 / (pi * f2 - pi * f1)
+    t = 0.037 - tpeak
+    raw = (A43 * S(f4, t) - A34 * S(f3, t)) - (A21 * S(f2, t) - A12 * S(f1, t))
+    t0 = 1e-9
+    peak = (A43 * S(f4, t0) - A34 * S(f3, t0)) - (A21 * S(f2, t0) - A12 * S(f1, t0))
+    assert abs(w[37] - raw / peak) < 1e-6
+    fp = findfreq_peak(w, 0.001)
+    assert pi * f1 <= fp <= pi * f4
+    wt = ormsby(f, tg, tperc=10.0)
+    assert wt[0] == 0.0 and wt[-1] == 0.0 and wt[ip] == w[ip]
+    x = taper(np.ones(20), 25.0)  # 5 samples each end: sin(k pi / 9)
+    assert np.allclose(x[:5], np.sin(np.arange(5) * math.pi / 9)) and np.allclose(x[5:15], 1.0)
+    assert np.allclose(x[15:], np.sin((20 - np.arange(16, 21)) * math.pi / 9))
