@@ -78,7 +78,7 @@ struct GGeo {
 // staggered difference of order ORDER along stride s (src/fdtd/diff2D.jl,
 // diff3D.jl: @d_?a / @d_?i), the reference's coefficients and sum order
 template <int ORDER>
-__device__ __forceinline__ float gstencil(const float *a, int64_t s) {
+__device__ __forceinline__ float gstencil(const float *a, int s) {
   if constexpr (ORDER == 2) {
     return a[s] - a[0];
   } else if constexpr (ORDER == 4) {
@@ -97,7 +97,8 @@ __device__ __forceinline__ float gstencil(const float *a, int64_t s) {
 struct GDer {
   const float *src;  // shot 0
   int n1, n2, n3;    // derivative extents (z, y, x)
-  int oz, oy, ox;    // source offset (inner: h on the other axes)
+  int soff, st;      // storage offset of the source cell from the derivative
+                     // cell (inner: h on the other axes); stride of the axis
   int axis;
   float dsI;
   // CPML
@@ -107,11 +108,11 @@ struct GDer {
   int npml, lo, hi, zsw;
 };
 
-// derivative cell (iz, iy, ix) of shot `shot`, its CPML memory advanced
+// derivative cell (iz, iy, ix) of shot `shot` at storage offset `base`
+// (shot included), its CPML memory advanced
 template <int ORDER>
-__device__ __forceinline__ float gder_at(const GGeo &g, const GDer &a, int shot, int iz, int iy, int ix) {
-  const int64_t st = a.axis == 0 ? 1 : a.axis == 1 ? (int64_t)g.NZP : (int64_t)g.NYP * g.NZP;
-  float D = gstencil<ORDER>(a.src + shot * g.fs + g.S(iz + a.oz, iy + a.oy, ix + a.ox), st) * a.dsI;
+__device__ __forceinline__ float gder_at(const GGeo &g, const GDer &a, int64_t base, int shot, int iz, int iy, int ix) {
+  float D = gstencil<ORDER>(a.src + base + a.soff, a.st) * a.dsI;
   if (a.psi) {
     const int ia = a.axis == 0 ? iz : a.axis == 1 ? iy : ix, nd = a.axis == 0 ? a.n1 : a.axis == 1 ? a.n2 : a.n3;
     const int j = pml_slot(ia, nd, a.npml, a.lo, a.hi);
@@ -155,21 +156,23 @@ __global__ void __launch_bounds__(GT) k_gvel(const GVel a) {
   const GGeo &g = a.g;
   const int iz = blockIdx.y * GT + threadIdx.x + 1;
   if (iz > a.r1) return;
-  const int iy = (int)(blockIdx.x % (unsigned)a.r2) + 1, ix = (int)(blockIdx.x / (unsigned)a.r2) + 1;
+  const bool flat = g.ndim == 2;  // one y plane: the column index is x
+  const int iy = flat ? 1 : (int)(blockIdx.x % (unsigned)a.r2) + 1;
+  const int ix = flat ? (int)blockIdx.x + 1 : (int)(blockIdx.x / (unsigned)a.r2) + 1;
   const int shot = blockIdx.z;
   {
-    const int64_t ov = g.S(iz + g.h, iy + a.hy, ix + g.h);
+    const int64_t ov = g.S(iz + g.h, iy + a.hy, ix + g.h), od = shot * g.fs + g.S(iz, iy, ix);
     const float c = a.cf[ov];
     float *v = a.v + shot * g.fs + ov;
-    const float D1 = gder_at<ORDER>(g, a.d[0], shot, iz, iy, ix);
+    const float D1 = gder_at<ORDER>(g, a.d[0], od, shot, iz, iy, ix);
     if (!a.elastic) {
       *v = *v + c * D1;
     } else if (a.nd == 2) {
-      const float D2 = gder_at<ORDER>(g, a.d[1], shot, iz, iy, ix);
+      const float D2 = gder_at<ORDER>(g, a.d[1], od, shot, iz, iy, ix);
       *v = *v - c * (D1 + D2);
     } else {
-      const float D2 = gder_at<ORDER>(g, a.d[1], shot, iz, iy, ix);
-      const float D3 = gder_at<ORDER>(g, a.d[2], shot, iz, iy, ix);
+      const float D2 = gder_at<ORDER>(g, a.d[1], od, shot, iz, iy, ix);
+      const float D3 = gder_at<ORDER>(g, a.d[2], od, shot, iz, iy, ix);
       *v = *v - c * (D1 + D2 + D3);
     }
   }
@@ -222,17 +225,17 @@ __global__ void __launch_bounds__(GT) k_gstress_a(const GStr a) {
   const unsigned n2 = g.ndim == 3 ? g.ny : 1;
   const int r = blockIdx.y * GT + threadIdx.x + 1;
   if (r > g.nz) return;
-  const int y = (int)(blockIdx.x % n2) + 1, c = (int)(blockIdx.x / n2) + 1;
+  const int y = n2 == 1 ? 1 : (int)(blockIdx.x % n2) + 1, c = n2 == 1 ? (int)blockIdx.x + 1 : (int)(blockIdx.x / n2) + 1;
   const int shot = blockIdx.z;
   {
-    const int64_t o = g.S(r, y, c), so = shot * g.fs;
-    float *p = a.f[GPI_P] + so + o;
+    const int64_t o = g.S(r, y, c), so = shot * g.fs, x = so + o;
+    float *p = a.f[GPI_P] + x;
     if (g.ndim == 3) {  // (dvxdx + dvzdz + dvydy) * dtK
-      const float dx = gder_at<ORDER>(g, a.d[0], shot, r, y, c), dy = gder_at<ORDER>(g, a.d[1], shot, r, y, c),
-                  dz = gder_at<ORDER>(g, a.d[2], shot, r, y, c);
+      const float dx = gder_at<ORDER>(g, a.d[0], x, shot, r, y, c), dy = gder_at<ORDER>(g, a.d[1], x, shot, r, y, c),
+                  dz = gder_at<ORDER>(g, a.d[2], x, shot, r, y, c);
       *p = *p + (dx + dz + dy) * a.cf[3][o];
     } else {
-      const float dx = gder_at<ORDER>(g, a.d[0], shot, r, 1, c), dz = gder_at<ORDER>(g, a.d[1], shot, r, 1, c);
+      const float dx = gder_at<ORDER>(g, a.d[0], x, shot, r, 1, c), dz = gder_at<ORDER>(g, a.d[1], x, shot, r, 1, c);
       *p = *p + (dx + dz) * a.cf[2][o];
     }
   }
@@ -248,41 +251,41 @@ __global__ void __launch_bounds__(GT) k_gstress_e(const GStr a) {
   const unsigned n2 = three ? g.ny : 1;
   const int r = blockIdx.y * GT + threadIdx.x + 1;
   if (r > g.nz) return;
-  const int y = (int)(blockIdx.x % n2) + 1, c = (int)(blockIdx.x / n2) + 1;
+  const int y = n2 == 1 ? 1 : (int)(blockIdx.x % n2) + 1, c = n2 == 1 ? (int)blockIdx.x + 1 : (int)(blockIdx.x / n2) + 1;
   const int shot = blockIdx.z;
   {
     const int64_t o = g.S(r, y, c), so = shot * g.fs, x = so + o;
     if (!three) {
       const float M = a.cf[3][o], L = a.cf[4][o];
-      const float dvxdx = gder_at<ORDER>(g, a.d[0], shot, r, 1, c), dvzdz = gder_at<ORDER>(g, a.d[1], shot, r, 1, c);
+      const float dvxdx = gder_at<ORDER>(g, a.d[0], x, shot, r, 1, c), dvzdz = gder_at<ORDER>(g, a.d[1], x, shot, r, 1, c);
       float *txx = a.f[GPI_TAUXX] + x, *tzz = a.f[GPI_TAUZZ] + x;
       *txx = *txx - (M * dvxdx) - (L * (dvzdz));
       *tzz = *tzz - (M * dvzdz) - (L * (dvxdx));
       if (r <= g.nz - h && c <= g.nx - h) {  // tauxz (n-h, n-h)
-        const float dvxdz = gder_at<ORDER>(g, a.d[2], shot, r, 1, c), dvzdx = gder_at<ORDER>(g, a.d[3], shot, r, 1, c);
+        const float dvxdz = gder_at<ORDER>(g, a.d[2], x, shot, r, 1, c), dvzdx = gder_at<ORDER>(g, a.d[3], x, shot, r, 1, c);
         float *txz = a.f[GPI_TAUXZ] + x;
         *txz = *txz - a.cf[2][o] * (dvxdz + dvzdx);
       }
     } else {
       const float M = a.cf[6][o], L = a.cf[7][o];
-      const float dvxdx = gder_at<ORDER>(g, a.d[0], shot, r, y, c), dvydy = gder_at<ORDER>(g, a.d[1], shot, r, y, c),
-                  dvzdz = gder_at<ORDER>(g, a.d[2], shot, r, y, c);
+      const float dvxdx = gder_at<ORDER>(g, a.d[0], x, shot, r, y, c), dvydy = gder_at<ORDER>(g, a.d[1], x, shot, r, y, c),
+                  dvzdz = gder_at<ORDER>(g, a.d[2], x, shot, r, y, c);
       float *txx = a.f[GPI_TAUXX] + x, *tyy = a.f[GPI_TAUYY] + x, *tzz = a.f[GPI_TAUZZ] + x;
       *txx = *txx - (M * dvxdx) - (L * (dvydy + dvzdz));
       *tyy = *tyy - (M * dvydy) - (L * (dvxdx + dvzdz));
       *tzz = *tzz - (M * dvzdz) - (L * (dvydy + dvxdx));
       if (r <= g.nz - h && y <= g.ny - 2 * h && c <= g.nx - h) {  // tauxz (n-h, n-2h, n-h)
-        const float d1 = gder_at<ORDER>(g, a.d[4], shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[7], shot, r, y, c);
+        const float d1 = gder_at<ORDER>(g, a.d[4], x, shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[7], x, shot, r, y, c);
         float *t = a.f[GPI_TAUXZ] + x;
         *t = *t - a.cf[3][o] * (d1 + d2);
       }
       if (r <= g.nz - 2 * h && y <= g.ny - h && c <= g.nx - h) {  // tauxy (n-2h, n-h, n-h)
-        const float d1 = gder_at<ORDER>(g, a.d[3], shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[5], shot, r, y, c);
+        const float d1 = gder_at<ORDER>(g, a.d[3], x, shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[5], x, shot, r, y, c);
         float *t = a.f[GPI_TAUXY] + x;
         *t = *t - a.cf[4][o] * (d1 + d2);
       }
       if (r <= g.nz - h && y <= g.ny - h && c <= g.nx - 2 * h) {  // tauyz (n-h, n-h, n-2h)
-        const float d1 = gder_at<ORDER>(g, a.d[6], shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[8], shot, r, y, c);
+        const float d1 = gder_at<ORDER>(g, a.d[6], x, shot, r, y, c), d2 = gder_at<ORDER>(g, a.d[8], x, shot, r, y, c);
         float *t = a.f[GPI_TAUYZ] + x;
         *t = *t - a.cf[5][o] * (d1 + d2);
       }
@@ -331,9 +334,10 @@ static int gstep_order(Plan *p, int vonly) {
     a.n1 = gext(s.kz, n[0], h);
     a.n2 = three ? gext(s.ky, n[1], h) : 1;
     a.n3 = gext(s.kx, n[2], h);
-    a.oz = s.inner && s.axis != 0 ? h : 0;
-    a.oy = three && s.inner && s.axis != 1 ? h : 0;
-    a.ox = s.inner && s.axis != 2 ? h : 0;
+    const int oz = s.inner && s.axis != 0 ? h : 0, oy = three && s.inner && s.axis != 1 ? h : 0,
+              ox = s.inner && s.axis != 2 ? h : 0;
+    a.soff = (int)(oz + (int64_t)oy * p->NZP + (int64_t)ox * p->NYP * p->NZP);
+    a.st = s.axis == 0 ? 1 : s.axis == 1 ? p->NZP : p->NYP * p->NZP;
     a.axis = s.axis;
     a.dsI = dsI[s.axis];
     a.psi = p->psi[0][0][q];
