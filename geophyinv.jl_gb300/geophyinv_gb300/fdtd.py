@@ -743,17 +743,23 @@ def _on_device(loss, pa):
     return type(loss) is L2DistLoss and pa.attrib.npw == 2 and all(f in ("vx", "vy", "vz") for f in pa.rfields)
 
 
-def _device_l2(pa, dobs):
+def _device_l2(pa, dobs, dobs_dev=None):
     """Adjoint sources 2 (dobs - dcal) reversed and the misfit sum
     (dobs - dcal)^2 from the records of the last run, on the device
-    (gpi_set_adjoint_l2); the misfit summed over the ranks."""
+    (gpi_set_adjoint_l2); the misfit summed over the ranks.  dobs_dev: the
+    same observed data already on the device (per local shot, per field, a
+    tensor in the Recs layout)."""
     pa._check(pa.L.gpi_clear_sources(pa.plan, 2, -1))
     J = 0.0
     for iss, o in enumerate(_local(pa, dobs)):
         for f in pa.rfields:
-            d = np.asfortranarray(o.d[f], dtype=np.float32)
             mis = ctypes.c_double()
-            pa._check(pa.L.gpi_set_adjoint_l2(pa.plan, iss, _lib.FIELD[f], _ptr(d), 0, ctypes.byref(mis)))
+            if dobs_dev is not None:
+                ptr = ctypes.cast(dobs_dev[iss][f].data_ptr(), ctypes.POINTER(ctypes.c_float))
+                pa._check(pa.L.gpi_set_adjoint_l2(pa.plan, iss, _lib.FIELD[f], ptr, 1, ctypes.byref(mis)))
+            else:
+                d = np.asfortranarray(o.d[f], dtype=np.float32)
+                pa._check(pa.L.gpi_set_adjoint_l2(pa.plan, iss, _lib.FIELD[f], _ptr(d), 0, ctypes.byref(mis)))
             J += mis.value
     return _shots.reduce_scalar(J) if pa.shard else J
 
@@ -773,31 +779,76 @@ def gradient(g, m, loss, dobs, pa, mparams=("invK", "rho")):
     adjoint run with src_types [-1, 1], chain rule g * exp(m) * ref.  With
     L2DistLoss the adjoint sources and the misfit are computed on the device
     from the records there (gpi_set_adjoint_l2); pa.srcwav[2] then keeps its
-    previous host contents."""
-    _forward_save(pa, m, mparams)
-    gv = _adjoint(pa, m, loss, dobs, mparams)
+    previous host contents.  On a plan with its own stream (and no
+    checkpoints) the host's copies run beside the device work: the observed
+    data go up on a second stream during the forward_save run, and the
+    records of that run come down on it during the adjoint run (which
+    records nothing)."""
+    if _on_device(loss, pa) and pa.stream is not None and not pa.checkpoints:
+        gv = _gradient_overlapped(pa, m, loss, dobs, mparams)
+    else:
+        _forward_save(pa, m, mparams)
+        gv = _adjoint(pa, m, loss, dobs, mparams)
     if g is not None:
         g[:] = gv
     J = getattr(pa, "_device_misfit", None)
     return J if J is not None else _loss(loss, dobs, pa)
 
 
-def _forward_save(pa, m, mparams):
+def _gradient_overlapped(pa, m, loss, dobs, mparams):
+    import torch
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    main = torch.cuda.ExternalStream(pa.stream, device=dev)
+    side = torch.cuda.Stream(device=dev)
+    _forward_save(pa, m, mparams, read_records=False)
+    fwd = torch.cuda.Event()
+    fwd.record(main)
+    with torch.cuda.stream(side):
+        dobs_dev = [{f: torch.from_numpy(np.ravel(np.asarray(o.d[f], np.float32), order="F")).to(dev, non_blocking=True)
+                     for f in pa.rfields} for o in _local(pa, dobs)]
+    up = torch.cuda.Event()
+    up.record(side)
+    main.wait_event(up)
+
+    def records_beside():
+        # the plan's record buffers on the second stream, after the
+        # forward_save run, while the adjoint run goes on
+        side.wait_event(fwd)
+        pa._check(pa.L.gpi_set_stream(pa.plan, ctypes.c_void_p(side.cuda_stream)))
+        try:
+            for iss in range(pa.nss):
+                for f in pa.rfields:
+                    pa.data[0][iss].d[f] = pa.records(iss, f)
+        finally:
+            pa._check(pa.L.gpi_set_stream(pa.plan, ctypes.c_void_p(pa.stream)))
+
+    gv = _adjoint(pa, m, loss, dobs, mparams, dobs_dev=dobs_dev, after_launch=records_beside)
+    main.synchronize()  # the observed data stay alive until the adjoint sources are formed
+    del dobs_dev
+    return gv
+
+
+def _forward_save(pa, m, mparams, read_records=True):
     """The first half of gradient!: update!(pa, m), forward_save run (the
     boundary store, or the checkpoints of a checkpointed plan, stay on the
-    device)."""
+    device); without read_records the run is only launched."""
     update(pa, m, list(mparams))
     mode_save = pa.attrib.mode
     pa.attrib.mode = "forward_save"
     update(pa, pa.srcwav, [1, 0])
-    update(pa)
+    if read_records:
+        update(pa)
+    else:
+        pa.run(_lib.FORWARD_SAVE)
     pa.attrib.mode = mode_save
 
 
-def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
+def _adjoint(pa, m, loss, dobs, mparams, scale=1.0, dobs_dev=None, after_launch=None):
     """The second half of gradient!: adjoint sources from the records of the
     last forward_save run, the adjoint run, the chain rule onto m (times
-    `scale`)."""
+    `scale`).  after_launch runs on the host once the adjoint run is
+    queued."""
     mparams = list(mparams)
     # a checkpointed plan recomputes wavefield 1 forward in time, with the
     # sources of its forward_save run (no time-reversed copy is needed)
@@ -806,7 +857,7 @@ def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
     if _on_device(loss, pa):
         # adjoint sources 2 (dobs - dcal) reversed, and the misfit, on the
         # device from the records there
-        pa._device_misfit = _device_l2(pa, dobs)
+        pa._device_misfit = _device_l2(pa, dobs, dobs_dev)
         _update_srcwav(pa, [pa.srcwav[0]], [st1], ipws=(0,))
     else:
         adj = []
@@ -822,6 +873,8 @@ def _adjoint(pa, m, loss, dobs, mparams, scale=1.0):
     pa.attrib.mode = "adjoint"
     update(pa)
     pa.attrib.mode = mode_save
+    if after_launch is not None:
+        after_launch()
     inn = _inner(pa)
     chunks = np.split(np.asarray(m, np.float32), len(mparams))
     out = []

@@ -76,3 +76,36 @@ def test_device_adjoint_sources_equal_host_ones(engine, checkpoints):
     assert np.array_equal(gd, gh)
     for k in rd:
         assert np.array_equal(rd[k], rh[k]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [0, 2])
+def test_gradient_with_copies_beside_the_runs_equals_the_plain_flow(engine, graph):
+    """On a plan with its own stream gradient! uploads the observed data
+    during the forward_save run and reads the records during the adjoint run;
+    misfit, gradient and records equal those of the plan without a stream."""
+    import torch
+
+    from geophyinv_gb300 import update
+
+    nz, nx, nt, nshots = 50, 90, 320, 3
+    true = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=nshots, nrec=nx // 2)
+    pt = true.expt()
+    update(pt)
+    dobs = [Recs(r.n, r.grid, r.fields, {f: np.array(r.d[f], order="F") for f in r.fields}) for r in pt.data[0]]
+    start = configs.acoustic2d_fwi(nz=nz, nx=nx, nt=nt, nshots=nshots, nrec=nx // 2, anomaly=False)
+    out = []
+    for stream in (None, torch.cuda.Stream()):
+        pa = start.expt(mode="forward_save", stream=None if stream is None else stream.cuda_stream)
+        pa.set_graph(graph)
+        m = get_modelvector(pa, ["invK", "rho"])
+        g = np.zeros_like(m)
+        J = gradient(g, m, L2DistLoss(), dobs, pa)
+        J2 = gradient(g, m, L2DistLoss(), dobs, pa)  # a second call reuses the plan
+        assert J2 == J
+        out.append((J, g.copy(), [pa.data[0][i].d["vz"].copy() for i in range(nshots)]))
+    (Ja, ga, ra), (Jb, gb, rb) = out
+    assert Ja == Jb and Ja > 0
+    assert np.array_equal(ga, gb)
+    for a, b in zip(ra, rb):
+        assert np.any(a != 0) and np.array_equal(a, b)
