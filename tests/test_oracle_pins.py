@@ -15,11 +15,11 @@ from oracle import oracle as O
 from oracle import setup_ref as S
 
 
-def _homog(nz, nx, d, nt, dt, vp=2000.0, rho=2000.0, f0=15.0, src=("p", None), rec=None, faces=63 & ~12):
+def _homog(nz, nx, d, nt, dt, vp=2000.0, rho=2000.0, f0=15.0, src=("p", None), rec=None, faces=63 & ~12, order=4):
     w = S.ricker(f0, nt, dt).astype(np.float32)
     field, pos = src
     pos = pos or (0.5 * (nz - 1) * d, 0.5 * (nx - 1) * d)
-    return dict(physics="acoustic", ndim=2, order=4, grid=[(0.0, d, nz), (0.0, d, nx)],
+    return dict(physics="acoustic", ndim=2, order=order, grid=[(0.0, d, nz), (0.0, d, nx)],
                 vp=np.full((nz, nx), vp, np.float32), rho=np.full((nz, nx), rho, np.float32),
                 pml_faces=faces, dt=dt, nt=nt, rfields=["p", "vx", "vz"],
                 shots=[dict(src={field: ([pos], w[:, None])}, rec=rec)])
@@ -47,15 +47,19 @@ def test_time_reversal_float64():
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-9
 
 
-def test_green_function_float64():
+@pytest.mark.parametrize("order,bound", [(2, 5e-3), (4, 2e-5), (6, 2e-5), (8, 2e-5)])
+def test_green_function_float64(order, bound):
     """accuracy2D.jl: FDTD pressure in a homogeneous medium against the 2-D
-    Green's function, normalised misfit < 1e-2 (same bound as the reference)."""
+    Green's function, normalised misfit < 1e-2 (same bound as the reference),
+    at every stencil order the reference offers (diff2D.jl): the analytic
+    solution knows nothing of the stencil, so it pins each order's
+    coefficients."""
     nz, nx, d, nt, dt = 161, 161, 5.0, 600, 0.0005
     vp, rho, f0 = 2000.0, 2000.0, 15.0
     sz, sx = 400.0, 400.0
     offs = np.array([100.0, 150.0, 200.0])
     rec = [(sz, sx + o) for o in offs]
-    ex = _homog(nz, nx, d, nt, dt, vp, rho, f0, src=("p", (sz, sx)), rec=rec, faces=63 & ~12)
+    ex = _homog(nz, nx, d, nt, dt, vp, rho, f0, src=("p", (sz, sx)), rec=rec, faces=63 & ~12, order=order)
     r = O.forward(ex, dtype=np.float64)["p"][0]
     w = S.ricker(f0, nt, dt)
     nf = 8 * nt
@@ -71,7 +75,7 @@ def test_green_function_float64():
         p_an = np.fft.irfft(H * W, nf)[:nt]
         err.append(np.sum((r[:, i] - p_an) ** 2) / np.sum(p_an ** 2))
     assert max(err) < 1e-2, err  # the reference's bound
-    assert max(err) < 1e-4, err  # amplitude and phase, absolute (no fitted scale)
+    assert max(err) < bound, err  # amplitude and phase, absolute (no fitted scale)
 
 
 def test_float32_against_float64():
