@@ -78,6 +78,37 @@ def test_green_function_float64(order, bound):
     assert max(err) < bound, err  # amplitude and phase, absolute (no fitted scale)
 
 
+@pytest.mark.parametrize("order,bound", [(4, 2e-5), (8, 6e-5), (2, 3e-2)])
+def test_green_function_3d_float64(order, bound):
+    """accuracy3D.jl (its check: normalised misfit < 1e-2 against an
+    analytic reference): 3-D homogeneous acoustic medium, pressure source,
+    p(r, t) = rho dV / (4 pi r) w'(t - r / c) (p_tt - c^2 lap p = K dV w'(t)
+    delta(x), K / c^2 = rho), the injected sample half a step late as in
+    2-D.  Receivers on the x axis at 100-200 m; the window ends before the
+    CPML faces can return anything.  Order 2 at 6.7 points per shortest
+    wavelength is dispersive (2 % at 200 m)."""
+    n, d, nt, dt = 61, 10.0, 260, 0.001
+    vp, rho, f0 = 2000.0, 2000.0, 12.0
+    c0 = 0.5 * (n - 1) * d
+    offs = np.array([100.0, 150.0, 200.0])
+    w = S.ricker(f0, nt, dt)
+    ex = dict(physics="acoustic", ndim=3, order=order, grid=[(0.0, d, n)] * 3,
+              vp=np.full((n, n, n), vp, np.float32), rho=np.full((n, n, n), rho, np.float32),
+              pml_faces=63, dt=dt, nt=nt, rfields=["p"], npml=13 + order - 1,
+              shots=[dict(src={"p": ([(c0, c0, c0)], w.astype(np.float32)[:, None])},
+                          rec=[(c0, c0, c0 + o) for o in offs])])
+    r = O.forward(ex, dtype=np.float64)["p"][0]
+    nf = 8 * nt
+    om = 2 * np.pi * np.fft.rfftfreq(nf, dt)
+    W = np.fft.rfft(w, nf) * np.exp(-1j * om * 0.5 * dt)
+    err = []
+    for i, o in enumerate(offs):
+        P = rho * d ** 3 / (4 * np.pi * o) * (1j * om) * W * np.exp(-1j * om * o / vp)
+        p_an = np.fft.irfft(P, nf)[:nt]
+        err.append(np.sum((r[:, i] - p_an) ** 2) / np.sum(p_an ** 2))
+    assert max(err) < bound, err
+
+
 def test_float32_against_float64():
     ex = _homog(51, 71, 5.0, 300, 0.0005, rec=[(20.0, x) for x in np.linspace(0, 350, 8)])
     ex["vp"][25:] = 3000.0
