@@ -52,6 +52,31 @@ def _free_port():
     return p
 
 
+def _illum_worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        # an FP64 column-major stack (pac.illum_stack of a sharded run)
+        a = np.asfortranarray(np.arange(24, dtype=np.float64).reshape(4, 6) * (rank + 1) + 0.25)
+        shots.reduce_gradient(a)
+        np.save(os.path.join(out, "i%d.npy" % rank), a)
+        assert a.flags.f_contiguous
+    finally:
+        dist.destroy_process_group()
+
+
+def test_fp64_column_major_stack_sums_over_two_ranks(tmp_path):
+    import torch.multiprocessing as mp
+
+    mp.spawn(_illum_worker, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
+    want = np.arange(24, dtype=np.float64).reshape(4, 6) * 3 + 0.5
+    for r in range(2):
+        assert np.array_equal(np.load(tmp_path / ("i%d.npy" % r)), want)
+
+
 @pytest.mark.parametrize("nss", [1, 5, 16])
 def test_gradient_sum_over_two_ranks(tmp_path, nss):
     import torch.multiprocessing as mp
