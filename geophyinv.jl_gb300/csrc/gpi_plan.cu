@@ -1449,6 +1449,7 @@ int get_snapshot(Plan &p, int ipw, int k, int shot, float *out, int on_device) {
 // its forward_save run)
 int set_illum(Plan &p, int enable) {
   if (enable && !p.present[GPI_P]) return fail(&p, GPI_E_UNSUPPORTED, "illumination sums p^2: acoustic media only");
+  if (enable && p.d.nshots > 65535) return fail(&p, GPI_E_UNSUPPORTED, "illumination: at most 65535 shots per plan");
   if (!enable) {
     if (p.illum) cudaFreeAsync(p.illum, p.stream);
     p.illum = nullptr;
