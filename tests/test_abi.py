@@ -78,3 +78,39 @@ def test_create_rejects_bad_checkpoint_requests(lib):
     assert b"acoustic" in lib.gpi_last_error(None)
     d.checkpoints = -1
     assert lib.gpi_plan_create(ctypes.byref(d), ctypes.byref(plan)) == -1
+
+
+def test_entry_points_reject_a_null_plan(lib):
+    """Every plan entry point answers GPI_E_INVALID for a null plan, before
+    touching a device."""
+    import ctypes
+
+    null = ctypes.c_void_p()
+    assert lib.gpi_set_illum(null, 1) == -1
+    assert lib.gpi_get_illum(null, None, 0) == -1
+    assert lib.gpi_run(null, 0) == -1
+    assert lib.gpi_set_graph(null, 1) == -1
+    assert lib.gpi_set_snapshots(null, 0, 0, None) == -1
+    out = ctypes.c_size_t()
+    assert lib.gpi_plan_bytes(null, ctypes.byref(out)) == -1
+
+
+def test_estimate_at_every_order(lib):
+    """gpi_plan_estimate takes every order of the reference; stencil orders
+    other than 4 need more than 65535 shots to be refused for their grid."""
+    import ctypes
+
+    d = _lib.PlanDesc()
+    d.physics, d.ndim = 1, 3
+    d.nz, d.ny, d.nx, d.nbound, d.nt, d.nshots, d.npw = 80, 80, 80, 3, 10, 1, 1
+    d.dt, d.dz, d.dx, d.dy = 1e-3, 10.0, 10.0, 10.0
+    d.pml_faces = 0x3F
+    sizes = []
+    for order in (2, 4, 6, 8):
+        d.order, d.npml = order, 10 + order - 1
+        b = ctypes.c_size_t()
+        assert lib.gpi_plan_estimate(ctypes.byref(d), ctypes.byref(b)) == 0, lib.gpi_last_error(None)
+        sizes.append(b.value)
+    assert all(s > 0 for s in sizes)
+    d.order, d.nshots = 2, 70000
+    assert lib.gpi_plan_estimate(ctypes.byref(d), ctypes.byref(ctypes.c_size_t())) == -4
