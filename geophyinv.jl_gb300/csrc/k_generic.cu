@@ -137,44 +137,56 @@ __device__ __forceinline__ float gder_at(const GGeo &g, const GDer &a, int64_t b
 
 // compute_v!: @inn(v) += c * D (acoustic, advance_acou.jl:273-284) or
 // -= c * (D1 + D2 [+ D3]) (elastic, advance_elastic.jl:69-110), the
-// coefficient stored at the velocity cell; the derivatives share the @inn
-// extents
-struct GVel {
-  GGeo g;
+// coefficient stored at the velocity cell; the derivatives of a component
+// share its @inn extents.  One thread updates every component whose domain
+// holds its cell (the components read the stresses only, so their order is
+// free), so the stress columns two components read come from L1.
+struct GVelC {
   float *v;  // shot 0
   const float *cf;
   GDer d[3];  // nd of them
-  int nd, r1, r2, r3, hy;
-  int elastic, nshots;
+  int nd, r1, r2, r3;
+};
+struct GVel {
+  GGeo g;
+  GVelC c[3];  // nc of them
+  int nc, hy, elastic;
 };
 // Launch shape of the per-cell kernels: GT threads along z, grid (the y-x
 // columns, z blocks, shots), so that a thread finds its cell without a
 // division.
 constexpr int GT = 128;
 template <int ORDER>
-__global__ void __launch_bounds__(GT) k_gvel(const GVel a) {
+__device__ __forceinline__ void gvel_one(const GGeo &g, const GVelC &a, int hy, int elastic, int shot, int iz, int iy,
+                                         int ix) {
+  const int64_t ov = g.S(iz + g.h, iy + hy, ix + g.h), od = shot * g.fs + g.S(iz, iy, ix);
+  const float c = a.cf[ov];
+  float *v = a.v + shot * g.fs + ov;
+  const float D1 = gder_at<ORDER>(g, a.d[0], od, shot, iz, iy, ix);
+  if (!elastic) {
+    *v = *v + c * D1;
+  } else if (a.nd == 2) {
+    const float D2 = gder_at<ORDER>(g, a.d[1], od, shot, iz, iy, ix);
+    *v = *v - c * (D1 + D2);
+  } else {
+    const float D2 = gder_at<ORDER>(g, a.d[1], od, shot, iz, iy, ix);
+    const float D3 = gder_at<ORDER>(g, a.d[2], od, shot, iz, iy, ix);
+    *v = *v - c * (D1 + D2 + D3);
+  }
+}
+// grid over the union of the components' domains (r2u columns per x)
+template <int ORDER>
+__global__ void __launch_bounds__(GT) k_gvel(const GVel a, int r1u, int r2u) {
   const GGeo &g = a.g;
   const int iz = blockIdx.y * GT + threadIdx.x + 1;
-  if (iz > a.r1) return;
+  if (iz > r1u) return;
   const bool flat = g.ndim == 2;  // one y plane: the column index is x
-  const int iy = flat ? 1 : (int)(blockIdx.x % (unsigned)a.r2) + 1;
-  const int ix = flat ? (int)blockIdx.x + 1 : (int)(blockIdx.x / (unsigned)a.r2) + 1;
+  const int iy = flat ? 1 : (int)(blockIdx.x % (unsigned)r2u) + 1;
+  const int ix = flat ? (int)blockIdx.x + 1 : (int)(blockIdx.x / (unsigned)r2u) + 1;
   const int shot = blockIdx.z;
-  {
-    const int64_t ov = g.S(iz + g.h, iy + a.hy, ix + g.h), od = shot * g.fs + g.S(iz, iy, ix);
-    const float c = a.cf[ov];
-    float *v = a.v + shot * g.fs + ov;
-    const float D1 = gder_at<ORDER>(g, a.d[0], od, shot, iz, iy, ix);
-    if (!a.elastic) {
-      *v = *v + c * D1;
-    } else if (a.nd == 2) {
-      const float D2 = gder_at<ORDER>(g, a.d[1], od, shot, iz, iy, ix);
-      *v = *v - c * (D1 + D2);
-    } else {
-      const float D2 = gder_at<ORDER>(g, a.d[1], od, shot, iz, iy, ix);
-      const float D3 = gder_at<ORDER>(g, a.d[2], od, shot, iz, iy, ix);
-      *v = *v - c * (D1 + D2 + D3);
-    }
+  for (int q = 0; q < a.nc; q++) {
+    const GVelC &c = a.c[q];
+    if (iz <= c.r1 && iy <= c.r2 && ix <= c.r3) gvel_one<ORDER>(g, c, a.hy, a.elastic, shot, iz, iy, ix);
   }
 }
 
@@ -354,34 +366,41 @@ static int gstep_order(Plan *p, int vonly) {
   };
   // update_dstress! + compute_v!
   const int vid[3] = {GPI_VX, GPI_VY, GPI_VZ};
-  for (int q = 0; q < 3; q++) {
-    if (q == 1 && !three) continue;
+  {
     GVel a;
     a.g = g;
-    a.v = f[vid[q]];
-    a.cf = p->coef[q == 0 ? 0 : q == 1 ? 1 : (three ? 2 : 1)];
-    int kz, ky, kx;
-    field_kinds(vid[q], &kz, &ky, &kx);
-    a.r1 = nkind(kz, n[0], h) - 2 * h;
-    a.r2 = three ? nkind(ky, n[1], h) - 2 * h : 1;
-    a.r3 = nkind(kx, n[2], h) - 2 * h;
     a.hy = three ? h : 0;
     a.elastic = !ac;
-    a.nshots = p->d.nshots;
-    if (ac) {
-      a.nd = 1;
-      a.d[0] = der(three ? q : (q == 0 ? 0 : 1));
-    } else if (!three) {
-      a.nd = 2;
-      a.d[0] = der(q == 0 ? 0 : 1);
-      a.d[1] = der(q == 0 ? 3 : 2);
-    } else {
-      const int i3[3][3] = {{0, 4, 8}, {1, 3, 7}, {2, 5, 6}};
-      a.nd = 3;
-      for (int k = 0; k < 3; k++) a.d[k] = der(i3[q][k]);
+    a.nc = 0;
+    int r1u = 0, r2u = 0, r3u = 0;
+    for (int q = 0; q < 3; q++) {
+      if (q == 1 && !three) continue;
+      GVelC &c = a.c[a.nc++];
+      c.v = f[vid[q]];
+      c.cf = p->coef[q == 0 ? 0 : q == 1 ? 1 : (three ? 2 : 1)];
+      int kz, ky, kx;
+      field_kinds(vid[q], &kz, &ky, &kx);
+      c.r1 = nkind(kz, n[0], h) - 2 * h;
+      c.r2 = three ? nkind(ky, n[1], h) - 2 * h : 1;
+      c.r3 = nkind(kx, n[2], h) - 2 * h;
+      r1u = std::max(r1u, c.r1);
+      r2u = std::max(r2u, c.r2);
+      r3u = std::max(r3u, c.r3);
+      if (ac) {
+        c.nd = 1;
+        c.d[0] = der(three ? q : (q == 0 ? 0 : 1));
+      } else if (!three) {
+        c.nd = 2;
+        c.d[0] = der(q == 0 ? 0 : 1);
+        c.d[1] = der(q == 0 ? 3 : 2);
+      } else {
+        const int i3[3][3] = {{0, 4, 8}, {1, 3, 7}, {2, 5, 6}};
+        c.nd = 3;
+        for (int k = 0; k < 3; k++) c.d[k] = der(i3[q][k]);
+      }
     }
-    const dim3 vg((unsigned)(a.r2 * a.r3), (a.r1 + GT - 1) / GT, p->d.nshots);
-    k_gvel<ORDER><<<vg, GT, 0, p->stream>>>(a);
+    const dim3 vg((unsigned)(r2u * r3u), (r1u + GT - 1) / GT, p->d.nshots);
+    k_gvel<ORDER><<<vg, GT, 0, p->stream>>>(a, r1u, r2u);
     p->launches++;
   }
   // rigid faces in the order x, y, z; min, max (update_v!)
