@@ -109,8 +109,9 @@ def test_green_function_3d_float64(order, bound):
     assert max(err) < bound, err
 
 
-def test_float32_against_float64():
-    ex = _homog(51, 71, 5.0, 300, 0.0005, rec=[(20.0, x) for x in np.linspace(0, 350, 8)])
+@pytest.mark.parametrize("order", [2, 4, 6, 8])
+def test_float32_against_float64(order):
+    ex = _homog(51, 71, 5.0, 300, 0.0005, rec=[(20.0, x) for x in np.linspace(0, 350, 8)], order=order)
     ex["vp"][25:] = 3000.0
     r32 = O.forward(ex, np.float32)
     r64 = O.forward(ex, np.float64)
