@@ -129,3 +129,30 @@ def test_elastic_oracle_runs_and_is_finite():
                           rec=[(20.0, x) for x in np.linspace(0, 350, 8)])])
     r = O.forward(ex)
     assert np.isfinite(r["vz"]).all() and np.abs(r["vz"]).max() > 0
+
+
+@pytest.mark.parametrize("order", [2, 4, 8])
+def test_elastic_explosion_equals_the_acoustic_pressure_source(order):
+    """An explosive source (tauxx and tauzz, src/fdtd/source.jl:61-121) in a
+    homogeneous elastic medium radiates P waves only: the velocity field is
+    irrotational and obeys the acoustic equations with K = lambda + 2 mu
+    and the same source scaling (dtM = dtK).  The elastic restatement
+    (advance_elastic.jl) must then give the velocity records of the
+    acoustic one (advance_acou.jl), which the Green's functions pin, up to
+    the opposite sign convention of the two systems' stresses.  FP64."""
+    nz = nx = 121
+    d, nt, dt = 5.0, 500, 0.0004
+    vp, vs, rho = 2500.0, 1400.0, 2000.0
+    w = S.ricker(15.0, nt, dt).astype(np.float32)
+    c = 0.5 * (nz - 1) * d
+    rec = [(c + 40.0, c + 60.0), (c - 80.0, c + 30.0), (c, c + 120.0), (c + 100.0, c - 100.0)]
+    base = dict(ndim=2, order=order, grid=[(0.0, d, nz), (0.0, d, nx)], rho=np.full((nz, nx), rho, np.float32),
+                vp=np.full((nz, nx), vp, np.float32), pml_faces=63 & ~12, dt=dt, nt=nt, rfields=["vx", "vz"])
+    el = dict(base, physics="elastic", vs=np.full((nz, nx), vs, np.float32),
+              shots=[dict(src={"tauxx": ([(c, c)], w[:, None])}, rec=rec)])
+    ac = dict(base, physics="acoustic", shots=[dict(src={"p": ([(c, c)], w[:, None])}, rec=rec)])
+    re, ra = O.forward(el, np.float64), O.forward(ac, np.float64)
+    for f in ("vx", "vz"):
+        a, b = re[f][0], ra[f][0]
+        assert np.abs(b).max() > 0.05
+        assert np.linalg.norm(a + b) / np.linalg.norm(b) < 1e-6, f
