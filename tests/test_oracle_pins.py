@@ -156,3 +156,25 @@ def test_elastic_explosion_equals_the_acoustic_pressure_source(order):
         a, b = re[f][0], ra[f][0]
         assert np.abs(b).max() > 0.05
         assert np.linalg.norm(a + b) / np.linalg.norm(b) < 1e-6, f
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_elastic3d_explosion_equals_the_acoustic_pressure_source(order):
+    """The same in 3-D (tauxx, tauyy, tauzz against p; advance_elastic.jl's
+    3-D kernels against advance_acou.jl's)."""
+    n, d, nt, dt = 41, 10.0, 160, 0.0008
+    vp, vs, rho = 2500.0, 1400.0, 2000.0
+    w = S.ricker(12.0, nt, dt).astype(np.float32)
+    c = 0.5 * (n - 1) * d
+    rec = [(c + 40.0, c - 30.0, c + 60.0), (c - 80.0, c + 50.0, c + 30.0), (c, c, c + 120.0)]
+    base = dict(ndim=3, order=order, grid=[(0.0, d, n)] * 3, rho=np.full((n, n, n), rho, np.float32),
+                vp=np.full((n, n, n), vp, np.float32), pml_faces=63, dt=dt, nt=nt, rfields=["vx", "vy", "vz"],
+                npml=10 + order - 1)
+    el = dict(base, physics="elastic", vs=np.full((n, n, n), vs, np.float32),
+              shots=[dict(src={"tauxx": ([(c, c, c)], w[:, None])}, rec=rec)])
+    ac = dict(base, physics="acoustic", shots=[dict(src={"p": ([(c, c, c)], w[:, None])}, rec=rec)])
+    re, ra = O.forward(el, np.float64), O.forward(ac, np.float64)
+    for f in ("vx", "vy", "vz"):
+        a, b = re[f][0], ra[f][0]
+        assert np.abs(b).max() > 1e-3
+        assert np.linalg.norm(a + b) / np.linalg.norm(b) < 1e-6, f
