@@ -71,3 +71,34 @@ def test_green_function_3d_on_the_engine(engine, order, bound):
         err.append(np.sum((r[:, i] - p_an) ** 2) / np.sum(p_an ** 2))
     assert max(err) < 1e-2, err  # the reference's bound
     assert max(err) < bound, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [4, 2])
+def test_engine_elastic_explosion_equals_the_acoustic_pressure_source(engine, order):
+    """P waves only: the engine's elastic steps with an explosive source give
+    the velocity records of its acoustic steps with a pressure source and
+    K = lambda + 2 mu, with the opposite sign (FP32)."""
+    nz = nx = 121
+    d, nt, dt = 5.0, 500, 0.0004
+    vp, vs, rho = 2500.0, 1400.0, 2000.0
+    tgrid = Grid(0.0, dt, nt)
+    w = ricker(15.0, tgrid)
+    c = 0.5 * (nz - 1) * d
+    rec = np.array([[c + 40.0, c + 60.0], [c - 80.0, c + 30.0], [c, c + 120.0], [c + 100.0, c - 100.0]])
+    grid = [Grid(0.0, d, nz), Grid(0.0, d, nx)]
+    faces = ("zmin", "zmax", "xmin", "xmax")
+    full = lambda v: np.full((nz, nx), v, np.float32)  # noqa: E731
+    el = configs.Workload("explosion", "elastic", grid, full(vp), full(rho), vs=full(vs),
+                          shots=[(np.array([[c, c]]), rec)], tgrid=tgrid, wavelet=w, rfields=("vx", "vz"),
+                          pml_faces=faces, src_field="tauxx")
+    ac = configs.Workload("pressure", "acoustic", grid, full(vp), full(rho), shots=[(np.array([[c, c]]), rec)],
+                          tgrid=tgrid, wavelet=w, rfields=("vx", "vz"), pml_faces=faces, src_field="p")
+    pe, pa = el.expt(order=order), ac.expt(order=order)
+    update(pe)
+    update(pa)
+    for f in ("vx", "vz"):
+        a = pe.data[0][0].d[f].astype(np.float64)
+        b = pa.data[0][0].d[f].astype(np.float64)
+        assert np.abs(b).max() > 0.05
+        assert np.linalg.norm(a + b) / np.linalg.norm(b) < 1e-5, f
